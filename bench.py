@@ -1,0 +1,410 @@
+"""Benchmark: converged velocity solves/s on the 640 x 80 (1 km, nσ = 4) synthetic channel.
+
+One step = one Picard-converged velocity solve (update_velocities!) on a perturbed-thickness state:
+the channel is first solved to convergence at thickness h_A (seed 1) and its wavelet coarse space
+updated (update_wavelets!), then the thickness is perturbed by 5 % seeded noise (seed 2).  Every step
+restores that state and solves it to ||b - A u|| / ||b|| < tol_picard.
+
+  value    mixed precision (float32 operator / V-cycle, float64 residual and reductions), fields resident
+           in HBM, device time per step from CUDA events on the solver's stream, L2 flushed between steps
+  e2e      the same solve through the host C ABI (wavi_solve_velocities) from pinned host buffers, the
+           host<->device copies inside the timed region
+  fp64_gpu the reference algorithm in float64 on the GPU (the comparison the metric names)
+  roofline the operator kernel (float32) timed alone at this size, algorithmic bytes / duration
+  cpu_baseline the CPU oracle (the FP64 restatement of the reference) on a bounded sample
+
+``--impl reference`` times only the CPU oracle on all host cores and prints its own line.
+Under torchrun (N > 1) every rank solves its own replica (no collective); value is the sum.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__  # noqa: E402
+
+TOL_PICARD = 1e-6
+MAXITER_PICARD = 100
+WORKLOAD = "channel 640x80 @1km nsigma=4, perturbed-thickness converged solve (tol_picard=1e-6)"
+METRIC = "converged velocity solves/s (640x80 channel, mixed precision)"
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def build_state(pkg, precision_warm="fp64"):
+    """The perturbed-thickness C2 state (host numpy fields) right before the timed solve."""
+    from wavi_gb300 import synthetic
+    from wavi_gb300.model import GPUParallelSpec, Model, post_solve_steps, pre_solve, update_velocities
+    g, bed, p, sp, ic = synthetic.channel_c2(tol_picard=TOL_PICARD, maxiter_picard=MAXITER_PICARD)
+    m = Model(g, bed, p, sp, ic, parallel_spec=GPUParallelSpec(precision=precision_warm))
+    pre_solve(m)
+    update_velocities(m)
+    post_solve_steps(m)
+    rng = np.random.default_rng(2)
+    m.fields["h"][...] = m.fields["h"] * (1.0 + rng.uniform(-0.05, 0.05, m.fields["h"].shape))
+    pre_solve(m)
+    return m
+
+
+def solve_field_names():
+    from wavi_gb300.gpu import ALL_FIELDS
+    return ALL_FIELDS
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in (self.out or "").splitlines():
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def time_device_solves(torch, solver, params, snapshot, steps, warmup, flush_bytes=256 << 20):
+    """Per-step device time (CUDA events on the solver's stream) of resident solves from the snapshot."""
+    names = solve_field_names()
+    stream = torch.cuda.ExternalStream(solver.stream())
+    dev = {}
+    work = {}
+    with torch.cuda.stream(stream):
+        for k in names:
+            a = snapshot[k]
+            dev[k] = torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F"))).cuda()
+            work[k] = dev[k].clone()
+        flush = torch.empty(flush_bytes // 4, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    times, stats = [], []
+    for it in range(warmup + steps):
+        with torch.cuda.stream(stream):
+            for k in names:
+                work[k].copy_(dev[k])
+            flush.fill_(float(it))  # evict the previous step's working set from L2 (129 MB)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        st = solver.solve_device(params, work)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        if it >= warmup:
+            times.append(e0.elapsed_time(e1) / 1e3)
+            stats.append(st)
+    out = {k: work[k].cpu().numpy() for k in ("u", "v")}
+    return times, stats, out
+
+
+def time_host_solves(torch, solver, params, snapshot, steps, warmup):
+    """e2e: the host C ABI from pinned buffers; H2D and D2H inside the timed region."""
+    names = solve_field_names()
+    stream = torch.cuda.ExternalStream(solver.stream())
+    pinned = {}
+    for k in names:
+        a = np.asarray(snapshot[k])
+        t = torch.empty(a.size, dtype=torch.float64 if a.dtype == np.float64 else torch.uint8, pin_memory=True)
+        pinned[k] = t
+    views = {}
+    for k in names:
+        a = np.asarray(snapshot[k])
+        views[k] = pinned[k].numpy().reshape(a.shape, order="F") if a.ndim > 1 else pinned[k].numpy()
+    in_bytes = sum(np.asarray(snapshot[k]).nbytes for k in names if k not in (
+        "shelf_strain_rate", "av_speed", "bed_speed", "tau_bed", "eta_av", "quad_f1", "beta_eff", "gu_residual",
+        "gv_residual"))
+    out_bytes = sum(np.asarray(snapshot[k]).nbytes for k in names if k not in (
+        "h", "s", "dsdh", "grounded_fraction", "weertman_c", "accumulation", "basal_melt", "gu_h", "gu_s",
+        "gu_grounded_fraction", "gv_h", "gv_s", "gv_grounded_fraction", "glen_b", "wu_mask", "wv_mask"))
+    times = []
+    for it in range(warmup + steps):
+        for k in names:
+            views[k][...] = snapshot[k]
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        solver.solve(params, views)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        if it >= warmup:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    return times, in_bytes, out_bytes
+
+
+def op_roofline(torch, solver, n_launch=200):
+    """Average duration of the float32 operator kernel alone at the workload size (CUDA events on the
+    solver's stream), against its algorithmic bytes."""
+    d = solver.grid
+    nx, ny = d.nx, d.ny
+    N = (nx + 1) * ny + nx * (ny + 1)
+    Nh, Nc = nx * ny, (nx - 1) * (ny - 1)
+    stream = torch.cuda.ExternalStream(solver.stream())
+    with torch.cuda.stream(stream):
+        x = torch.randn(N, dtype=torch.float32, device="cuda")
+        y = torch.zeros_like(x)
+    torch.cuda.synchronize()
+    for _ in range(20):
+        solver.apply_operator_device(x, y, "mixed")
+    # bytes: read x, write y, heta_h, dimp (Nh), heta_c (Nc), beta_m, h_m (N) in float32 + interior mask
+    alg_bytes = 4.0 * (2 * N + 2 * Nh + Nc + 2 * N) + N
+    with torch.cuda.stream(stream):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+    for _ in range(n_launch):
+        solver.apply_operator_device(x, y, "mixed")
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    e1.synchronize()
+    dur = e0.elapsed_time(e1) / 1e3 / n_launch
+    return alg_bytes, dur
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def ncu_traffic():
+    """dram bytes per launch of the operator kernel from the committed ncu summary, if present."""
+    fn = os.path.join(ROOT, "profiles", "op_kernel_c2.md")
+    try:
+        for ln in open(fn):
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------------------------------
+# CPU oracle (the reference restated in C++), bounded sample on host threads
+# ---------------------------------------------------------------------------------------------------
+def cpu_sample(threads, picard_iters_sample=1):
+    """Each thread builds the same perturbed-thickness state in its own oracle model and runs
+    ``picard_iters_sample`` Picard iterations of the solve.  Returns (seconds per Picard iteration per
+    thread, threads, picard count of the full solve measured by the oracle's warm-state run length)."""
+    oracle = __graft_entry__.load_oracle()
+    pkg = __graft_entry__.load_package()
+    from wavi_gb300 import synthetic
+    import ctypes as C
+
+    def make():
+        g, bed, p, sp, ic = synthetic.channel_c2(tol_picard=TOL_PICARD, maxiter_picard=MAXITER_PICARD)
+        om = oracle.build_model(g, bed, p, sp, ic)
+        return om, g, p, sp
+
+    results = [None] * threads
+
+    def work(i):
+        om, g, p, sp = make()
+        om.pre_solve()
+        sp1 = type(sp)(**{**sp.__dict__, "maxiter_picard": picard_iters_sample})
+        oracle.lib().oracle_set_params(om.h, C.byref(p.to_c()), C.byref(sp1.to_c()), 0.0)
+        t0 = time.perf_counter()
+        om.update_velocities()
+        results[i] = (time.perf_counter() - t0) / picard_iters_sample
+
+    ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+    t0 = time.perf_counter()
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    wall = time.perf_counter() - t0
+    return results, wall
+
+
+# Picard iterations of the timed solve (same algorithm and state on every arm; the FP64 GPU arm reports
+# its own count, which the CPU extrapolation uses when available).
+PICARD_FALLBACK = 40
+
+
+def reference_arm(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    per_iter = []
+    for it in range(args.warmup + args.steps):
+        res, wall = cpu_sample(threads)
+        if it >= args.warmup:
+            per_iter.append(statistics.median(res))
+    sec_per_iter = statistics.median(per_iter)
+    solves_per_s = threads / (sec_per_iter * PICARD_FALLBACK)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": solves_per_s, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec_per_iter * PICARD_FALLBACK,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "parallelism": f"{threads} host threads, independent replicas"},
+        "cpu_baseline": {"value": solves_per_s, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"first Picard iteration of the solve per thread ({threads} threads), "
+                                   f"extrapolated x{PICARD_FALLBACK} Picard iterations"},
+        "e2e": {"value": solves_per_s, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def gpu_arm(args):
+    import torch
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    pkg = __graft_entry__.load_package()
+    from wavi_gb300 import build
+    build.build_library()
+    from wavi_gb300.gpu import VelocitySolver
+    from wavi_gb300.model import release_solver
+
+    m = build_state(pkg)
+    snapshot = {k: np.array(v, copy=True) for k, v in m.fields.items()}
+    release_solver(m)
+    g, p, sp = m.grid, m.params, m.solver_params
+
+    mixed = VelocitySolver(g, sp, precision="mixed", device=local)
+    fp64 = VelocitySolver(g, sp, precision="fp64", device=local)
+
+    # float64 reference algorithm on the GPU
+    t64, st64, out64 = time_device_solves(torch, fp64, p, snapshot, max(1, args.steps // 2), 1)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        tmix, stmix, outmix = time_device_solves(torch, mixed, p, snapshot, args.steps, args.warmup)
+    torch.cuda.synchronize()
+    clocks = clk.summary()
+    # max over ranks of the timed-region time
+    total = sum(tmix)
+    if world > 1:
+        tt = torch.tensor([total], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total = float(tt.item())
+    value = world * args.steps / total
+
+    te2e, hb, db = time_host_solves(torch, mixed, p, snapshot, args.steps, max(1, args.warmup // 2))
+    e2e_value = world * len(te2e) / sum(te2e)
+
+    alg_bytes, dur = op_roofline(torch, mixed)
+    peaks = measured_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = alg_bytes / dur / 1e9
+
+    err = np.sqrt(np.sum((outmix["u"] - out64["u"]) ** 2) + np.sum((outmix["v"] - out64["v"]) ** 2)) / \
+        np.sqrt(np.sum(out64["u"] ** 2) + np.sum(out64["v"] ** 2))
+    fp64_value = world * len(t64) / sum(t64)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        res, wall = cpu_sample(threads)
+        sec = statistics.median(res)
+        picard = int(statistics.median([s["picard_iterations"] for s in st64]))
+        cpu = {"value": threads / (sec * picard), "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": f"first Picard iteration of this solve on each of {threads} threads "
+                         f"({sec:.2f} s each), extrapolated x{picard} Picard iterations (the FP64 GPU count)"}
+
+    launches = sum(s["kernel_launches"] for s in stmix)
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nx": g.nx, "ny": g.ny, "nsigma": g.nσ, "dx_m": g.dx,
+                   "unknowns": int(m.u_inner.sum() + m.v_inner.sum()), "tol_picard": TOL_PICARD,
+                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(hb), "d2h_bytes_per_step": int(db)},
+        "gpu_launches": int(launches),
+        "fp64_gpu": {"value": fp64_value, "unit": "solves/s", "ms_per_step": 1e3 * sum(t64) / len(t64),
+                     "picard_iterations": st64[-1]["picard_iterations"],
+                     "coarse_cg_iterations": st64[-1]["coarse_cg_iterations"]},
+        "mixed_over_fp64": value / fp64_value if fp64_value else None,
+        "rel_err_mixed_vs_fp64": float(err),
+        "solve": {k: stmix[-1][k] for k in ("picard_iterations", "coarse_cg_iterations", "op_applications",
+                                             "rel_residual", "kernel_launches", "host_syncs", "status_name")},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": ncu_traffic(), "kernel": "k_op<float> (operator, 640x80)",
+                     "alg_bytes_per_launch": alg_bytes, "avg_launch_us": dur * 1e6,
+                     "peak_source": "measured" if peaks else "fallback"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    mixed.close()
+    fp64.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,213 @@
+/*
+ * wavi_gpu.h — C ABI of libwavi_gpu.so, the GB300 (sm_103a) backend for WAVI.jl's velocity solve.
+ *
+ * The library replaces one call of the reference: `update_velocities!(model)`
+ * (src/Models/update_velocities.jl:11-29), the Picard loop around the matrix-free momentum operator
+ * (src/utilities.jl:13-149) with the Haar-wavelet multigrid V-cycle and coarse conjugate-gradient solve
+ * (src/Wavelets/update_preconditioners.jl:7-83, :153-216).  The reference reaches that call from
+ * `update_model_velocities!` (src/Models/update_state.jl:154-157) and dispatches on the model's
+ * parallel-spec type parameter (src/WAVI.jl:17-18, src/Models/Model.jl:1-8), so a Julia host binds these
+ * entry points from a new `GPUParallelSpec <: AbstractParallelSpec` method of `update_velocities!`.
+ *
+ * Conventions
+ *  - Every 2-D array is column-major with x (the first Julia index) fastest, exactly as the reference
+ *    stores it: h grid nx*ny, u grid (nx+1)*ny, v grid nx*(ny+1), c grid (nx-1)*(ny-1),
+ *    3-D sigma fields nx*ny*nsigma (src/Fields/*.jl).
+ *  - Masks are one byte per point (Julia Array{Bool} layout): 0 = false, anything else = true.
+ *  - Floating-point arrays are IEEE float64 on the host side of the boundary.
+ *  - Every entry point returns 0 on success or a negative wavi_status; the message of the last failure
+ *    of a context is available from wavi_last_error().  No entry point aborts, throws or traps.
+ *  - A context owns one CUDA stream and its device buffers; it is not re-entrant, but distinct
+ *    contexts may be used from distinct host threads at the same time.
+ */
+#ifndef WAVI_GPU_H
+#define WAVI_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WAVI_ABI_VERSION 1
+
+typedef enum wavi_status {
+  WAVI_OK = 0,
+  WAVI_ERR_ARGUMENT = -1,          /* bad sizes, null pointers, inconsistent masks */
+  WAVI_ERR_CUDA = -2,              /* a CUDA runtime call failed (message holds cudaGetErrorString) */
+  WAVI_ERR_NONFINITE = -3,         /* NaN/Inf met in a residual norm or a CG scalar */
+  WAVI_ERR_NOT_CONVERGED = -4,     /* soft: Picard stopped at maxiter_picard; outputs are written */
+  WAVI_ERR_COARSE_CAP = -5,        /* soft: the coarse CG stopped at maxiter_coarse; outputs are written */
+  WAVI_ERR_WATCHDOG = -6,          /* a bounded device-side wait gave up */
+  WAVI_ERR_NO_DEVICE = -7,         /* no usable CUDA device / extension not built for it */
+  WAVI_ERR_ALLOC = -8              /* device or pinned allocation failed */
+} wavi_status;
+
+/* Precision modes of a context. */
+typedef enum wavi_precision {
+  WAVI_PRECISION_FP64 = 0,         /* the reference algorithm in float64 throughout (parity mode) */
+  WAVI_PRECISION_MIXED = 1         /* float32 operator, viscosity and V-cycle; float64 Picard residual,
+                                      convergence test, CG scalars / coarse iterate and dot products */
+} wavi_precision;
+
+/* Grid geometry and the masks that fix the problem's sparsity (src/Grid.jl:1-27, :66-201;
+ * masks derived as in src/Fields/Fields.jl:26-35). */
+typedef struct wavi_grid_desc {
+  int32_t nx, ny, nsigma;
+  int32_t reserved0;
+  double dx, dy;
+  const double* sigma;               /* nsigma, sigma[0] = 0, sigma[nsigma-1] = 1 */
+  const double* quadrature_weights;  /* nsigma */
+  const uint8_t* h_mask;             /* nx*ny */
+  const uint8_t* u_iszero;           /* (nx+1)*ny */
+  const uint8_t* v_iszero;           /* nx*(ny+1) */
+  const uint8_t* u_isfixed;          /* (nx+1)*ny */
+  const uint8_t* v_isfixed;          /* nx*(ny+1) */
+} wavi_grid_desc;
+
+/* Scalar physical parameters (src/Params.jl:1-25, defaults :59-110).  Array-valued members of the
+ * reference's Params (accumulation_rate, glen_a_ref, weertman_c) travel as per-cell fields. */
+typedef struct wavi_params {
+  double dt, g, density_ice, density_ocean, gas_const;
+  double glen_a_activation_energy, glen_temperature_ref, glen_n, glen_reg_strain_rate;
+  double weertman_m, weertman_reg_speed, sea_level_wrt_geoid, minimum_thickness, small_haf;
+  int32_t evolve_shelves;
+  int32_t reserved0;
+} wavi_params;
+
+/* Solver parameters (src/SolverParams.jl:2-13). */
+typedef struct wavi_solver_params {
+  int32_t n_iter_viscosity;          /* the reference asserts == 2 */
+  int32_t maxiter_picard;
+  int32_t maxiter_coarse;
+  int32_t levels;                    /* Haar levels; the transform acts on blocks of 2^(levels+1) */
+  int32_t nsmooth;
+  int32_t stencil_margin;
+  double tol_picard, tol_coarse, wavelet_threshold, smoother_omega, super_implicitness;
+} wavi_solver_params;
+
+/* Options of a context (no counterpart in the reference: backend choices). */
+typedef struct wavi_options {
+  int32_t device;                    /* CUDA ordinal */
+  int32_t precision;                 /* wavi_precision */
+  int32_t use_graphs;                /* 1: capture each Picard iteration in a CUDA graph */
+  int32_t picard_test;               /* 0: reference residual test ||b-Au||/||b|| < tol_picard;
+                                        1: additionally require ||du||/||u|| <= tol_picard */
+} wavi_options;
+
+/* The model fields the velocity solve reads and writes (src/Models/update_velocities.jl:202-383,
+ * src/Fields/HGrid.jl:1-38, UGrid.jl:1-29, VGrid.jl:1-29, SigmaGrid.jl, Wavelets/UWavelets.jl:2-15).
+ * Pointers are host pointers for wavi_solve_velocities() and device pointers for
+ * wavi_solve_velocities_device(). */
+typedef struct wavi_fields {
+  /* inputs, h grid */
+  const double* h;                   /* gh.h */
+  const double* s;                   /* gh.s */
+  const double* dsdh;                /* gh.dsdh */
+  const double* grounded_fraction;   /* gh.grounded_fraction */
+  const double* weertman_c;          /* gh.weertman_c (= C * grounded fraction, update_state.jl:129-134) */
+  const double* accumulation;        /* gh.accumulation */
+  const double* basal_melt;          /* gh.basal_melt */
+  /* inputs, u and v grids */
+  const double* gu_h; const double* gu_s; const double* gu_grounded_fraction;
+  const double* gv_h; const double* gv_s; const double* gv_grounded_fraction;
+  /* input, 3-D */
+  const double* glen_b;              /* g3d.glen_b, nx*ny*nsigma */
+  /* Picard state, read and written */
+  double* u;                         /* gu.u */
+  double* v;                         /* gv.v */
+  double* eta;                       /* g3d.η, nx*ny*nsigma */
+  double* beta;                      /* gh.β */
+  double* quad_f2;                   /* gh.quad_f2 */
+  /* adaptive coarse space (wu.mask, wv.mask) and its cached coarse correction, compact in mask order */
+  const uint8_t* wu_mask;            /* (nx+1)*ny */
+  const uint8_t* wv_mask;            /* nx*(ny+1) */
+  double* wu_correction_coarse;      /* count(wu_mask) */
+  double* wv_correction_coarse;      /* count(wv_mask) */
+  /* outputs (written where the reference writes them) */
+  double* shelf_strain_rate; double* av_speed; double* bed_speed; double* tau_bed;
+  double* eta_av; double* quad_f1; double* beta_eff;
+  double* gu_beta_eff; double* gv_beta_eff;
+  double* gu_residual; double* gv_residual;
+} wavi_fields;
+
+/* Per-solve statistics (the reference prints the residual and Picard count, update_velocities.jl:25). */
+typedef struct wavi_stats {
+  int32_t status;
+  int32_t picard_iterations;
+  int32_t coarse_cg_iterations;      /* summed over the solve's V-cycles */
+  int32_t op_applications;           /* fine-operator applications, all precisions */
+  double rel_residual;               /* last ||b - A u|| / ||b|| (float64) */
+  double rel_update;                 /* last ||du|| / ||u|| */
+  double algorithmic_bytes;          /* sum over launches of each kernel's algorithmic bytes */
+  double elapsed_ms;                 /* device time of the solve (CUDA events) */
+  int32_t kernel_launches;           /* kernels this library launched during the solve */
+  int32_t host_syncs;                /* host round trips (convergence tests, CG batches) */
+} wavi_stats;
+
+typedef struct wavi_ctx wavi_ctx;
+
+/* ABI version compiled into the library (== WAVI_ABI_VERSION of its header). */
+int wavi_abi_version(void);
+
+/* sizeof of wavi_grid_desc, wavi_params, wavi_solver_params, wavi_options, wavi_fields, wavi_stats as
+ * compiled into the library, written to out[0..min(n,6)); returns 6.  Lets a binding (Julia struct,
+ * ctypes) check its layout without a GPU.  No counterpart in the reference (a binding check). */
+int wavi_abi_struct_sizes(int32_t* out, int n);
+
+/* Number of CUDA devices, or a negative wavi_status. */
+int wavi_device_count(void);
+
+/* Create a context for one grid: validates the masks, derives the u/v/c masks
+ * (src/Fields/Fields.jl:28-35, utilities.jl:475-507) and allocates every device buffer once. */
+int wavi_ctx_create(const wavi_grid_desc* grid, const wavi_solver_params* solver,
+                    const wavi_options* options, wavi_ctx** out);
+
+/* The cudaStream_t (as void*) on which the context launches everything, so a caller can order its own
+ * work or CUDA events against the solve.  No counterpart in the reference (a backend detail). */
+void* wavi_ctx_stream(const wavi_ctx* ctx);
+
+/* Release a context and its device memory.  Null is accepted. */
+int wavi_ctx_destroy(wavi_ctx* ctx);
+
+/* Message of the last failing call on this context (or of the last failing wavi_ctx_create when
+ * ctx is null).  The string stays valid until the next call on the same context. */
+const char* wavi_last_error(const wavi_ctx* ctx);
+
+/* One velocity solve with host buffers: copies the inputs and Picard state to the device, runs
+ * update_velocities! (update_velocities.jl:11-29) and copies the state and outputs back.
+ * Replaces update_velocities.jl:11-29 as called from update_state.jl:154-157. */
+int wavi_solve_velocities(wavi_ctx* ctx, const wavi_params* params, wavi_fields* fields,
+                          wavi_stats* stats);
+
+/* The same solve on device-resident buffers (every pointer in fields is a device pointer on the
+ * context's device).  Runs on the context's stream and synchronises it before returning. */
+int wavi_solve_velocities_device(wavi_ctx* ctx, const wavi_params* params, wavi_fields* fields,
+                                 wavi_stats* stats);
+
+/* Run inner_update! (update_velocities.jl:32-45) once on device fields, leaving the operator
+ * coefficients in the context and writing the relinearised fields back.  Test and benchmark hook. */
+int wavi_relinearise_device(wavi_ctx* ctx, const wavi_params* params, wavi_fields* fields);
+
+/* One application of the momentum operator (op_fun!, utilities.jl:61-145, with vecSampled=false) with
+ * the coefficients of the last relinearisation.  in_uv / out_uv are device vectors [u (nx+1)*ny | v
+ * nx*(ny+1)] of float64 (precision WAVI_PRECISION_FP64) or float32 (WAVI_PRECISION_MIXED, mixed
+ * contexts only); out_uv is the operator sampled at the interior points and zero elsewhere.
+ * Test and benchmark hook. */
+int wavi_apply_operator_device(wavi_ctx* ctx, int precision, const void* in_uv, void* out_uv);
+
+/* Diagonal of the operator at the interior points (what get_op_diag probes, update_preconditioners.jl
+ * :92-109), same vector layout and precision rules as wavi_apply_operator_device.  Test hook. */
+int wavi_op_diagonal_device(wavi_ctx* ctx, int precision, void* diag_uv);
+
+/* Haar transforms on float64 device vectors of the [u | v] layout (update_wavelets.jl:38-89):
+ * kind 0 = mask ⊙ idwt(in) (prolongation, default mask = interior), kind 1 = mask ⊙ idwtᵀ(in)
+ * (restriction, default mask = the last uploaded wavelet mask), kind 2 = dwt(mask ⊙ in) (the forward
+ * transform of update_wavelets!, default mask = the u/v model masks).  mask_uv may be null.  Test hook. */
+int wavi_haar_device(wavi_ctx* ctx, int kind, const double* in_uv, double* out_uv, const uint8_t* mask_uv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WAVI_GPU_H */

@@ -1,0 +1,49 @@
+"""The C-ABI library builds, loads, exports every symbol include/*.h declares, and its structs match the
+ctypes mirror.  No compute call is made (this runs without a GPU)."""
+import ctypes as C
+import os
+import subprocess
+
+import pytest
+
+
+@pytest.fixture(scope="module")
+def lib(pkg):
+    from wavi_gb300 import abi, build
+    build.build_library()
+    return abi.load_library()
+
+
+def test_exports_every_header_symbol(lib, pkg):
+    from wavi_gb300 import abi
+    out = subprocess.run(["nm", "-D", "--defined-only", abi.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    declared = abi.header_symbols()
+    assert declared, "no declarations found"
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+
+
+def test_struct_layout_matches_header(lib, pkg):
+    from wavi_gb300 import abi
+    sizes = (C.c_int32 * 8)()
+    n = lib.wavi_abi_struct_sizes(sizes, 8)
+    names = ("wavi_grid_desc", "wavi_params", "wavi_solver_params", "wavi_options", "wavi_fields", "wavi_stats")
+    mirror = (abi.GridDesc, abi.Params, abi.SolverParams, abi.Options, abi.Fields, abi.Stats)
+    assert n == len(names)
+    for i, (nm, st) in enumerate(zip(names, mirror)):
+        assert sizes[i] == C.sizeof(st), nm
+
+
+def test_no_device_is_an_error_not_a_crash(lib, pkg):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from wavi_gb300 import abi, synthetic
+    g, bed, p, sp, ic = synthetic.small_case()
+    desc = g.descriptor()
+    ctx = C.c_void_p()
+    st = lib.wavi_ctx_create(C.byref(desc.desc), C.byref(sp.to_c()), C.byref(abi.Options(0, 0, 0, 0)), C.byref(ctx))
+    assert st in (-7, -2)
+    assert lib.wavi_last_error(None)
+    assert lib.wavi_ctx_destroy(None) == 0

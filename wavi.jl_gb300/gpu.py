@@ -1,0 +1,154 @@
+"""Python binding of libwavi_gpu.so's velocity solve (include/wavi_gpu.h).
+
+``VelocitySolver`` owns one wavi_ctx (one CUDA stream, all device buffers) for one grid.  ``solve``
+takes host numpy arrays (the e2e path: copies in and out inside the call); ``solve_device`` takes
+device tensors (anything with ``data_ptr()``), the path used when the fields already live in HBM.
+
+Field names are those of ``wavi_fields``; arrays are float64, Fortran order, reference shapes.
+There is no CPU fallback: construction raises if the library or a GPU is missing.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+PRECISIONS = {"fp64": abi.PRECISION_FP64, "mixed": abi.PRECISION_MIXED}
+
+
+def _shape_of(name, nx, ny, ns):
+    if name in ("u", "gu_h", "gu_s", "gu_grounded_fraction", "gu_beta_eff", "gu_residual", "wu_mask"):
+        return (nx + 1, ny)
+    if name in ("v", "gv_h", "gv_s", "gv_grounded_fraction", "gv_beta_eff", "gv_residual", "wv_mask"):
+        return (nx, ny + 1)
+    if name in ("glen_b", "eta"):
+        return (nx, ny, ns)
+    if name in ("wu_correction_coarse", "wv_correction_coarse"):
+        return None
+    return (nx, ny)
+
+
+ALL_FIELDS = abi.FIELD_INPUTS + abi.FIELD_STATE + ("wu_mask", "wv_mask", "wu_correction_coarse",
+                                                   "wv_correction_coarse") + abi.FIELD_OUTPUTS
+
+
+class VelocitySolver:
+    """One GPU velocity-solve context (``wavi_ctx``) for a fixed grid and solver parameters."""
+
+    def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=False, picard_test=0):
+        self.lib = abi.load_library()
+        self.grid = grid
+        self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ
+        self.solver_params = solver_params
+        self.precision = precision
+        self._desc = grid.descriptor()
+        self._sp = solver_params.to_c()
+        self._opt = abi.Options(int(device), PRECISIONS[precision], 1 if use_graphs else 0, int(picard_test))
+        ctx = C.c_void_p()
+        st = self.lib.wavi_ctx_create(C.byref(self._desc.desc), C.byref(self._sp), C.byref(self._opt), C.byref(ctx))
+        if st != 0:
+            raise abi.WaviError(st, self.lib.wavi_last_error(None).decode())
+        self.ctx = ctx
+
+    def close(self):
+        if getattr(self, "ctx", None) and self.ctx.value:
+            self.lib.wavi_ctx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    __del__ = close
+
+    def stream(self):
+        """The context's cudaStream_t as an integer handle (for torch.cuda.ExternalStream)."""
+        return self.lib.wavi_ctx_stream(self.ctx) or 0
+
+    def _err(self, st):
+        return abi.WaviError(st, self.lib.wavi_last_error(self.ctx).decode())
+
+    # -- host arrays -------------------------------------------------------------------------------
+    def _host_fields(self, fields):
+        f = abi.Fields()
+        keep = []
+        for name in ALL_FIELDS:
+            a = fields[name]
+            shp = _shape_of(name, self.nx, self.ny, self.ns)
+            if name in ("wu_mask", "wv_mask"):
+                if a.dtype != np.uint8 and a.dtype != np.bool_:
+                    raise TypeError(f"{name} must be bool/uint8")
+                arr = np.asfortranarray(a).view(np.uint8) if a.dtype == np.bool_ else np.asfortranarray(a)
+                ptr = arr.ctypes.data_as(C.POINTER(C.c_uint8))
+            else:
+                if a.dtype != np.float64:
+                    raise TypeError(f"{name} must be float64")
+                if shp is not None and a.shape != shp:
+                    raise ValueError(f"{name}: shape {a.shape} != {shp}")
+                if not a.flags.f_contiguous:
+                    raise ValueError(f"{name} must be Fortran-contiguous (it is written in place)")
+                arr = a
+                ptr = arr.ctypes.data_as(C.POINTER(C.c_double))
+            keep.append(arr)
+            setattr(f, name, ptr)
+        n_wu, n_wv = int(np.count_nonzero(fields["wu_mask"])), int(np.count_nonzero(fields["wv_mask"]))
+        if fields["wu_correction_coarse"].size != n_wu or fields["wv_correction_coarse"].size != n_wv:
+            raise ValueError("coarse corrections must have count(wavelet mask) entries")
+        return f, keep
+
+    def solve(self, params, fields):
+        """update_velocities! on host arrays (modified in place).  Returns the stats dict."""
+        f, keep = self._host_fields(fields)
+        stats = abi.Stats()
+        st = self.lib.wavi_solve_velocities(self.ctx, C.byref(params.to_c()), C.byref(f), C.byref(stats))
+        if st != 0:
+            raise self._err(st)
+        return stats_dict(stats)
+
+    # -- device tensors ----------------------------------------------------------------------------
+    def _device_fields(self, tensors):
+        f = abi.Fields()
+        for name in ALL_FIELDS:
+            t = tensors[name]
+            ptr = t.data_ptr()
+            if name in ("wu_mask", "wv_mask"):
+                setattr(f, name, C.cast(C.c_void_p(ptr), C.POINTER(C.c_uint8)))
+            else:
+                setattr(f, name, C.cast(C.c_void_p(ptr), C.POINTER(C.c_double)))
+        return f
+
+    def solve_device(self, params, tensors):
+        """update_velocities! on device tensors (dict of name -> tensor with data_ptr()), in place."""
+        f = self._device_fields(tensors)
+        stats = abi.Stats()
+        st = self.lib.wavi_solve_velocities_device(self.ctx, C.byref(params.to_c()), C.byref(f), C.byref(stats))
+        if st != 0:
+            raise self._err(st)
+        return stats_dict(stats)
+
+    def relinearise_device(self, params, tensors):
+        f = self._device_fields(tensors)
+        st = self.lib.wavi_relinearise_device(self.ctx, C.byref(params.to_c()), C.byref(f))
+        if st != 0:
+            raise self._err(st)
+
+    def apply_operator_device(self, in_uv, out_uv, precision="fp64"):
+        st = self.lib.wavi_apply_operator_device(self.ctx, PRECISIONS[precision], C.c_void_p(in_uv.data_ptr()),
+                                                 C.c_void_p(out_uv.data_ptr()))
+        if st != 0:
+            raise self._err(st)
+
+    def op_diagonal_device(self, out_uv, precision="fp64"):
+        st = self.lib.wavi_op_diagonal_device(self.ctx, PRECISIONS[precision], C.c_void_p(out_uv.data_ptr()))
+        if st != 0:
+            raise self._err(st)
+
+    def haar_device(self, kind, in_uv, out_uv, mask_uv=None):
+        m = C.c_void_p(mask_uv.data_ptr()) if mask_uv is not None else None
+        st = self.lib.wavi_haar_device(self.ctx, int(kind), C.c_void_p(in_uv.data_ptr()), C.c_void_p(out_uv.data_ptr()), m)
+        if st != 0:
+            raise self._err(st)
+
+
+def stats_dict(s):
+    return {"status": s.status, "status_name": abi.STATUS.get(s.status, str(s.status)),
+            "picard_iterations": s.picard_iterations, "coarse_cg_iterations": s.coarse_cg_iterations,
+            "op_applications": s.op_applications, "rel_residual": s.rel_residual, "rel_update": s.rel_update,
+            "algorithmic_bytes": s.algorithmic_bytes, "elapsed_ms": s.elapsed_ms,
+            "kernel_launches": s.kernel_launches, "host_syncs": s.host_syncs}

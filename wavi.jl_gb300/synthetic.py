@@ -1,0 +1,129 @@
+"""Seeded synthetic inputs for the benchmark and parity workloads.
+
+There is no external benchmark data for this path: the synthetic channel follows the MISMIP+ geometry
+the reference ships (``mismip_plus_bed``, src/utilities.jl:401-409, used by test_version_updates.jl and
+example_drivers/MISMIP_PLUS) with seeded roughness, thickness noise, and, for the large domain, a
+log-normal drag field and a vertical temperature profile.
+
+  channel_c1   80 x 10 at 8 km, nσ = 4                (time-stepping case)
+  channel_c2   640 x 80 at 1 km, nσ = 4               (single converged solve; the benchmark workload)
+  channel_c3   2560 x 320 at 250 m, nσ = 8            (large single domain)
+  ensemble     ragged members, dx = dy = 2 km, nσ = 4
+"""
+import numpy as np
+
+from .config import Grid, InitialConditions, Params, SolverParams
+
+
+def mismip_plus_bed(x, y):
+    """MISMIP+ bed elevation (src/utilities.jl:401-409), vectorised."""
+    xbar = 300000.0
+    b0, b2, b4, b6 = -150.0, -728.8, 343.91, -50.75
+    wc, fc, dc = 24000.0, 4000.0, 500.0
+    xs = x / xbar
+    bx = b0 + b2 * xs ** 2 + b4 * xs ** 4 + b6 * xs ** 6
+    by = dc * ((1 + np.exp(-2 * (y - wc) / fc)) ** (-1) + (1 + np.exp(2 * (y + wc) / fc)) ** (-1))
+    return np.maximum(bx + by, -720.0)
+
+
+def channel_bed(grid, seed=0, roughness=20.0, xscale=1.0, yscale=1.0):
+    """MISMIP+ channel on the grid's h points plus N(0, roughness) per cell, re-clipped at -720 m."""
+    rng = np.random.default_rng(seed)
+    b = mismip_plus_bed(grid.xxh * xscale, grid.yyh * yscale)
+    b = b + roughness * rng.standard_normal(b.shape)
+    return np.asfortranarray(np.maximum(b, -720.0))
+
+
+def noisy_thickness(shape, seed, mean=300.0, rel=0.05):
+    rng = np.random.default_rng(seed)
+    return np.asfortranarray(mean * (1.0 + rng.uniform(-rel, rel, size=shape)))
+
+
+def gaussian_filter_periodic(z, sigma_cells):
+    """Gaussian smoothing by FFT (periodic), renormalised to unit variance."""
+    nx, ny = z.shape
+    kx = np.fft.fftfreq(nx)[:, None]
+    ky = np.fft.fftfreq(ny)[None, :]
+    g = np.exp(-2.0 * (np.pi ** 2) * (sigma_cells ** 2) * (kx ** 2 + ky ** 2))
+    out = np.real(np.fft.ifft2(np.fft.fft2(z) * g))
+    out = (out - out.mean()) / out.std()
+    return out
+
+
+def _grid(nx, ny, dx, ns):
+    return Grid(nx=nx, ny=ny, nσ=ns, dx=dx, dy=dx, x0=0.0, y0=-40000.0 * (ny * dx) / 80000.0,
+                u_iszero=["north"], v_iszero=["west", "east"])
+
+
+def channel_case(nx, ny, dx, ns, seed_bed=0, seed_h=1, tol_picard=1e-5, maxiter_picard=30, C=1.0e4,
+                 temperature=None, accumulation=0.3):
+    """A channel configuration: (grid, bed, params, solver_params, initial_conditions).
+
+    Physics as the benchmark configurations state: Glen n = 3 with A = 2e-17 Pa^-3 yr^-1 (glen_a_ref at
+    the reference temperature), Weertman m = 3, C = 1e4 (or a per-cell field), accumulation 0.3 m/yr.
+    """
+    g = _grid(nx, ny, dx, ns)
+    bed = channel_bed(g, seed=seed_bed, xscale=(640000.0 / (nx * dx)), yscale=(80000.0 / (ny * dx)))
+    p = Params(accumulation_rate=accumulation, glen_a_ref=2.0e-17, weertman_c=C, default_temperature=263.15)
+    sp = SolverParams(tol_picard=tol_picard, maxiter_picard=maxiter_picard)
+    ic = InitialConditions(initial_thickness=noisy_thickness((nx, ny), seed_h),
+                           initial_temperature=temperature)
+    return g, bed, p, sp, ic
+
+
+def channel_c1(**kw):
+    return channel_case(80, 10, 8000.0, 4, **kw)
+
+
+def channel_c2(**kw):
+    return channel_case(640, 80, 1000.0, 4, **kw)
+
+
+def channel_c3(**kw):
+    """2560 x 320 at 250 m, nσ = 8; log-normal C (median 1e4, σ_log 0.5, 20 km correlation, seed 3);
+    temperature linear in σ from 268 K at the bed to 243 K at the surface."""
+    nx, ny, dx, ns = 2560, 320, 250.0, 8
+    rng = np.random.default_rng(3)
+    z = gaussian_filter_periodic(rng.standard_normal((nx, ny)), 20000.0 / dx)
+    C = np.asfortranarray(np.exp(np.log(1.0e4) + 0.5 * z))
+    sigma = np.linspace(0.0, 1.0, ns)
+    T = 243.0 + (268.0 - 243.0) * (1.0 - sigma)  # σ = 0 at the bed (ζ = 1), σ = 1 at the surface
+    temp = np.asfortranarray(np.broadcast_to(T[None, None, :], (nx, ny, ns)).copy())
+    return channel_case(nx, ny, dx, ns, C=C, temperature=temp, **kw)
+
+
+def small_case(nx=24, ny=12, dx=4000.0, ns=4, seed=0, mask="full", fixed=False, **kw):
+    """Small ragged test cases: masks 'full', 'disc' (a circular ice mask, calving fronts on all sides),
+    optional Dirichlet lines (u_isfixed / v_isfixed) as in the reference's iceberg test."""
+    rng = np.random.default_rng(seed)
+    x0, y0 = 0.0, -0.5 * ny * dx
+    h_mask = None
+    if mask == "disc":
+        xc, yc = 0.5 * nx * dx, 0.0
+        xx = x0 + (np.arange(nx)[:, None] + 0.5) * dx
+        yy = y0 + (np.arange(ny)[None, :] + 0.5) * dx
+        h_mask = np.sqrt((xx - xc) ** 2 + (yy - yc) ** 2) < 0.45 * min(nx, ny) * dx
+    u_isfixed = v_isfixed = None
+    if fixed:
+        u_isfixed = np.zeros((nx + 1, ny), bool)
+        u_isfixed[nx // 2, :] = True
+        v_isfixed = np.zeros((nx, ny + 1), bool)
+        v_isfixed[:, ny // 2] = True
+    g = Grid(nx=nx, ny=ny, nσ=ns, dx=dx, dy=dx, x0=x0, y0=y0, h_mask=h_mask,
+             u_iszero=None if mask == "disc" else ["north"], v_iszero=None if mask == "disc" else ["west", "east"],
+             u_isfixed=u_isfixed, v_isfixed=v_isfixed)
+    bed = np.asfortranarray(mismip_plus_bed(g.xxh * (640000.0 / (nx * dx)), g.yyh * (80000.0 / (ny * dx)))
+                            + 20.0 * rng.standard_normal((nx, ny)))
+    h = np.asfortranarray(300.0 * (1.0 + rng.uniform(-0.05, 0.05, (nx, ny))))
+    if h_mask is not None:
+        h[~h_mask] = 0.0
+    u0 = v0 = None
+    if fixed:
+        u0 = np.zeros((nx + 1, ny), order="F")
+        u0[u_isfixed] = 5.0 - 6e-4 * g.yyu[u_isfixed] * 1e-3
+        v0 = np.zeros((nx, ny + 1), order="F")
+        v0[v_isfixed] = 3.0 + 6e-4 * g.xxv[v_isfixed] * 1e-3
+    p = Params(accumulation_rate=0.3, glen_a_ref=2.0e-17, default_temperature=263.15)
+    sp = SolverParams(**kw)
+    ic = InitialConditions(initial_thickness=h, initial_u_veloc=u0, initial_v_veloc=v0)
+    return g, bed, p, sp, ic
