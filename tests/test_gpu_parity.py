@@ -108,15 +108,16 @@ def test_haar_transforms_match_oracle(oracle, name):
     s.close()
 
 
+@pytest.mark.parametrize("graphs", [True, False])
 @pytest.mark.parametrize("name", list(CASES))
-def test_one_vcycle_fixed_cg_count_matches_oracle(oracle, name):
+def test_one_vcycle_fixed_cg_count_matches_oracle(oracle, name, graphs):
     """One Picard iteration whose coarse CG runs exactly 25 iterations (tol_coarse = 0): relinearisation,
     float64 residual, 2 x 20 smoother sweeps, restriction, CG, prolongation, bit-for-bit the same algorithm
     as the oracle, so the velocities agree to rounding."""
     from wavi_gb300.gpu import VelocitySolver
     g, p, sp, om = _setup(oracle, name, maxiter_picard=1, maxiter_coarse=25, tol_coarse=0.0)
     f = fields_from_oracle(om, g)
-    s = VelocitySolver(g, sp, precision="fp64")
+    s = VelocitySolver(g, sp, precision="fp64", use_graphs=graphs)
     st = s.solve(p, f)
     om.update_velocities()
     ost = om.stats()
@@ -149,12 +150,13 @@ def test_one_picard_iteration_matches_oracle(oracle, name):
     s.close()
 
 
+@pytest.mark.parametrize("graphs", [True, False])
 @pytest.mark.parametrize("name", list(CASES))
-def test_converged_solve_matches_oracle(oracle, name):
+def test_converged_solve_matches_oracle(oracle, name, graphs):
     from wavi_gb300.gpu import VelocitySolver
     g, p, sp, om = _setup(oracle, name, maxiter_picard=30, tol_picard=1e-6)
     f = fields_from_oracle(om, g)
-    s = VelocitySolver(g, sp, precision="fp64")
+    s = VelocitySolver(g, sp, precision="fp64", use_graphs=graphs)
     st = s.solve(p, f)
     om.update_velocities()
     ost = om.stats()

@@ -1,0 +1,648 @@
+// fused.cuh — the fused, graph-resident kernels of the velocity solve.
+//
+// Every kernel here is launched inside one CUDA graph per solve (Picard WHILE node -> V-cycle IF node ->
+// coarse-CG WHILE node).  Kernels that end a reduction use the last-block pattern: each block writes a
+// partial, the last block to arrive sums all partials in a fixed order (deterministic) and publishes
+// the scalar, and, where the scalar decides control flow, sets the enclosing conditional node.
+//
+// The operator is evaluated on shared-memory tiles: stage 1 loads the velocity region
+// [i0-1, i0+TX] x [j0-1, j0+TY] (optionally transformed, e.g. by a Jacobi colour update), stage 2 the
+// h-cell / c-point stresses of [i0-1, i0+TX) x [j0-1, j0+TY), stage 3 the divergences at the tile's
+// own points.  A TILE x TILE tile with TILE a multiple of the Haar block 2^(levels+1) also holds whole
+// Haar blocks of both velocity components, so the coarse-grid restriction follows in shared memory.
+#pragma once
+#include "kernels.cuh"
+
+namespace wavi {
+
+// Device-side solver state: scalars, counters and the flags that steer the conditional nodes.
+struct DevState {
+  double rr, bb, rel, rel_prev_update;   // Picard residual norms
+  double du2, uu2, rel_update;
+  double cg_res, cg_prev, cg_tol, cg_alpha, cg_bnorm;
+  int picard_it, picard_continue, vcycle_needed, converged;
+  int cg_it, cg_continue, cg_total, status;
+  unsigned counter[8];                   // last-block counters, one per reduction site
+};
+enum { CNT_A = 0, CNT_B = 1, CNT_C = 2, CNT_D = 3 };
+
+struct CondHandles {
+  cudaGraphConditionalHandle picard, vcycle, cg;
+  int active;  // 0: launched outside a graph, do not touch the handles
+};
+
+__device__ __forceinline__ int flat_tid() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
+__device__ __forceinline__ int flat_nthreads() { return blockDim.x * blockDim.y * blockDim.z; }
+__device__ __forceinline__ int flat_bid() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+__device__ __forceinline__ int flat_nblocks() { return gridDim.x * gridDim.y * gridDim.z; }
+
+__device__ __forceinline__ double block_sum_any(double v, double* sh) {
+  const int t = flat_tid(), nt = flat_nthreads();
+  const int lane = t & 31, wid = t >> 5, nw = (nt + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = lane < nw ? sh[lane] : 0.0;
+    r = warp_sum(r);
+  }
+  return r;  // valid in thread 0
+}
+
+// Each block contributes (v0, v1); the last block to finish receives the two totals, summed over all
+// blocks' partials in block order, in tot[0..1] (valid for every thread of that block) and returns
+// true.  Other blocks return false.  Uses partials[0 .. 2*nblocks).
+__device__ __forceinline__ bool last_block_sum2(double v0, double v1, double* __restrict__ partials,
+                                                unsigned* counter, double tot[2]) {
+  __shared__ double sh[32];
+  __shared__ double stot[2];
+  __shared__ int slast;
+  const int t = flat_tid(), nb = flat_nblocks(), b = flat_bid();
+  double s0 = block_sum_any(v0, sh);
+  __syncthreads();
+  double s1 = block_sum_any(v1, sh);
+  if (t == 0) {
+    partials[b] = s0;
+    partials[nb + b] = s1;
+    __threadfence();
+    const unsigned prev = atomicAdd(counter, 1u);
+    slast = (prev == (unsigned)nb - 1u);
+  }
+  __syncthreads();
+  if (!slast) return false;
+  __threadfence();
+  double a0 = 0.0, a1 = 0.0;
+  for (int k = t; k < nb; k += flat_nthreads()) {
+    a0 += __ldcg(partials + k);
+    a1 += __ldcg(partials + nb + k);
+  }
+  a0 = block_sum_any(a0, sh);
+  __syncthreads();
+  a1 = block_sum_any(a1, sh);
+  if (t == 0) {
+    stot[0] = a0;
+    stot[1] = a1;
+    *counter = 0u;
+  }
+  __syncthreads();
+  tot[0] = stot[0];
+  tot[1] = stot[1];
+  return true;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Staged operator tile
+// ------------------------------------------------------------------------------------------------
+template <typename T, int TX, int TY>
+struct OpTile {
+  T xu[TY + 2][TX + 2];
+  T xv[TY + 2][TX + 2];
+  T rxx[TY + 1][TX + 1];
+  T ryy[TY + 1][TX + 1];
+  T e[TY + 1][TX + 1];
+  T rxy[TY + 1][TX + 1];
+};
+
+// Stage 1: x region; f(q) gives the (transformed) value of solver-vector entry q.
+template <typename T, int TX, int TY, typename F>
+__device__ __forceinline__ void stage_x(const Dims& d, int i0, int j0, OpTile<T, TX, TY>& s, F&& f) {
+  for (int p = flat_tid(); p < (TX + 2) * (TY + 2); p += flat_nthreads()) {
+    const int li = p % (TX + 2), lj = p / (TX + 2);
+    const int i = i0 - 1 + li, j = j0 - 1 + lj;
+    s.xu[lj][li] = (i >= 0 && i <= d.nx && j >= 0 && j < d.ny) ? f(uidx(d, i, j)) : (T)0;
+    s.xv[lj][li] = (i >= 0 && i < d.nx && j >= 0 && j <= d.ny) ? f(vidx(d, i, j)) : (T)0;
+  }
+}
+
+// Stage 2: stresses (see k_op for the formulas).
+template <typename T, int TX, int TY>
+__device__ __forceinline__ void stage_stress(const Dims& d, const OpCoef<T>& cf, int i0, int j0, OpTile<T, TX, TY>& s) {
+  const T rdx = (T)d.rdx, rdy = (T)d.rdy;
+  for (int p = flat_tid(); p < (TX + 1) * (TY + 1); p += flat_nthreads()) {
+    const int la = p % (TX + 1), lb = p / (TX + 1);
+    const int a = i0 - 1 + la, b = j0 - 1 + lb;
+    T rxx = 0, ryy = 0, e = 0, rxy = 0;
+    if (a >= 0 && a < d.nx && b >= 0 && b < d.ny) {
+      const int hc = hidx(d, a, b);
+      const T u0 = s.xu[lb][la], u1 = s.xu[lb][la + 1], v0 = s.xv[lb][la], v1 = s.xv[lb + 1][la];
+      const T ux = (u1 - u0) * rdx, vy = (v1 - v0) * rdy;
+      const T he2 = (T)2 * cf.heta_h[hc];
+      rxx = he2 * ((T)2 * ux + vy);
+      ryy = he2 * ((T)2 * vy + ux);
+      const T dm = cf.dimp[hc];
+      if (dm != (T)0) {
+        const T divq = (cf.h_m[uidx(d, a + 1, b)] * u1 - cf.h_m[uidx(d, a, b)] * u0) * rdx +
+                       (cf.h_m[vidx(d, a, b + 1)] * v1 - cf.h_m[vidx(d, a, b)] * v0) * rdy;
+        e = dm * divq;
+      }
+    }
+    if (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) {
+      const T hc = cf.heta_c[cidx(d, a, b)];
+      if (hc != (T)0) {
+        const T uy = (s.xu[lb + 1][la + 1] - s.xu[lb][la + 1]) * rdy;
+        const T vx = (s.xv[lb + 1][la + 1] - s.xv[lb + 1][la]) * rdx;
+        rxy = hc * (uy + vx);
+      }
+    }
+    s.rxx[lb][la] = rxx;
+    s.ryy[lb][la] = ryy;
+    s.e[lb][la] = e;
+    s.rxy[lb][la] = rxy;
+  }
+}
+
+// Stage 3: operator at the u point of local (li, lj) (1-based in the tile) / at the v point.
+template <typename T, int TX, int TY>
+__device__ __forceinline__ T stage_out_u(const Dims& d, const OpCoef<T>& cf, const OpTile<T, TX, TY>& s, int li, int lj, int q) {
+  const T rdx = (T)d.rdx, rdy = (T)d.rdy;
+  return (s.rxx[lj][li] - s.rxx[lj][li - 1]) * rdx + (s.rxy[lj][li - 1] - s.rxy[lj - 1][li - 1]) * rdy -
+         cf.beta_m[q] * s.xu[lj][li] - cf.h_m[q] * ((s.e[lj][li] - s.e[lj][li - 1]) * rdx);
+}
+template <typename T, int TX, int TY>
+__device__ __forceinline__ T stage_out_v(const Dims& d, const OpCoef<T>& cf, const OpTile<T, TX, TY>& s, int li, int lj, int q) {
+  const T rdx = (T)d.rdx, rdy = (T)d.rdy;
+  return (s.ryy[lj][li] - s.ryy[lj - 1][li]) * rdy + (s.rxy[lj - 1][li] - s.rxy[lj - 1][li - 1]) * rdx -
+         cf.beta_m[q] * s.xv[lj][li] - cf.h_m[q] * ((s.e[lj][li] - s.e[lj - 1][li]) * rdy);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Haar lifting on a TILE x TILE shared-memory tile (one thread per element), for the grid component
+// whose extent is (nxg, nyg) and whose tile origin is (bx0, by0).  KIND 0: idwt (M_B ... M_2 applied
+// coarse-first), KIND 1: idwtᵀ (M_2ᵀ first), KIND 2: dwt (F_2 first); along y, then x.
+// ------------------------------------------------------------------------------------------------
+template <int TILE, int KIND, typename TT>
+__device__ __forceinline__ void haar_tile(TT (*tile)[TILE + 1], int levels, int bx0, int by0, int nxg, int nyg) {
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int B = 1 << (levels + 1);
+  const bool inside = (bx0 + tx) < nxg && (by0 + ty) < nyg;
+  for (int dir = 0; dir < 2; ++dir) {
+    const int n = dir == 0 ? nyg : nxg;
+    const int base = dir == 0 ? by0 : bx0;
+    const int pos = dir == 0 ? ty : tx;
+    for (int lv = 0; lv <= levels; ++lv) {
+      const int st = (KIND == 0) ? (B >> lv) : (2 << lv);
+      const int half = st >> 1;
+      const TT a = tile[ty][tx];
+      TT nv = a;
+      const int r = pos % st;
+      if (inside && (r == 0 || r == half)) {
+        const int po = r == 0 ? pos : pos - half;
+        const int pe = po + half;
+        if (base + pe < n) {
+          const TT xo = dir == 0 ? tile[po][tx] : tile[ty][po];
+          const TT xe = dir == 0 ? tile[pe][tx] : tile[ty][pe];
+          const bool is_o = r == 0;
+          if (KIND == 0) nv = is_o ? xo - xe : xe + xo;
+          else if (KIND == 1) nv = is_o ? xo + xe : xe - xo;
+          else nv = is_o ? (TT)0.5 * (xo + xe) : (TT)0.5 * (xe - xo);
+        }
+      }
+      __syncthreads();
+      tile[ty][tx] = nv;
+      __syncthreads();
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Picard-level kernels
+// ------------------------------------------------------------------------------------------------
+// Right-hand side, start guess, Dirichlet values, and |b|^2 (last block -> st->bb).
+__global__ void k_rhs_fused(Dims d, RhsIn in, const DevParams* __restrict__ P, double* __restrict__ b,
+                            double* __restrict__ x, double* __restrict__ xfixed, double* __restrict__ partials,
+                            DevState* st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  const double rho_i = P->rho_i, rho_w = P->rho_w, g = P->g, sl = P->sea_level, tdt = P->theta_dt;
+  auto sadj = [&](int a, int c) -> double {
+    if (a < 0 || a >= d.nx || c < 0 || c >= d.ny) return 0.0;
+    const int q = hidx(d, a, c);
+    if (!in.h_mask[q]) return 0.0;
+    return in.s[q] + tdt * in.dsdh[q] * (in.acc[q] - in.melt[q]);
+  };
+  auto hmk = [&](int a, int c) -> double {
+    return (a >= 0 && a < d.nx && c >= 0 && c < d.ny && in.h_mask[hidx(d, a, c)]) ? 1.0 : 0.0;
+  };
+  double bb = 0.0;
+  auto point = [&](int q, int a0, int b0, int a1, int b1, double rd) {
+    double bv = 0.0;
+    if (in.inner[q]) {
+      const double ds = sadj(a1, b1) * rd - sadj(a0, b0) * rd;
+      const double dm = hmk(a1, b1) * rd - hmk(a0, b0) * rd;
+      const double hh = in.h_uv[q], ss = in.s_uv[q];
+      const double draft = fmax(hh - (ss - sl), 0.0);
+      const double f1 = (rho_i * g * hh) * ds;
+      const double f2 = dm * g * (0.5 * rho_i * (hh * hh) - 0.5 * rho_w * (draft * draft) - rho_i * hh * ss);
+      bv = f1 + f2;
+    }
+    b[q] = bv;
+    bb += bv * bv;
+    x[q] = in.inner[q] ? in.uv[q] : 0.0;
+    xfixed[q] = in.fixed[q] ? in.uv[q] : 0.0;
+  };
+  if (i <= d.nx && j < d.ny) point(uidx(d, i, j), i - 1, j, i, j, d.rdx);
+  if (i < d.nx && j <= d.ny) point(vidx(d, i, j), i, j - 1, i, j, d.rdy);
+  double tot[2];
+  if (last_block_sum2(bb, 0.0, partials, &st->counter[CNT_A], tot)) {
+    if (flat_tid() == 0) st->bb = tot[0];
+  }
+}
+
+// b -= A xfixed (the Dirichlet lift, get_rhs_dirichlet!, update_velocities.jl:406-421), recomputing |b|^2.
+template <int TX, int TY>
+__global__ void __launch_bounds__(TX* TY)
+    k_lift(Dims d, OpCoef<double> cf, const double* __restrict__ xfixed, double* __restrict__ b,
+           double* __restrict__ partials, DevState* st) {
+  __shared__ OpTile<double, TX, TY> s;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  stage_x(d, i0, j0, s, [&](int q) { return xfixed[q]; });
+  __syncthreads();
+  stage_stress(d, cf, i0, j0, s);
+  __syncthreads();
+  const int li = threadIdx.x + 1, lj = threadIdx.y + 1, i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  double bb = 0.0;
+  if (i <= d.nx && j < d.ny) {
+    const int q = uidx(d, i, j);
+    double v = b[q];
+    if (cf.inner[q]) v = v - stage_out_u(d, cf, s, li, lj, q);
+    b[q] = v;
+    bb += v * v;
+  }
+  if (i < d.nx && j <= d.ny) {
+    const int q = vidx(d, i, j);
+    double v = b[q];
+    if (cf.inner[q]) v = v - stage_out_v(d, cf, s, li, lj, q);
+    b[q] = v;
+    bb += v * v;
+  }
+  double tot[2];
+  if (last_block_sum2(bb, 0.0, partials, &st->counter[CNT_B], tot)) {
+    if (flat_tid() == 0) st->bb = tot[0];
+  }
+}
+
+// r = b - A x (float64), |r|^2; the last block takes the Picard decision (update_velocities.jl:20, :59-65)
+// and sets the Picard WHILE and V-cycle IF conditions.
+template <int TX, int TY>
+__global__ void __launch_bounds__(TX* TY)
+    k_picard_residual(Dims d, OpCoef<double> cf, const double* __restrict__ x, const double* __restrict__ b,
+                      double* __restrict__ r, double* __restrict__ resid_out, double* __restrict__ partials,
+                      DevState* st, const DevParams* __restrict__ P, CondHandles h) {
+  __shared__ OpTile<double, TX, TY> s;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  stage_x(d, i0, j0, s, [&](int q) { return x[q]; });
+  __syncthreads();
+  stage_stress(d, cf, i0, j0, s);
+  __syncthreads();
+  const int li = threadIdx.x + 1, lj = threadIdx.y + 1, i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  double rr = 0.0;
+  if (i <= d.nx && j < d.ny) {
+    const int q = uidx(d, i, j);
+    double v = 0.0;
+    if (cf.inner[q]) {
+      v = b[q] - stage_out_u(d, cf, s, li, lj, q);
+      resid_out[q] = v;
+    }
+    r[q] = v;
+    rr += v * v;
+  }
+  if (i < d.nx && j <= d.ny) {
+    const int q = vidx(d, i, j);
+    double v = 0.0;
+    if (cf.inner[q]) {
+      v = b[q] - stage_out_v(d, cf, s, li, lj, q);
+      resid_out[q] = v;
+    }
+    r[q] = v;
+    rr += v * v;
+  }
+  double tot[2];
+  if (last_block_sum2(rr, 0.0, partials, &st->counter[CNT_C], tot)) {
+    if (flat_tid() == 0) {
+      st->rr = tot[0];
+      const double rel = sqrt(tot[0]) / sqrt(st->bb);
+      st->rel = rel;
+      const int it = st->picard_it + 1;
+      st->picard_it = it;
+      bool conv = rel < P->tol_picard;
+      if (conv && P->picard_test == 1 && it > 1 && !(st->rel_update <= P->tol_picard)) conv = false;
+      if (!(rel == rel)) {
+        st->status = WAVI_ERR_NONFINITE;
+        conv = true;  // stop: nothing sensible can follow a non-finite residual
+      }
+      st->converged = conv ? 1 : 0;
+      st->vcycle_needed = conv ? 0 : 1;
+      st->picard_continue = (!conv && it < P->maxiter_picard) ? 1 : 0;
+      if (h.active) {
+        cudaGraphSetConditional(h.vcycle, st->vcycle_needed);
+        cudaGraphSetConditional(h.picard, st->picard_continue);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// V-cycle kernels
+// ------------------------------------------------------------------------------------------------
+// V-cycle start: rs = (T) r, rsm = rs, corr = 0, xc = (T) xc64, diag = op diagonal (closed form).
+template <typename T>
+__global__ void k_vcycle_init(Dims d, OpCoef<T> cf, const double* __restrict__ r64, const double* __restrict__ xc64,
+                              T* __restrict__ rs, T* __restrict__ rsm, T* __restrict__ corr, T* __restrict__ xc,
+                              T* __restrict__ diag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  const T rdx = (T)d.rdx, rdy = (T)d.rdy, rdx2 = rdx * rdx, rdy2 = rdy * rdy;
+  auto heh = [&](int a, int b) -> T { return (a >= 0 && a < d.nx && b >= 0 && b < d.ny) ? cf.heta_h[hidx(d, a, b)] : (T)0; };
+  auto dim = [&](int a, int b) -> T { return (a >= 0 && a < d.nx && b >= 0 && b < d.ny) ? cf.dimp[hidx(d, a, b)] : (T)0; };
+  auto hec = [&](int a, int b) -> T {
+    return (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) ? cf.heta_c[cidx(d, a, b)] : (T)0;
+  };
+  if (i <= d.nx && j < d.ny) {
+    const int q = uidx(d, i, j);
+    const T rv = (T)r64[q];
+    rs[q] = rv;
+    rsm[q] = rv;
+    corr[q] = (T)0;
+    xc[q] = (T)xc64[q];
+    T v = 0;
+    if (cf.inner[q]) {
+      const T hu = cf.h_m[q];
+      v = -(T)4 * rdx2 * (heh(i, j) + heh(i - 1, j)) - rdy2 * (hec(i - 1, j) + hec(i - 1, j - 1)) - cf.beta_m[q] +
+          hu * hu * rdx2 * (dim(i, j) + dim(i - 1, j));
+    }
+    diag[q] = v;
+  }
+  if (i < d.nx && j <= d.ny) {
+    const int q = vidx(d, i, j);
+    const T rv = (T)r64[q];
+    rs[q] = rv;
+    rsm[q] = rv;
+    corr[q] = (T)0;
+    xc[q] = (T)xc64[q];
+    T v = 0;
+    if (cf.inner[q]) {
+      const T hv = cf.h_m[q];
+      v = -(T)4 * rdy2 * (heh(i, j) + heh(i, j - 1)) - rdx2 * (hec(i, j - 1) + hec(i - 1, j - 1)) - cf.beta_m[q] +
+          hv * hv * rdy2 * (dim(i, j) + dim(i, j - 1));
+    }
+    diag[q] = v;
+  }
+}
+
+// One smoother sweep (gauss_seidel_smoother!, update_preconditioners.jl:133-150), fused: the Jacobi
+// update of colour `colour` (x += ω r / diag, recomputed for the tile and its halo from the previous
+// x and r) followed by the full residual r = b - A x on the tile.  Ping-pong buffers: reads (x_in,
+// r_in), writes (x_out, r_out).  UPDATE = false computes only r_out = b - A x_in.
+template <typename T, int TX, int TY, bool UPDATE>
+__global__ void __launch_bounds__(TX* TY)
+    k_smooth(Dims d, OpCoef<T> cf, int colour, const DevParams* __restrict__ P, const T* __restrict__ b,
+             const T* __restrict__ diag, const T* __restrict__ x_in, const T* __restrict__ r_in,
+             T* __restrict__ x_out, T* __restrict__ r_out) {
+  __shared__ OpTile<T, TX, TY> s;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const T omega = (T)P->omega;
+  const int Nu = d.Nu, nxu = d.nx + 1, nxv = d.nx;
+  stage_x(d, i0, j0, s, [&](int q) -> T {
+    T v = x_in[q];
+    if (UPDATE && cf.inner[q]) {
+      int i, j, base;
+      if (q < Nu) { i = q % nxu; j = q / nxu; base = 1; }
+      else { i = (q - Nu) % nxv; j = (q - Nu) / nxv; base = 3; }
+      const int par = ((i - j) % 2 + 2) % 2;
+      if (base + par == colour) v = v + omega * r_in[q] / diag[q];
+    }
+    return v;
+  });
+  __syncthreads();
+  stage_stress(d, cf, i0, j0, s);
+  __syncthreads();
+  const int li = threadIdx.x + 1, lj = threadIdx.y + 1, i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  if (i <= d.nx && j < d.ny) {
+    const int q = uidx(d, i, j);
+    T f = 0;
+    if (cf.inner[q]) f = b[q] - stage_out_u(d, cf, s, li, lj, q);
+    r_out[q] = f;
+    if (UPDATE) x_out[q] = s.xu[lj][li];
+  }
+  if (i < d.nx && j <= d.ny) {
+    const int q = vidx(d, i, j);
+    T f = 0;
+    if (cf.inner[q]) f = b[q] - stage_out_v(d, cf, s, li, lj, q);
+    r_out[q] = f;
+    if (UPDATE) x_out[q] = s.xv[lj][li];
+  }
+}
+
+// Haar restriction of a fine vector (KIND 1, masked by the wavelet mask) with |out|^2; the last block
+// stores |b_c| = sqrt(total) for the coarse CG's absolute tolerance (update_preconditioners.jl:65-70).
+template <typename T, int TILE>
+__global__ void __launch_bounds__(TILE* TILE)
+    k_restrict_norm(Dims d, int levels, const T* __restrict__ in, const uint8_t* __restrict__ wmask, T* __restrict__ out,
+                    double* __restrict__ partials, DevState* st) {
+  __shared__ T tile[2][TILE][TILE + 1];
+  const int bx0 = blockIdx.x * TILE, by0 = blockIdx.y * TILE, tx = threadIdx.x, ty = threadIdx.y;
+  const int i = bx0 + tx, j = by0 + ty;
+  const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+  tile[0][ty][tx] = inu ? in[uidx(d, i, j)] : (T)0;
+  tile[1][ty][tx] = inv ? in[vidx(d, i, j)] : (T)0;
+  __syncthreads();
+  haar_tile<TILE, 1>(tile[0], levels, bx0, by0, d.nx + 1, d.ny);
+  haar_tile<TILE, 1>(tile[1], levels, bx0, by0, d.nx, d.ny + 1);
+  double s2 = 0.0;
+  if (inu) {
+    const int q = uidx(d, i, j);
+    const T o = wmask[q] ? tile[0][ty][tx] : (T)0;
+    out[q] = o;
+    s2 += (double)o * (double)o;
+  }
+  if (inv) {
+    const int q = vidx(d, i, j);
+    const T o = wmask[q] ? tile[1][ty][tx] : (T)0;
+    out[q] = o;
+    s2 += (double)o * (double)o;
+  }
+  double tot[2];
+  if (last_block_sum2(s2, 0.0, partials, &st->counter[CNT_A], tot)) {
+    if (flat_tid() == 0) st->cg_bnorm = sqrt(tot[0]);
+  }
+}
+
+// Prolongation (KIND 0, masked by the interior mask).  MODE 0: out = P in.  MODE 1: out += P in.
+// MODE 2 (CG direction): first u = r + β u on the tile (β = |r|^2/|r_prev|^2 from the state), written
+// back to `dir`, then out = P u.
+template <typename T, int TILE, int MODE>
+__global__ void __launch_bounds__(TILE* TILE)
+    k_prolong(Dims d, int levels, const uint8_t* __restrict__ inner, const T* __restrict__ in, T* __restrict__ out,
+              const T* __restrict__ rvec, T* __restrict__ dir, const DevState* __restrict__ st, const int* __restrict__ live) {
+  if (live && !*live) return;
+  __shared__ T tile[2][TILE][TILE + 1];
+  const int bx0 = blockIdx.x * TILE, by0 = blockIdx.y * TILE, tx = threadIdx.x, ty = threadIdx.y;
+  const int i = bx0 + tx, j = by0 + ty;
+  const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+  if (MODE == 2) {
+    const double res = st->cg_res, prev = st->cg_prev;
+    const double beta = (res * res) / (prev * prev);
+    if (inu) {
+      const int q = uidx(d, i, j);
+      const T u = (T)((double)rvec[q] + beta * (double)dir[q]);
+      dir[q] = u;
+      tile[0][ty][tx] = u;
+    } else {
+      tile[0][ty][tx] = (T)0;
+    }
+    if (inv) {
+      const int q = vidx(d, i, j);
+      const T u = (T)((double)rvec[q] + beta * (double)dir[q]);
+      dir[q] = u;
+      tile[1][ty][tx] = u;
+    } else {
+      tile[1][ty][tx] = (T)0;
+    }
+  } else {
+    tile[0][ty][tx] = inu ? in[uidx(d, i, j)] : (T)0;
+    tile[1][ty][tx] = inv ? in[vidx(d, i, j)] : (T)0;
+  }
+  __syncthreads();
+  haar_tile<TILE, 0>(tile[0], levels, bx0, by0, d.nx + 1, d.ny);
+  haar_tile<TILE, 0>(tile[1], levels, bx0, by0, d.nx, d.ny + 1);
+  if (inu) {
+    const int q = uidx(d, i, j);
+    const T o = inner[q] ? tile[0][ty][tx] : (T)0;
+    out[q] = MODE == 1 ? (T)(out[q] + o) : o;
+  }
+  if (inv) {
+    const int q = vidx(d, i, j);
+    const T o = inner[q] ? tile[1][ty][tx] : (T)0;
+    out[q] = MODE == 1 ? (T)(out[q] + o) : o;
+  }
+}
+
+// Coarse operator application c = R A P u with P u = w given: the operator on a TILE x TILE tile, then
+// the Haar restriction of the tile in shared memory (op_coarse_fun!, update_preconditioners.jl:176-193).
+// DOT: partial <u, c>; the last block sets α = |r|^2 / <u, c> (cg.jl iterate).  START: instead write
+// r = b - c, u = 0, |r|^2, and the last block initialises the CG scalars and its WHILE condition.
+template <typename T, int TILE, bool START>
+__global__ void __launch_bounds__(TILE* TILE)
+    k_coarse_op(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, const T* __restrict__ w,
+                T* __restrict__ c, T* __restrict__ u, T* __restrict__ rvec, const T* __restrict__ bvec,
+                double* __restrict__ partials, DevState* st, const DevParams* __restrict__ P, CondHandles h,
+                const int* __restrict__ live) {
+  if (live && !*live) return;
+  __shared__ OpTile<T, TILE, TILE> s;
+  __shared__ T tile[2][TILE][TILE + 1];
+  const int i0 = blockIdx.x * TILE, j0 = blockIdx.y * TILE;
+  stage_x(d, i0, j0, s, [&](int q) { return w[q]; });
+  __syncthreads();
+  stage_stress(d, cf, i0, j0, s);
+  __syncthreads();
+  const int tx = threadIdx.x, ty = threadIdx.y, li = tx + 1, lj = ty + 1, i = i0 + tx, j = j0 + ty;
+  const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+  tile[0][ty][tx] = (inu && cf.inner[uidx(d, i, j)]) ? stage_out_u(d, cf, s, li, lj, uidx(d, i, j)) : (T)0;
+  tile[1][ty][tx] = (inv && cf.inner[vidx(d, i, j)]) ? stage_out_v(d, cf, s, li, lj, vidx(d, i, j)) : (T)0;
+  __syncthreads();
+  haar_tile<TILE, 1>(tile[0], levels, i0, j0, d.nx + 1, d.ny);
+  haar_tile<TILE, 1>(tile[1], levels, i0, j0, d.nx, d.ny + 1);
+  double acc = 0.0;
+  auto finish = [&](int q, T cv) {
+    cv = wmask[q] ? cv : (T)0;
+    if (START) {
+      const T rv = bvec[q] - cv;
+      rvec[q] = rv;
+      u[q] = (T)0;
+      acc += (double)rv * (double)rv;
+    } else {
+      c[q] = cv;
+      acc += (double)u[q] * (double)cv;
+    }
+  };
+  if (inu) finish(uidx(d, i, j), tile[0][ty][tx]);
+  if (inv) finish(vidx(d, i, j), tile[1][ty][tx]);
+  double tot[2];
+  if (last_block_sum2(acc, 0.0, partials, &st->counter[START ? CNT_B : CNT_C], tot)) {
+    if (flat_tid() == 0) {
+      if (START) {
+        const double res = sqrt(tot[0]);
+        const double abstol = P->tol_coarse * st->cg_bnorm;
+        st->cg_res = res;
+        st->cg_prev = 1.0;
+        st->cg_tol = fmax(1.4901161193847656e-08 * res, abstol);  // reltol = sqrt(eps(Float64))
+        st->cg_it = 0;
+        const bool done = (0 >= P->maxiter_coarse) || res <= st->cg_tol || !(res == res);
+        st->cg_continue = done ? 0 : 1;
+        if (h.active) cudaGraphSetConditional(h.cg, st->cg_continue);
+      } else {
+        st->cg_alpha = (st->cg_res * st->cg_res) / tot[0];
+      }
+    }
+  }
+}
+
+// x += α u; r -= α c; |r|^2; the last block advances the CG scalars and its WHILE condition.
+template <typename T>
+__global__ void k_cg_update(int n, const T* __restrict__ u, const T* __restrict__ c, T* __restrict__ x, T* __restrict__ r,
+                            double* __restrict__ partials, DevState* st, const DevParams* __restrict__ P, CondHandles h,
+                            int* live) {
+  if (live && !*live) return;
+  const double alpha = st->cg_alpha;
+  double s = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    x[k] = (T)((double)x[k] + alpha * (double)u[k]);
+    const T rv = (T)((double)r[k] - alpha * (double)c[k]);
+    r[k] = rv;
+    s += (double)rv * (double)rv;
+  }
+  double tot[2];
+  if (last_block_sum2(s, 0.0, partials, &st->counter[CNT_D], tot)) {
+    if (flat_tid() == 0) {
+      st->cg_prev = st->cg_res;
+      const double res = sqrt(tot[0]);
+      st->cg_res = res;
+      const int it = st->cg_it + 1;
+      st->cg_it = it;
+      st->cg_total += 1;
+      const bool done = it >= P->maxiter_coarse || res <= st->cg_tol || !(res == res);
+      st->cg_continue = done ? 0 : 1;
+      if (live) *live = st->cg_continue;
+      if (h.active) cudaGraphSetConditional(h.cg, st->cg_continue);
+    }
+  }
+}
+
+// End of the V-cycle: x64 += corr; u/v = x at the interior; xc64 = xc; |corr|^2 and |x|^2 for the
+// relative update.
+template <typename T>
+__global__ void k_vcycle_finish(int n, const uint8_t* __restrict__ inner, const T* __restrict__ corr, const T* __restrict__ xc,
+                                double* __restrict__ x, double* __restrict__ uv, double* __restrict__ xc64,
+                                double* __restrict__ partials, DevState* st) {
+  double s0 = 0.0, s1 = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const double cv = (double)corr[k];
+    const double v = x[k] + cv;
+    x[k] = v;
+    if (inner[k]) uv[k] = v;
+    xc64[k] = (double)xc[k];
+    s0 += cv * cv;
+    s1 += v * v;
+  }
+  double tot[2];
+  if (last_block_sum2(s0, s1, partials, &st->counter[CNT_A], tot)) {
+    if (flat_tid() == 0) {
+      st->du2 = tot[0];
+      st->uu2 = tot[1];
+      st->rel_update = sqrt(tot[0]) / sqrt(tot[1]);
+    }
+  }
+}
+
+// Solve start: zero the counters and flags.
+__global__ void k_state_init(DevState* st) {
+  if (threadIdx.x == 0) {
+    DevState z = {};
+    z.rel = INFINITY;
+    z.rel_update = INFINITY;
+    z.picard_continue = 1;
+    *st = z;
+  }
+}
+
+}  // namespace wavi

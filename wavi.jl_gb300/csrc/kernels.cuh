@@ -217,6 +217,17 @@ __global__ void k_op_diag(Dims d, OpCoef<T> cf, T* __restrict__ diag) {
 // two fixed-point sweeps of the σ-level Glen viscosity :264-283, quadratures :292-328, βeff :335-339,
 // and the h-grid operator coefficients :374-383.  TR is the arithmetic type of the viscosity sweeps.
 // ------------------------------------------------------------------------------------------------
+// Device-side copy of the per-solve scalars, read by the kernels through a pointer so that a captured
+// CUDA graph never freezes a parameter value (Params.jl / SolverParams.jl members used by the solve).
+struct DevParams {
+  double weertman_m, weertman_reg_speed, glen_n, glen_reg_strain_rate;
+  double c0;        // -ρ g θ dt  (update_rheological_operators!, update_velocities.jl:381)
+  double rho_i, rho_w, g, sea_level, theta_dt;
+  double tol_picard, tol_coarse, omega;
+  int maxiter_picard, maxiter_coarse, nsmooth, n_iter_viscosity;
+  int picard_test;
+};
+
 struct RelinIn {
   const double* uv;      // velocities (u | v), full rectangles
   const uint8_t* mask;   // u mask | v mask
@@ -228,9 +239,7 @@ struct RelinIn {
   const double* dsdh;
   const double* zeta;    // ns (device)
   const double* qw;      // ns (device)
-  double weertman_m, weertman_reg_speed, glen_n, glen_reg_strain_rate;
-  double c0;             // -ρ g θ dt
-  int n_iter_viscosity;
+  const DevParams* P;
 };
 struct RelinOut {
   double *shelf_strain_rate, *av_speed, *bed_speed, *beta, *tau_bed, *eta, *eta_av, *quad_f1, *quad_f2, *beta_eff;
@@ -287,8 +296,8 @@ __global__ void k_relin_h(Dims d, RelinIn in, RelinOut out) {
   const double avs = sqrt(uc * uc + vc * vc);
   const double f2_prev = out.quad_f2[c], beta_prev = out.beta[c];
   const double bs = avs / (1.0 + f2_prev * beta_prev);
-  const double ur = in.weertman_reg_speed;
-  const double beta = in.wc[c] * pow(sqrt(bs * bs + ur * ur), 1.0 / in.weertman_m - 1.0);
+  const double ur = in.P->weertman_reg_speed;
+  const double beta = in.wc[c] * pow(sqrt(bs * bs + ur * ur), 1.0 / in.P->weertman_m - 1.0);
   const double tau = beta * bs;
   out.shelf_strain_rate[c] = ssr;
   out.av_speed[c] = avs;
@@ -297,8 +306,9 @@ __global__ void k_relin_h(Dims d, RelinIn in, RelinOut out) {
   out.tau_bed[c] = tau;
   double eav = 0.0, f1 = 0.0, f2 = 0.0;
   if (hm) {
-    const TR ex = (TR)(1.0 / in.glen_n - 1.0);
-    const TR er2 = (TR)(in.glen_reg_strain_rate * in.glen_reg_strain_rate);
+    const TR ex = (TR)(1.0 / in.P->glen_n - 1.0);
+    const TR er2 = (TR)(in.P->glen_reg_strain_rate * in.P->glen_reg_strain_rate);
+    const int n_iter_viscosity = in.P->n_iter_viscosity;
     const TR e2 = (TR)(ssr * ssr);
     const double hh = in.h[c];
     for (int k = 0; k < d.ns; ++k) {
@@ -306,7 +316,7 @@ __global__ void k_relin_h(Dims d, RelinIn in, RelinOut out) {
       TR eta = (TR)out.eta[q];
       const TR B = (TR)in.glen_b[q];
       const TR tz = (TR)(tau * in.zeta[k]);
-      for (int it = 0; it < in.n_iter_viscosity; ++it) {
+      for (int it = 0; it < n_iter_viscosity; ++it) {
         const TR t = tz / eta;
         eta = (TR)0.5 * B * powT<TR>(sqrt(e2 + (TR)0.25 * (t * t) + er2), ex);
       }
@@ -324,7 +334,7 @@ __global__ void k_relin_h(Dims d, RelinIn in, RelinOut out) {
   const double hn = in.h[c] * eav;
   out.hn[c] = hn;
   const double hh_m = hm ? hn : 0.0;
-  const double dm = hm ? in.c0 * in.dsdh[c] : 0.0;
+  const double dm = hm ? in.P->c0 * in.dsdh[c] : 0.0;
   out.heta_h64[c] = hh_m;
   out.dimp64[c] = dm;
   if (out.heta_h32) {

@@ -1,10 +1,22 @@
-// wavi_gpu.cu — libwavi_gpu.so: context, buffers, the Picard loop and the C ABI of include/wavi_gpu.h.
+// wavi_gpu.cu — libwavi_gpu.so: context, buffers, the solve graph and the C ABI of include/wavi_gpu.h.
 //
 // The solve is update_velocities! (src/Models/update_velocities.jl:11-29): per Picard iteration one
-// relinearisation (inner_update!, :32-45), the float64 residual and convergence test (:50-65), and one
-// wavelet-multigrid V-cycle (Wavelets/update_preconditioners.jl:54-83) whose coarse CG runs with its
-// scalars on the device.  Everything stays on the context's stream; the host only reads the Picard
-// convergence scalars and, every CG_BATCH coarse iterations, the CG termination flag.
+// relinearisation (inner_update!, :32-45), the float64 right-hand side and residual with the
+// convergence test (:50-65, :106-182), and one wavelet-multigrid V-cycle (Wavelets/
+// update_preconditioners.jl:54-83) with its coarse conjugate-gradient solve.  The whole control flow is
+// one CUDA graph per context:
+//
+//   [state init] -> WHILE(picard_continue) {
+//       relinearise h, relinearise u/v, rhs, (Dirichlet lift), residual + Picard decision
+//       IF(vcycle_needed) {
+//           V-cycle init + diagonal, 2*nsmooth*... smoother sweeps, restriction, coarse-CG start
+//           WHILE(cg_continue) { direction + prolongation, coarse operator + restriction, update }
+//           prolongation of the coarse correction, post-smoother, correction / write-back
+//       }
+//   }
+//
+// so a solve is one graph launch and one host synchronisation.  With use_graphs = 0 the same kernels
+// run from a host loop that reads the decisions back (a debugging path).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -17,6 +29,7 @@
 
 #include "../../include/wavi_gpu.h"
 #include "kernels.cuh"
+#include "fused.cuh"
 
 using namespace wavi;
 
@@ -35,12 +48,13 @@ struct wavi_ctx {
   wavi_solver_params sp{};
   wavi_options opt{};
   bool has_fixed = false;
+  int tile = 16;  // Haar / coarse-operator tile: 16 (levels <= 3) or 32 (levels = 4)
   std::string err;
   std::vector<void*> allocs;
   // static masks (device)
   uint8_t *h_mask = nullptr, *c_mask = nullptr, *mask_uv = nullptr, *inner_uv = nullptr, *fixed_uv = nullptr;
   uint8_t* wmask_uv = nullptr;
-  std::vector<uint8_t> h_inner_host, h_mask_uv_host;  // host copies for masked downloads
+  std::vector<uint8_t> h_inner_host;
   // inputs
   double *h = nullptr, *s = nullptr, *dsdh = nullptr, *gf = nullptr, *wc = nullptr, *acc = nullptr, *melt = nullptr;
   double *h_uv = nullptr, *s_uv = nullptr, *gf_uv = nullptr, *glen_b = nullptr;
@@ -55,25 +69,29 @@ struct wavi_ctx {
   double *heta_h64 = nullptr, *heta_c64 = nullptr, *dimp64 = nullptr, *beta_m64 = nullptr, *h_m64 = nullptr;
   float *heta_h32 = nullptr, *heta_c32 = nullptr, *dimp32 = nullptr, *beta_m32 = nullptr, *h_m32 = nullptr;
   // Picard vectors (float64)
-  double *x64 = nullptr, *b64 = nullptr, *r64 = nullptr, *t64 = nullptr, *xfix64 = nullptr;
+  double *x64 = nullptr, *b64 = nullptr, *r64 = nullptr, *xfix64 = nullptr;
   // V-cycle vectors (float or double; sized for double)
-  void *rs = nullptr, *rsm = nullptr, *corr = nullptr, *diag = nullptr, *xc = nullptr, *rc = nullptr, *uc = nullptr,
-       *cc = nullptr, *w = nullptr, *y = nullptr, *bc = nullptr;
-  // reductions
+  void *rs = nullptr, *corr[2] = {nullptr, nullptr}, *rsm[2] = {nullptr, nullptr}, *diag = nullptr, *xc = nullptr,
+       *rc = nullptr, *uc = nullptr, *cc = nullptr, *w = nullptr, *bc = nullptr;
+  // reductions and device state
   double* partials = nullptr;
   int max_partials = 0;
-  double* S = nullptr;
-  int* I = nullptr;
-  double* h_S = nullptr;  // pinned
-  int* h_I = nullptr;     // pinned
+  DevParams* P = nullptr;     // device
+  DevParams* hP = nullptr;    // pinned host staging
+  DevState* S = nullptr;      // device
+  DevState* hS = nullptr;     // pinned host copy
   // launch shapes
-  dim3 op_grid, op_block, pt_grid, pt_block, haar_grid, haar_block;
+  dim3 op_grid, op_block, pt_grid, pt_block, haar_grid, haar_block, tile_grid, tile_block;
   int ew_blocks = 0;
-  // statistics of the current solve
-  int op_apps = 0;
-  double alg_bytes = 0.0;
+  // solve graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  // statistics of the current solve (host-side bookkeeping of what one launch sequence issues)
   long launches = 0;
   int host_syncs = 0;
+  double picard_head_bytes = 0, vcycle_fixed_bytes = 0, cg_iter_bytes = 0;
+  int picard_head_launches = 0, vcycle_fixed_launches = 0, cg_iter_launches = 0;
+  int picard_head_ops = 0, vcycle_fixed_ops = 0, cg_iter_ops = 0;
 };
 
 namespace {
@@ -106,6 +124,12 @@ int fail(wavi_ctx* c, int code, const char* fmt, ...) {
     if (e_ != cudaSuccess) return fail(c, WAVI_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
   } while (0)
 
+#define TRY(expr)            \
+  do {                       \
+    int r_ = (expr);         \
+    if (r_) return r_;       \
+  } while (0)
+
 template <typename T>
 int dalloc(wavi_ctx* c, T** p, size_t n) {
   void* q = nullptr;
@@ -132,129 +156,24 @@ OpCoef<float> coef<float>(const wavi_ctx* c) {
   return {c->heta_h32, c->heta_c32, c->dimp32, c->beta_m32, c->h_m32, c->inner_uv};
 }
 
-// Algorithmic bytes of one operator application: read x, write y, coefficients heta_h, dimp (Nh),
-// heta_c (Nc), beta_m, h_m (N), interior mask (N bytes), b for the residual form.
+// Algorithmic bytes of one operator application (see the design doc's byte model): read x, write y,
+// coefficients heta_h, dimp (Nh), heta_c (Nc), beta_m, h_m (N), the interior mask (N bytes), plus the
+// right-hand side for the residual form.
 double op_bytes(const Dims& d, int w, bool resid) {
   return (double)w * (2.0 * d.N + 2.0 * d.Nh + d.Nc + 2.0 * d.N + (resid ? d.N : 0)) + d.N;
 }
 
-template <typename T>
-int launch_op(wavi_ctx* c, const T* x, const T* b, T* y, bool resid, const int* skip = nullptr) {
-  if (resid)
-    k_op<T, T, 1><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<T>(c), x, b, y, c->partials, skip);
-  else
-    k_op<T, T, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<T>(c), x, b, y, c->partials, skip);
-  CKL();
-  c->op_apps++;
-  c->alg_bytes += op_bytes(c->d, (int)sizeof(T), resid);
-  return 0;
-}
-int op_partials(const wavi_ctx* c) { return (int)(c->op_grid.x * c->op_grid.y); }
-int haar_partials(const wavi_ctx* c) { return (int)(c->haar_grid.x * c->haar_grid.y * c->haar_grid.z); }
-
-template <typename TI, typename TO, int KIND, bool ACC, bool DOT>
-int launch_haar(wavi_ctx* c, const TI* in, TO* out, const uint8_t* outmask, const uint8_t* inmask, const TO* dotv,
-                const int* skip) {
-  k_haar<TI, TO, KIND, ACC, DOT><<<c->haar_grid, c->haar_block, 0, c->st>>>(c->d, c->sp.levels, in, out, outmask, inmask,
-                                                                             dotv, c->partials, skip);
-  CKL();
-  c->alg_bytes += (double)(sizeof(TI) + sizeof(TO) * (ACC ? 2 : 1) + (DOT ? sizeof(TO) : 0)) * c->d.N + c->d.N;
-  return 0;
-}
-
-int reduce_to(wavi_ctx* c, int np, double* out) {
-  k_reduce<<<1, 1024, 0, c->st>>>(c->partials, np, out);
-  CKL();
-  return 0;
-}
-
 // ---------------------------------------------------------------------------------------------
-// One V-cycle (precondition!(x, p, b), update_preconditioners.jl:54-83) on the T vectors:
-// corr = V(rs), with the coarse iterate xc warm-started from its current contents.
+// Launch sequences (shared by the graph capture and the host-driven path)
 // ---------------------------------------------------------------------------------------------
-template <typename T>
-int vcycle(wavi_ctx* c, int* cg_iters) {
-  const Dims& d = c->d;
-  const int N = d.N;
-  T* rs = (T*)c->rs;
-  T* rsm = (T*)c->rsm;
-  T* corr = (T*)c->corr;
-  T* diag = (T*)c->diag;
-  T* xc = (T*)c->xc;
-  T* rc = (T*)c->rc;
-  T* uc = (T*)c->uc;
-  T* cvec = (T*)c->cc;
-  T* w = (T*)c->w;
-  T* y = (T*)c->y;
-  T* bc = (T*)c->bc;
-  const T omega = (T)c->sp.smoother_omega;
-  int rc_;
-  k_op_diag<T><<<c->pt_grid, c->pt_block, 0, c->st>>>(d, coef<T>(c), diag);
-  CKL();
-  k_fill<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(N, corr, (T)0);
-  CKL();
-  // smoother residual starts as rs - A*0 = rs
-  CK(cudaMemcpyAsync(rsm, rs, sizeof(T) * N, cudaMemcpyDeviceToDevice, c->st));
-  static const int fwd[4] = {1, 3, 2, 4}, bwd[4] = {4, 2, 3, 1};
-  auto smooth = [&](const int* order) -> int {
-    for (int it = 0; it < c->sp.nsmooth; ++it)
-      for (int oc = 0; oc < 4; ++oc) {
-        k_colour_update<T><<<c->pt_grid, c->pt_block, 0, c->st>>>(d, order[oc], omega, c->inner_uv, rsm, diag, corr);
-        CKL();
-        int r = launch_op<T>(c, corr, rs, rsm, true);
-        if (r) return r;
-      }
-    return 0;
-  };
-  if ((rc_ = smooth(fwd))) return rc_;
-  // b_coarse = R r;  abstol = tol_coarse |b_coarse|
-  if ((rc_ = launch_haar<T, T, 1, false, true>(c, rsm, bc, c->wmask_uv, nullptr, bc, nullptr))) return rc_;
-  if ((rc_ = reduce_to(c, haar_partials(c), c->S + CG_SUM))) return rc_;
-  // r_c = b_c - R A P xc
-  if ((rc_ = launch_haar<T, T, 0, false, false>(c, xc, w, c->inner_uv, nullptr, nullptr, nullptr))) return rc_;
-  if ((rc_ = launch_op<T>(c, w, nullptr, y, false))) return rc_;
-  if ((rc_ = launch_haar<T, T, 1, false, false>(c, y, cvec, c->wmask_uv, nullptr, nullptr, nullptr))) return rc_;
-  k_cg_start_sub<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(N, bc, cvec, rc, uc, c->partials);
-  CKL();
-  // |b_c| from the reduced sum, then the CG scalars
-  k_sqrt_slot<<<1, 1, 0, c->st>>>(c->S + CG_SUM, c->S + CG_BNORM);
-  CKL();
-  k_cg_start_scalars<<<1, 1024, 0, c->st>>>(c->partials, c->ew_blocks, c->sp.tol_coarse, c->sp.maxiter_coarse, c->S, c->I);
-  CKL();
-  const int* done = c->I + CG_DONE;
-  for (;;) {
-    for (int k = 0; k < CG_BATCH; ++k) {
-      k_cg_dir<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(N, c->S, c->I, rc, uc);
-      CKL();
-      if ((rc_ = launch_haar<T, T, 0, false, false>(c, uc, w, c->inner_uv, nullptr, nullptr, done))) return rc_;
-      if ((rc_ = launch_op<T>(c, w, nullptr, y, false, done))) return rc_;
-      if ((rc_ = launch_haar<T, T, 1, false, true>(c, y, cvec, c->wmask_uv, nullptr, uc, done))) return rc_;
-      k_cg_alpha<<<1, 1024, 0, c->st>>>(c->partials, haar_partials(c), c->S, c->I);
-      CKL();
-      k_cg_axpy<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(N, c->S, c->I, uc, cvec, xc, rc, c->partials);
-      CKL();
-      k_cg_res<<<1, 1024, 0, c->st>>>(c->partials, c->ew_blocks, c->S, c->I);
-      CKL();
-    }
-    CK(cudaMemcpyAsync(c->h_I, c->I, sizeof(int) * I_COUNT, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
-    c->host_syncs++;
-    if (c->h_I[CG_DONE]) break;
-  }
-  *cg_iters = c->h_I[CG_IT];
-  // corr += P xc
-  if ((rc_ = launch_haar<T, T, 0, true, false>(c, xc, corr, c->inner_uv, nullptr, nullptr, nullptr))) return rc_;
-  // post-smoother starts from rs - A corr
-  if ((rc_ = launch_op<T>(c, corr, rs, rsm, true))) return rc_;
-  if ((rc_ = smooth(bwd))) return rc_;
-  return 0;
-}
+struct Tally {
+  double bytes = 0;
+  int launches = 0, ops = 0;
+};
 
-int relinearise(wavi_ctx* c, const wavi_params* P) {
+int enqueue_picard_head(wavi_ctx* c, const CondHandles& h, Tally& t) {
   const Dims& d = c->d;
-  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw,
-             P->weertman_m, P->weertman_reg_speed, P->glen_n, P->glen_reg_strain_rate,
-             -P->density_ice * P->g * c->sp.super_implicitness * P->dt, c->sp.n_iter_viscosity};
+  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw, c->P};
   RelinOut out{c->shelf, c->av_speed, c->bed_speed, c->beta, c->tau, c->eta, c->eta_av, c->quad_f1, c->quad_f2,
                c->beta_eff, c->heta_h64, c->dimp64, mixed(c) ? c->heta_h32 : nullptr, mixed(c) ? c->dimp32 : nullptr,
                c->hn};
@@ -269,100 +188,317 @@ int relinearise(wavi_ctx* c, const wavi_params* P) {
                   mixed(c) ? c->h_m32 : nullptr, mixed(c) ? c->heta_c32 : nullptr};
   k_relin_uv<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, uin, uout);
   CKL();
-  c->alg_bytes += 8.0 * (2.0 * d.Nh * d.ns + 22.0 * d.Nh + 8.0 * d.N) + 4.0 * d.N;
-  return 0;
-}
-
-// Build b (get_rhs incl. the Dirichlet lift), x (start guess), r = b - A x and ||r||^2, ||b||^2.
-int picard_residual(wavi_ctx* c, const wavi_params* P) {
-  const Dims& d = c->d;
-  RhsIn in{c->h_mask, c->inner_uv, c->fixed_uv, c->s, c->dsdh, c->acc, c->melt, c->h_uv, c->s_uv, c->uv,
-           P->density_ice, P->density_ocean, P->g, P->sea_level_wrt_geoid, c->sp.super_implicitness * P->dt};
-  k_rhs<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, in, c->b64, c->x64, c->xfix64);
+  RhsIn rin{c->h_mask, c->inner_uv, c->fixed_uv, c->s, c->dsdh, c->acc, c->melt, c->h_uv, c->s_uv, c->uv, 0, 0, 0, 0, 0};
+  k_rhs_fused<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, rin, c->P, c->b64, c->x64, c->xfix64, c->partials, c->S);
   CKL();
-  int r;
+  int nlaunch = 3;
   if (c->has_fixed) {
-    if ((r = launch_op<double>(c, c->xfix64, nullptr, c->t64, false))) return r;
-    k_sub<double><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->b64, c->t64, c->b64);
+    k_lift<OP_TX, OP_TY><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<double>(c), c->xfix64, c->b64, c->partials, c->S);
     CKL();
+    nlaunch++;
+    t.ops++;
+    t.bytes += op_bytes(d, 8, true);
   }
-  if ((r = launch_op<double>(c, c->x64, c->b64, c->r64, true))) return r;
-  if ((r = reduce_to(c, op_partials(c), c->S + S_RR))) return r;
-  k_dot<double, double><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->b64, c->b64, c->partials);
+  k_picard_residual<OP_TX, OP_TY><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<double>(c), c->x64, c->b64, c->r64,
+                                                                         c->resid_uv, c->partials, c->S, c->P, h);
   CKL();
-  if ((r = reduce_to(c, c->ew_blocks, c->S + S_BB))) return r;
+  nlaunch++;
+  t.ops++;
+  t.launches += nlaunch;
+  t.bytes += op_bytes(d, 8, true) + 8.0 * (2.0 * d.Nh * d.ns + 22.0 * d.Nh + 8.0 * d.N) + 4.0 * d.N;
   return 0;
 }
 
-int solve_resident(wavi_ctx* c, const wavi_params* P, wavi_stats* st) {
+template <typename T, int TILE>
+int enqueue_vcycle_pre(wavi_ctx* c, const CondHandles& h, Tally& t) {
   const Dims& d = c->d;
-  c->op_apps = 0;
-  c->alg_bytes = 0.0;
+  const int L = c->sp.levels;
+  T* rs = (T*)c->rs;
+  T* corr[2] = {(T*)c->corr[0], (T*)c->corr[1]};
+  T* rsm[2] = {(T*)c->rsm[0], (T*)c->rsm[1]};
+  T* diag = (T*)c->diag;
+  k_vcycle_init<T><<<c->pt_grid, c->pt_block, 0, c->st>>>(d, coef<T>(c), c->r64, c->xc_full64, rs, rsm[0], corr[0],
+                                                          (T*)c->xc, diag);
+  CKL();
+  t.launches++;
+  static const int fwd[4] = {1, 3, 2, 4};
+  int cur = 0;
+  for (int it = 0; it < c->sp.nsmooth; ++it)
+    for (int oc = 0; oc < 4; ++oc) {
+      k_smooth<T, OP_TX, OP_TY, true><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<T>(c), fwd[oc], c->P, rs, diag,
+                                                                            corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]);
+      CKL();
+      cur = 1 - cur;
+      t.launches++;
+      t.ops++;
+      t.bytes += op_bytes(d, sizeof(T), true) + 4.0 * sizeof(T) * d.N;
+    }
+  // b_c = R r  and |b_c|
+  k_restrict_norm<T, TILE><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, L, rsm[cur], c->wmask_uv, (T*)c->bc,
+                                                                      c->partials, c->S);
+  CKL();
+  // r_c = b_c - R A P xc, u_c = 0, CG scalars
+  k_prolong<T, TILE, 0><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, L, c->inner_uv, (const T*)c->xc, (T*)c->w,
+                                                                   nullptr, nullptr, c->S, nullptr);
+  CKL();
+  k_coarse_op<T, TILE, true><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, L, coef<T>(c), c->wmask_uv, (const T*)c->w,
+                                                                        nullptr, (T*)c->uc, (T*)c->rc, (const T*)c->bc,
+                                                                        c->partials, c->S, c->P, h, nullptr);
+  CKL();
+  t.launches += 3;
+  t.ops++;
+  t.bytes += op_bytes(d, sizeof(T), false) + 8.0 * sizeof(T) * d.N + 3.0 * d.N;
+  if (cur != 0) return fail(c, WAVI_ERR_ARGUMENT, "internal: smoother parity");
+  return 0;
+}
+
+template <typename T, int TILE>
+int enqueue_cg_iteration(wavi_ctx* c, const CondHandles& h, int* live, Tally& t) {
+  const Dims& d = c->d;
+  const int L = c->sp.levels;
+  k_prolong<T, TILE, 2><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, L, c->inner_uv, nullptr, (T*)c->w, (const T*)c->rc,
+                                                                   (T*)c->uc, c->S, live);
+  CKL();
+  k_coarse_op<T, TILE, false><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, L, coef<T>(c), c->wmask_uv, (const T*)c->w,
+                                                                         (T*)c->cc, (T*)c->uc, nullptr, nullptr,
+                                                                         c->partials, c->S, c->P, h, live);
+  CKL();
+  k_cg_update<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, (const T*)c->uc, (const T*)c->cc, (T*)c->xc, (T*)c->rc,
+                                                         c->partials, c->S, c->P, h, live);
+  CKL();
+  t.launches += 3;
+  t.ops++;
+  t.bytes += op_bytes(d, sizeof(T), false) + sizeof(T) * (4.0 * d.N + 6.0 * d.N) + 2.0 * d.N;
+  return 0;
+}
+
+template <typename T, int TILE>
+int enqueue_vcycle_post(wavi_ctx* c, const CondHandles& h, Tally& t) {
+  (void)h;
+  const Dims& d = c->d;
+  const int L = c->sp.levels;
+  T* rs = (T*)c->rs;
+  T* corr[2] = {(T*)c->corr[0], (T*)c->corr[1]};
+  T* rsm[2] = {(T*)c->rsm[0], (T*)c->rsm[1]};
+  T* diag = (T*)c->diag;
+  // corr += P xc
+  k_prolong<T, TILE, 1><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, L, c->inner_uv, (const T*)c->xc, corr[0], nullptr,
+                                                                   nullptr, c->S, nullptr);
+  CKL();
+  // r = b - A corr, then the sweeps in reversed colour order
+  k_smooth<T, OP_TX, OP_TY, false><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<T>(c), 0, c->P, rs, diag, corr[0],
+                                                                          nullptr, nullptr, rsm[0]);
+  CKL();
+  t.launches += 2;
+  t.ops++;
+  t.bytes += op_bytes(d, sizeof(T), true) + 3.0 * sizeof(T) * d.N;
+  static const int bwd[4] = {4, 2, 3, 1};
+  int cur = 0;
+  for (int it = 0; it < c->sp.nsmooth; ++it)
+    for (int oc = 0; oc < 4; ++oc) {
+      k_smooth<T, OP_TX, OP_TY, true><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<T>(c), bwd[oc], c->P, rs, diag,
+                                                                            corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]);
+      CKL();
+      cur = 1 - cur;
+      t.launches++;
+      t.ops++;
+      t.bytes += op_bytes(d, sizeof(T), true) + 4.0 * sizeof(T) * d.N;
+    }
+  k_vcycle_finish<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, corr[cur], (const T*)c->xc, c->x64, c->uv,
+                                                             c->xc_full64, c->partials, c->S);
+  CKL();
+  t.launches++;
+  t.bytes += (double)(2 * sizeof(T) + 8 * 3) * d.N + d.N;
+  return 0;
+}
+
+template <typename T, int TILE>
+int enqueue_all_host_driven(wavi_ctx* c) {
+  // The same launch sequence as the graph, with the decisions read back on the host.
+  CondHandles h{};
+  h.active = 0;
+  Tally tp, tv, tc;
+  k_state_init<<<1, 32, 0, c->st>>>(c->S);
+  CKL();
+  for (;;) {
+    TRY(enqueue_picard_head(c, h, tp));
+    CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->host_syncs++;
+    if (c->hS->vcycle_needed) {
+      TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv)));
+      CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      c->host_syncs++;
+      int* live = &c->S->cg_continue;
+      while (c->hS->cg_continue) {
+        for (int k = 0; k < CG_BATCH; ++k) TRY((enqueue_cg_iteration<T, TILE>(c, h, live, tc)));
+        CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        c->host_syncs++;
+      }
+      TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
+    }
+    if (!c->hS->picard_continue) break;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Graph construction: capture segments into the top graph and the conditional bodies.
+// ---------------------------------------------------------------------------------------------
+struct Segment {
+  std::vector<cudaGraphNode_t> sinks;
+};
+
+int begin_capture(wavi_ctx* c, cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps) {
+  CK(cudaStreamBeginCaptureToGraph(c->st, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                   cudaStreamCaptureModeThreadLocal));
+  return 0;
+}
+int end_capture(wavi_ctx* c, cudaGraph_t g, std::vector<cudaGraphNode_t>& sinks) {
+  cudaStreamCaptureStatus status;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t n = 0;
+  CK(cudaStreamGetCaptureInfo(c->st, &status, nullptr, nullptr, &deps, nullptr, &n));
+  sinks.assign(deps, deps + n);
+  cudaGraph_t out = nullptr;
+  CK(cudaStreamEndCapture(c->st, &out));
+  if (out != g) return fail(c, WAVI_ERR_CUDA, "capture returned a different graph");
+  return 0;
+}
+int add_conditional(wavi_ctx* c, cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps,
+                    cudaGraphConditionalHandle handle, cudaGraphConditionalNodeType type, cudaGraph_t* body,
+                    cudaGraphNode_t* node) {
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = handle;
+  p.conditional.type = type;
+  p.conditional.size = 1;
+  CK(cudaGraphAddNode(node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &p));
+  *body = p.conditional.phGraph_out[0];
+  return 0;
+}
+
+template <typename T, int TILE>
+int build_graph(wavi_ctx* c) {
+  cudaGraph_t top = nullptr;
+  CK(cudaGraphCreate(&top, 0));
+  c->graph = top;
+  CondHandles h{};
+  h.active = 1;
+  CK(cudaGraphConditionalHandleCreate(&h.picard, top, 1, cudaGraphCondAssignDefault));
+  std::vector<cudaGraphNode_t> sinks;
+  Tally tp, tv, tc;
+  const long saved = c->launches;
+  // top: state init -> WHILE(picard)
+  TRY(begin_capture(c, top, {}));
+  k_state_init<<<1, 32, 0, c->st>>>(c->S);
+  CKL();
+  TRY(end_capture(c, top, sinks));
+  cudaGraph_t pbody = nullptr, vbody = nullptr, cbody = nullptr;
+  cudaGraphNode_t pnode, vnode, cnode;
+  TRY(add_conditional(c, top, sinks, h.picard, cudaGraphCondTypeWhile, &pbody, &pnode));
+  CK(cudaGraphConditionalHandleCreate(&h.vcycle, pbody, 0, cudaGraphCondAssignDefault));
+  // Picard body: head, then IF(vcycle)
+  TRY(begin_capture(c, pbody, {}));
+  TRY(enqueue_picard_head(c, h, tp));
+  TRY(end_capture(c, pbody, sinks));
+  TRY(add_conditional(c, pbody, sinks, h.vcycle, cudaGraphCondTypeIf, &vbody, &vnode));
+  CK(cudaGraphConditionalHandleCreate(&h.cg, vbody, 0, cudaGraphCondAssignDefault));
+  // V-cycle body: pre part, WHILE(cg), post part
+  TRY(begin_capture(c, vbody, {}));
+  TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv)));
+  TRY(end_capture(c, vbody, sinks));
+  TRY(add_conditional(c, vbody, sinks, h.cg, cudaGraphCondTypeWhile, &cbody, &cnode));
+  TRY(begin_capture(c, cbody, {}));
+  TRY((enqueue_cg_iteration<T, TILE>(c, h, nullptr, tc)));
+  TRY(end_capture(c, cbody, sinks));
+  TRY(begin_capture(c, vbody, {cnode}));
+  TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
+  TRY(end_capture(c, vbody, sinks));
+  CK(cudaGraphInstantiate(&c->exec, top, 0));
+  c->launches = saved;
+  c->picard_head_bytes = tp.bytes;
+  c->picard_head_launches = tp.launches;
+  c->picard_head_ops = tp.ops;
+  c->vcycle_fixed_bytes = tv.bytes;
+  c->vcycle_fixed_launches = tv.launches;
+  c->vcycle_fixed_ops = tv.ops;
+  c->cg_iter_bytes = tc.bytes;
+  c->cg_iter_launches = tc.launches;
+  c->cg_iter_ops = tc.ops;
+  return 0;
+}
+
+int ensure_graph(wavi_ctx* c) {
+  if (c->exec) return 0;
+  if (mixed(c)) return c->tile == 16 ? build_graph<float, 16>(c) : build_graph<float, 32>(c);
+  return c->tile == 16 ? build_graph<double, 16>(c) : build_graph<double, 32>(c);
+}
+
+int set_params(wavi_ctx* c, const wavi_params* p) {
+  DevParams& P = *c->hP;
+  P.weertman_m = p->weertman_m;
+  P.weertman_reg_speed = p->weertman_reg_speed;
+  P.glen_n = p->glen_n;
+  P.glen_reg_strain_rate = p->glen_reg_strain_rate;
+  P.c0 = -p->density_ice * p->g * c->sp.super_implicitness * p->dt;
+  P.rho_i = p->density_ice;
+  P.rho_w = p->density_ocean;
+  P.g = p->g;
+  P.sea_level = p->sea_level_wrt_geoid;
+  P.theta_dt = c->sp.super_implicitness * p->dt;
+  P.tol_picard = c->sp.tol_picard;
+  P.tol_coarse = c->sp.tol_coarse;
+  P.omega = c->sp.smoother_omega;
+  P.maxiter_picard = c->sp.maxiter_picard;
+  P.maxiter_coarse = c->sp.maxiter_coarse;
+  P.nsmooth = c->sp.nsmooth;
+  P.n_iter_viscosity = c->sp.n_iter_viscosity;
+  P.picard_test = c->opt.picard_test;
+  CK(cudaMemcpyAsync(c->P, c->hP, sizeof(DevParams), cudaMemcpyHostToDevice, c->st));
+  return 0;
+}
+
+int solve_resident(wavi_ctx* c, const wavi_params* p, wavi_stats* st) {
   c->launches = 0;
   c->host_syncs = 0;
-  int total_cg = 0, it = 0, r;
-  bool converged = false;
-  double rel = INFINITY, relu = INFINITY;
+  TRY(set_params(c, p));
+  if (c->sp.maxiter_picard <= 0) {
+    if (st) *st = wavi_stats{};
+    return 0;
+  }
   CK(cudaEventRecord(c->ev0, c->st));
-  while (!converged && it < c->sp.maxiter_picard) {
-    ++it;
-    if ((r = relinearise(c, P))) return r;
-    if ((r = picard_residual(c, P))) return r;
-    CK(cudaMemcpyAsync(c->h_S, c->S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
-    c->host_syncs++;
-    rel = std::sqrt(c->h_S[S_RR]) / std::sqrt(c->h_S[S_BB]);
-    if (!std::isfinite(rel)) return fail(c, WAVI_ERR_NONFINITE, "non-finite Picard residual at iteration %d", it);
-    CK(cudaMemcpyAsync(c->resid_uv, c->r64, sizeof(double) * d.N, cudaMemcpyDeviceToDevice, c->st));
-    converged = rel < c->sp.tol_picard;
-    if (converged && c->opt.picard_test == 1 && it > 1 && !(relu <= c->sp.tol_picard)) converged = false;
-    if (converged) break;
-    int cg = 0;
-    if (mixed(c)) {
-      k_convert<double, float><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->r64, (float*)c->rs);
-      CKL();
-      k_convert<double, float><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->xc_full64, (float*)c->xc);
-      CKL();
-      if ((r = vcycle<float>(c, &cg))) return r;
-      k_convert<float, double><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, (float*)c->xc, c->xc_full64);
-      CKL();
-      k_update_norms<float><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, (float*)c->corr, c->x64, c->partials);
-      CKL();
-      k_apply_correction<float><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, (float*)c->corr, c->x64, c->uv);
-      CKL();
-    } else {
-      CK(cudaMemcpyAsync(c->rs, c->r64, sizeof(double) * d.N, cudaMemcpyDeviceToDevice, c->st));
-      CK(cudaMemcpyAsync(c->xc, c->xc_full64, sizeof(double) * d.N, cudaMemcpyDeviceToDevice, c->st));
-      if ((r = vcycle<double>(c, &cg))) return r;
-      CK(cudaMemcpyAsync(c->xc_full64, c->xc, sizeof(double) * d.N, cudaMemcpyDeviceToDevice, c->st));
-      k_update_norms<double><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, (double*)c->corr, c->x64, c->partials);
-      CKL();
-      k_apply_correction<double><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, (double*)c->corr, c->x64, c->uv);
-      CKL();
-    }
-    k_reduce<<<1, 1024, 0, c->st>>>(c->partials, c->ew_blocks, c->S + S_DU);
-    CKL();
-    k_reduce<<<1, 1024, 0, c->st>>>(c->partials + c->ew_blocks, c->ew_blocks, c->S + S_UU);
-    CKL();
-    CK(cudaMemcpyAsync(c->h_S, c->S, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
-    c->host_syncs++;
-    relu = std::sqrt(c->h_S[S_DU]) / std::sqrt(c->h_S[S_UU]);
-    total_cg += cg;
+  if (c->opt.use_graphs) {
+    TRY(ensure_graph(c));
+    CK(cudaGraphLaunch(c->exec, c->st));
+  } else if (mixed(c)) {
+    TRY((c->tile == 16 ? enqueue_all_host_driven<float, 16>(c) : enqueue_all_host_driven<float, 32>(c)));
+  } else {
+    TRY((c->tile == 16 ? enqueue_all_host_driven<double, 16>(c) : enqueue_all_host_driven<double, 32>(c)));
   }
   CK(cudaEventRecord(c->ev1, c->st));
+  CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
+  c->host_syncs++;
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
-  int status = converged ? WAVI_OK : WAVI_ERR_NOT_CONVERGED;
+  const DevState& S = *c->hS;
+  const int picard = S.picard_it, vcycles = S.converged ? picard - 1 : picard;
+  if (c->opt.use_graphs) {  // launches the graph issued, from the per-segment tallies
+    c->launches = 1 + (long)picard * c->picard_head_launches + (long)vcycles * c->vcycle_fixed_launches +
+                  (long)S.cg_total * c->cg_iter_launches;
+  }
+  if (S.status == WAVI_ERR_NONFINITE) return fail(c, WAVI_ERR_NONFINITE, "non-finite Picard residual at iteration %d", picard);
   if (st) {
-    st->status = status;
-    st->picard_iterations = it;
-    st->coarse_cg_iterations = total_cg;
-    st->op_applications = c->op_apps;
-    st->rel_residual = rel;
-    st->rel_update = relu;
-    st->algorithmic_bytes = c->alg_bytes;
+    st->status = S.converged ? WAVI_OK : WAVI_ERR_NOT_CONVERGED;
+    st->picard_iterations = picard;
+    st->coarse_cg_iterations = S.cg_total;
+    st->op_applications = picard * c->picard_head_ops + vcycles * c->vcycle_fixed_ops + S.cg_total * c->cg_iter_ops;
+    st->rel_residual = S.rel;
+    st->rel_update = S.rel_update;
+    st->algorithmic_bytes = picard * c->picard_head_bytes + vcycles * c->vcycle_fixed_bytes + S.cg_total * c->cg_iter_bytes;
     st->elapsed_ms = ms;
     st->kernel_launches = (int32_t)std::min<long>(c->launches, 2147483647L);
     st->host_syncs = c->host_syncs;
@@ -387,9 +523,7 @@ int copy_out(wavi_ctx* c, double* dst, const double* src, size_t n, cudaMemcpyKi
 int upload(wavi_ctx* c, const wavi_fields* f, bool host) {
   const Dims& d = c->d;
   const cudaMemcpyKind k = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  int r;
-#define IN(dst, src, n) \
-  if ((r = copy_in(c, dst, src, n, k, #src))) return r;
+#define IN(dst, src, n) TRY(copy_in(c, dst, src, n, k, #src));
   IN(c->h, f->h, d.Nh) IN(c->s, f->s, d.Nh) IN(c->dsdh, f->dsdh, d.Nh) IN(c->gf, f->grounded_fraction, d.Nh)
   IN(c->wc, f->weertman_c, d.Nh) IN(c->acc, f->accumulation, d.Nh) IN(c->melt, f->basal_melt, d.Nh)
   IN(c->h_uv, f->gu_h, d.Nu) IN(c->h_uv + d.Nu, f->gv_h, d.Nv)
@@ -400,20 +534,22 @@ int upload(wavi_ctx* c, const wavi_fields* f, bool host) {
   IN(c->eta, f->eta, (size_t)d.Nh * d.ns) IN(c->beta, f->beta, d.Nh) IN(c->quad_f2, f->quad_f2, d.Nh)
   // outputs that the reference only partially overwrites start from the caller's values
   IN(c->beta_eff_uv, f->gu_beta_eff, d.Nu) IN(c->beta_eff_uv + d.Nu, f->gv_beta_eff, d.Nv)
+  IN(c->resid_uv, f->gu_residual, d.Nu) IN(c->resid_uv + d.Nu, f->gv_residual, d.Nv)
 #undef IN
   // adaptive coarse space and its compact correction cache -> full layout
   if (!f->wu_mask || !f->wv_mask || !f->wu_correction_coarse || !f->wv_correction_coarse)
     return fail(c, WAVI_ERR_ARGUMENT, "wavelet masks / coarse corrections are null");
+  const cudaMemcpyKind kh = host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost;
   std::vector<uint8_t> wm((size_t)d.N);
-  CK(cudaMemcpyAsync(wm.data(), f->wu_mask, d.Nu, host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, c->st));
-  CK(cudaMemcpyAsync(wm.data() + d.Nu, f->wv_mask, d.Nv, host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(wm.data(), f->wu_mask, d.Nu, kh, c->st));
+  CK(cudaMemcpyAsync(wm.data() + d.Nu, f->wv_mask, d.Nv, kh, c->st));
   CK(cudaStreamSynchronize(c->st));
   size_t nwu = 0, nwv = 0;
   for (int i = 0; i < d.Nu; ++i) nwu += (wm[i] = wm[i] ? 1 : 0);
   for (int i = d.Nu; i < d.N; ++i) nwv += (wm[i] = wm[i] ? 1 : 0);
   std::vector<double> cu(nwu), cv(nwv), full((size_t)d.N, 0.0);
-  CK(cudaMemcpyAsync(cu.data(), f->wu_correction_coarse, nwu * sizeof(double), host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, c->st));
-  CK(cudaMemcpyAsync(cv.data(), f->wv_correction_coarse, nwv * sizeof(double), host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, c->st));
+  if (nwu) CK(cudaMemcpyAsync(cu.data(), f->wu_correction_coarse, nwu * sizeof(double), kh, c->st));
+  if (nwv) CK(cudaMemcpyAsync(cv.data(), f->wv_correction_coarse, nwv * sizeof(double), kh, c->st));
   CK(cudaStreamSynchronize(c->st));
   size_t a = 0, b = 0;
   for (int i = 0; i < d.Nu; ++i)
@@ -429,40 +565,29 @@ int upload(wavi_ctx* c, const wavi_fields* f, bool host) {
 int download(wavi_ctx* c, wavi_fields* f, bool host) {
   const Dims& d = c->d;
   const cudaMemcpyKind k = host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-  int r;
-#define OUT(dst, src, n) \
-  if ((r = copy_out(c, dst, src, n, k, #dst))) return r;
+#define OUT(dst, src, n) TRY(copy_out(c, dst, src, n, k, #dst));
   OUT(f->u, c->uv, d.Nu) OUT(f->v, c->uv + d.Nu, d.Nv) OUT(f->eta, c->eta, (size_t)d.Nh * d.ns)
   OUT(f->beta, c->beta, d.Nh) OUT(f->quad_f2, c->quad_f2, d.Nh)
   OUT(f->shelf_strain_rate, c->shelf, d.Nh) OUT(f->av_speed, c->av_speed, d.Nh) OUT(f->bed_speed, c->bed_speed, d.Nh)
   OUT(f->tau_bed, c->tau, d.Nh) OUT(f->eta_av, c->eta_av, d.Nh) OUT(f->quad_f1, c->quad_f1, d.Nh)
   OUT(f->beta_eff, c->beta_eff, d.Nh)
   OUT(f->gu_beta_eff, c->beta_eff_uv, d.Nu) OUT(f->gv_beta_eff, c->beta_eff_uv + d.Nu, d.Nv)
+  OUT(f->gu_residual, c->resid_uv, d.Nu) OUT(f->gv_residual, c->resid_uv + d.Nu, d.Nv)
 #undef OUT
-  // residual: written at the interior points only (set_residual!, update_velocities.jl:428-433)
-  if (!f->gu_residual || !f->gv_residual) return fail(c, WAVI_ERR_ARGUMENT, "residual outputs are null");
-  std::vector<double> res((size_t)d.N), gu((size_t)d.Nu), gv((size_t)d.Nv);
-  CK(cudaMemcpyAsync(res.data(), c->resid_uv, sizeof(double) * d.N, cudaMemcpyDeviceToHost, c->st));
-  CK(cudaMemcpyAsync(gu.data(), f->gu_residual, sizeof(double) * d.Nu, host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, c->st));
-  CK(cudaMemcpyAsync(gv.data(), f->gv_residual, sizeof(double) * d.Nv, host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost, c->st));
   // coarse correction cache: full -> compact in mask order
   std::vector<double> full((size_t)d.N);
   std::vector<uint8_t> wm((size_t)d.N);
   CK(cudaMemcpyAsync(full.data(), c->xc_full64, sizeof(double) * d.N, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(wm.data(), c->wmask_uv, d.N, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
-  for (int i = 0; i < d.Nu; ++i)
-    if (c->h_inner_host[i]) gu[i] = res[i];
-  for (int i = 0; i < d.Nv; ++i)
-    if (c->h_inner_host[d.Nu + i]) gv[i] = res[d.Nu + i];
   std::vector<double> cu, cv;
+  cu.reserve(d.Nu);
+  cv.reserve(d.Nv);
   for (int i = 0; i < d.Nu; ++i)
     if (wm[i]) cu.push_back(full[i]);
   for (int i = d.Nu; i < d.N; ++i)
     if (wm[i]) cv.push_back(full[i]);
   const cudaMemcpyKind hk = host ? cudaMemcpyHostToHost : cudaMemcpyHostToDevice;
-  CK(cudaMemcpyAsync(f->gu_residual, gu.data(), sizeof(double) * d.Nu, hk, c->st));
-  CK(cudaMemcpyAsync(f->gv_residual, gv.data(), sizeof(double) * d.Nv, hk, c->st));
   if (!cu.empty()) CK(cudaMemcpyAsync(f->wu_correction_coarse, cu.data(), sizeof(double) * cu.size(), hk, c->st));
   if (!cv.empty()) CK(cudaMemcpyAsync(f->wv_correction_coarse, cv.data(), sizeof(double) * cv.size(), hk, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -473,6 +598,12 @@ int check_ctx(wavi_ctx* c) {
   if (!c) return WAVI_ERR_ARGUMENT;
   cudaError_t e = cudaSetDevice(c->dev);
   if (e != cudaSuccess) return fail(c, WAVI_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+  return 0;
+}
+
+int check_params(wavi_ctx* c, const wavi_params* p) {
+  if (!p) return fail(c, WAVI_ERR_ARGUMENT, "params is null");
+  if (!(p->glen_n > 0) || !(p->weertman_m > 0)) return fail(c, WAVI_ERR_ARGUMENT, "glen_n and weertman_m must be positive");
   return 0;
 }
 
@@ -514,17 +645,18 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
     return fail(nullptr, WAVI_ERR_ARGUMENT, "grid arrays must not be null");
   if (sp->levels < 0 || sp->levels > 4) return fail(nullptr, WAVI_ERR_ARGUMENT, "levels must be in 0..4 (got %d)", sp->levels);
   if (sp->n_iter_viscosity < 1) return fail(nullptr, WAVI_ERR_ARGUMENT, "n_iter_viscosity must be >= 1");
+  if (sp->nsmooth < 0) return fail(nullptr, WAVI_ERR_ARGUMENT, "nsmooth must be >= 0");
   if (opt->precision != WAVI_PRECISION_FP64 && opt->precision != WAVI_PRECISION_MIXED)
     return fail(nullptr, WAVI_ERR_ARGUMENT, "unknown precision %d", opt->precision);
   int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
-    return fail(nullptr, WAVI_ERR_NO_DEVICE, "no CUDA device");
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, WAVI_ERR_NO_DEVICE, "no CUDA device");
   if (opt->device < 0 || opt->device >= ndev) return fail(nullptr, WAVI_ERR_ARGUMENT, "device %d out of range", opt->device);
   if ((long)(g->nx + 1) * (g->ny + 1) > (1L << 30)) return fail(nullptr, WAVI_ERR_ARGUMENT, "grid too large");
   c = new wavi_ctx();
   c->dev = opt->device;
   c->sp = *sp;
   c->opt = *opt;
+  c->tile = sp->levels <= 3 ? 16 : 32;
   auto bail = [&](int code) {
     g_create_error = c->err;
     wavi_ctx_destroy(c);
@@ -576,7 +708,6 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   }
   if (ninner == 0) return bail(fail(c, WAVI_ERR_ARGUMENT, "the interior mask is empty"));
   c->h_inner_host = in;
-  c->h_mask_uv_host = mk;
   int r = 0;
   const size_t Nh = d.Nh, Nc = d.Nc, N = d.N, N3 = (size_t)d.Nh * d.ns;
 #define A(p, n) \
@@ -589,9 +720,10 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   A(beta_eff_uv, N) A(resid_uv, N) A(hn, Nh)
   A(heta_h64, Nh) A(heta_c64, Nc) A(dimp64, Nh) A(beta_m64, N) A(h_m64, N)
   A(heta_h32, Nh) A(heta_c32, Nc) A(dimp32, Nh) A(beta_m32, N) A(h_m32, N)
-  A(x64, N) A(b64, N) A(r64, N) A(t64, N) A(xfix64, N)
+  A(x64, N) A(b64, N) A(r64, N) A(xfix64, N)
 #undef A
-  for (void** p : {&c->rs, &c->rsm, &c->corr, &c->diag, &c->xc, &c->rc, &c->uc, &c->cc, &c->w, &c->y, &c->bc}) {
+  for (void** p : {&c->rs, &c->corr[0], &c->corr[1], &c->rsm[0], &c->rsm[1], &c->diag, &c->xc, &c->rc, &c->uc, &c->cc,
+                   &c->w, &c->bc}) {
     double* q = nullptr;
     if ((r = dalloc(c, &q, N))) return bail(r);
     *p = q;
@@ -604,13 +736,18 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   const int B = 1 << (sp->levels + 1);
   c->haar_block = dim3(B, B);
   c->haar_grid = dim3((d.nx + 1 + B - 1) / B, (d.ny + 1 + B - 1) / B, 2);
-  c->ew_blocks = (int)std::min<size_t>((N + EW_THREADS - 1) / EW_THREADS, 152 * 8);
-  c->max_partials = std::max({op_partials(c), haar_partials(c), 2 * c->ew_blocks, 1});
+  c->tile_block = dim3(c->tile, c->tile);
+  c->tile_grid = dim3((d.nx + 1 + c->tile - 1) / c->tile, (d.ny + 1 + c->tile - 1) / c->tile);
+  c->ew_blocks = (int)std::min<size_t>((N + EW_THREADS - 1) / EW_THREADS, 152 * 4);
+  const int pt_blocks = (int)(c->pt_grid.x * c->pt_grid.y);
+  const int op_blocks = (int)(c->op_grid.x * c->op_grid.y);
+  const int tile_blocks = (int)(c->tile_grid.x * c->tile_grid.y);
+  const int haar_blocks = (int)(c->haar_grid.x * c->haar_grid.y * c->haar_grid.z);
+  c->max_partials = 2 * std::max({pt_blocks, op_blocks, tile_blocks, haar_blocks, c->ew_blocks, 1});
   if ((r = dalloc(c, &c->partials, (size_t)c->max_partials))) return bail(r);
-  if ((r = dalloc(c, &c->S, (size_t)S_COUNT))) return bail(r);
-  if ((r = dalloc(c, &c->I, (size_t)I_COUNT))) return bail(r);
-  if (cudaMallocHost(&c->h_S, sizeof(double) * S_COUNT) != cudaSuccess ||
-      cudaMallocHost(&c->h_I, sizeof(int) * I_COUNT) != cudaSuccess)
+  if ((r = dalloc(c, &c->P, 1))) return bail(r);
+  if ((r = dalloc(c, &c->S, 1))) return bail(r);
+  if (cudaMallocHost(&c->hP, sizeof(DevParams)) != cudaSuccess || cudaMallocHost(&c->hS, sizeof(DevState)) != cudaSuccess)
     return bail(fail(c, WAVI_ERR_ALLOC, "pinned allocation failed"));
   std::vector<double> zeta((size_t)d.ns);
   for (int k = 0; k < d.ns; ++k) zeta[k] = 1.0 - g->sigma[k];  // Grid.jl:170
@@ -631,9 +768,11 @@ int wavi_ctx_destroy(wavi_ctx* c) {
   if (!c) return WAVI_OK;
   cudaSetDevice(c->dev);
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->exec) cudaGraphExecDestroy(c->exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
   for (void* p : c->allocs) cudaFree(p);
-  if (c->h_S) cudaFreeHost(c->h_S);
-  if (c->h_I) cudaFreeHost(c->h_I);
+  if (c->hP) cudaFreeHost(c->hP);
+  if (c->hS) cudaFreeHost(c->hS);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->st) cudaStreamDestroy(c->st);
@@ -641,61 +780,69 @@ int wavi_ctx_destroy(wavi_ctx* c) {
   return WAVI_OK;
 }
 
-static int check_params(wavi_ctx* c, const wavi_params* p) {
-  if (!p) return fail(c, WAVI_ERR_ARGUMENT, "params is null");
-  if (!(p->glen_n > 0) || !(p->weertman_m > 0)) return fail(c, WAVI_ERR_ARGUMENT, "glen_n and weertman_m must be positive");
-  return 0;
-}
-
 int wavi_solve_velocities(wavi_ctx* c, const wavi_params* p, wavi_fields* f, wavi_stats* st) {
-  int r;
-  if ((r = check_ctx(c))) return r;
-  if ((r = check_params(c, p))) return r;
+  TRY(check_ctx(c));
+  TRY(check_params(c, p));
   if (!f) return fail(c, WAVI_ERR_ARGUMENT, "fields is null");
-  if ((r = upload(c, f, true))) return r;
-  if ((r = solve_resident(c, p, st))) return r;
+  TRY(upload(c, f, true));
+  TRY(solve_resident(c, p, st));
   return download(c, f, true);
 }
 
 int wavi_solve_velocities_device(wavi_ctx* c, const wavi_params* p, wavi_fields* f, wavi_stats* st) {
-  int r;
-  if ((r = check_ctx(c))) return r;
-  if ((r = check_params(c, p))) return r;
+  TRY(check_ctx(c));
+  TRY(check_params(c, p));
   if (!f) return fail(c, WAVI_ERR_ARGUMENT, "fields is null");
-  if ((r = upload(c, f, false))) return r;
-  if ((r = solve_resident(c, p, st))) return r;
+  TRY(upload(c, f, false));
+  TRY(solve_resident(c, p, st));
   return download(c, f, false);
 }
 
 int wavi_relinearise_device(wavi_ctx* c, const wavi_params* p, wavi_fields* f) {
-  int r;
-  if ((r = check_ctx(c))) return r;
-  if ((r = check_params(c, p))) return r;
+  TRY(check_ctx(c));
+  TRY(check_params(c, p));
   if (!f) return fail(c, WAVI_ERR_ARGUMENT, "fields is null");
-  if ((r = upload(c, f, false))) return r;
-  if ((r = relinearise(c, p))) return r;
+  TRY(upload(c, f, false));
+  TRY(set_params(c, p));
+  const Dims& d = c->d;
+  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw, c->P};
+  RelinOut out{c->shelf, c->av_speed, c->bed_speed, c->beta, c->tau, c->eta, c->eta_av, c->quad_f1, c->quad_f2,
+               c->beta_eff, c->heta_h64, c->dimp64, mixed(c) ? c->heta_h32 : nullptr, mixed(c) ? c->dimp32 : nullptr,
+               c->hn};
+  const int nb = (d.Nh + 127) / 128;
+  if (mixed(c))
+    k_relin_h<float><<<nb, 128, 0, c->st>>>(d, in, out);
+  else
+    k_relin_h<double><<<nb, 128, 0, c->st>>>(d, in, out);
+  CKL();
+  RelinUVIn uin{c->mask_uv, c->h_mask, c->c_mask, c->beta_eff, c->gf, c->gf_uv, c->h_uv, c->hn};
+  RelinUVOut uout{c->beta_eff_uv, c->beta_m64, c->h_m64, c->heta_c64, mixed(c) ? c->beta_m32 : nullptr,
+                  mixed(c) ? c->h_m32 : nullptr, mixed(c) ? c->heta_c32 : nullptr};
+  k_relin_uv<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, uin, uout);
+  CKL();
   CK(cudaStreamSynchronize(c->st));
   return download(c, f, false);
 }
 
 int wavi_apply_operator_device(wavi_ctx* c, int precision, const void* in_uv, void* out_uv) {
-  int r;
-  if ((r = check_ctx(c))) return r;
+  TRY(check_ctx(c));
   if (!in_uv || !out_uv) return fail(c, WAVI_ERR_ARGUMENT, "null vector");
-  if (precision == WAVI_PRECISION_FP64)
-    r = launch_op<double>(c, (const double*)in_uv, nullptr, (double*)out_uv, false);
-  else if (precision == WAVI_PRECISION_MIXED && mixed(c))
-    r = launch_op<float>(c, (const float*)in_uv, nullptr, (float*)out_uv, false);
-  else
+  if (precision == WAVI_PRECISION_FP64) {
+    k_op<double, double, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<double>(c), (const double*)in_uv, nullptr,
+                                                                   (double*)out_uv, c->partials, nullptr);
+  } else if (precision == WAVI_PRECISION_MIXED && mixed(c)) {
+    k_op<float, float, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<float>(c), (const float*)in_uv, nullptr,
+                                                                 (float*)out_uv, c->partials, nullptr);
+  } else {
     return fail(c, WAVI_ERR_ARGUMENT, "float32 operator needs a mixed-precision context");
-  if (r) return r;
+  }
+  CKL();
   CK(cudaStreamSynchronize(c->st));
   return 0;
 }
 
 int wavi_op_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
-  int r;
-  if ((r = check_ctx(c))) return r;
+  TRY(check_ctx(c));
   if (!diag_uv) return fail(c, WAVI_ERR_ARGUMENT, "null vector");
   if (precision == WAVI_PRECISION_FP64)
     k_op_diag<double><<<c->pt_grid, c->pt_block, 0, c->st>>>(c->d, coef<double>(c), (double*)diag_uv);
@@ -709,18 +856,22 @@ int wavi_op_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
 }
 
 int wavi_haar_device(wavi_ctx* c, int kind, const double* in_uv, double* out_uv, const uint8_t* mask_uv) {
-  int r;
-  if ((r = check_ctx(c))) return r;
+  TRY(check_ctx(c));
   if (!in_uv || !out_uv) return fail(c, WAVI_ERR_ARGUMENT, "null vector");
+  const Dims& d = c->d;
+  const int L = c->sp.levels;
   if (kind == 0)
-    r = launch_haar<double, double, 0, false, false>(c, in_uv, out_uv, mask_uv ? mask_uv : c->inner_uv, nullptr, nullptr, nullptr);
+    k_haar<double, double, 0, false, false><<<c->haar_grid, c->haar_block, 0, c->st>>>(
+        d, L, in_uv, out_uv, mask_uv ? mask_uv : c->inner_uv, nullptr, nullptr, c->partials, nullptr);
   else if (kind == 1)
-    r = launch_haar<double, double, 1, false, false>(c, in_uv, out_uv, mask_uv ? mask_uv : c->wmask_uv, nullptr, nullptr, nullptr);
+    k_haar<double, double, 1, false, false><<<c->haar_grid, c->haar_block, 0, c->st>>>(
+        d, L, in_uv, out_uv, mask_uv ? mask_uv : c->wmask_uv, nullptr, nullptr, c->partials, nullptr);
   else if (kind == 2)
-    r = launch_haar<double, double, 2, false, false>(c, in_uv, out_uv, nullptr, mask_uv ? mask_uv : c->mask_uv, nullptr, nullptr);
+    k_haar<double, double, 2, false, false><<<c->haar_grid, c->haar_block, 0, c->st>>>(
+        d, L, in_uv, out_uv, nullptr, mask_uv ? mask_uv : c->mask_uv, nullptr, c->partials, nullptr);
   else
     return fail(c, WAVI_ERR_ARGUMENT, "unknown transform %d", kind);
-  if (r) return r;
+  CKL();
   CK(cudaStreamSynchronize(c->st));
   return 0;
 }

@@ -35,7 +35,7 @@ ALL_FIELDS = abi.FIELD_INPUTS + abi.FIELD_STATE + ("wu_mask", "wv_mask", "wu_cor
 class VelocitySolver:
     """One GPU velocity-solve context (``wavi_ctx``) for a fixed grid and solver parameters."""
 
-    def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=False, picard_test=0):
+    def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0):
         self.lib = abi.load_library()
         self.grid = grid
         self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ

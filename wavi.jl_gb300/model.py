@@ -29,7 +29,7 @@ class GPUParallelSpec:
     src/WAVI.jl:17).  Plain data only, so a saved model never holds a device handle."""
     device: int = 0
     precision: str = "fp64"     # "fp64" (reference algorithm) or "mixed"
-    use_graphs: bool = False
+    use_graphs: bool = True
     picard_test: int = 0
 
 

@@ -39,6 +39,26 @@ def noisy_thickness(shape, seed, mean=300.0, rel=0.05):
     return np.asfortranarray(mean * (1.0 + rng.uniform(-rel, rel, size=shape)))
 
 
+def coarse_noise(shape, seed, coarse=(80, 10), rel=0.05):
+    """Uniform ±rel noise drawn on a coarse (80 x 10, i.e. 8 km) grid over the same 640 x 80 km domain
+    and interpolated bilinearly to the cell centres of ``shape``: the 8 km thickness field refined."""
+    rng = np.random.default_rng(seed)
+    z = rng.uniform(-rel, rel, size=coarse)
+    nx, ny = shape
+    cx, cy = coarse
+    xs = (np.arange(nx) + 0.5) * cx / nx - 0.5
+    ys = (np.arange(ny) + 0.5) * cy / ny - 0.5
+    x0 = np.clip(np.floor(xs).astype(int), 0, cx - 1)
+    y0 = np.clip(np.floor(ys).astype(int), 0, cy - 1)
+    x1 = np.clip(x0 + 1, 0, cx - 1)
+    y1 = np.clip(y0 + 1, 0, cy - 1)
+    fx = np.clip(xs - x0, 0.0, 1.0)[:, None]
+    fy = np.clip(ys - y0, 0.0, 1.0)[None, :]
+    out = ((1 - fx) * (1 - fy) * z[x0][:, y0] + fx * (1 - fy) * z[x1][:, y0] +
+           (1 - fx) * fy * z[x0][:, y1] + fx * fy * z[x1][:, y1])
+    return np.asfortranarray(out)
+
+
 def gaussian_filter_periodic(z, sigma_cells):
     """Gaussian smoothing by FFT (periodic), renormalised to unit variance."""
     nx, ny = z.shape
