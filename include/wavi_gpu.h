@@ -207,6 +207,46 @@ int wavi_op_diagonal_device(wavi_ctx* ctx, int precision, void* diag_uv);
  * transform of update_wavelets!, default mask = the u/v model masks).  mask_uv may be null.  Test hook. */
 int wavi_haar_device(wavi_ctx* ctx, int kind, const double* in_uv, double* out_uv, const uint8_t* mask_uv);
 
+/* ---------------------------------------------------------------------------------------------------
+ * Allocation-free entry point.  No counterpart in the reference: it exists for callers of this library
+ * that cannot call cudaMalloc — a host framework that owns the device heap through its own pool
+ * allocator, code running under stream capture or inside a callback where allocating is forbidden, or a
+ * service whose device-memory budget is fixed at start-up.  Such a caller already holds the operator's
+ * coefficients and vectors in its own device buffers.
+ * ------------------------------------------------------------------------------------------------- */
+
+/* The linearised momentum operator's coefficients as device arrays (the crops of
+ * update_rheological_operators! folded in): heta_h = h_mask*h*ηav (nx*ny), heta_c = c_mask*cent_xy(h*ηav)
+ * ((nx-1)*(ny-1)), dimp = h_mask*(-ρ_i g θ dt dsdh) (nx*ny), beta_m = mask*βeff and h_m = mask*h on
+ * [u | v] (the u and v grids concatenated), inner = the interior mask on [u | v] (one byte per point). */
+typedef struct wavi_operator_desc {
+  int32_t nx, ny;
+  double dx, dy;
+  const double* heta_h;
+  const double* heta_c;
+  const double* dimp;
+  const double* beta_m;
+  const double* h_m;
+  const uint8_t* inner;
+} wavi_operator_desc;
+
+/* Largest grid wavi_residual_noalloc accepts: (nx+1)*(ny+1) split into tiles of 32 x 8 points must
+ * need at most this many tiles (about 4.19 million points, e.g. 2560 x 320 fits). */
+#define WAVI_NOALLOC_MAX_TILES 16384
+
+/* r = b - A x (float64) and rr_out[0] = ||r||^2, allocating nothing.  x_uv, b_uv, r_uv are device
+ * vectors [u (nx+1)*ny | v nx*(ny+1)]; r is zero off the interior; rr_out is a device pointer.  The work
+ * is queued on `stream` (a cudaStream_t, null for the legacy default stream) and not waited for.
+ * The reduction scratch is a fixed static device array of 2*WAVI_NOALLOC_MAX_TILES+32 doubles
+ * (about 256 KiB) that every device loading the library keeps until the process exits; grids beyond
+ * WAVI_NOALLOC_MAX_TILES tiles are rejected with WAVI_ERR_ARGUMENT and a message in
+ * wavi_last_error(NULL).  The first call on each device looks up that array's device address (with the
+ * device current) and caches it: make that first call before any stream capture.  Every call shares the
+ * one array (its counter is cleared at the start of each call), so calls that overlap on the GPU — on
+ * different streams, or from different host threads — race and must be ordered by the caller. */
+int wavi_residual_noalloc(const wavi_operator_desc* op, const double* x_uv, const double* b_uv, double* r_uv,
+                          double* rr_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,16 @@ class Stats(C.Structure):
                 ("kernel_launches", C.c_int32), ("host_syncs", C.c_int32)]
 
 
+class OperatorDesc(C.Structure):
+    """wavi_operator_desc: device coefficient arrays of the linearised operator (wavi_residual_noalloc)."""
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("dx", C.c_double), ("dy", C.c_double),
+                ("heta_h", C.c_void_p), ("heta_c", C.c_void_p), ("dimp", C.c_void_p), ("beta_m", C.c_void_p),
+                ("h_m", C.c_void_p), ("inner", C.c_void_p)]
+
+
+NOALLOC_MAX_TILES = 16384
+
+
 class WaviError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"{STATUS.get(status, status)}: {message}")
@@ -112,6 +122,7 @@ def load_library(path=None):
         "wavi_apply_operator_device": (C.c_int, [vp, C.c_int, vp, vp]),
         "wavi_op_diagonal_device": (C.c_int, [vp, C.c_int, vp]),
         "wavi_haar_device": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+        "wavi_residual_noalloc": (C.c_int, [C.POINTER(OperatorDesc), vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

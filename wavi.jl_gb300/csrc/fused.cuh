@@ -210,7 +210,7 @@ __device__ __forceinline__ void haar_tile(TT (*tile)[TILE + 1], int levels, int 
 // Picard-level kernels
 // ------------------------------------------------------------------------------------------------
 // Right-hand side, start guess, Dirichlet values, and |b|^2 (last block -> st->bb).
-__global__ void k_rhs_fused(Dims d, RhsIn in, const DevParams* __restrict__ P, double* __restrict__ b,
+static __global__ void k_rhs_fused(Dims d, RhsIn in, const DevParams* __restrict__ P, double* __restrict__ b,
                             double* __restrict__ x, double* __restrict__ xfixed, double* __restrict__ partials,
                             DevState* st) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -635,7 +635,7 @@ __global__ void k_vcycle_finish(int n, const uint8_t* __restrict__ inner, const 
 }
 
 // Solve start: zero the counters and flags.
-__global__ void k_state_init(DevState* st) {
+static __global__ void k_state_init(DevState* st) {
   if (threadIdx.x == 0) {
     DevState z = {};
     z.rel = INFINITY;

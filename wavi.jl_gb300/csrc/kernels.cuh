@@ -83,7 +83,7 @@ __device__ __forceinline__ double block_sum_2d(double v, double* sh) {
 }
 
 // Sum partials[0..n) into *out (one block, fixed order).
-__global__ void k_reduce(const double* __restrict__ partials, int n, double* __restrict__ out) {
+static __global__ void k_reduce(const double* __restrict__ partials, int n, double* __restrict__ out) {
   __shared__ double sh[32];
   double s = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) s += partials[i];
@@ -360,7 +360,7 @@ struct RelinUVOut {
   double *beta_m64, *h_m64, *heta_c64;
   float *beta_m32, *h_m32, *heta_c32;
 };
-__global__ void k_relin_uv(Dims d, RelinUVIn in, RelinUVOut out) {
+static __global__ void k_relin_uv(Dims d, RelinUVIn in, RelinUVOut out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   auto hmk = [&](int a, int b) { return (a >= 0 && a < d.nx && b >= 0 && b < d.ny && in.h_mask[hidx(d, a, b)]) ? 1.0 : 0.0; };
   auto hv = [&](const double* f, int a, int b) {
@@ -419,7 +419,7 @@ struct RhsIn {
   const double* uv;
   double rho_i, rho_w, g, sea_level, theta_dt;
 };
-__global__ void k_rhs(Dims d, RhsIn in, double* __restrict__ b, double* __restrict__ x, double* __restrict__ xfixed) {
+static __global__ void k_rhs(Dims d, RhsIn in, double* __restrict__ b, double* __restrict__ x, double* __restrict__ xfixed) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   auto sadj = [&](int a, int c) -> double {
     if (a < 0 || a >= d.nx || c < 0 || c >= d.ny) return 0.0;
@@ -626,7 +626,7 @@ __global__ void k_cg_dir(int n, const double* __restrict__ S, const int* __restr
     u[k] = (T)((double)r[k] + beta * (double)u[k]);
 }
 // α = |r|^2 / <u, c>  (reduces the partials of <u,c> itself; one block)
-__global__ void k_cg_alpha(const double* __restrict__ partials, int np, double* __restrict__ S, const int* __restrict__ I) {
+static __global__ void k_cg_alpha(const double* __restrict__ partials, int np, double* __restrict__ S, const int* __restrict__ I) {
   if (I[CG_DONE]) return;
   __shared__ double sh[32];
   double s = 0.0;
@@ -652,7 +652,7 @@ __global__ void k_cg_axpy(int n, const double* __restrict__ S, const int* __rest
   if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 // prev = res; res = |r|; it++; done = it >= maxiter || res <= tol  (one block)
-__global__ void k_cg_res(const double* __restrict__ partials, int np, double* __restrict__ S, int* __restrict__ I) {
+static __global__ void k_cg_res(const double* __restrict__ partials, int np, double* __restrict__ S, int* __restrict__ I) {
   if (I[CG_DONE]) return;
   __shared__ double sh[32];
   double s = 0.0;
@@ -668,7 +668,7 @@ __global__ void k_cg_res(const double* __restrict__ partials, int np, double* __
   }
 }
 // out = sqrt(*in)
-__global__ void k_sqrt_slot(const double* __restrict__ in, double* __restrict__ out) { *out = sqrt(*in); }
+static __global__ void k_sqrt_slot(const double* __restrict__ in, double* __restrict__ out) { *out = sqrt(*in); }
 // CG start: r = b - c (c = A x0), |r|, tol = max(reltol |r0|, abstol), abstol = tol_coarse |b|
 template <typename T>
 __global__ void k_cg_start_sub(int n, const T* __restrict__ b, const T* __restrict__ c, T* __restrict__ r, T* __restrict__ u,
@@ -684,7 +684,7 @@ __global__ void k_cg_start_sub(int n, const T* __restrict__ b, const T* __restri
   s = block_sum(s, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
-__global__ void k_cg_start_scalars(const double* __restrict__ partials, int np, double tol_coarse, int maxiter,
+static __global__ void k_cg_start_scalars(const double* __restrict__ partials, int np, double tol_coarse, int maxiter,
                                    double* __restrict__ S, int* __restrict__ I) {
   __shared__ double sh[32];
   double s = 0.0;

@@ -609,6 +609,11 @@ int check_params(wavi_ctx* c, const wavi_params* p) {
 
 }  // namespace
 
+namespace wavi {
+// Errors of entry points that have no context (wavi_ctx_create, wavi_residual_noalloc).
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace wavi
+
 // ---------------------------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------------------------
