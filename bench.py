@@ -1,10 +1,11 @@
 """Benchmark: converged velocity solves/s on the 640 x 80 (1 km, nσ = 4) synthetic channel.
 
-One step = one Picard-converged velocity solve (update_velocities!) of the seeded channel whose
-300 m thickness carries a 5 % perturbation correlated at 8 km (seed 2), from the model's initial state
-(u = 0, default viscosity, the reference's initial all-true wavelet coarse space) after the update_state!
-steps that precede the solve.  Every step restores that state and solves it to
-||b - A u|| / ||b|| < 1e-6 (maxiter_picard = 100; the reference's other solver parameters).
+One step = one Picard-converged velocity solve (update_velocities!) of the seeded 8 km channel refined
+to 1 km (MISMIP+ bed with 20 m roughness, 300 m thickness with a 5 % perturbation, both drawn on the
+8 km grid and interpolated), from the model's initial state (u = 0, default viscosity, the reference's
+initial all-true wavelet coarse space) after the update_state! steps that precede the solve.  Every
+step restores that state and solves it to ||b - A u|| / ||b|| < 1e-6 (maxiter_picard = 100; the
+reference's other solver parameters).
 
   value    mixed precision (float32 operator / V-cycle, float64 residual and reductions), fields resident
            in HBM, device time per step from CUDA events on the solver's stream, L2 flushed between steps
@@ -34,7 +35,7 @@ import __graft_entry__  # noqa: E402
 
 TOL_PICARD = 1e-6
 MAXITER_PICARD = 100
-WORKLOAD = ("channel 640x80 @1km nsigma=4, 5% (8 km-correlated) thickness perturbation, Picard-converged solve "
+WORKLOAD = ("8 km channel refined to 640x80 @1km, nsigma=4, 5% thickness perturbation, Picard-converged solve "
             "from the initial state to rel. residual < 1e-6")
 METRIC = "converged velocity solves/s (640x80 channel, mixed precision)"
 
@@ -46,27 +47,17 @@ def dist_info():
     return rank, world, local
 
 
-def build_state(pkg, warm=False):
-    """The C2 state right before the timed solve (host numpy fields).
-
-    Thickness: 300 m with a 5 % seeded perturbation correlated at 8 km (the 80 x 10 field refined,
-    seed 2).  The solve starts from the model's initial state (u = 0, default viscosity, the reference's
-    initial all-true wavelet coarse space, UWavelets.jl:38), after the update_state! steps that precede
-    the velocity solve.  With warm = True it starts instead from the converged velocities of the
-    unperturbed thickness, keeping the all-true coarse space.
-    """
+def build_state(pkg):
+    """The state right before the timed solve (host numpy fields): the 8 km channel refined to 1 km —
+    MISMIP+ bed with 20 m roughness and 300 m thickness with a 5 % perturbation, both drawn on the 8 km
+    template grid (seeds 0 and 1) and interpolated — at the model's initial state (u = 0, default
+    viscosity, the reference's initial all-true wavelet coarse space, UWavelets.jl:38), after the
+    update_state! steps that precede the velocity solve."""
     from wavi_gb300 import synthetic
-    from wavi_gb300.model import GPUParallelSpec, Model, pre_solve, update_velocities
+    from wavi_gb300.model import GPUParallelSpec, Model, pre_solve
     g, bed, p, sp, ic = synthetic.channel_c2(tol_picard=TOL_PICARD, maxiter_picard=MAXITER_PICARD)
-    base = ic.initial_thickness.copy(order="F")
-    pert = np.asfortranarray(300.0 * (1.0 + synthetic.coarse_noise((g.nx, g.ny), 2)))
-    ic.initial_thickness = base if warm else pert
     m = Model(g, bed, p, sp, ic, parallel_spec=GPUParallelSpec(precision="fp64"))
     pre_solve(m)
-    if warm:
-        update_velocities(m)
-        m.fields["h"][...] = pert
-        pre_solve(m)
     return m
 
 
@@ -256,7 +247,6 @@ def cpu_sample(threads, picard_iters_sample=1, state=None):
 
     def make():
         g, bed, p, sp, ic = synthetic.channel_c2(tol_picard=TOL_PICARD, maxiter_picard=MAXITER_PICARD)
-        ic.initial_thickness = np.asfortranarray(300.0 * (1.0 + synthetic.coarse_noise((g.nx, g.ny), 2)))
         om = oracle.build_model(g, bed, p, sp, ic)
         return om, g, p, sp
 

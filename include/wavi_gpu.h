@@ -94,6 +94,10 @@ typedef struct wavi_options {
   int32_t use_graphs;                /* 1: capture each Picard iteration in a CUDA graph */
   int32_t picard_test;               /* 0: reference residual test ||b-Au||/||b|| < tol_picard;
                                         1: additionally require ||du||/||u|| <= tol_picard */
+  int32_t coarse_kernel;             /* coarse CG: 0 = one persistent kernel per V-cycle when the grid's
+                                        tiles fit the device's resident CTAs, else per-iteration kernels;
+                                        1 = persistent (error if it does not fit); 2 = per-iteration */
+  int32_t reserved0;
 } wavi_options;
 
 /* The model fields the velocity solve reads and writes (src/Models/update_velocities.jl:202-383,

@@ -197,16 +197,71 @@ struct Kron {
 };
 Kron kron(const Op1D& a, const Op1D& b) { return Kron{a, b, {}}; }
 
-double norm2(const Vec& x) {
-  double s = 0.0;
-  for (double v : x) s += v * v;
-  return std::sqrt(s);
+// Summation order of the coarse CG's norms and dot products.  The reference calls BLAS for both
+// (LinearAlgebra `dot` -> BLAS.dot; `norm` -> BLAS.nrm2 for length >= 32), and a coarse CG of hundreds of
+// iterations is sensitive to that order at the 1e-5 level, which a 1000-step coupled run carries to its
+// end.  Orders 2 and 3 restate the x86-64 OpenBLAS kernels Julia ships: ddot with fused multiply-add
+// lanes (order 2: four 4-wide accumulators over blocks of 16, the AVX2 shape; order 3, the default:
+// four 8-wide accumulators over blocks of 32, the AVX-512 shape), accumulators combined pairwise, the
+// remainder added left to right; dnrm2 accumulated in extended precision.  Order 3 reproduces the
+// reference's v1.8.3 golden file within its own tolerance (Julia's isapprox, rtol = sqrt(eps)), so that
+// file was made on an AVX-512 machine.  Order 0 is a plain left-to-right sum; order 1 blocked partial
+// sums of 64.
+int g_sum_order = 3;
+
+double dot_openblas_x86(const double* a, const double* b, size_t n) {
+  const size_t n1 = n & ~(size_t)15;
+  double lane[16] = {0.0};
+  for (size_t i = 0; i < n1; i += 16)
+    for (int l = 0; l < 16; ++l) lane[l] = std::fma(a[i + l], b[i + l], lane[l]);
+  double acc[4];
+  for (int l = 0; l < 4; ++l) acc[l] = (lane[l] + lane[4 + l]) + (lane[8 + l] + lane[12 + l]);
+  double dot = n1 ? (acc[0] + acc[2]) + (acc[1] + acc[3]) : 0.0;
+  for (size_t i = n1; i < n; ++i) dot += b[i] * a[i];
+  return dot;
 }
-double dotp(const Vec& a, const Vec& b) {
+
+// The AVX-512 shape of the same kernel: four 8-wide accumulators over blocks of 32.
+double dot_openblas_x86_avx512(const double* a, const double* b, size_t n) {
+  const size_t n1 = n & ~(size_t)31;
+  double lane[32] = {0.0};
+  for (size_t i = 0; i < n1; i += 32)
+    for (int l = 0; l < 32; ++l) lane[l] = std::fma(a[i + l], b[i + l], lane[l]);
+  double acc[8];
+  for (int l = 0; l < 8; ++l) acc[l] = (lane[l] + lane[8 + l]) + (lane[16 + l] + lane[24 + l]);
+  double h4[4], h2[2];
+  for (int l = 0; l < 4; ++l) h4[l] = acc[l] + acc[4 + l];
+  for (int l = 0; l < 2; ++l) h2[l] = h4[l] + h4[2 + l];
+  double dot = n1 ? h2[0] + h2[1] : 0.0;
+  for (size_t i = n1; i < n; ++i) dot += b[i] * a[i];
+  return dot;
+}
+
+double sum_products(const double* a, const double* b, size_t n) {
+  if (g_sum_order == 2) return dot_openblas_x86(a, b, n);
+  if (g_sum_order == 3) return dot_openblas_x86_avx512(a, b, n);
+  if (g_sum_order == 0) {
+    double s = 0.0;
+    for (size_t i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+  }
   double s = 0.0;
-  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  for (size_t k = 0; k < n; k += 64) {
+    double p = 0.0;
+    for (size_t i = k; i < std::min(n, k + 64); ++i) p += a[i] * b[i];
+    s += p;
+  }
   return s;
 }
+double norm2(const Vec& x) {
+  if (g_sum_order >= 2 && x.size() >= 32) {
+    long double s[4] = {0.0L, 0.0L, 0.0L, 0.0L};
+    for (size_t i = 0; i < x.size(); ++i) s[i & 3] += (long double)x[i] * (long double)x[i];
+    return (double)std::sqrt((s[0] + s[1]) + (s[2] + s[3]));
+  }
+  return std::sqrt(sum_products(x.data(), x.data(), x.size()));
+}
+double dotp(const Vec& a, const Vec& b) { return sum_products(a.data(), b.data(), a.size()); }
 
 // ---------------------------------------------------------------------------------------------
 // Model state.  src/Fields/*.jl, src/Models/Model.jl:1-9
@@ -1067,6 +1122,7 @@ void* oracle_create(const wavi_grid_desc* g, const wavi_params* p, const wavi_so
   return m;
 }
 void oracle_destroy(void* h) { delete static_cast<Model*>(h); }
+void oracle_set_sum_order(int order) { g_sum_order = order; }
 
 // Pointer to a float64 field (length written to *len), or null for an unknown name.
 double* oracle_field(void* h, const char* name, int64_t* len) {

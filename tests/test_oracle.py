@@ -55,15 +55,19 @@ def _mismip_golden_model(oracle, pkg):
     return oracle.build_model(g, lambda x, y: float(mismip_plus_bed(x, y)), p, sp)
 
 
-# Agreement the restatement reaches with the v1.8.3 golden file after 1000 coupled solves (the
-# reference's own test asks for Julia's isapprox, rtol 1.5e-8).  The measured gaps are u 1.2e-4,
-# bed_speed 1.2e-4, ηav 3.0e-4, v 2.3e-5, grounded fraction 2.5e-5, h 7.3e-6; a 1e-12 input perturbation
-# moves the result by only 2e-9, so the gap is a small systematic difference (the golden file may predate
-# the current sources; IterativeSolvers.jl is unpinned), not rounding.  Other Julia versions' goldens
-# differ from v1.8.3 by 16 % in u and are not used.
-GOLDEN_TOL = {"h": 2e-5, "u": 2.5e-4, "v": 5e-5, "viscosity": 5e-4, "grounded_fraction": 5e-5, "bed_speed": 2.5e-4}
+# The reference's own test (test_version_updates.jl:90-97) asks for Julia's isapprox: norm(a - b) <=
+# sqrt(eps) * max(norm(a), norm(b)).  The oracle meets it on every field once its coarse-CG dot products
+# and norms follow the summation order of the OpenBLAS kernels Julia calls (wavi_oracle.cpp, g_sum_order):
+# a coarse CG of hundreds of iterations carries that order into a 1e-5 difference that 1000 coupled solves
+# keep.  Other Julia versions' golden files differ from v1.8.3 by 16 % in u and are not used.
+RTOL_JULIA = float(np.sqrt(np.finfo(np.float64).eps))
 GOLDEN_KEYS = {"h": "h", "u": "u", "v": "v", "viscosity": "eta_av", "grounded_fraction": "grounded_fraction",
                "bed_speed": "bed_speed"}
+
+
+def isapprox(a, b, rtol=RTOL_JULIA):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.linalg.norm(a - b) <= rtol * max(np.linalg.norm(a), np.linalg.norm(b))
 
 
 def test_mismip_golden_1000_steps(oracle, pkg):
@@ -72,7 +76,7 @@ def test_mismip_golden_1000_steps(oracle, pkg):
     gold = np.load(os.path.join(HERE, "golden", "mismip_100yr_v1_8_3.npz"))
     for name, key in GOLDEN_KEYS.items():
         r = np.linalg.norm(m.field(key) - gold[name]) / np.linalg.norm(gold[name])
-        assert r < GOLDEN_TOL[name], (name, r)
+        assert isapprox(m.field(key), gold[name]), (name, r)
 
 
 def test_operator_symmetric_negative_definite(oracle, pkg):

@@ -30,6 +30,7 @@
 #include "../../include/wavi_gpu.h"
 #include "kernels.cuh"
 #include "fused.cuh"
+#include "persistent.cuh"
 
 using namespace wavi;
 
@@ -83,6 +84,9 @@ struct wavi_ctx {
   // launch shapes
   dim3 op_grid, op_block, pt_grid, pt_block, haar_grid, haar_block, tile_grid, tile_block;
   int ew_blocks = 0;
+  // persistent coarse CG: grid barrier, launch shape, tiles per CTA (0 = per-iteration kernels)
+  GridBar* bar = nullptr;
+  int pers_maxt = 0, pers_grid = 0, ntx = 0, nty = 0;
   // solve graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -210,7 +214,7 @@ int enqueue_picard_head(wavi_ctx* c, const CondHandles& h, Tally& t) {
 }
 
 template <typename T, int TILE>
-int enqueue_vcycle_pre(wavi_ctx* c, const CondHandles& h, Tally& t) {
+int enqueue_vcycle_pre(wavi_ctx* c, const CondHandles& h, Tally& t, bool cg_start = true) {
   const Dims& d = c->d;
   const int L = c->sp.levels;
   T* rs = (T*)c->rs;
@@ -237,6 +241,12 @@ int enqueue_vcycle_pre(wavi_ctx* c, const CondHandles& h, Tally& t) {
   k_restrict_norm<T, TILE><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, L, rsm[cur], c->wmask_uv, (T*)c->bc,
                                                                       c->partials, c->S);
   CKL();
+  if (cur != 0) return fail(c, WAVI_ERR_ARGUMENT, "internal: smoother parity");
+  if (!cg_start) {  // the persistent coarse CG computes its own start
+    t.launches++;
+    t.bytes += 2.0 * sizeof(T) * d.N + d.N;
+    return 0;
+  }
   // r_c = b_c - R A P xc, u_c = 0, CG scalars
   k_prolong<T, TILE, 0><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, L, c->inner_uv, (const T*)c->xc, (T*)c->w,
                                                                    nullptr, nullptr, c->S, nullptr);
@@ -248,7 +258,6 @@ int enqueue_vcycle_pre(wavi_ctx* c, const CondHandles& h, Tally& t) {
   t.launches += 3;
   t.ops++;
   t.bytes += op_bytes(d, sizeof(T), false) + 8.0 * sizeof(T) * d.N + 3.0 * d.N;
-  if (cur != 0) return fail(c, WAVI_ERR_ARGUMENT, "internal: smoother parity");
   return 0;
 }
 
@@ -269,6 +278,47 @@ int enqueue_cg_iteration(wavi_ctx* c, const CondHandles& h, int* live, Tally& t)
   t.launches += 3;
   t.ops++;
   t.bytes += op_bytes(d, sizeof(T), false) + sizeof(T) * (4.0 * d.N + 6.0 * d.N) + 2.0 * d.N;
+  return 0;
+}
+
+// The whole coarse CG as one cooperative persistent kernel (persistent.cuh), then the watchdog check.
+template <typename T, int TILE, int MAXT>
+int launch_cg_persistent(wavi_ctx* c) {
+  const Dims& d = c->d;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)c->pers_grid);
+  cfg.blockDim = dim3(TILE, TILE);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, k_cg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
+                        (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar, c->ntx,
+                        c->nty));
+  c->launches++;
+  return 0;
+}
+
+template <typename T, int TILE>
+int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& tc) {
+  const Dims& d = c->d;
+  k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar);
+  CKL();
+  if (c->pers_maxt == 1)
+    TRY((launch_cg_persistent<T, TILE, 1>(c)));
+  else if (c->pers_maxt == 2)
+    TRY((launch_cg_persistent<T, TILE, 2>(c)));
+  else
+    TRY((launch_cg_persistent<T, TILE, 4>(c)));
+  k_check_barrier<<<1, 32, 0, c->st>>>(c->bar, c->S, h);
+  CKL();
+  tv.launches += 3;
+  tv.ops++;  // the start's R A P xc
+  tc.ops++;
+  tc.bytes += op_bytes(d, sizeof(T), false) + sizeof(T) * 2.0 * d.N + d.N;
   return 0;
 }
 
@@ -325,7 +375,11 @@ int enqueue_all_host_driven(wavi_ctx* c) {
     CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     c->host_syncs++;
-    if (c->hS->vcycle_needed) {
+    if (c->hS->vcycle_needed && c->pers_maxt > 0) {
+      TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
+      TRY((enqueue_cg_persistent<T, TILE>(c, h, tv, tc)));
+      TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
+    } else if (c->hS->vcycle_needed) {
       TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv)));
       CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
       CK(cudaStreamSynchronize(c->st));
@@ -405,18 +459,27 @@ int build_graph(wavi_ctx* c) {
   TRY(enqueue_picard_head(c, h, tp));
   TRY(end_capture(c, pbody, sinks));
   TRY(add_conditional(c, pbody, sinks, h.vcycle, cudaGraphCondTypeIf, &vbody, &vnode));
-  CK(cudaGraphConditionalHandleCreate(&h.cg, vbody, 0, cudaGraphCondAssignDefault));
-  // V-cycle body: pre part, WHILE(cg), post part
-  TRY(begin_capture(c, vbody, {}));
-  TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv)));
-  TRY(end_capture(c, vbody, sinks));
-  TRY(add_conditional(c, vbody, sinks, h.cg, cudaGraphCondTypeWhile, &cbody, &cnode));
-  TRY(begin_capture(c, cbody, {}));
-  TRY((enqueue_cg_iteration<T, TILE>(c, h, nullptr, tc)));
-  TRY(end_capture(c, cbody, sinks));
-  TRY(begin_capture(c, vbody, {cnode}));
-  TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
-  TRY(end_capture(c, vbody, sinks));
+  if (c->pers_maxt > 0) {
+    // V-cycle body: pre part, one persistent coarse-CG kernel, post part
+    TRY(begin_capture(c, vbody, {}));
+    TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
+    TRY((enqueue_cg_persistent<T, TILE>(c, h, tv, tc)));
+    TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
+    TRY(end_capture(c, vbody, sinks));
+  } else {
+    CK(cudaGraphConditionalHandleCreate(&h.cg, vbody, 0, cudaGraphCondAssignDefault));
+    // V-cycle body: pre part, WHILE(cg), post part
+    TRY(begin_capture(c, vbody, {}));
+    TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv)));
+    TRY(end_capture(c, vbody, sinks));
+    TRY(add_conditional(c, vbody, sinks, h.cg, cudaGraphCondTypeWhile, &cbody, &cnode));
+    TRY(begin_capture(c, cbody, {}));
+    TRY((enqueue_cg_iteration<T, TILE>(c, h, nullptr, tc)));
+    TRY(end_capture(c, cbody, sinks));
+    TRY(begin_capture(c, vbody, {cnode}));
+    TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
+    TRY(end_capture(c, vbody, sinks));
+  }
   CK(cudaGraphInstantiate(&c->exec, top, 0));
   c->launches = saved;
   c->picard_head_bytes = tp.bytes;
@@ -429,6 +492,35 @@ int build_graph(wavi_ctx* c) {
   c->cg_iter_launches = tc.launches;
   c->cg_iter_ops = tc.ops;
   return 0;
+}
+
+// Persistent coarse CG: the smallest tiles-per-CTA (1, 2, 4) for which every CTA of the launch is
+// resident at once (the cooperative launch needs that); 0 if none fits.
+template <int MAXT, typename T, int TILE>
+int resident_ctas(int nsm) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent<T, TILE, MAXT>, TILE * TILE, 0) != cudaSuccess)
+    return 0;
+  return per_sm * nsm;
+}
+template <typename T, int TILE>
+void choose_persistent(wavi_ctx* c) {
+  c->pers_maxt = 0;
+  int nsm = 0, coop = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->dev);
+  if (!coop || nsm <= 0) return;
+  const long ntiles = (long)c->ntx * c->nty;
+  const int caps[3] = {resident_ctas<1, T, TILE>(nsm), resident_ctas<2, T, TILE>(nsm), resident_ctas<4, T, TILE>(nsm)};
+  const int maxts[3] = {1, 2, 4};
+  for (int k = 0; k < 3; ++k) {
+    const long g = (ntiles + maxts[k] - 1) / maxts[k];
+    if (caps[k] > 0 && g <= caps[k]) {
+      c->pers_maxt = maxts[k];
+      c->pers_grid = (int)g;
+      return;
+    }
+  }
 }
 
 int ensure_graph(wavi_ctx* c) {
@@ -750,6 +842,17 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   const int haar_blocks = (int)(c->haar_grid.x * c->haar_grid.y * c->haar_grid.z);
   c->max_partials = 2 * std::max({pt_blocks, op_blocks, tile_blocks, haar_blocks, c->ew_blocks, 1});
   if ((r = dalloc(c, &c->partials, (size_t)c->max_partials))) return bail(r);
+  if ((r = dalloc(c, &c->bar, 1))) return bail(r);
+  c->ntx = (int)c->tile_grid.x;
+  c->nty = (int)c->tile_grid.y;
+  if (opt->coarse_kernel != 2) {
+    if (mixed(c))
+      c->tile == 16 ? choose_persistent<float, 16>(c) : choose_persistent<float, 32>(c);
+    else
+      c->tile == 16 ? choose_persistent<double, 16>(c) : choose_persistent<double, 32>(c);
+    if (opt->coarse_kernel == 1 && c->pers_maxt == 0)
+      return bail(fail(c, WAVI_ERR_ARGUMENT, "the persistent coarse CG does not fit this grid on this device"));
+  }
   if ((r = dalloc(c, &c->P, 1))) return bail(r);
   if ((r = dalloc(c, &c->S, 1))) return bail(r);
   if (cudaMallocHost(&c->hP, sizeof(DevParams)) != cudaSuccess || cudaMallocHost(&c->hS, sizeof(DevState)) != cudaSuccess)

@@ -35,7 +35,10 @@ ALL_FIELDS = abi.FIELD_INPUTS + abi.FIELD_STATE + ("wu_mask", "wv_mask", "wu_cor
 class VelocitySolver:
     """One GPU velocity-solve context (``wavi_ctx``) for a fixed grid and solver parameters."""
 
-    def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0):
+    COARSE_KERNELS = {"auto": 0, "persistent": 1, "iterations": 2}
+
+    def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0,
+                 coarse_kernel="auto"):
         self.lib = abi.load_library()
         self.grid = grid
         self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ
@@ -43,7 +46,8 @@ class VelocitySolver:
         self.precision = precision
         self._desc = grid.descriptor()
         self._sp = solver_params.to_c()
-        self._opt = abi.Options(int(device), PRECISIONS[precision], 1 if use_graphs else 0, int(picard_test))
+        self._opt = abi.Options(int(device), PRECISIONS[precision], 1 if use_graphs else 0, int(picard_test),
+                                self.COARSE_KERNELS[coarse_kernel], 0)
         ctx = C.c_void_p()
         st = self.lib.wavi_ctx_create(C.byref(self._desc.desc), C.byref(self._sp), C.byref(self._opt), C.byref(ctx))
         if st != 0:

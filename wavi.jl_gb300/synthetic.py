@@ -39,24 +39,6 @@ def noisy_thickness(shape, seed, mean=300.0, rel=0.05):
     return np.asfortranarray(mean * (1.0 + rng.uniform(-rel, rel, size=shape)))
 
 
-def coarse_noise(shape, seed, coarse=(80, 10), rel=0.05):
-    """Uniform ±rel noise drawn on a coarse (80 x 10, i.e. 8 km) grid over the same 640 x 80 km domain
-    and interpolated bilinearly to the cell centres of ``shape``: the 8 km thickness field refined."""
-    rng = np.random.default_rng(seed)
-    z = rng.uniform(-rel, rel, size=coarse)
-    nx, ny = shape
-    cx, cy = coarse
-    xs = (np.arange(nx) + 0.5) * cx / nx - 0.5
-    ys = (np.arange(ny) + 0.5) * cy / ny - 0.5
-    x0 = np.clip(np.floor(xs).astype(int), 0, cx - 1)
-    y0 = np.clip(np.floor(ys).astype(int), 0, cy - 1)
-    x1 = np.clip(x0 + 1, 0, cx - 1)
-    y1 = np.clip(y0 + 1, 0, cy - 1)
-    fx = np.clip(xs - x0, 0.0, 1.0)[:, None]
-    fy = np.clip(ys - y0, 0.0, 1.0)[None, :]
-    out = ((1 - fx) * (1 - fy) * z[x0][:, y0] + fx * (1 - fy) * z[x1][:, y0] +
-           (1 - fx) * fy * z[x0][:, y1] + fx * fy * z[x1][:, y1])
-    return np.asfortranarray(out)
 
 
 def gaussian_filter_periodic(z, sigma_cells):
@@ -83,12 +65,51 @@ def channel_case(nx, ny, dx, ns, seed_bed=0, seed_h=1, tol_picard=1e-5, maxiter_
     the reference temperature), Weertman m = 3, C = 1e4 (or a per-cell field), accumulation 0.3 m/yr.
     """
     g = _grid(nx, ny, dx, ns)
-    bed = channel_bed(g, seed=seed_bed, xscale=(640000.0 / (nx * dx)), yscale=(80000.0 / (ny * dx)))
+    bed = refined_channel_bed(g, seed=seed_bed)
     p = Params(accumulation_rate=accumulation, glen_a_ref=2.0e-17, weertman_c=C, default_temperature=263.15)
     sp = SolverParams(tol_picard=tol_picard, maxiter_picard=maxiter_picard)
-    ic = InitialConditions(initial_thickness=noisy_thickness((nx, ny), seed_h),
+    ic = InitialConditions(initial_thickness=np.asfortranarray(300.0 * (1.0 + template_field((nx, ny), seed_h, "uniform"))),
                            initial_temperature=temperature)
     return g, bed, p, sp, ic
+
+
+TEMPLATE = (80, 10)  # the 8 km channel grid on which every seeded field is drawn
+
+
+def template_field(shape, seed, kind, amplitude=0.05):
+    """A seeded field drawn on the 80 x 10 (8 km) template grid — U(-amplitude, amplitude) ('uniform') or
+    N(0, amplitude) ('normal') per template cell — and interpolated bilinearly to the cell centres of an
+    nx x ny grid covering the same 640 x 80 km.  On the template grid itself it is the raw draw, so the
+    8 km case and its refinements share one geometry."""
+    rng = np.random.default_rng(seed)
+    z = rng.uniform(-amplitude, amplitude, size=TEMPLATE) if kind == "uniform" else amplitude * rng.standard_normal(TEMPLATE)
+    if tuple(shape) == TEMPLATE:
+        return np.asfortranarray(z)
+    return _bilinear(z, shape)
+
+
+def _bilinear(z, shape):
+    nx, ny = shape
+    cx, cy = z.shape
+    xs = (np.arange(nx) + 0.5) * cx / nx - 0.5
+    ys = (np.arange(ny) + 0.5) * cy / ny - 0.5
+    x0 = np.clip(np.floor(xs).astype(int), 0, cx - 1)
+    y0 = np.clip(np.floor(ys).astype(int), 0, cy - 1)
+    x1 = np.clip(x0 + 1, 0, cx - 1)
+    y1 = np.clip(y0 + 1, 0, cy - 1)
+    fx = np.clip(xs - x0, 0.0, 1.0)[:, None]
+    fy = np.clip(ys - y0, 0.0, 1.0)[None, :]
+    out = ((1 - fx) * (1 - fy) * z[x0][:, y0] + fx * (1 - fy) * z[x1][:, y0] +
+           (1 - fx) * fy * z[x0][:, y1] + fx * fy * z[x1][:, y1])
+    return np.asfortranarray(out)
+
+
+def refined_channel_bed(grid, seed=0, roughness=20.0):
+    """The MISMIP+ channel on the grid's h points plus 20 m Gaussian roughness drawn on the 8 km
+    template (seed 0) and refined, re-clipped at -720 m."""
+    b = mismip_plus_bed(grid.xxh * (640000.0 / (grid.nx * grid.dx)), grid.yyh * (80000.0 / (grid.ny * grid.dy)))
+    b = b + template_field((grid.nx, grid.ny), seed, "normal", amplitude=roughness)
+    return np.asfortranarray(np.maximum(b, -720.0))
 
 
 def channel_c1(**kw):
