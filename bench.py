@@ -185,33 +185,33 @@ def time_host_solves(torch, solver, params, snapshot, steps, warmup):
     return times, in_bytes, out_bytes
 
 
-def op_roofline(torch, solver, n_launch=200):
-    """Average duration of the float32 operator kernel alone at the workload size (CUDA events on the
-    solver's stream), against its algorithmic bytes."""
+def op_roofline(torch, solver, n_launch=200, precision="mixed"):
+    """Mean duration of the operator kernel alone at the workload size: n_launch back-to-back launches
+    timed with CUDA events on the solver's stream (wavi_time_operator_device), against its algorithmic
+    bytes: read x, write y, heta_h, dimp (Nh), heta_c (Nc), beta_m, h_m (N) in w-byte words plus the
+    interior mask (N bytes)."""
     d = solver.grid
     nx, ny = d.nx, d.ny
     N = (nx + 1) * ny + nx * (ny + 1)
     Nh, Nc = nx * ny, (nx - 1) * (ny - 1)
-    stream = torch.cuda.ExternalStream(solver.stream())
-    with torch.cuda.stream(stream):
-        x = torch.randn(N, dtype=torch.float32, device="cuda")
-        y = torch.zeros_like(x)
+    w = 4 if precision == "mixed" else 8
+    x = torch.randn(N, dtype=torch.float32 if w == 4 else torch.float64, device="cuda")
+    y = torch.zeros_like(x)
     torch.cuda.synchronize()
-    for _ in range(20):
-        solver.apply_operator_device(x, y, "mixed")
-    # bytes: read x, write y, heta_h, dimp (Nh), heta_c (Nc), beta_m, h_m (N) in float32 + interior mask
-    alg_bytes = 4.0 * (2 * N + 2 * Nh + Nc + 2 * N) + N
-    with torch.cuda.stream(stream):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-    for _ in range(n_launch):
-        solver.apply_operator_device(x, y, "mixed")
-    with torch.cuda.stream(stream):
-        e1.record(stream)
-    e1.synchronize()
-    dur = e0.elapsed_time(e1) / 1e3 / n_launch
+    solver.time_operator_device(x, y, precision, 20)  # warm-up
+    dur = solver.time_operator_device(x, y, precision, n_launch)
+    alg_bytes = w * (2.0 * N + 2.0 * Nh + Nc + 2.0 * N) + N
     return alg_bytes, dur
+
+
+def aggregate_ranks(torch, dist, world, local_seconds, steps, device):
+    """Whole-job throughput: max over ranks of the timed-region time, every rank's steps counted."""
+    total = float(local_seconds)
+    if world > 1:
+        tt = torch.tensor([total], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total = float(tt.item())
+    return world * steps / total, total
 
 
 def measured_peaks():
@@ -333,12 +333,7 @@ def gpu_arm(args):
     torch.cuda.synchronize()
     clocks = clk.summary()
     # max over ranks of the timed-region time
-    total = sum(tmix)
-    if world > 1:
-        tt = torch.tensor([total], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total = float(tt.item())
-    value = world * args.steps / total
+    value, total = aggregate_ranks(torch, dist if world > 1 else None, world, sum(tmix), args.steps, "cuda")
 
     te2e, hb, db = time_host_solves(torch, mixed, p, snapshot, args.steps, max(1, args.warmup // 2))
     e2e_value = world * len(te2e) / sum(te2e)

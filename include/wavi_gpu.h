@@ -97,8 +97,19 @@ typedef struct wavi_options {
   int32_t coarse_kernel;             /* coarse CG: 0 = one persistent kernel per V-cycle when the grid's
                                         tiles fit the device's resident CTAs, else per-iteration kernels;
                                         1 = persistent (error if it does not fit); 2 = per-iteration */
-  int32_t reserved0;
+  int32_t coarse_solver;             /* wavi_coarse_solver */
 } wavi_options;
+
+/* Coarse solve of each V-cycle (R A P x = b_c, update_preconditioners.jl:54-83).  The reference calls
+ * IterativeSolvers cg!; the single-reduction variants (not in the reference; Chronopoulos & Gear 1989)
+ * compute both inner products of an iteration in one grid reduction, keep cg!'s stopping rule on the
+ * unpreconditioned residual, and need the persistent coarse kernel. */
+typedef enum wavi_coarse_solver {
+  WAVI_COARSE_AUTO = 0,              /* FP64: cg!; mixed: SRCG_JACOBI when the persistent kernel fits */
+  WAVI_COARSE_CG = 1,                /* the reference's cg! recurrence */
+  WAVI_COARSE_SRCG = 2,              /* single-reduction CG, no preconditioner (same iterates as cg!) */
+  WAVI_COARSE_SRCG_JACOBI = 3        /* single-reduction CG preconditioned by diag(R A P) */
+} wavi_coarse_solver;
 
 /* The model fields the velocity solve reads and writes (src/Models/update_velocities.jl:202-383,
  * src/Fields/HGrid.jl:1-38, UGrid.jl:1-29, VGrid.jl:1-29, SigmaGrid.jl, Wavelets/UWavelets.jl:2-15).
@@ -201,9 +212,22 @@ int wavi_relinearise_device(wavi_ctx* ctx, const wavi_params* params, wavi_field
  * Test and benchmark hook. */
 int wavi_apply_operator_device(wavi_ctx* ctx, int precision, const void* in_uv, void* out_uv);
 
+/* Benchmark hook: `repeats` back-to-back launches of the operator kernel (as wavi_apply_operator_device)
+ * on the context's stream, timed with CUDA events on that stream; *avg_ms receives the mean duration of
+ * one launch.  No counterpart in the reference. */
+int wavi_time_operator_device(wavi_ctx* ctx, int precision, const void* in_uv, void* out_uv, int repeats,
+                              double* avg_ms);
+
 /* Diagonal of the operator at the interior points (what get_op_diag probes, update_preconditioners.jl
  * :92-109), same vector layout and precision rules as wavi_apply_operator_device.  Test hook. */
 int wavi_op_diagonal_device(wavi_ctx* ctx, int precision, void* diag_uv);
+
+/* diag(R A P) of the coarse operator (restriction R = wavelet-masked Haar analysis of the interior,
+ * prolongation P = its transpose; update_preconditioners.jl:176-193) for the current coefficients and
+ * the wavelet mask of the last solve, on the full wavelet grids (zero off the coarse space); the Jacobi
+ * preconditioner of WAVI_COARSE_SRCG_JACOBI.  No reference counterpart: the reference's coarse
+ * solve is unpreconditioned.  precision as wavi_apply_operator_device. */
+int wavi_coarse_diagonal_device(wavi_ctx* ctx, int precision, void* diag_uv);
 
 /* Haar transforms on float64 device vectors of the [u | v] layout (update_wavelets.jl:38-89):
  * kind 0 = mask ⊙ idwt(in) (prolongation, default mask = interior), kind 1 = mask ⊙ idwtᵀ(in)

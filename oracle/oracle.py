@@ -61,6 +61,8 @@ def lib():
         L.oracle_cg_history.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
         L.oracle_pos_fraction.argtypes = [C.c_int, C.c_int, dp, u8p, dp, dp, dp]
         L.oracle_kron_apply.argtypes = [C.c_int, C.c_int, dp, C.c_int, C.c_int, dp, dp, dp]
+        L.oracle_set_coarse_variant.argtypes = [C.c_int]
+        L.oracle_coarse_diag.argtypes = [vp, dp, dp]
         _lib = L
     return _lib
 
@@ -196,6 +198,22 @@ class OracleModel:
         cu, cv = np.zeros_like(ru), np.zeros_like(rv)
         it = lib().oracle_vcycle(self.h, _dp(ru), _dp(rv), _dp(cu), _dp(cv))
         return cu, cv, it
+
+    def coarse_diag(self):
+        """diag(R A P) on the full wavelet grids (zero off the coarse space)."""
+        du = np.zeros((self.nx + 1, self.ny), order="F")
+        dv = np.zeros((self.nx, self.ny + 1), order="F")
+        lib().oracle_coarse_diag(self.h, _dp(du), _dp(dv))
+        return du, dv
+
+
+COARSE_VARIANTS = {"cg": 0, "srcg": 2, "srcg_jacobi": 3}
+
+
+def set_coarse_variant(name):
+    """Coarse solve of every later oracle V-cycle: the reference's cg! ("cg", the default) or a restatement
+    of one of the GPU library's opt-in coarse solvers."""
+    lib().oracle_set_coarse_variant(COARSE_VARIANTS[name])
 
 
 def pos_fraction(z, mask=None):

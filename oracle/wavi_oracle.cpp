@@ -823,6 +823,92 @@ int coarse_cg(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, doubl
   return it;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Coarse-solve variants that the reference does not have.  They restate the GPU library's opt-in coarse
+// solvers so that those can be checked step for step; the default (0) is the reference's cg!.
+//   0  cg! (coarse_cg above)
+//   2  single-reduction CG (Chronopoulos & Gear, "s-step iterative methods for symmetric linear
+//      systems", J. Comput. Appl. Math. 25 (1989)): the same Krylov iterates in exact arithmetic, with
+//      the two inner products of an iteration computed together after its operator application
+//   3  the same, preconditioned by the Jacobi diagonal of R A P
+// ---------------------------------------------------------------------------------------------
+int g_coarse_variant = 0;
+
+// diag(R A P) by probing: the Haar basis functions of one component, one in-block offset and one parity
+// of the block position are far enough apart (two blocks of 2^(levels+1) points) that A, a nearest-
+// neighbour operator, couples none of them, so one coarse application yields all their diagonal entries.
+Vec coarse_diag(Model& m, OpWork& w, const Precond& p) {
+  const int B = 1 << (m.S.levels + 1);
+  const size_t nu = p.wu_idx.size(), n = nu + p.wv_idx.size();
+  Vec d(n, 0.0), e(n), y;
+  for (int comp = 0; comp < 2; ++comp) {
+    const int nxg = comp == 0 ? m.nx + 1 : m.nx;
+    const size_t k0 = comp == 0 ? 0 : nu, k1 = comp == 0 ? nu : n;
+    for (int oy = 0; oy < B; ++oy)
+      for (int ox = 0; ox < B; ++ox)
+        for (int par = 0; par < 4; ++par) {
+          std::fill(e.begin(), e.end(), 0.0);
+          bool any = false;
+          for (size_t k = k0; k < k1; ++k) {
+            const int q = comp == 0 ? p.wu_idx[k] : p.wv_idx[k - nu], i = q % nxg, j = q / nxg;
+            if (i % B == ox && j % B == oy && (i / B) % 2 == (par & 1) && (j / B) % 2 == (par >> 1)) {
+              e[k] = 1.0;
+              any = true;
+            }
+          }
+          if (!any) continue;
+          op_coarse(m, w, p, e, y);
+          for (size_t k = k0; k < k1; ++k)
+            if (e[k] != 0.0) d[k] = y[k];
+        }
+  }
+  return d;
+}
+
+// Chronopoulos-Gear CG with cg!'s stopping rule on the unpreconditioned residual.  Per iteration:
+//   x += α p;  r -= α s;  z = M⁻¹ r;  w = A z;  γ = (r,z), δ = (w,z), |r|;  stop?
+//   β = γ/γ';  α = γ/(δ - β γ/α');  p = z + β p;  s = w + β s
+// started from r = b - A x, z = M⁻¹ r, w = A z, α = γ/δ, p = z, s = w.
+int coarse_srcg(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, double abstol, int maxiter,
+                bool jacobi) {
+  const size_t n = b.size();
+  Vec minv(n, 1.0);
+  if (jacobi) {
+    Vec d = coarse_diag(m, w, p);
+    for (size_t i = 0; i < n; ++i) minv[i] = d[i] != 0.0 ? 1.0 / d[i] : 0.0;
+  }
+  Vec c, r = b, z(n), wv;
+  op_coarse(m, w, p, x, c);
+  for (size_t i = 0; i < n; ++i) r[i] -= c[i];
+  for (size_t i = 0; i < n; ++i) z[i] = minv[i] * r[i];
+  op_coarse(m, w, p, z, wv);
+  double gamma = dotp(r, z), delta = dotp(wv, z), res = norm2(r);
+  const double reltol = std::sqrt(2.220446049250313e-16);
+  const double tol = std::max(reltol * res, abstol);
+  Vec pp = z, s = wv;
+  double alpha = gamma / delta;
+  int it = 0;
+  bool stop = it >= maxiter || res <= tol || !(res == res) || !(alpha == alpha) || std::isinf(alpha);
+  while (!stop) {
+    for (size_t i = 0; i < n; ++i) x[i] += alpha * pp[i];
+    for (size_t i = 0; i < n; ++i) r[i] -= alpha * s[i];
+    for (size_t i = 0; i < n; ++i) z[i] = minv[i] * r[i];
+    op_coarse(m, w, p, z, wv);
+    ++it;
+    const double g2 = dotp(r, z), d2 = dotp(wv, z);
+    res = norm2(r);
+    stop = it >= maxiter || res <= tol || !(res == res);
+    if (stop) break;
+    const double beta = g2 / gamma;
+    alpha = g2 / (d2 - beta * g2 / alpha);
+    gamma = g2;
+    if (!(alpha == alpha) || std::isinf(alpha)) break;
+    for (size_t i = 0; i < n; ++i) pp[i] = z[i] + beta * pp[i];
+    for (size_t i = 0; i < n; ++i) s[i] = wv[i] + beta * s[i];
+  }
+  return it;
+}
+
 // gauss_seidel_smoother! (4-colour Jacobi with a full residual after each colour)   :133-150
 void smoother(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, const int* order) {
   Vec r;
@@ -846,7 +932,9 @@ void vcycle(Model& m, OpWork& w, Precond& p, Vec& x, const Vec& b) {
   Vec bc;
   restrict_vec(m, p, r, bc);
   double abstol = m.S.tol_coarse * norm2(bc);
-  p.last_cg = coarse_cg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse);
+  p.last_cg = g_coarse_variant == 0
+                  ? coarse_cg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
+                  : coarse_srcg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse, g_coarse_variant == 3);
   Vec pc;
   prolong_vec(m, p, p.corr, pc);
   for (size_t i = 0; i < x.size(); ++i) x[i] = x[i] + pc[i];
@@ -1231,6 +1319,23 @@ int oracle_vcycle(void* h, const double* ru, const double* rv, double* cu, doubl
   for (size_t k = 0; k < p.wu_idx.size(); ++k) m.wu_corr[p.wu_idx[k]] = p.corr[k];
   for (size_t k = 0; k < p.wv_idx.size(); ++k) m.wv_corr[p.wv_idx[k]] = p.corr[p.wu_idx.size() + k];
   return p.last_cg;
+}
+void oracle_set_coarse_variant(int variant) { g_coarse_variant = variant; }
+// diag(R A P) of the model's current linearisation and coarse space, scattered to the full wavelet
+// grids (zero off the coarse space).
+void oracle_coarse_diag(void* h, double* du, double* dv) {
+  Model& m = *static_cast<Model*>(h);
+  OpWork w;
+  Precond p;
+  for (int i = 0; i < m.Nu; ++i)
+    if (m.wu_mask[i]) p.wu_idx.push_back(i);
+  for (int i = 0; i < m.Nv; ++i)
+    if (m.wv_mask[i]) p.wv_idx.push_back(i);
+  Vec d = coarse_diag(m, w, p);
+  std::fill(du, du + m.Nu, 0.0);
+  std::fill(dv, dv + m.Nv, 0.0);
+  for (size_t k = 0; k < p.wu_idx.size(); ++k) du[p.wu_idx[k]] = d[k];
+  for (size_t k = 0; k < p.wv_idx.size(); ++k) dv[p.wv_idx[k]] = d[p.wu_idx.size() + k];
 }
 // statistics of the last update_velocities!
 void oracle_stats(void* h, int* picard, double* rel_resid, int64_t* cg_iters, int64_t* op_applies) {

@@ -1,0 +1,123 @@
+"""The opt-in coarse solvers of the persistent coarse kernel (single-reduction CG, Jacobi-preconditioned
+single-reduction CG) against the oracle's restatements of the same iterations, and the mixed-precision default
+(single-reduction Jacobi) against the reference's FP64 solve.  Through the C ABI."""
+import numpy as np
+import pytest
+
+from helpers import fields_from_oracle, rel, to_dev, uv_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+CASES = {
+    "full": dict(nx=40, ny=16, dx=4000.0, mask="full"),
+    "disc": dict(nx=24, ny=24, dx=4000.0, mask="disc"),
+    "fixed": dict(nx=20, ny=20, dx=5000.0, mask="disc", fixed=True),
+    "ragged": dict(nx=37, ny=13, dx=3000.0, mask="full"),
+}
+
+
+@pytest.fixture
+def reference_cg(oracle):
+    yield
+    oracle.set_coarse_variant("cg")
+
+
+def _setup(oracle, name, **kw):
+    from wavi_gb300 import synthetic
+    c = dict(CASES[name])
+    c.update(kw)
+    g, bed, p, sp, ic = synthetic.small_case(**c)
+    om = oracle.build_model(g, bed, p, sp, ic)
+    om.pre_solve()
+    return g, p, sp, om
+
+
+def _uv(u, v):
+    return np.concatenate([np.asarray(u).ravel(order="F"), np.asarray(v).ravel(order="F")])
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_coarse_diagonal_matches_oracle(oracle, name):
+    """diag(R A P) from the quadratic form (k_coarse_diag) against the oracle's probing, on a coarse space
+    with holes."""
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, name)
+    rng = np.random.default_rng(11)
+    om.field("u")[...] = 50 * rng.standard_normal(om.field("u").shape)
+    om.field("v")[...] = 20 * rng.standard_normal(om.field("v").shape)
+    for m in ("wu_mask", "wv_mask"):
+        om.mask(m)[...] = (rng.uniform(size=om.mask(m).shape) > 0.3).astype(np.uint8)
+    f = fields_from_oracle(om, g)
+    om.inner_update()
+    du, dv = om.coarse_diag()
+    ref = _uv(du, dv)
+    for prec, tol in (("fp64", 1e-12), ("mixed", 2e-5)):
+        s = VelocitySolver(g, sp, precision=prec)
+        s.relinearise_device(p, to_dev(f, torch))
+        d = torch.zeros(ref.size, dtype=torch.float64 if prec == "fp64" else torch.float32, device="cuda")
+        s.coarse_diagonal_device(d, prec)
+        got = d.double().cpu().numpy()
+        assert rel(got, ref) < tol, prec
+        assert np.all(got[ref == 0] == 0), prec
+        s.close()
+
+
+@pytest.mark.parametrize("solver", ["srcg", "srcg_jacobi"])
+@pytest.mark.parametrize("name", list(CASES))
+def test_single_reduction_fixed_cg_count_matches_oracle(oracle, reference_cg, name, solver):
+    """One Picard iteration whose coarse solve runs exactly 10 single-reduction iterations (tol_coarse = 0),
+    in FP64 on both sides: the same recurrences, so the velocities agree to rounding.  (Masking makes some
+    Haar basis functions coincide on the interior, so R A P of a masked grid can be singular; with the
+    Jacobi preconditioner and tol_coarse = 0, 25 iterations amplify rounding along that null space until
+    the oracle alone moves by up to 8e-5 when only its summation order changes.  After 10 iterations it
+    moves by < 1e-13, and real solves stop at tol_coarse.)"""
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, name, maxiter_picard=1, maxiter_coarse=10, tol_coarse=0.0)
+    f = fields_from_oracle(om, g)
+    s = VelocitySolver(g, sp, precision="fp64", coarse_kernel="persistent", coarse_solver=solver)
+    st = s.solve(p, f)
+    oracle.set_coarse_variant(solver)
+    om.update_velocities()
+    ost = om.stats()
+    assert st["picard_iterations"] == 1
+    assert st["coarse_cg_iterations"] == ost["coarse_cg_iterations"] == 10
+    assert uv_err(f, om) < 1e-10
+    wu = np.asarray(om.field("wu_correction_full")).ravel(order="F")[f["wu_mask"].ravel(order="F") != 0]
+    assert rel(f["wu_correction_coarse"], wu) < 1e-8
+    s.close()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_srcg_jacobi_converged_solve_matches_reference(oracle, name):
+    """The Jacobi-preconditioned single-reduction coarse solve changes the V-cycle, not the fixed point: converged
+    FP64 and mixed solves agree with the reference's (cg!) FP64 solve to 1e-6."""
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, name, maxiter_picard=80, tol_picard=1e-7)
+    f0 = fields_from_oracle(om, g)
+    om.update_velocities()
+    ost = om.stats()
+    for prec in ("fp64", "mixed"):
+        f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
+        s = VelocitySolver(g, sp, precision=prec, coarse_kernel="persistent", coarse_solver="srcg_jacobi")
+        st = s.solve(p, f)
+        assert st["status"] == 0, (prec, st)
+        assert uv_err(f, om) < 1e-6, (prec, st, ost)
+        if name == "full":  # on ice-shelf discs the masked coarse space blunts the Jacobi gain
+            assert st["coarse_cg_iterations"] < ost["coarse_cg_iterations"], (prec, st, ost)
+        s.close()
+
+
+def test_single_reduction_solvers_need_the_persistent_kernel(oracle):
+    from wavi_gb300.abi import WaviError
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, "full")
+    for solver in ("srcg", "srcg_jacobi"):
+        with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):
+            VelocitySolver(g, sp, precision="mixed", coarse_kernel="iterations", coarse_solver=solver)
+    # auto falls back to the reference recurrence with per-iteration kernels
+    s = VelocitySolver(g, sp, precision="mixed", coarse_kernel="iterations")
+    f = fields_from_oracle(om, g)
+    assert s.solve(p, f)["status"] in (0, -4)
+    s.close()

@@ -22,6 +22,8 @@ SOFT_STATUS = (-4, -5)  # results are written; mirrors the reference's silent st
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
+COARSE_SOLVERS = {"auto": 0, "cg": 1, "srcg": 2, "srcg_jacobi": 3}  # wavi_coarse_solver
+
 _dp = C.POINTER(C.c_double)
 _u8p = C.POINTER(C.c_uint8)
 
@@ -52,7 +54,7 @@ class SolverParams(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graphs", C.c_int32),
-                ("picard_test", C.c_int32), ("coarse_kernel", C.c_int32), ("reserved0", C.c_int32)]
+                ("picard_test", C.c_int32), ("coarse_kernel", C.c_int32), ("coarse_solver", C.c_int32)]
 
 
 FIELD_INPUTS = ("h", "s", "dsdh", "grounded_fraction", "weertman_c", "accumulation", "basal_melt",
@@ -121,6 +123,8 @@ def load_library(path=None):
         "wavi_relinearise_device": (C.c_int, [vp, C.POINTER(Params), C.POINTER(Fields)]),
         "wavi_apply_operator_device": (C.c_int, [vp, C.c_int, vp, vp]),
         "wavi_op_diagonal_device": (C.c_int, [vp, C.c_int, vp]),
+        "wavi_coarse_diagonal_device": (C.c_int, [vp, C.c_int, vp]),
+        "wavi_time_operator_device": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.POINTER(C.c_double)]),
         "wavi_haar_device": (C.c_int, [vp, C.c_int, vp, vp, vp]),
         "wavi_residual_noalloc": (C.c_int, [C.POINTER(OperatorDesc), vp, vp, vp, vp, vp]),
     }

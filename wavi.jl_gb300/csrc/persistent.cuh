@@ -3,30 +3,39 @@
 // The coarse solve (IterativeSolvers cg! on R A P, update_preconditioners.jl:54-83) is a long chain of
 // small dependent steps: at 640 x 80 one iteration moves ~1 MB, far below what a launch costs.  Here one
 // cooperative launch runs every iteration.  Each CTA owns up to MAXT tiles of TILE x TILE points (a tile
-// holds whole Haar blocks of both velocity components); each thread keeps, in registers, the CG
-// vectors (direction u, residual r, iterate x, and R A P u) of its own point of every owned tile for the
-// whole solve.  Per iteration only the prolonged direction w = P u crosses L2 (the operator needs a
-// one-point halo of it); three grid barriers separate the phases:
+// holds whole Haar blocks of both velocity components); each thread keeps, in registers, the CG vectors
+// of its own point of every owned tile for the whole solve.  Per iteration only a prolonged vector
+// w = P u crosses L2 (the operator needs a one-point halo of it), separated from its readers by a grid
+// barrier.  Two kernels:
 //
-//   1. u = r + β u;  w = P u (Haar synthesis of the tile, masked by the interior)  -> barrier
-//   2. c = R A w (operator on the tile + halo of w, Haar analysis, wavelet mask); partial <u, c>
-//                                                                                  -> barrier + sum
-//   3. α = |r|^2/<u,c>;  x += α u;  r -= α c;  partial |r|^2                       -> barrier + sum
+//   k_cg_persistent   the reference's cg! recurrence: three barriers per iteration
+//                       1. u = r + β u;  w = P u                                   -> barrier
+//                       2. c = R A w (operator on tile + halo, Haar analysis, wavelet mask);
+//                          partial <u, c>                                          -> barrier + sum
+//                       3. α = |r|^2/<u,c>;  x += α u;  r -= α c;  partial |r|^2   -> barrier + sum
+//   k_srcg_persistent single-reduction CG (Chronopoulos & Gear 1989), optionally Jacobi-preconditioned:
+//                     both inner products of an iteration follow its operator application, so an
+//                     iteration costs one halo barrier and one reduction barrier.
 //
-// Every CTA derives the scalars from the same sums, so all CTAs take the same decisions.  The sums are
-// deterministic (the last CTA to arrive adds the per-CTA partials in CTA order).  Every wait is
-// bounded: after ~2^22 polls a CTA records WAVI_ERR_WATCHDOG and all CTAs leave the kernel.
+// GB300 executes FP64 at a small fraction of its FP32 rate, so the per-point work of the FP32 (mixed)
+// instantiations stays in FP32: vector updates are FP32 FMAs with the scalars rounded once per CTA,
+// per-thread dot-product terms are FP32, and the FP64 accumulation starts at the warp sums (CTA sums,
+// grid sums and every CG scalar are FP64).  Scalars are computed by one thread per CTA.
+//
+// Grid sums are deterministic and identical in every CTA: each CTA publishes its FP64 partials, and
+// after the barrier every CTA adds all partials in the same fixed order.  Every wait is bounded: after
+// ~2^22 polls a CTA records WAVI_ERR_WATCHDOG and all CTAs leave the kernel.
 #pragma once
 #include "fused.cuh"
 
 namespace wavi {
 
 struct GridBar {
-  unsigned count;
+  unsigned count;  // arrivals since the launch began (monotonic; epoch e is complete at e * gridDim.x)
   unsigned gen;
   int err;
   int pad;
-  double sum[2];
+  double sum[4];
 };
 
 constexpr long kBarrierSpinLimit = 1L << 22;
@@ -36,76 +45,98 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+}
 
-// Grid-wide barrier over gridDim.x CTAs.  With REDUCE, (v0, v1) of every thread are summed over the grid
-// and returned in out[0..1] to every thread.  Returns false (for every thread of the CTA) if the wait
-// gave up or another CTA reported an error.
-template <bool REDUCE>
-__device__ __forceinline__ bool grid_barrier(GridBar* bar, double* __restrict__ partials, double v0, double v1,
-                                             double out[2]) {
-  __shared__ double sh[32];
-  __shared__ int s_last, s_ok;
-  __shared__ unsigned s_gen;
-  const int t = flat_tid(), nt = flat_nthreads();
+// Shared memory of the grid synchronisation.
+struct SyncShared {
+  double warp[32][4];  // FP64 warp sums
+  double tot[4];       // grid totals
+  int ok;
+};
+
+// Grid-wide barrier over gridDim.x CTAs.  v[0..NS) are this thread's terms (type A: float or double);
+// after the barrier tot[0..NS) in shared memory hold their grid sums (FP64) and `scalars(tot)` has run in
+// thread 0 (it derives the CG scalars once per CTA); the barrier ends with a __syncthreads, so its
+// results are visible to the whole CTA.  `epoch` counts this thread's barriers since the launch (the
+// same in every thread); partials holds 2 x 4 x gridDim.x doubles (the two parities of the epoch, so a
+// slot is rewritten only after every CTA has read it).  Returns false (in every thread of the CTA) if
+// the wait gave up or another CTA reported an error.
+template <int NS, typename A, typename F>
+__device__ __forceinline__ bool grid_sync(GridBar* bar, double* __restrict__ partials, unsigned& epoch, SyncShared& ss,
+                                          const A (&v)[4], F&& scalars) {
+  const int t = flat_tid(), lane = t & 31, wid = t >> 5, nw = (flat_nthreads() + 31) >> 5;
   const unsigned nb = gridDim.x;
-  double a0 = 0.0, a1 = 0.0;
-  if (REDUCE) {
-    a0 = block_sum_any(v0, sh);
-    __syncthreads();
-    a1 = block_sum_any(v1, sh);
+  ++epoch;
+  double* slot = partials + (size_t)(epoch & 1u) * 4u * nb;
+  if (NS > 0) {
+    A x[4];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+      x[q] = v[q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x[q] += __shfl_xor_sync(0xffffffffu, x[q], o);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < NS; ++q) ss.warp[wid][q] = (double)x[q];
   }
-  __syncthreads();
+  __syncthreads();  // the CTA's writes (halo vector, warp sums) precede the arrival
   if (t == 0) {
-    if (REDUCE) {
-      partials[2 * blockIdx.x] = a0;
-      partials[2 * blockIdx.x + 1] = a1;
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+      double s = 0.0;
+      for (int k = 0; k < nw; ++k) s += ss.warp[k][q];
+      slot[q * nb + blockIdx.x] = s;
     }
-    s_gen = ld_acquire_u32(&bar->gen);
     __threadfence();
-    const unsigned prev = atomicAdd(&bar->count, 1u);
-    s_last = (prev == nb - 1u) ? 1 : 0;
-    s_ok = 1;
-  }
-  __syncthreads();
-  if (s_last) {
-    if (REDUCE) {
-      __threadfence();
-      double b0 = 0.0, b1 = 0.0;
-      for (int k = t; k < (int)nb; k += nt) {
-        b0 += __ldcg(partials + 2 * k);
-        b1 += __ldcg(partials + 2 * k + 1);
-      }
-      b0 = block_sum_any(b0, sh);
-      __syncthreads();
-      b1 = block_sum_any(b1, sh);
-      if (t == 0) {
-        bar->sum[0] = b0;
-        bar->sum[1] = b1;
-      }
-    }
-    if (t == 0) {
-      bar->count = 0u;
-      __threadfence();
-      atomicAdd(&bar->gen, 1u);
-    }
-  } else if (t == 0) {
+    red_release_add_u32(&bar->count, 1u);
+    const unsigned target = epoch * nb;
+    int ok = 1;
     long polls = 0;
-    while (ld_acquire_u32(&bar->gen) == s_gen) {
-      if (++polls > kBarrierSpinLimit || *(volatile int*)&bar->err) {
-        atomicExch(&bar->err, 1);
-        s_ok = 0;
+    while ((int)(ld_acquire_u32(&bar->count) - target) < 0) {
+      if (++polls > kBarrierSpinLimit || ((polls & 255) == 0 && *(volatile int*)&bar->err)) {
+        ok = 0;
         break;
       }
-      __nanosleep(64);
+      if (polls > 8) __nanosleep(32);
     }
+    if (!ok) atomicExch(&bar->err, 1);
+    ss.ok = ok;
   }
   __syncthreads();
-  __threadfence();
-  if (REDUCE) {
-    out[0] = __ldcg(&bar->sum[0]);
-    out[1] = __ldcg(&bar->sum[1]);
+  if (!ss.ok) return false;
+  if (NS > 0) {
+    // warp q adds partial q of every CTA: lane-strided sequential sums, then a butterfly (fixed order)
+    if (wid < NS) {
+      const double* src = slot + wid * nb;
+      double s = 0.0;
+      for (unsigned k0 = 0; k0 < nb; k0 += 256) {
+        double b[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const unsigned k = k0 + lane + 32u * e;
+          b[e] = k < nb ? __ldcg(src + k) : 0.0;
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s += b[e];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) ss.tot[wid] = s;
+    }
+    __syncthreads();
+    if (t == 0) scalars(ss.tot);
+    __syncthreads();
   }
-  return s_ok != 0;
+  return true;
+}
+
+template <typename A>
+__device__ __forceinline__ bool grid_barrier(GridBar* bar, double* __restrict__ partials, unsigned& epoch, SyncShared& ss) {
+  const A v[4] = {A(0), A(0), A(0), A(0)};
+  return grid_sync<0>(bar, partials, epoch, ss, v, [](const double*) {});
 }
 
 // One lifting pass along a 1-D line held one element per lane (lane bits below TILE select the
@@ -197,14 +228,34 @@ __device__ __forceinline__ void prolong_store(const Dims& d, int levels, const u
   }
 }
 
-// The whole coarse CG of one V-cycle: from the warm start xc and right-hand side bc (both global, full
-// layout) to the final xc.  Writes the CG statistics into st (CTA 0).
+// CG scalars broadcast to the CTA (written by thread 0 inside grid_sync).
+template <typename T>
+struct CGScalars {
+  double res, tol, alpha, beta, gamma_prev, alpha_prev;
+  T alpha_t, beta_t;
+  int stop;
+};
+
+template <typename T>
+__device__ __forceinline__ T fmul_add(T a, T b, T c) {
+  return fma(a, b, c);
+}
+template <>
+__device__ __forceinline__ float fmul_add<float>(float a, float b, float c) {
+  return fmaf(a, b, c);
+}
+
+// The whole coarse CG of one V-cycle with the reference's cg! recurrence: from the warm start xc and
+// right-hand side bc (both global, full layout) to the final xc.  Writes the CG statistics into st (CTA 0).
+// Stopping rule of cg!: |r| <= max(sqrt(eps) |r0|, abstol) with abstol = tol_coarse |b_c|, or maxiter.
 template <typename T, int TILE, int MAXT>
 __global__ void __launch_bounds__(TILE* TILE)
     k_cg_persistent(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, T* __restrict__ w,
                     const T* __restrict__ bc, T* __restrict__ xc, double* __restrict__ partials, DevState* st,
                     const DevParams* __restrict__ P, GridBar* bar, int ntx, int nty) {
   __shared__ CGShared<T, TILE> sm;
+  __shared__ SyncShared ss;
+  __shared__ CGScalars<T> sc;
   const int ntiles = ntx * nty;
   const int tx = threadIdx.x, ty = threadIdx.y;
   T xu[MAXT], xv[MAXT], ru[MAXT], rv[MAXT], uu[MAXT], uv[MAXT], cu[MAXT], cv[MAXT];
@@ -221,67 +272,82 @@ __global__ void __launch_bounds__(TILE* TILE)
     xv[k] = (own[k] && i < d.nx && j <= d.ny) ? xc[vidx(d, i, j)] : (T)0;
     uu[k] = uv[k] = cu[k] = cv[k] = ru[k] = rv[k] = (T)0;
   }
-  double sums[2];
+  unsigned epoch = 0;
+  int it = 0;
+  const int maxit = P->maxiter_coarse;
+  const double tol_coarse = P->tol_coarse;
   // start: w = P xc
 #pragma unroll
   for (int k = 0; k < MAXT; ++k)
     if (own[k]) prolong_store<T, TILE>(d, levels, cf.inner, xu[k], xv[k], i0s[k], j0s[k], sm, w);
-  if (!grid_barrier<false>(bar, partials, 0, 0, sums)) return;
+  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
   // r = b_c - R A P xc, u = 0;  |r|^2 and |b_c|^2
-  double a0 = 0.0, a1 = 0.0;
-#pragma unroll
-  for (int k = 0; k < MAXT; ++k)
-    if (own[k]) {
-      coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, cu[k], cv[k]);
-      const int i = i0s[k] + tx, j = j0s[k] + ty;
-      const T bu = (i <= d.nx && j < d.ny) ? bc[uidx(d, i, j)] : (T)0;
-      const T bv = (i < d.nx && j <= d.ny) ? bc[vidx(d, i, j)] : (T)0;
-      ru[k] = bu - cu[k];
-      rv[k] = bv - cv[k];
-      a0 += (double)ru[k] * (double)ru[k] + (double)rv[k] * (double)rv[k];
-      a1 += (double)bu * (double)bu + (double)bv * (double)bv;
-    }
-  if (!grid_barrier<true>(bar, partials, a0, a1, sums)) return;
-  double res = sqrt(sums[0]);
-  const double tol = fmax(1.4901161193847656e-08 * res, P->tol_coarse * sqrt(sums[1]));  // reltol = sqrt(eps)
-  double prev = 1.0;
-  const int maxit = P->maxiter_coarse;
-  int it = 0;
-  bool done = (0 >= maxit) || res <= tol || !(res == res);
-  while (!done) {
-    const double beta = (res * res) / (prev * prev);
-#pragma unroll
-    for (int k = 0; k < MAXT; ++k)
-      if (own[k]) {
-        uu[k] = (T)((double)ru[k] + beta * (double)uu[k]);
-        uv[k] = (T)((double)rv[k] + beta * (double)uv[k]);
-        prolong_store<T, TILE>(d, levels, cf.inner, uu[k], uv[k], i0s[k], j0s[k], sm, w);
-      }
-    if (!grid_barrier<false>(bar, partials, 0, 0, sums)) return;
-    double dot = 0.0;
+  {
+    T a[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
         coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, cu[k], cv[k]);
-        dot += (double)uu[k] * (double)cu[k] + (double)uv[k] * (double)cv[k];
+        const int i = i0s[k] + tx, j = j0s[k] + ty;
+        const T bu = (i <= d.nx && j < d.ny) ? bc[uidx(d, i, j)] : (T)0;
+        const T bv = (i < d.nx && j <= d.ny) ? bc[vidx(d, i, j)] : (T)0;
+        ru[k] = bu - cu[k];
+        rv[k] = bv - cv[k];
+        a[0] += ru[k] * ru[k] + rv[k] * rv[k];
+        a[1] += bu * bu + bv * bv;
       }
-    if (!grid_barrier<true>(bar, partials, dot, 0.0, sums)) return;
-    const double alpha = (res * res) / sums[0];
-    double rr = 0.0;
+    if (!grid_sync<2>(bar, partials, epoch, ss, a, [&](const double* tot) {
+          sc.res = sqrt(tot[0]);
+          sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[1]));  // reltol = sqrt(eps)
+          sc.alpha_prev = 1.0;  // prev
+          sc.stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
+          sc.beta = sc.res * sc.res;
+          sc.beta_t = (T)0;  // u = 0: the first direction is r (and res^2 may not fit in T)
+        }))
+      return;
+  }
+  while (!sc.stop) {
+    const T beta = sc.beta_t;
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
-        xu[k] = (T)((double)xu[k] + alpha * (double)uu[k]);
-        xv[k] = (T)((double)xv[k] + alpha * (double)uv[k]);
-        ru[k] = (T)((double)ru[k] - alpha * (double)cu[k]);
-        rv[k] = (T)((double)rv[k] - alpha * (double)cv[k]);
-        rr += (double)ru[k] * (double)ru[k] + (double)rv[k] * (double)rv[k];
+        uu[k] = fmul_add(beta, uu[k], ru[k]);
+        uv[k] = fmul_add(beta, uv[k], rv[k]);
+        prolong_store<T, TILE>(d, levels, cf.inner, uu[k], uv[k], i0s[k], j0s[k], sm, w);
       }
-    if (!grid_barrier<true>(bar, partials, rr, 0.0, sums)) return;
-    prev = res;
-    res = sqrt(sums[0]);
+    if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+    T dot[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, cu[k], cv[k]);
+        dot[0] += uu[k] * cu[k] + uv[k] * cv[k];
+      }
+    if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const double* tot) {
+          sc.alpha = (sc.res * sc.res) / tot[0];
+          sc.alpha_t = (T)sc.alpha;
+        }))
+      return;
+    const T alpha = sc.alpha_t;
+    T rr[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        xu[k] = fmul_add(alpha, uu[k], xu[k]);
+        xv[k] = fmul_add(alpha, uv[k], xv[k]);
+        ru[k] = fmul_add(-alpha, cu[k], ru[k]);
+        rv[k] = fmul_add(-alpha, cv[k], rv[k]);
+        rr[0] += ru[k] * ru[k] + rv[k] * rv[k];
+      }
     ++it;
-    done = it >= maxit || res <= tol || !(res == res);
+    if (!grid_sync<1>(bar, partials, epoch, ss, rr, [&](const double* tot) {
+          sc.alpha_prev = sc.res;  // prev
+          sc.res = sqrt(tot[0]);
+          sc.stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
+          sc.beta = (sc.res * sc.res) / (sc.alpha_prev * sc.alpha_prev);
+          sc.beta_t = (T)sc.beta;
+        }))
+      return;
   }
 #pragma unroll
   for (int k = 0; k < MAXT; ++k)
@@ -293,9 +359,270 @@ __global__ void __launch_bounds__(TILE* TILE)
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {
     st->cg_it = it;
     st->cg_total += it;
-    st->cg_res = res;
-    st->cg_prev = prev;
-    st->cg_tol = tol;
+    st->cg_res = sc.res;
+    st->cg_prev = sc.alpha_prev;
+    st->cg_tol = sc.tol;
+  }
+}
+
+// Single-reduction CG (Chronopoulos & Gear, "s-step iterative methods for symmetric linear systems",
+// J. Comput. Appl. Math. 25 (1989)) on R A P x = b_c, an opt-in alternative to the reference's cg!, with
+// M = diag(R A P) (dcoarse) or M = I (dcoarse == nullptr), and cg!'s stopping rule on the
+// unpreconditioned residual.  Both inner products of an iteration follow its one operator application,
+// so an iteration costs one halo barrier and one reduction barrier (cg! needs two reductions):
+//   x += α p;  r -= α s;  z = M⁻¹ r;  w = P z                                       -> barrier
+//   w = R A w;  partial (r,z), (w,z), |r|^2                                         -> barrier + sums
+//   β = γ/γ';  α = γ/(δ - β γ/α');  p = z + β p;  s = w + β s
+// In FP32 this form keeps the attainable accuracy of standard CG (unlike the pipelined variants, whose
+// recursively updated residual drifts by ~1e-3 in FP32).  The oracle's coarse_srcg states the same
+// iteration in FP64.
+template <typename T, int TILE, int MAXT>
+__global__ void __launch_bounds__(TILE* TILE)
+    k_srcg_persistent(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, const T* __restrict__ dcoarse,
+                      T* __restrict__ w, const T* __restrict__ bc, T* __restrict__ xc, double* __restrict__ partials,
+                      DevState* st, const DevParams* __restrict__ P, GridBar* bar, int ntx, int nty) {
+  __shared__ CGShared<T, TILE> sm;
+  __shared__ SyncShared ss;
+  __shared__ CGScalars<T> sc;
+  const int ntiles = ntx * nty;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  T xu[MAXT], xv[MAXT], ru[MAXT], rv[MAXT], zu[MAXT], zv[MAXT], wu[MAXT], wv[MAXT];
+  T pu[MAXT], pv[MAXT], su[MAXT], sv[MAXT], iu[MAXT], iv[MAXT];  // iu, iv: M⁻¹ (0 off the coarse space)
+  int i0s[MAXT], j0s[MAXT];
+  bool own[MAXT];
+#pragma unroll
+  for (int k = 0; k < MAXT; ++k) {
+    const int t = blockIdx.x + k * gridDim.x;
+    own[k] = t < ntiles;
+    i0s[k] = own[k] ? (t % ntx) * TILE : 0;
+    j0s[k] = own[k] ? (t / ntx) * TILE : 0;
+    const int i = i0s[k] + tx, j = j0s[k] + ty;
+    const bool inu = own[k] && i <= d.nx && j < d.ny, inv = own[k] && i < d.nx && j <= d.ny;
+    xu[k] = inu ? xc[uidx(d, i, j)] : (T)0;
+    xv[k] = inv ? xc[vidx(d, i, j)] : (T)0;
+    if (dcoarse) {
+      const T du = inu ? dcoarse[uidx(d, i, j)] : (T)0, dv = inv ? dcoarse[vidx(d, i, j)] : (T)0;
+      iu[k] = du != (T)0 ? (T)1 / du : (T)0;
+      iv[k] = dv != (T)0 ? (T)1 / dv : (T)0;
+    } else {
+      iu[k] = iv[k] = (T)1;
+    }
+    ru[k] = rv[k] = zu[k] = zv[k] = wu[k] = wv[k] = pu[k] = pv[k] = su[k] = sv[k] = (T)0;
+  }
+  unsigned epoch = 0;
+  int it = 0;
+  const int maxit = P->maxiter_coarse;
+  const double tol_coarse = P->tol_coarse;
+  // r = b_c - R A P xc;  z = M⁻¹ r
+#pragma unroll
+  for (int k = 0; k < MAXT; ++k)
+    if (own[k]) prolong_store<T, TILE>(d, levels, cf.inner, xu[k], xv[k], i0s[k], j0s[k], sm, w);
+  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+  T bb = 0;
+#pragma unroll
+  for (int k = 0; k < MAXT; ++k)
+    if (own[k]) {
+      T cu, cv;
+      coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, cu, cv);
+      const int i = i0s[k] + tx, j = j0s[k] + ty;
+      const T bu = (i <= d.nx && j < d.ny) ? bc[uidx(d, i, j)] : (T)0;
+      const T bv = (i < d.nx && j <= d.ny) ? bc[vidx(d, i, j)] : (T)0;
+      ru[k] = bu - cu;
+      rv[k] = bv - cv;
+      bb += bu * bu + bv * bv;
+      zu[k] = iu[k] * ru[k];
+      zv[k] = iv[k] * rv[k];
+    }
+  // (every CTA has read w: the barrier below orders the rewrite)
+  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+  bool first = true;
+  for (;;) {
+    if (!first) {
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k)
+        if (own[k]) {
+          const T alpha = sc.alpha_t;
+          xu[k] = fmul_add(alpha, pu[k], xu[k]);
+          xv[k] = fmul_add(alpha, pv[k], xv[k]);
+          ru[k] = fmul_add(-alpha, su[k], ru[k]);
+          rv[k] = fmul_add(-alpha, sv[k], rv[k]);
+          zu[k] = iu[k] * ru[k];
+          zv[k] = iv[k] * rv[k];
+        }
+      ++it;
+    }
+    // w = R A P z
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) prolong_store<T, TILE>(d, levels, cf.inner, zu[k], zv[k], i0s[k], j0s[k], sm, w);
+    if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+    T a[4] = {T(0), T(0), T(0), first ? bb : T(0)};
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, wu[k], wv[k]);
+        a[0] += ru[k] * zu[k] + rv[k] * zv[k];
+        a[1] += wu[k] * zu[k] + wv[k] * zv[k];
+        a[2] += ru[k] * ru[k] + rv[k] * rv[k];
+      }
+    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const double* tot) {
+          const double gamma = tot[0], delta = tot[1];
+          sc.res = sqrt(tot[2]);
+          int stop;
+          if (first) {
+            sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[3]));  // reltol = sqrt(eps)
+            sc.beta = 0.0;
+            sc.alpha = gamma / delta;
+            stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
+          } else {
+            stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
+            if (!stop) {
+              sc.beta = gamma / sc.gamma_prev;
+              sc.alpha = gamma / (delta - sc.beta * gamma / sc.alpha);
+            }
+          }
+          if (!stop && (!(sc.alpha == sc.alpha) || isinf(sc.alpha))) stop = 1;
+          sc.gamma_prev = gamma;
+          sc.alpha_t = (T)sc.alpha;
+          sc.beta_t = (T)sc.beta;
+          sc.stop = stop;
+        }))
+      return;
+    if (sc.stop) break;
+    const T beta = sc.beta_t;
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        pu[k] = fmul_add(beta, pu[k], zu[k]);
+        pv[k] = fmul_add(beta, pv[k], zv[k]);
+        su[k] = fmul_add(beta, su[k], wu[k]);
+        sv[k] = fmul_add(beta, sv[k], wv[k]);
+      }
+    first = false;
+  }
+#pragma unroll
+  for (int k = 0; k < MAXT; ++k)
+    if (own[k]) {
+      const int i = i0s[k] + tx, j = j0s[k] + ty;
+      if (i <= d.nx && j < d.ny) xc[uidx(d, i, j)] = xu[k];
+      if (i < d.nx && j <= d.ny) xc[vidx(d, i, j)] = xv[k];
+    }
+  if (blockIdx.x == 0 && tx == 0 && ty == 0) {
+    st->cg_it = it;
+    st->cg_total += it;
+    st->cg_res = sc.res;
+    st->cg_tol = sc.tol;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Exact diagonal of the coarse operator R A P (a Jacobi preconditioner for the mixed-precision coarse
+// solve).  With P e_k = inner ⊙ (φ ⊗ ψ) a Haar basis function and A symmetric, summation by parts of the
+// operator's differences gives its quadratic form
+//   xᵀ A x = -Σ_h 4 hη (u_x² + v_y² + u_x v_y) - Σ_c hη_c (u_y + v_x)² - Σ β x² + Σ_h dimp (div q)²,
+// so diag_k = E(P e_k) is a sum over the cells touching the basis function's support.  One thread per
+// basis function of a TILE x TILE block (u and v component each).
+// ------------------------------------------------------------------------------------------------
+// The 1-D reverse Haar basis function of in-block offset k for a block of `len` existing points
+// (len < B at a ragged grid edge): the lifting of the unit vector, as wavelet_matrix builds it.
+template <int B>
+__device__ __forceinline__ void basis_1d(int k, int len, int levels, float (&phi)[B]) {
+#pragma unroll
+  for (int p = 0; p < B; ++p) phi[p] = (p == k) ? 1.f : 0.f;
+  const int Bl = 1 << (levels + 1);
+  for (int lv = 0; lv <= levels; ++lv) {
+    const int st = Bl >> lv, half = st >> 1;
+#pragma unroll
+    for (int o = 0; o < B; ++o) {
+      if ((o % st) == 0 && o + half < len) {
+        const float xo = phi[o], xe = phi[o + half];
+        phi[o + half] = xe + xo;
+        phi[o] = xo - xe;
+      }
+    }
+  }
+}
+
+template <typename T, int TILE>
+__global__ void __launch_bounds__(TILE* TILE)
+    k_coarse_diag(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, T* __restrict__ dc) {
+  __shared__ T s_heh[TILE + 1][TILE + 1], s_hec[TILE + 1][TILE + 1], s_dim[TILE + 1][TILE + 1];
+  const int bx0 = blockIdx.x * TILE, by0 = blockIdx.y * TILE, tx = threadIdx.x, ty = threadIdx.y;
+  // h cells / c points [bx0-1, bx0+TILE) x [by0-1, by0+TILE) at local index +1
+  for (int p = tx + TILE * ty; p < (TILE + 1) * (TILE + 1); p += TILE * TILE) {
+    const int la = p % (TILE + 1), lb = p / (TILE + 1), a = bx0 - 1 + la, b = by0 - 1 + lb;
+    const bool hv = a >= 0 && a < d.nx && b >= 0 && b < d.ny;
+    const bool cv = a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1;
+    s_heh[lb][la] = hv ? cf.heta_h[hidx(d, a, b)] : (T)0;
+    s_dim[lb][la] = hv ? cf.dimp[hidx(d, a, b)] : (T)0;
+    s_hec[lb][la] = cv ? cf.heta_c[cidx(d, a, b)] : (T)0;
+  }
+  __syncthreads();
+  const T rdx = (T)d.rdx, rdy = (T)d.rdy;
+  for (int comp = 0; comp < 2; ++comp) {
+    const int nxg = comp == 0 ? d.nx + 1 : d.nx, nyg = comp == 0 ? d.ny : d.ny + 1;
+    const int i = bx0 + tx, j = by0 + ty;
+    if (i >= nxg || j >= nyg) continue;
+    const int lenx = min(TILE, nxg - bx0), leny = min(TILE, nyg - by0);
+    float phi[TILE], psi[TILE];
+    basis_1d<TILE>(tx, lenx, levels, phi);
+    basis_1d<TILE>(ty, leny, levels, psi);
+    auto gq = [&](int gi, int gj) { return comp == 0 ? uidx(d, gi, gj) : vidx(d, gi, gj); };
+    // x at block-local (p, r); zero outside the block, off the grid, or off the interior
+    auto xval = [&](int p, int r) -> T {
+      if (p < 0 || p >= lenx || r < 0 || r >= leny) return (T)0;
+      const float s = phi[p] * psi[r];
+      if (s == 0.f) return (T)0;
+      return cf.inner[gq(bx0 + p, by0 + r)] ? (T)s : (T)0;
+    };
+    auto hm = [&](int p, int r) -> T {  // h_m at block-local (p, r) (0 off the block: x is 0 there)
+      if (p < 0 || p >= lenx || r < 0 || r >= leny) return (T)0;
+      return cf.h_m[gq(bx0 + p, by0 + r)];
+    };
+    int p0 = TILE, p1 = -1, r0 = TILE, r1 = -1;  // support bounds
+    for (int p = 0; p < lenx; ++p)
+      if (phi[p] != 0.f) { p0 = min(p0, p); p1 = max(p1, p); }
+    for (int r = 0; r < leny; ++r)
+      if (psi[r] != 0.f) { r0 = min(r0, r); r1 = max(r1, r); }
+    T e = (T)0;
+    if (comp == 0) {
+      // h cells (a, r) with a = bx0 + p - 1 .. : u_x = x(p) - x(p-1) over the cell between u points p-1, p
+      for (int r = r0; r <= r1; ++r)
+        for (int p = p0; p <= p1 + 1; ++p) {  // cell between u points p-1 and p  (h index bx0 + p - 1)
+          const T ux = (xval(p, r) - xval(p - 1, r)) * rdx;
+          const T dq = (hm(p, r) * xval(p, r) - hm(p - 1, r) * xval(p - 1, r)) * rdx;
+          const int la = p, lb = r + 1;  // smem index of h cell (bx0 + p - 1, by0 + r)
+          e += s_dim[lb][la] * dq * dq - (T)4 * s_heh[lb][la] * ux * ux;
+        }
+      // c points (a, b) = (bx0 + p - 1, by0 + r - 1): u_y = x(p, r) - x(p, r-1)
+      for (int r = r0; r <= r1 + 1; ++r)
+        for (int p = p0; p <= p1; ++p) {
+          const T uy = (xval(p, r) - xval(p, r - 1)) * rdy;
+          e -= s_hec[r][p] * uy * uy;
+        }
+    } else {
+      // h cells (p, b) between v points r-1 and r: v_y
+      for (int r = r0; r <= r1 + 1; ++r)
+        for (int p = p0; p <= p1; ++p) {
+          const T vy = (xval(p, r) - xval(p, r - 1)) * rdy;
+          const T dq = (hm(p, r) * xval(p, r) - hm(p, r - 1) * xval(p, r - 1)) * rdy;
+          const int la = p + 1, lb = r;  // h cell (bx0 + p, by0 + r - 1)
+          e += s_dim[lb][la] * dq * dq - (T)4 * s_heh[lb][la] * vy * vy;
+        }
+      // c points (a, b) = (bx0 + p - 1, by0 + r - 1): v_x = y(p, r) - y(p-1, r)
+      for (int r = r0; r <= r1; ++r)
+        for (int p = p0; p <= p1 + 1; ++p) {
+          const T vx = (xval(p, r) - xval(p - 1, r)) * rdx;
+          e -= s_hec[r][p] * vx * vx;
+        }
+    }
+    for (int r = r0; r <= r1; ++r)
+      for (int p = p0; p <= p1; ++p) {
+        const T x = xval(p, r);
+        if (x != (T)0) e -= cf.beta_m[gq(bx0 + p, by0 + r)] * x * x;
+      }
+    const int q = gq(i, j);
+    dc[q] = wmask[q] ? e : (T)0;
   }
 }
 

@@ -87,6 +87,8 @@ struct wavi_ctx {
   // persistent coarse CG: grid barrier, launch shape, tiles per CTA (0 = per-iteration kernels)
   GridBar* bar = nullptr;
   int pers_maxt = 0, pers_grid = 0, ntx = 0, nty = 0;
+  int coarse_solver = WAVI_COARSE_CG;  // resolved coarse solver (never WAVI_COARSE_AUTO)
+  void* dcoarse = nullptr;             // diag(R A P) for the Jacobi-preconditioned single-reduction CG
   // solve graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -295,9 +297,16 @@ int launch_cg_persistent(wavi_ctx* c) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  CK(cudaLaunchKernelEx(&cfg, k_cg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
-                        (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar, c->ntx,
-                        c->nty));
+  if (c->coarse_solver == WAVI_COARSE_CG) {
+    CK(cudaLaunchKernelEx(&cfg, k_cg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
+                          (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar, c->ntx,
+                          c->nty));
+  } else {
+    const T* dc = c->coarse_solver == WAVI_COARSE_SRCG_JACOBI ? (const T*)c->dcoarse : nullptr;
+    CK(cudaLaunchKernelEx(&cfg, k_srcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
+                          dc, (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
+                          c->ntx, c->nty));
+  }
   c->launches++;
   return 0;
 }
@@ -305,6 +314,12 @@ int launch_cg_persistent(wavi_ctx* c) {
 template <typename T, int TILE>
 int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& tc) {
   const Dims& d = c->d;
+  if (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI) {
+    k_coarse_diag<T, TILE><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, c->sp.levels, coef<T>(c), c->wmask_uv,
+                                                                      (T*)c->dcoarse);
+    CKL();
+    tv.launches++;
+  }
   k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar);
   CKL();
   if (c->pers_maxt == 1)
@@ -497,10 +512,12 @@ int build_graph(wavi_ctx* c) {
 // Persistent coarse CG: the smallest tiles-per-CTA (1, 2, 4) for which every CTA of the launch is
 // resident at once (the cooperative launch needs that); 0 if none fits.
 template <int MAXT, typename T, int TILE>
-int resident_ctas(int nsm) {
+int resident_ctas(int nsm, int solver) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent<T, TILE, MAXT>, TILE * TILE, 0) != cudaSuccess)
-    return 0;
+  cudaError_t e = solver == WAVI_COARSE_CG
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent<T, TILE, MAXT>, TILE * TILE, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_srcg_persistent<T, TILE, MAXT>, TILE * TILE, 0);
+  if (e != cudaSuccess) return 0;
   return per_sm * nsm;
 }
 template <typename T, int TILE>
@@ -511,7 +528,9 @@ void choose_persistent(wavi_ctx* c) {
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, c->dev);
   if (!coop || nsm <= 0) return;
   const long ntiles = (long)c->ntx * c->nty;
-  const int caps[3] = {resident_ctas<1, T, TILE>(nsm), resident_ctas<2, T, TILE>(nsm), resident_ctas<4, T, TILE>(nsm)};
+  const int s = c->coarse_solver;
+  const int caps[3] = {resident_ctas<1, T, TILE>(nsm, s), resident_ctas<2, T, TILE>(nsm, s),
+                       resident_ctas<4, T, TILE>(nsm, s)};
   const int maxts[3] = {1, 2, 4};
   for (int k = 0; k < 3; ++k) {
     const long g = (ntiles + maxts[k] - 1) / maxts[k];
@@ -840,18 +859,42 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   const int op_blocks = (int)(c->op_grid.x * c->op_grid.y);
   const int tile_blocks = (int)(c->tile_grid.x * c->tile_grid.y);
   const int haar_blocks = (int)(c->haar_grid.x * c->haar_grid.y * c->haar_grid.z);
-  c->max_partials = 2 * std::max({pt_blocks, op_blocks, tile_blocks, haar_blocks, c->ew_blocks, 1});
-  if ((r = dalloc(c, &c->partials, (size_t)c->max_partials))) return bail(r);
-  if ((r = dalloc(c, &c->bar, 1))) return bail(r);
   c->ntx = (int)c->tile_grid.x;
   c->nty = (int)c->tile_grid.y;
+  // coarse solver: the reference's cg! recurrence, or (persistent kernel only) single-reduction CG
+  const int want = opt->coarse_solver;
+  if (want < WAVI_COARSE_AUTO || want > WAVI_COARSE_SRCG_JACOBI)
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_solver %d", want));
+  if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));
+  c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) ? WAVI_COARSE_SRCG_JACOBI : WAVI_COARSE_CG) : want;
   if (opt->coarse_kernel != 2) {
     if (mixed(c))
       c->tile == 16 ? choose_persistent<float, 16>(c) : choose_persistent<float, 32>(c);
     else
       c->tile == 16 ? choose_persistent<double, 16>(c) : choose_persistent<double, 32>(c);
+    if (c->pers_maxt == 0 && c->coarse_solver != WAVI_COARSE_CG) {
+      if (want != WAVI_COARSE_AUTO)
+        return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse CG does not fit this grid on this device"));
+      c->coarse_solver = WAVI_COARSE_CG;
+      c->tile == 16 ? (mixed(c) ? choose_persistent<float, 16>(c) : choose_persistent<double, 16>(c))
+                    : (mixed(c) ? choose_persistent<float, 32>(c) : choose_persistent<double, 32>(c));
+    }
     if (opt->coarse_kernel == 1 && c->pers_maxt == 0)
       return bail(fail(c, WAVI_ERR_ARGUMENT, "the persistent coarse CG does not fit this grid on this device"));
+  } else {
+    c->coarse_solver = WAVI_COARSE_CG;
+  }
+  // reduction partials: per-block slots of the one-pass kernels, and 2 parities x 4 sums per CTA of the
+  // persistent kernel
+  c->max_partials = 4 * std::max({pt_blocks, op_blocks, tile_blocks, haar_blocks, c->ew_blocks, 1});
+  c->max_partials = std::max(c->max_partials, 8 * std::max(c->pers_grid, 1));
+  if ((r = dalloc(c, &c->partials, (size_t)c->max_partials))) return bail(r);
+  if ((r = dalloc(c, &c->bar, 1))) return bail(r);
+  {
+    double* q = nullptr;
+    if ((r = dalloc(c, &q, N))) return bail(r);
+    c->dcoarse = q;
   }
   if ((r = dalloc(c, &c->P, 1))) return bail(r);
   if ((r = dalloc(c, &c->S, 1))) return bail(r);
@@ -949,6 +992,29 @@ int wavi_apply_operator_device(wavi_ctx* c, int precision, const void* in_uv, vo
   return 0;
 }
 
+int wavi_time_operator_device(wavi_ctx* c, int precision, const void* in_uv, void* out_uv, int repeats, double* avg_ms) {
+  TRY(check_ctx(c));
+  if (!in_uv || !out_uv || !avg_ms || repeats < 1) return fail(c, WAVI_ERR_ARGUMENT, "bad arguments");
+  if (precision != WAVI_PRECISION_FP64 && !(precision == WAVI_PRECISION_MIXED && mixed(c)))
+    return fail(c, WAVI_ERR_ARGUMENT, "float32 operator needs a mixed-precision context");
+  CK(cudaEventRecord(c->ev0, c->st));
+  for (int k = 0; k < repeats; ++k) {
+    if (precision == WAVI_PRECISION_FP64)
+      k_op<double, double, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<double>(c), (const double*)in_uv,
+                                                                     nullptr, (double*)out_uv, c->partials, nullptr);
+    else
+      k_op<float, float, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<float>(c), (const float*)in_uv, nullptr,
+                                                                   (float*)out_uv, c->partials, nullptr);
+    CKL();
+  }
+  CK(cudaEventRecord(c->ev1, c->st));
+  CK(cudaEventSynchronize(c->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  *avg_ms = (double)ms / repeats;
+  return 0;
+}
+
 int wavi_op_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
   TRY(check_ctx(c));
   if (!diag_uv) return fail(c, WAVI_ERR_ARGUMENT, "null vector");
@@ -958,6 +1024,28 @@ int wavi_op_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
     k_op_diag<float><<<c->pt_grid, c->pt_block, 0, c->st>>>(c->d, coef<float>(c), (float*)diag_uv);
   else
     return fail(c, WAVI_ERR_ARGUMENT, "float32 diagonal needs a mixed-precision context");
+  CKL();
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+int wavi_coarse_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
+  TRY(check_ctx(c));
+  if (!diag_uv) return fail(c, WAVI_ERR_ARGUMENT, "null vector");
+  const int L = c->sp.levels;
+  if (precision == WAVI_PRECISION_FP64) {
+    if (c->tile == 16)
+      k_coarse_diag<double, 16><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, L, coef<double>(c), c->wmask_uv, (double*)diag_uv);
+    else
+      k_coarse_diag<double, 32><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, L, coef<double>(c), c->wmask_uv, (double*)diag_uv);
+  } else if (precision == WAVI_PRECISION_MIXED && mixed(c)) {
+    if (c->tile == 16)
+      k_coarse_diag<float, 16><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, L, coef<float>(c), c->wmask_uv, (float*)diag_uv);
+    else
+      k_coarse_diag<float, 32><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, L, coef<float>(c), c->wmask_uv, (float*)diag_uv);
+  } else {
+    return fail(c, WAVI_ERR_ARGUMENT, "float32 diagonal needs a mixed-precision context");
+  }
   CKL();
   CK(cudaStreamSynchronize(c->st));
   return 0;

@@ -38,7 +38,7 @@ class VelocitySolver:
     COARSE_KERNELS = {"auto": 0, "persistent": 1, "iterations": 2}
 
     def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0,
-                 coarse_kernel="auto"):
+                 coarse_kernel="auto", coarse_solver="auto"):
         self.lib = abi.load_library()
         self.grid = grid
         self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ
@@ -47,7 +47,7 @@ class VelocitySolver:
         self._desc = grid.descriptor()
         self._sp = solver_params.to_c()
         self._opt = abi.Options(int(device), PRECISIONS[precision], 1 if use_graphs else 0, int(picard_test),
-                                self.COARSE_KERNELS[coarse_kernel], 0)
+                                self.COARSE_KERNELS[coarse_kernel], abi.COARSE_SOLVERS[coarse_solver])
         ctx = C.c_void_p()
         st = self.lib.wavi_ctx_create(C.byref(self._desc.desc), C.byref(self._sp), C.byref(self._opt), C.byref(ctx))
         if st != 0:
@@ -138,8 +138,23 @@ class VelocitySolver:
         if st != 0:
             raise self._err(st)
 
+    def time_operator_device(self, in_uv, out_uv, precision="fp64", repeats=200):
+        """Mean duration (s) of one operator launch over `repeats` back-to-back launches (CUDA events)."""
+        ms = C.c_double()
+        st = self.lib.wavi_time_operator_device(self.ctx, PRECISIONS[precision], C.c_void_p(in_uv.data_ptr()),
+                                                C.c_void_p(out_uv.data_ptr()), int(repeats), C.byref(ms))
+        if st != 0:
+            raise self._err(st)
+        return ms.value / 1e3
+
     def op_diagonal_device(self, out_uv, precision="fp64"):
         st = self.lib.wavi_op_diagonal_device(self.ctx, PRECISIONS[precision], C.c_void_p(out_uv.data_ptr()))
+        if st != 0:
+            raise self._err(st)
+
+    def coarse_diagonal_device(self, out_uv, precision="fp64"):
+        """diag(R A P) for the current coefficients and wavelet mask, on the full wavelet grids."""
+        st = self.lib.wavi_coarse_diagonal_device(self.ctx, PRECISIONS[precision], C.c_void_p(out_uv.data_ptr()))
         if st != 0:
             raise self._err(st)
 

@@ -31,6 +31,7 @@ class GPUParallelSpec:
     precision: str = "fp64"     # "fp64" (reference algorithm) or "mixed"
     use_graphs: bool = True
     picard_test: int = 0
+    coarse_solver: str = "auto"  # "auto", "cg" (reference), "srcg", "srcg_jacobi" (single-reduction CG)
 
 
 _SOLVERS = {}
@@ -42,7 +43,8 @@ def _solver_for(model):
     if s is None:
         ps = model.parallel_spec
         s = gpu.VelocitySolver(model.grid, model.solver_params, precision=ps.precision, device=ps.device,
-                               use_graphs=ps.use_graphs, picard_test=ps.picard_test)
+                               use_graphs=ps.use_graphs, picard_test=ps.picard_test,
+                               coarse_solver=ps.coarse_solver)
         _SOLVERS[key] = s
     return s
 
