@@ -12,11 +12,18 @@ reference's other solver parameters).
   e2e      the same solve through the host C ABI (wavi_solve_velocities) from pinned host buffers, the
            host<->device copies inside the timed region
   fp64_gpu the reference algorithm in float64 on the GPU (the comparison the metric names)
-  roofline the operator kernel (float32) timed alone at this size, algorithmic bytes / duration
+  roofline the dominant kernel of the step, the persistent coarse CG (k_srcg_persistent<float>), timed
+           with CUDA events around each launch in a host-driven solve of the same state; per CG
+           iteration: algorithmic bytes / duration against the measured HBM peak (the kernel's working
+           set, ~3 MB, is L2-resident: it is bound by grid-barrier latency, not by HBM)
+  roofline_stencil the fused operator kernel (float32) on a 4096 x 1024 grid (~190 MB per application,
+           larger than L2), back-to-back launches timed with CUDA events: the HBM-bound stencil figure
   cpu_baseline the CPU oracle (the FP64 restatement of the reference) on a bounded sample
 
 ``--impl reference`` times only the CPU oracle on all host cores and prints its own line.
 Under torchrun (N > 1) every rank solves its own replica (no collective); value is the sum.
+``--profile solve|op`` runs one small untimed case for ncu (a host-driven solve of the workload capped
+at ``--picard`` Picard iterations, or operator launches on the 4096 x 1024 grid) and prints nothing.
 """
 import argparse
 import json
@@ -185,23 +192,54 @@ def time_host_solves(torch, solver, params, snapshot, steps, warmup):
     return times, in_bytes, out_bytes
 
 
-def op_roofline(torch, solver, n_launch=200, precision="mixed"):
-    """Mean duration of the operator kernel alone at the workload size: n_launch back-to-back launches
-    timed with CUDA events on the solver's stream (wavi_time_operator_device), against its algorithmic
-    bytes: read x, write y, heta_h, dimp (Nh), heta_c (Nc), beta_m, h_m (N) in w-byte words plus the
-    interior mask (N bytes)."""
-    d = solver.grid
-    nx, ny = d.nx, d.ny
+STENCIL_GRID = (4096, 1024)
+
+
+def op_bytes(nx, ny, w):
+    """Algorithmic bytes of one operator application: read x, write y, heta_h, dimp (Nh), heta_c (Nc),
+    beta_m, h_m (N) in w-byte words plus the interior mask (N bytes)."""
     N = (nx + 1) * ny + nx * (ny + 1)
     Nh, Nc = nx * ny, (nx - 1) * (ny - 1)
+    return w * (2.0 * N + 2.0 * Nh + Nc + 2.0 * N) + N
+
+
+def cg_iteration_bytes(nx, ny, w):
+    """Algorithmic bytes of one coarse-CG iteration of the persistent kernel: one operator application
+    on the prolonged vector plus its write and the wavelet-mask read (N words, N bytes)."""
+    N = (nx + 1) * ny + nx * (ny + 1)
+    return op_bytes(nx, ny, w) + w * 2.0 * N + N
+
+
+def stencil_solver(torch, device):
+    from wavi_gb300 import synthetic
+    from wavi_gb300.config import SolverParams
+    from wavi_gb300.gpu import VelocitySolver
+    nx, ny = STENCIL_GRID
+    g = synthetic.Grid(nx=nx, ny=ny, nσ=4, dx=1000.0, dy=1000.0, u_iszero=["north"], v_iszero=["west", "east"])
+    return VelocitySolver(g, SolverParams(), precision="mixed", device=device)
+
+
+def op_roofline(torch, solver, n_launch=50, precision="mixed"):
+    """Mean duration of the fused operator kernel: n_launch back-to-back launches timed with CUDA events
+    on the solver's stream (wavi_time_operator_device), and its algorithmic bytes."""
+    g = solver.grid
+    N = (g.nx + 1) * g.ny + g.nx * (g.ny + 1)
     w = 4 if precision == "mixed" else 8
     x = torch.randn(N, dtype=torch.float32 if w == 4 else torch.float64, device="cuda")
     y = torch.zeros_like(x)
     torch.cuda.synchronize()
-    solver.time_operator_device(x, y, precision, 20)  # warm-up
+    solver.time_operator_device(x, y, precision, 5)  # warm-up
     dur = solver.time_operator_device(x, y, precision, n_launch)
-    alg_bytes = w * (2.0 * N + 2.0 * Nh + Nc + 2.0 * N) + N
-    return alg_bytes, dur
+    return op_bytes(g.nx, g.ny, w), dur
+
+
+def coarse_roofline(torch, solver, params, snapshot):
+    """The persistent coarse CG timed launch by launch (CUDA events around each launch) in a host-driven
+    solve of the workload state: (seconds per CG iteration, CG iterations, launches)."""
+    names = solve_field_names()
+    dev = {k: torch.from_numpy(np.ascontiguousarray(np.asarray(snapshot[k]).ravel(order="F"))).cuda() for k in names}
+    st = solver.solve_device(params, dev)
+    return st["coarse_ms"] / 1e3 / max(1, st["coarse_cg_iterations"]), st["coarse_cg_iterations"], st["coarse_launches"]
 
 
 def aggregate_ranks(torch, dist, world, local_seconds, steps, device):
@@ -221,14 +259,13 @@ def measured_peaks():
         return None
 
 
-def ncu_traffic():
-    """dram bytes per launch of the operator kernel from the committed ncu summary, if present."""
-    fn = os.path.join(ROOT, "profiles", "op_kernel_c2.md")
+def ncu_traffic(fn, key):
+    """A `key: value` figure (dram bytes) from a committed ncu summary under profiles/, if present."""
     try:
-        for ln in open(fn):
-            if ln.startswith("traffic_bytes_per_launch:"):
+        for ln in open(os.path.join(ROOT, "profiles", fn)):
+            if ln.startswith(key + ":"):
                 return float(ln.split(":", 1)[1].strip())
-    except OSError:
+    except (OSError, ValueError):
         pass
     return None
 
@@ -338,9 +375,18 @@ def gpu_arm(args):
     te2e, hb, db = time_host_solves(torch, mixed, p, snapshot, args.steps, max(1, args.warmup // 2))
     e2e_value = world * len(te2e) / sum(te2e)
 
-    alg_bytes, dur = op_roofline(torch, mixed)
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
+    # dominant kernel: the persistent coarse CG, per CG iteration
+    prof = VelocitySolver(g, sp, precision="mixed", device=local, use_graphs=False)
+    sec_it, cg_its, cg_launches = coarse_roofline(torch, prof, p, snapshot)
+    prof.close()
+    cg_bytes = cg_iteration_bytes(g.nx, g.ny, 4)
+    cg_achieved = cg_bytes / sec_it / 1e9
+    # the fused operator on a grid larger than L2
+    big = stencil_solver(torch, local)
+    alg_bytes, dur = op_roofline(torch, big)
+    big.close()
     achieved = alg_bytes / dur / 1e9
 
     err = np.sqrt(np.sum((outmix["u"] - out64["u"]) ** 2) + np.sum((outmix["v"] - out64["v"]) ** 2)) / \
@@ -374,10 +420,19 @@ def gpu_arm(args):
         "rel_err_mixed_vs_fp64": float(err),
         "solve": {k: stmix[-1][k] for k in ("picard_iterations", "coarse_cg_iterations", "op_applications",
                                              "rel_residual", "kernel_launches", "host_syncs", "status_name")},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": ncu_traffic(), "kernel": "k_op<float> (operator, 640x80)",
-                     "alg_bytes_per_launch": alg_bytes, "avg_launch_us": dur * 1e6,
-                     "peak_source": "measured" if peaks else "fallback"},
+        "roofline": {"bound": "hbm", "achieved": cg_achieved, "peak": peak, "unit": "GB/s",
+                     "frac": cg_achieved / peak,
+                     "traffic": ncu_traffic("coarse_cg_c2.md", "traffic_bytes_per_cg_iteration"),
+                     "kernel": "k_srcg_persistent<float> (coarse CG, one launch per V-cycle, 640x80)",
+                     "per": "CG iteration", "alg_bytes_per_iteration": cg_bytes, "us_per_iteration": sec_it * 1e6,
+                     "cg_iterations": cg_its, "launches": cg_launches, "peak_source": "measured" if peaks else "fallback",
+                     "note": "L2-resident working set; bound by grid-barrier latency (2 barriers per iteration)"},
+        "roofline_stencil": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak,
+                             "traffic": ncu_traffic("op_kernel_4096x1024.md", "traffic_bytes_per_launch"),
+                             "kernel": "k_op<float> (fused operator, %dx%d)" % STENCIL_GRID,
+                             "alg_bytes_per_launch": alg_bytes, "avg_launch_us": dur * 1e6,
+                             "peak_source": "measured" if peaks else "fallback"},
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
@@ -390,6 +445,35 @@ def gpu_arm(args):
     return 0
 
 
+def profile_case(args):
+    """One untimed case for ncu: the workload solved host-driven (every kernel a separate launch) and
+    capped at --picard Picard iterations, or --op-launches operator launches on the stencil grid."""
+    import torch
+    __graft_entry__.load_package()
+    from wavi_gb300 import build
+    build.build_library()
+    from wavi_gb300.config import SolverParams
+    from wavi_gb300.gpu import VelocitySolver
+    from wavi_gb300.model import release_solver
+    if args.profile == "op":
+        big = stencil_solver(torch, 0)
+        op_roofline(torch, big, n_launch=args.op_launches)
+        big.close()
+        return 0
+    m = build_state(None)
+    snapshot = {k: np.array(v, copy=True) for k, v in m.fields.items()}
+    release_solver(m)
+    sp = SolverParams(**{**m.solver_params.__dict__, "maxiter_picard": args.picard})
+    s = VelocitySolver(m.grid, sp, precision=args.precision, use_graphs=False)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(np.asarray(snapshot[k]).ravel(order="F"))).cuda()
+           for k in solve_field_names()}
+    st = s.solve_device(m.params, dev)
+    torch.cuda.synchronize()
+    s.close()
+    print(json.dumps({"profile": args.profile, "stats": st}), file=sys.stderr)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -397,7 +481,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline leg")
+    ap.add_argument("--profile", choices=("solve", "op"), help="run one small untimed case for ncu and exit")
+    ap.add_argument("--picard", type=int, default=1, help="--profile solve: Picard iterations")
+    ap.add_argument("--precision", default="mixed", choices=("mixed", "fp64"), help="--profile solve: precision")
+    ap.add_argument("--op-launches", type=int, default=3, help="--profile op: operator launches")
     args = ap.parse_args()
+    if args.profile:
+        return profile_case(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gpu_arm(args)

@@ -98,6 +98,10 @@ typedef struct wavi_options {
                                         tiles fit the device's resident CTAs, else per-iteration kernels;
                                         1 = persistent (error if it does not fit); 2 = per-iteration */
   int32_t coarse_solver;             /* wavi_coarse_solver */
+  int32_t stencil_kernel;            /* operator and smoother sweeps: 0 = by grid size (row-streaming from
+                                        2^19 points of the (nx+1) x (ny+1) index space), 1 = shared-memory
+                                        tiles, 2 = row-streaming */
+  int32_t reserved0;
 } wavi_options;
 
 /* Coarse solve of each V-cycle (R A P x = b_c, update_preconditioners.jl:54-83).  The reference calls
@@ -159,6 +163,10 @@ typedef struct wavi_stats {
   double elapsed_ms;                 /* device time of the solve (CUDA events) */
   int32_t kernel_launches;           /* kernels this library launched during the solve */
   int32_t host_syncs;                /* host round trips (convergence tests, CG batches) */
+  double coarse_ms;                  /* device time of the persistent coarse-CG launches (CUDA events;
+                                        host-driven solves, use_graphs = 0, only; else -1) */
+  int32_t coarse_solver;             /* the wavi_coarse_solver the solve used (never AUTO) */
+  int32_t coarse_launches;           /* persistent coarse-CG launches timed in coarse_ms */
 } wavi_stats;
 
 typedef struct wavi_ctx wavi_ctx;

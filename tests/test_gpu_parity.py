@@ -55,17 +55,18 @@ def test_relinearise_matches_oracle(oracle, name):
     s.close()
 
 
+@pytest.mark.parametrize("stencil", ["tiled", "streaming"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_operator_and_diagonal_match_oracle(oracle, name):
+def test_operator_and_diagonal_match_oracle(oracle, name, stencil):
     from wavi_gb300.gpu import VelocitySolver
     g, p, sp, om = _setup(oracle, name)
     rng = np.random.default_rng(6)
     om.field("u")[...] = 50 * rng.standard_normal(om.field("u").shape)
     om.field("v")[...] = 20 * rng.standard_normal(om.field("v").shape)
     f = fields_from_oracle(om, g)
-    s = VelocitySolver(g, sp, precision="fp64")
+    s = VelocitySolver(g, sp, precision="fp64", stencil_kernel=stencil)
     s.relinearise_device(p, to_dev(f, torch))
-    sm = VelocitySolver(g, sp, precision="mixed")  # float32 viscosity and coefficients
+    sm = VelocitySolver(g, sp, precision="mixed", stencil_kernel=stencil)  # float32 viscosity and coefficients
     sm.relinearise_device(p, to_dev(f, torch))
     om.inner_update()
     xu = rng.standard_normal((g.nx + 1, g.ny))
@@ -109,7 +110,7 @@ def test_haar_transforms_match_oracle(oracle, name):
 
 
 @pytest.mark.parametrize("mode", [(True, "persistent"), (True, "iterations"), (False, "persistent"),
-                                  (False, "iterations")])
+                                  (False, "iterations"), (True, "persistent", "streaming")])
 @pytest.mark.parametrize("name", list(CASES))
 def test_one_vcycle_fixed_cg_count_matches_oracle(oracle, name, mode):
     """One Picard iteration whose coarse CG runs exactly 25 iterations (tol_coarse = 0): relinearisation,
@@ -118,8 +119,9 @@ def test_one_vcycle_fixed_cg_count_matches_oracle(oracle, name, mode):
     from wavi_gb300.gpu import VelocitySolver
     g, p, sp, om = _setup(oracle, name, maxiter_picard=1, maxiter_coarse=25, tol_coarse=0.0)
     f = fields_from_oracle(om, g)
-    graphs, coarse = mode
-    s = VelocitySolver(g, sp, precision="fp64", use_graphs=graphs, coarse_kernel=coarse)
+    graphs, coarse = mode[:2]
+    stencil = mode[2] if len(mode) > 2 else "auto"
+    s = VelocitySolver(g, sp, precision="fp64", use_graphs=graphs, coarse_kernel=coarse, stencil_kernel=stencil)
     st = s.solve(p, f)
     om.update_velocities()
     ost = om.stats()

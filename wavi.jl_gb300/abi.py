@@ -23,6 +23,7 @@ PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
 COARSE_SOLVERS = {"auto": 0, "cg": 1, "srcg": 2, "srcg_jacobi": 3}  # wavi_coarse_solver
+COARSE_SOLVER_NAMES = {v: k for k, v in COARSE_SOLVERS.items()}
 
 _dp = C.POINTER(C.c_double)
 _u8p = C.POINTER(C.c_uint8)
@@ -54,7 +55,8 @@ class SolverParams(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graphs", C.c_int32),
-                ("picard_test", C.c_int32), ("coarse_kernel", C.c_int32), ("coarse_solver", C.c_int32)]
+                ("picard_test", C.c_int32), ("coarse_kernel", C.c_int32), ("coarse_solver", C.c_int32),
+                ("stencil_kernel", C.c_int32), ("reserved0", C.c_int32)]
 
 
 FIELD_INPUTS = ("h", "s", "dsdh", "grounded_fraction", "weertman_c", "accumulation", "basal_melt",
@@ -76,7 +78,8 @@ class Stats(C.Structure):
                 ("coarse_cg_iterations", C.c_int32), ("op_applications", C.c_int32),
                 ("rel_residual", C.c_double), ("rel_update", C.c_double),
                 ("algorithmic_bytes", C.c_double), ("elapsed_ms", C.c_double),
-                ("kernel_launches", C.c_int32), ("host_syncs", C.c_int32)]
+                ("kernel_launches", C.c_int32), ("host_syncs", C.c_int32),
+                ("coarse_ms", C.c_double), ("coarse_solver", C.c_int32), ("coarse_launches", C.c_int32)]
 
 
 class OperatorDesc(C.Structure):

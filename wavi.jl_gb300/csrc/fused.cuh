@@ -11,6 +11,8 @@
 // own points.  A TILE x TILE tile with TILE a multiple of the Haar block 2^(levels+1) also holds whole
 // Haar blocks of both velocity components, so the coarse-grid restriction follows in shared memory.
 #pragma once
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace wavi {
@@ -119,7 +121,7 @@ __device__ __forceinline__ void stage_x(const Dims& d, int i0, int j0, OpTile<T,
 // Stage 2: stresses (see k_op for the formulas).
 template <typename T, int TX, int TY>
 __device__ __forceinline__ void stage_stress(const Dims& d, const OpCoef<T>& cf, int i0, int j0, OpTile<T, TX, TY>& s) {
-  const T rdx = (T)d.rdx, rdy = (T)d.rdy;
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
   for (int p = flat_tid(); p < (TX + 1) * (TY + 1); p += flat_nthreads()) {
     const int la = p % (TX + 1), lb = p / (TX + 1);
     const int a = i0 - 1 + la, b = j0 - 1 + lb;
@@ -156,13 +158,13 @@ __device__ __forceinline__ void stage_stress(const Dims& d, const OpCoef<T>& cf,
 // Stage 3: operator at the u point of local (li, lj) (1-based in the tile) / at the v point.
 template <typename T, int TX, int TY>
 __device__ __forceinline__ T stage_out_u(const Dims& d, const OpCoef<T>& cf, const OpTile<T, TX, TY>& s, int li, int lj, int q) {
-  const T rdx = (T)d.rdx, rdy = (T)d.rdy;
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
   return (s.rxx[lj][li] - s.rxx[lj][li - 1]) * rdx + (s.rxy[lj][li - 1] - s.rxy[lj - 1][li - 1]) * rdy -
          cf.beta_m[q] * s.xu[lj][li] - cf.h_m[q] * ((s.e[lj][li] - s.e[lj][li - 1]) * rdx);
 }
 template <typename T, int TX, int TY>
 __device__ __forceinline__ T stage_out_v(const Dims& d, const OpCoef<T>& cf, const OpTile<T, TX, TY>& s, int li, int lj, int q) {
-  const T rdx = (T)d.rdx, rdy = (T)d.rdy;
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
   return (s.ryy[lj][li] - s.ryy[lj - 1][li]) * rdy + (s.rxy[lj - 1][li] - s.rxy[lj - 1][li - 1]) * rdx -
          cf.beta_m[q] * s.xv[lj][li] - cf.h_m[q] * ((s.e[lj][li] - s.e[lj - 1][li]) * rdy);
 }
@@ -351,7 +353,7 @@ __global__ void k_vcycle_init(Dims d, OpCoef<T> cf, const double* __restrict__ r
                               T* __restrict__ rs, T* __restrict__ rsm, T* __restrict__ corr, T* __restrict__ xc,
                               T* __restrict__ diag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-  const T rdx = (T)d.rdx, rdy = (T)d.rdy, rdx2 = rdx * rdx, rdy2 = rdy * rdy;
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d), rdx2 = rdx * rdx, rdy2 = rdy * rdy;
   auto heh = [&](int a, int b) -> T { return (a >= 0 && a < d.nx && b >= 0 && b < d.ny) ? cf.heta_h[hidx(d, a, b)] : (T)0; };
   auto dim = [&](int a, int b) -> T { return (a >= 0 && a < d.nx && b >= 0 && b < d.ny) ? cf.dimp[hidx(d, a, b)] : (T)0; };
   auto hec = [&](int a, int b) -> T {
@@ -431,6 +433,119 @@ __global__ void __launch_bounds__(TX* TY)
     r_out[q] = f;
     if (UPDATE) x_out[q] = s.xv[lj][li];
   }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Row-streaming operator for large grids (the same arithmetic as k_op / k_smooth, in the same order).
+// A warp owns 32 consecutive columns i = ib-1 .. ib+30 of the (nx+1) x (ny+1) index space and walks up
+// the rows of its strip; lanes 1..30 write the outputs of columns ib .. ib+29.  The x-neighbours of a
+// point come from the adjacent lanes (warp shuffles) and its y-neighbours from the registers of the
+// previous row, so every array element is read once per strip, with whole-row coalesced loads, and no
+// shared memory or block barrier is involved.  Per row a lane loads u(i,j+2), v(i,j+2), h_v(i,j+2),
+// h_u(i,j+1) (the next rows, in flight while this row computes), hη_h, dimp, hη_c, β_u, β_v and the
+// interior masks of row j, and writes f_u(i,j), f_v(i,j).
+//   MODE 0: y = A x      MODE 2: smoother sweep: x_out = x_in + ω r_in / diag on colour `colour`,
+//                                r_out = b - A x_out on the interior (the fused k_smooth<UPDATE>)
+//   MODE 1: y = b - A x on the interior (k_smooth<!UPDATE>)
+// ------------------------------------------------------------------------------------------------
+constexpr int ST_WARPS = 4;   // warps per block
+constexpr int ST_COLS = 30;   // output columns per warp
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(32 * ST_WARPS)
+    k_op_stream(Dims d, OpCoef<T> cf, int rows, const T* __restrict__ x, const T* __restrict__ b, T* __restrict__ y,
+                int colour, const DevParams* __restrict__ P, const T* __restrict__ diag, const T* __restrict__ r_in,
+                T* __restrict__ x_out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ib = (blockIdx.x * ST_WARPS + warp) * ST_COLS;
+  const int i = ib - 1 + lane;
+  const int j0 = blockIdx.y * rows, j1 = min(j0 + rows, d.ny + 1);
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
+  const T omega = MODE == 2 ? (T)P->omega : (T)0;
+  const bool out_lane = lane >= 1 && lane <= ST_COLS;
+  const bool col_u = i >= 0 && i <= d.nx, col_v = i >= 0 && i < d.nx;
+  auto xu_at = [&](int jj) -> T {
+    if (!col_u || jj < 0 || jj >= d.ny) return (T)0;
+    const int q = uidx(d, i, jj);
+    T v = x[q];
+    if (MODE == 2 && 1 + ((i - jj) & 1) == colour && cf.inner[q]) v = v + omega * r_in[q] / diag[q];
+    return v;
+  };
+  auto xv_at = [&](int jj) -> T {
+    if (!col_v || jj < 0 || jj > d.ny) return (T)0;
+    const int q = vidx(d, i, jj);
+    T v = x[q];
+    if (MODE == 2 && 3 + ((i - jj) & 1) == colour && cf.inner[q]) v = v + omega * r_in[q] / diag[q];
+    return v;
+  };
+  auto hu_at = [&](int jj) -> T { return (col_u && jj >= 0 && jj < d.ny) ? cf.h_m[uidx(d, i, jj)] : (T)0; };
+  auto hv_at = [&](int jj) -> T { return (col_v && jj >= 0 && jj <= d.ny) ? cf.h_m[vidx(d, i, jj)] : (T)0; };
+  int j = j0 - 1;
+  T u_c = xu_at(j), v_c = xv_at(j), hu_c = hu_at(j), hv_c = hv_at(j);
+  T u_n = xu_at(j + 1), v_n = xv_at(j + 1), hv_n = hv_at(j + 1);
+  T ryy_p = 0, e_p = 0, rxyc_p = 0, rxyc_pl = 0;
+  for (; j < j1; ++j) {
+    const bool hcell = col_v && j >= 0 && j < d.ny;
+    const bool cpt = i >= 0 && i < d.nx - 1 && j >= 0 && j < d.ny - 1;
+    const T heh = hcell ? cf.heta_h[hidx(d, i, j)] : (T)0;
+    const T dm = hcell ? cf.dimp[hidx(d, i, j)] : (T)0;
+    const T hec = cpt ? cf.heta_c[cidx(d, i, j)] : (T)0;
+    const T u_nn = xu_at(j + 2), v_nn = xv_at(j + 2), hv_nn = hv_at(j + 2), hu_n = hu_at(j + 1);
+    const T uR = __shfl_down_sync(0xffffffffu, u_c, 1), huR = __shfl_down_sync(0xffffffffu, hu_c, 1);
+    const T u_nR = __shfl_down_sync(0xffffffffu, u_n, 1), v_nR = __shfl_down_sync(0xffffffffu, v_n, 1);
+    T rxx = 0, ryy = 0, e = 0, rxyc = 0;
+    if (hcell) {
+      const T ux = (uR - u_c) * rdx, vy = (v_n - v_c) * rdy;
+      const T he2 = (T)2 * heh;
+      rxx = he2 * ((T)2 * ux + vy);
+      ryy = he2 * ((T)2 * vy + ux);
+      if (dm != (T)0) e = dm * ((huR * uR - hu_c * u_c) * rdx + (hv_n * v_n - hv_c * v_c) * rdy);
+    }
+    if (cpt && hec != (T)0) rxyc = hec * ((u_nR - uR) * rdy + (v_nR - v_n) * rdx);
+    const T rxx_l = __shfl_up_sync(0xffffffffu, rxx, 1), e_l = __shfl_up_sync(0xffffffffu, e, 1);
+    const T rxyc_l = __shfl_up_sync(0xffffffffu, rxyc, 1);
+    if (j >= j0 && out_lane) {
+      if (col_u && j < d.ny) {
+        const int q = uidx(d, i, j);
+        T f = 0;
+        if (cf.inner[q]) {
+          f = (rxx - rxx_l) * rdx + (rxyc_l - rxyc_pl) * rdy - cf.beta_m[q] * u_c - hu_c * ((e - e_l) * rdx);
+          if (MODE != 0) f = b[q] - f;
+        }
+        y[q] = f;
+        if (MODE == 2) x_out[q] = u_c;
+      }
+      if (col_v && j <= d.ny) {
+        const int q = vidx(d, i, j);
+        T f = 0;
+        if (cf.inner[q]) {
+          f = (ryy - ryy_p) * rdy + (rxyc_p - rxyc_pl) * rdx - cf.beta_m[q] * v_c - hv_c * ((e - e_p) * rdy);
+          if (MODE != 0) f = b[q] - f;
+        }
+        y[q] = f;
+        if (MODE == 2) x_out[q] = v_c;
+      }
+    }
+    ryy_p = ryy;
+    e_p = e;
+    rxyc_p = rxyc;
+    rxyc_pl = rxyc_l;
+    u_c = u_n;
+    v_c = v_n;
+    hu_c = hu_n;
+    hv_c = hv_n;
+    u_n = u_nn;
+    v_n = v_nn;
+    hv_n = hv_nn;
+  }
+}
+
+// Launch shape of k_op_stream: column blocks of ST_WARPS * ST_COLS, row strips sized for ~8 blocks per SM.
+inline void stream_shape(const Dims& d, int nsm, dim3& grid, int& rows) {
+  const int ncb = (d.nx + 1 + ST_WARPS * ST_COLS - 1) / (ST_WARPS * ST_COLS);
+  const long target = 8L * nsm;
+  rows = (int)std::min<long>(64, std::max<long>(8, ((long)(d.ny + 1) * ncb + target - 1) / target));
+  grid = dim3((unsigned)ncb, (unsigned)((d.ny + 1 + rows - 1) / rows));
 }
 
 // Haar restriction of a fine vector (KIND 1, masked by the wavelet mask) with |out|^2; the last block

@@ -23,7 +23,26 @@ struct Dims {
   int nx, ny, ns;
   int Nh, Nu, Nv, Nc, N;
   double dx, dy, rdx, rdy;
+  float rdx_f, rdy_f;  // FP32 copies: a per-thread FP64 -> FP32 conversion runs on GB300's slow FP64 pipe
 };
+
+// 1/dx and 1/dy in the kernel's arithmetic type.
+template <typename T>
+__device__ __forceinline__ T rdx_of(const Dims& d) {
+  return (T)d.rdx;
+}
+template <>
+__device__ __forceinline__ float rdx_of<float>(const Dims& d) {
+  return d.rdx_f;
+}
+template <typename T>
+__device__ __forceinline__ T rdy_of(const Dims& d) {
+  return (T)d.rdy;
+}
+template <>
+__device__ __forceinline__ float rdy_of<float>(const Dims& d) {
+  return d.rdy_f;
+}
 
 __device__ __forceinline__ int hidx(const Dims& d, int i, int j) { return i + d.nx * j; }
 __device__ __forceinline__ int uidx(const Dims& d, int i, int j) { return i + (d.nx + 1) * j; }
@@ -114,7 +133,7 @@ __global__ void __launch_bounds__(OP_TX* OP_TY)
   __shared__ T sRxy[OP_TY + 1][OP_TX + 1];
   const int i0 = blockIdx.x * OP_TX, j0 = blockIdx.y * OP_TY;
   const int tid = threadIdx.x + OP_TX * threadIdx.y;
-  const T rdx = (T)d.rdx, rdy = (T)d.rdy;
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
   const TI* xu = x;
   for (int p = tid; p < (OP_TX + 1) * (OP_TY + 1); p += OP_TX * OP_TY) {
     const int li = p % (OP_TX + 1), lj = p / (OP_TX + 1);
@@ -183,7 +202,7 @@ __global__ void __launch_bounds__(OP_TX* OP_TY)
 template <typename T>
 __global__ void k_op_diag(Dims d, OpCoef<T> cf, T* __restrict__ diag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-  const T rdx = (T)d.rdx, rdy = (T)d.rdy, rdx2 = rdx * rdx, rdy2 = rdy * rdy;
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d), rdx2 = rdx * rdx, rdy2 = rdy * rdy;
   auto heh = [&](int a, int b) -> T { return (a >= 0 && a < d.nx && b >= 0 && b < d.ny) ? cf.heta_h[hidx(d, a, b)] : (T)0; };
   auto dim = [&](int a, int b) -> T { return (a >= 0 && a < d.nx && b >= 0 && b < d.ny) ? cf.dimp[hidx(d, a, b)] : (T)0; };
   auto hec = [&](int a, int b) -> T {

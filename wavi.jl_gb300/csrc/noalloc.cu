@@ -126,6 +126,8 @@ int wavi_residual_noalloc(const wavi_operator_desc* op, const double* x_uv, cons
   d.dy = op->dy;
   d.rdx = 1.0 / op->dx;
   d.rdy = 1.0 / op->dy;
+  d.rdx_f = (float)d.rdx;
+  d.rdy_f = (float)d.rdy;
   OpCoef<double> cf{op->heta_h, op->heta_c, op->dimp, op->beta_m, op->h_m, op->inner};
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // the last-block counter must start at zero; the partial sums are fully rewritten by every call

@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(TILE* TILE)
     s_hec[lb][la] = cv ? cf.heta_c[cidx(d, a, b)] : (T)0;
   }
   __syncthreads();
-  const T rdx = (T)d.rdx, rdy = (T)d.rdy;
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
   for (int comp = 0; comp < 2; ++comp) {
     const int nxg = comp == 0 ? d.nx + 1 : d.nx, nyg = comp == 0 ? d.ny : d.ny + 1;
     const int i = bx0 + tx, j = by0 + ty;

@@ -38,6 +38,8 @@ namespace {
 
 constexpr int EW_THREADS = 256;
 constexpr int CG_BATCH = 8;
+// grids with at least this many (nx+1) x (ny+1) points use the row-streaming operator by default
+constexpr long kStreamMinPoints = 1L << 19;
 
 }  // namespace
 
@@ -45,6 +47,10 @@ struct wavi_ctx {
   int dev = 0;
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t evc0 = nullptr, evc1 = nullptr;  // around a persistent coarse-CG launch (host-driven mode)
+  double coarse_ms = 0.0;
+  int coarse_launches = 0;
+  bool coarse_pending = false;
   Dims d{};
   wavi_solver_params sp{};
   wavi_options opt{};
@@ -83,6 +89,9 @@ struct wavi_ctx {
   DevState* hS = nullptr;     // pinned host copy
   // launch shapes
   dim3 op_grid, op_block, pt_grid, pt_block, haar_grid, haar_block, tile_grid, tile_block;
+  bool stream_op = false;  // operator and smoother sweeps by the row-streaming kernel (large grids)
+  dim3 st_grid;
+  int st_rows = 0;
   int ew_blocks = 0;
   // persistent coarse CG: grid barrier, launch shape, tiles per CTA (0 = per-iteration kernels)
   GridBar* bar = nullptr;
@@ -215,6 +224,42 @@ int enqueue_picard_head(wavi_ctx* c, const CondHandles& h, Tally& t) {
   return 0;
 }
 
+// One smoother sweep: update = true: the colour update of x_in, then r_out = b - A x_out; update =
+// false: r_out = b - A x_in.  Tiled (k_smooth) or row-streaming (k_op_stream) by grid size.
+template <typename T>
+int launch_smooth(wavi_ctx* c, bool update, int colour, const T* b, const T* diag, const T* x_in, const T* r_in,
+                  T* x_out, T* r_out) {
+  const Dims& d = c->d;
+  if (c->stream_op) {
+    if (update)
+      k_op_stream<T, 2><<<c->st_grid, 32 * ST_WARPS, 0, c->st>>>(d, coef<T>(c), c->st_rows, x_in, b, r_out, colour, c->P,
+                                                                 diag, r_in, x_out);
+    else
+      k_op_stream<T, 1><<<c->st_grid, 32 * ST_WARPS, 0, c->st>>>(d, coef<T>(c), c->st_rows, x_in, b, r_out, 0, c->P,
+                                                                 nullptr, nullptr, nullptr);
+  } else {
+    if (update)
+      k_smooth<T, OP_TX, OP_TY, true><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<T>(c), colour, c->P, b, diag, x_in,
+                                                                            r_in, x_out, r_out);
+    else
+      k_smooth<T, OP_TX, OP_TY, false><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<T>(c), 0, c->P, b, diag, x_in,
+                                                                             nullptr, nullptr, r_out);
+  }
+  CKL();
+  return 0;
+}
+
+template <typename T>
+int launch_op(wavi_ctx* c, const T* x, T* y) {
+  if (c->stream_op)
+    k_op_stream<T, 0><<<c->st_grid, 32 * ST_WARPS, 0, c->st>>>(c->d, coef<T>(c), c->st_rows, x, nullptr, y, 0, c->P,
+                                                               nullptr, nullptr, nullptr);
+  else
+    k_op<T, T, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<T>(c), x, nullptr, y, c->partials, nullptr);
+  CKL();
+  return 0;
+}
+
 template <typename T, int TILE>
 int enqueue_vcycle_pre(wavi_ctx* c, const CondHandles& h, Tally& t, bool cg_start = true) {
   const Dims& d = c->d;
@@ -231,9 +276,7 @@ int enqueue_vcycle_pre(wavi_ctx* c, const CondHandles& h, Tally& t, bool cg_star
   int cur = 0;
   for (int it = 0; it < c->sp.nsmooth; ++it)
     for (int oc = 0; oc < 4; ++oc) {
-      k_smooth<T, OP_TX, OP_TY, true><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<T>(c), fwd[oc], c->P, rs, diag,
-                                                                            corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]);
-      CKL();
+      TRY(launch_smooth<T>(c, true, fwd[oc], rs, diag, corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]));
       cur = 1 - cur;
       t.launches++;
       t.ops++;
@@ -351,9 +394,7 @@ int enqueue_vcycle_post(wavi_ctx* c, const CondHandles& h, Tally& t) {
                                                                    nullptr, c->S, nullptr);
   CKL();
   // r = b - A corr, then the sweeps in reversed colour order
-  k_smooth<T, OP_TX, OP_TY, false><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<T>(c), 0, c->P, rs, diag, corr[0],
-                                                                          nullptr, nullptr, rsm[0]);
-  CKL();
+  TRY(launch_smooth<T>(c, false, 0, rs, diag, corr[0], nullptr, nullptr, rsm[0]));
   t.launches += 2;
   t.ops++;
   t.bytes += op_bytes(d, sizeof(T), true) + 3.0 * sizeof(T) * d.N;
@@ -361,9 +402,7 @@ int enqueue_vcycle_post(wavi_ctx* c, const CondHandles& h, Tally& t) {
   int cur = 0;
   for (int it = 0; it < c->sp.nsmooth; ++it)
     for (int oc = 0; oc < 4; ++oc) {
-      k_smooth<T, OP_TX, OP_TY, true><<<c->op_grid, c->op_block, 0, c->st>>>(d, coef<T>(c), bwd[oc], c->P, rs, diag,
-                                                                            corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]);
-      CKL();
+      TRY(launch_smooth<T>(c, true, bwd[oc], rs, diag, corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]));
       cur = 1 - cur;
       t.launches++;
       t.ops++;
@@ -374,6 +413,18 @@ int enqueue_vcycle_post(wavi_ctx* c, const CondHandles& h, Tally& t) {
   CKL();
   t.launches++;
   t.bytes += (double)(2 * sizeof(T) + 8 * 3) * d.N + d.N;
+  return 0;
+}
+
+// Host-driven mode: add the duration of the last timed persistent coarse-CG launch (its stream has
+// been synchronised since).
+int collect_coarse_time(wavi_ctx* c) {
+  if (!c->coarse_pending) return 0;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->evc0, c->evc1));
+  c->coarse_ms += ms;
+  c->coarse_launches++;
+  c->coarse_pending = false;
   return 0;
 }
 
@@ -390,9 +441,13 @@ int enqueue_all_host_driven(wavi_ctx* c) {
     CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     c->host_syncs++;
+    TRY(collect_coarse_time(c));
     if (c->hS->vcycle_needed && c->pers_maxt > 0) {
       TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
+      CK(cudaEventRecord(c->evc0, c->st));
       TRY((enqueue_cg_persistent<T, TILE>(c, h, tv, tc)));
+      CK(cudaEventRecord(c->evc1, c->st));
+      c->coarse_pending = true;
       TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
     } else if (c->hS->vcycle_needed) {
       TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv)));
@@ -575,6 +630,9 @@ int set_params(wavi_ctx* c, const wavi_params* p) {
 int solve_resident(wavi_ctx* c, const wavi_params* p, wavi_stats* st) {
   c->launches = 0;
   c->host_syncs = 0;
+  c->coarse_ms = 0.0;
+  c->coarse_launches = 0;
+  c->coarse_pending = false;
   TRY(set_params(c, p));
   if (c->sp.maxiter_picard <= 0) {
     if (st) *st = wavi_stats{};
@@ -595,6 +653,7 @@ int solve_resident(wavi_ctx* c, const wavi_params* p, wavi_stats* st) {
   c->host_syncs++;
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  TRY(collect_coarse_time(c));
   const DevState& S = *c->hS;
   const int picard = S.picard_it, vcycles = S.converged ? picard - 1 : picard;
   if (c->opt.use_graphs) {  // launches the graph issued, from the per-segment tallies
@@ -613,6 +672,9 @@ int solve_resident(wavi_ctx* c, const wavi_params* p, wavi_stats* st) {
     st->elapsed_ms = ms;
     st->kernel_launches = (int32_t)std::min<long>(c->launches, 2147483647L);
     st->host_syncs = c->host_syncs;
+    st->coarse_ms = c->opt.use_graphs ? -1.0 : c->coarse_ms;
+    st->coarse_solver = c->coarse_solver;
+    st->coarse_launches = c->opt.use_graphs ? 0 : c->coarse_launches;
   }
   return 0;  // not converging is reported through stats.status only, like the reference's silent stop
 }
@@ -792,10 +854,14 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   d.dy = g->dy;
   d.rdx = 1.0 / g->dx;
   d.rdy = 1.0 / g->dy;
+  d.rdx_f = (float)d.rdx;
+  d.rdy_f = (float)d.rdy;
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(c, WAVI_ERR_CUDA, "stream creation failed"));
   cudaEventCreate(&c->ev0);
   cudaEventCreate(&c->ev1);
+  cudaEventCreate(&c->evc0);
+  cudaEventCreate(&c->evc1);
   // masks (src/Fields/Fields.jl:28-35; utilities.jl:475-507; UGrid.jl:76)
   std::vector<uint8_t> hm((size_t)d.Nh), cm((size_t)d.Nc, 0), mk((size_t)d.N, 0), in((size_t)d.N, 0), fx((size_t)d.N, 0);
   for (int i = 0; i < d.Nh; ++i) hm[i] = g->h_mask[i] ? 1 : 0;
@@ -855,6 +921,15 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   c->tile_block = dim3(c->tile, c->tile);
   c->tile_grid = dim3((d.nx + 1 + c->tile - 1) / c->tile, (d.ny + 1 + c->tile - 1) / c->tile);
   c->ew_blocks = (int)std::min<size_t>((N + EW_THREADS - 1) / EW_THREADS, 152 * 4);
+  {
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
+    stream_shape(d, std::max(nsm, 1), c->st_grid, c->st_rows);
+    const long points = (long)(d.nx + 1) * (d.ny + 1);
+    if (opt->stencil_kernel < 0 || opt->stencil_kernel > 2)
+      return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown stencil_kernel %d", opt->stencil_kernel));
+    c->stream_op = opt->stencil_kernel == 2 || (opt->stencil_kernel == 0 && points >= kStreamMinPoints);
+  }
   const int pt_blocks = (int)(c->pt_grid.x * c->pt_grid.y);
   const int op_blocks = (int)(c->op_grid.x * c->op_grid.y);
   const int tile_blocks = (int)(c->tile_grid.x * c->tile_grid.y);
@@ -926,6 +1001,8 @@ int wavi_ctx_destroy(wavi_ctx* c) {
   if (c->hS) cudaFreeHost(c->hS);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->evc0) cudaEventDestroy(c->evc0);
+  if (c->evc1) cudaEventDestroy(c->evc1);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return WAVI_OK;
@@ -979,15 +1056,12 @@ int wavi_apply_operator_device(wavi_ctx* c, int precision, const void* in_uv, vo
   TRY(check_ctx(c));
   if (!in_uv || !out_uv) return fail(c, WAVI_ERR_ARGUMENT, "null vector");
   if (precision == WAVI_PRECISION_FP64) {
-    k_op<double, double, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<double>(c), (const double*)in_uv, nullptr,
-                                                                   (double*)out_uv, c->partials, nullptr);
+    TRY(launch_op<double>(c, (const double*)in_uv, (double*)out_uv));
   } else if (precision == WAVI_PRECISION_MIXED && mixed(c)) {
-    k_op<float, float, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<float>(c), (const float*)in_uv, nullptr,
-                                                                 (float*)out_uv, c->partials, nullptr);
+    TRY(launch_op<float>(c, (const float*)in_uv, (float*)out_uv));
   } else {
     return fail(c, WAVI_ERR_ARGUMENT, "float32 operator needs a mixed-precision context");
   }
-  CKL();
   CK(cudaStreamSynchronize(c->st));
   return 0;
 }
@@ -1000,12 +1074,9 @@ int wavi_time_operator_device(wavi_ctx* c, int precision, const void* in_uv, voi
   CK(cudaEventRecord(c->ev0, c->st));
   for (int k = 0; k < repeats; ++k) {
     if (precision == WAVI_PRECISION_FP64)
-      k_op<double, double, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<double>(c), (const double*)in_uv,
-                                                                     nullptr, (double*)out_uv, c->partials, nullptr);
+      TRY(launch_op<double>(c, (const double*)in_uv, (double*)out_uv));
     else
-      k_op<float, float, 0><<<c->op_grid, c->op_block, 0, c->st>>>(c->d, coef<float>(c), (const float*)in_uv, nullptr,
-                                                                   (float*)out_uv, c->partials, nullptr);
-    CKL();
+      TRY(launch_op<float>(c, (const float*)in_uv, (float*)out_uv));
   }
   CK(cudaEventRecord(c->ev1, c->st));
   CK(cudaEventSynchronize(c->ev1));

@@ -36,9 +36,10 @@ class VelocitySolver:
     """One GPU velocity-solve context (``wavi_ctx``) for a fixed grid and solver parameters."""
 
     COARSE_KERNELS = {"auto": 0, "persistent": 1, "iterations": 2}
+    STENCIL_KERNELS = {"auto": 0, "tiled": 1, "streaming": 2}
 
     def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0,
-                 coarse_kernel="auto", coarse_solver="auto"):
+                 coarse_kernel="auto", coarse_solver="auto", stencil_kernel="auto"):
         self.lib = abi.load_library()
         self.grid = grid
         self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ
@@ -47,7 +48,8 @@ class VelocitySolver:
         self._desc = grid.descriptor()
         self._sp = solver_params.to_c()
         self._opt = abi.Options(int(device), PRECISIONS[precision], 1 if use_graphs else 0, int(picard_test),
-                                self.COARSE_KERNELS[coarse_kernel], abi.COARSE_SOLVERS[coarse_solver])
+                                self.COARSE_KERNELS[coarse_kernel], abi.COARSE_SOLVERS[coarse_solver],
+                                self.STENCIL_KERNELS[stencil_kernel], 0)
         ctx = C.c_void_p()
         st = self.lib.wavi_ctx_create(C.byref(self._desc.desc), C.byref(self._sp), C.byref(self._opt), C.byref(ctx))
         if st != 0:
@@ -170,4 +172,6 @@ def stats_dict(s):
             "picard_iterations": s.picard_iterations, "coarse_cg_iterations": s.coarse_cg_iterations,
             "op_applications": s.op_applications, "rel_residual": s.rel_residual, "rel_update": s.rel_update,
             "algorithmic_bytes": s.algorithmic_bytes, "elapsed_ms": s.elapsed_ms,
-            "kernel_launches": s.kernel_launches, "host_syncs": s.host_syncs}
+            "kernel_launches": s.kernel_launches, "host_syncs": s.host_syncs, "coarse_ms": s.coarse_ms,
+            "coarse_solver": abi.COARSE_SOLVER_NAMES.get(s.coarse_solver, s.coarse_solver),
+            "coarse_launches": s.coarse_launches}
