@@ -94,9 +94,10 @@ typedef struct wavi_options {
   int32_t use_graphs;                /* 1: capture each Picard iteration in a CUDA graph */
   int32_t picard_test;               /* 0: reference residual test ||b-Au||/||b|| < tol_picard;
                                         1: additionally require ||du||/||u|| <= tol_picard */
-  int32_t coarse_kernel;             /* coarse CG: 0 = one persistent kernel per V-cycle when the grid's
-                                        tiles fit the device's resident CTAs, else per-iteration kernels;
-                                        1 = persistent (error if it does not fit); 2 = per-iteration */
+  int32_t coarse_kernel;             /* coarse CG: 0 = one persistent kernel per V-cycle (CG vectors in
+                                        registers when the grid's tiles fit the device's resident CTAs,
+                                        else in global memory); 1 = persistent (error if it cannot run);
+                                        2 = per-iteration kernels; 3 = persistent, global-memory vectors */
   int32_t coarse_solver;             /* wavi_coarse_solver */
   int32_t stencil_kernel;            /* operator and smoother sweeps: 0 = by grid size (row-streaming from
                                         2^19 points of the (nx+1) x (ny+1) index space), 1 = shared-memory

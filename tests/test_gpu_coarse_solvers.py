@@ -64,9 +64,10 @@ def test_coarse_diagonal_matches_oracle(oracle, name):
         s.close()
 
 
+@pytest.mark.parametrize("kernel", ["persistent", "persistent_global"])
 @pytest.mark.parametrize("solver", ["srcg", "srcg_jacobi"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_single_reduction_fixed_cg_count_matches_oracle(oracle, reference_cg, name, solver):
+def test_single_reduction_fixed_cg_count_matches_oracle(oracle, reference_cg, name, solver, kernel):
     """One Picard iteration whose coarse solve runs exactly 10 single-reduction iterations (tol_coarse = 0),
     in FP64 on both sides: the same recurrences, so the velocities agree to rounding.  (Masking makes some
     Haar basis functions coincide on the interior, so R A P of a masked grid can be singular; with the
@@ -76,7 +77,7 @@ def test_single_reduction_fixed_cg_count_matches_oracle(oracle, reference_cg, na
     from wavi_gb300.gpu import VelocitySolver
     g, p, sp, om = _setup(oracle, name, maxiter_picard=1, maxiter_coarse=10, tol_coarse=0.0)
     f = fields_from_oracle(om, g)
-    s = VelocitySolver(g, sp, precision="fp64", coarse_kernel="persistent", coarse_solver=solver)
+    s = VelocitySolver(g, sp, precision="fp64", coarse_kernel=kernel, coarse_solver=solver)
     st = s.solve(p, f)
     oracle.set_coarse_variant(solver)
     om.update_velocities()
@@ -89,8 +90,9 @@ def test_single_reduction_fixed_cg_count_matches_oracle(oracle, reference_cg, na
     s.close()
 
 
+@pytest.mark.parametrize("kernel", ["persistent", "persistent_global"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_srcg_jacobi_converged_solve_matches_reference(oracle, name):
+def test_srcg_jacobi_converged_solve_matches_reference(oracle, name, kernel):
     """The Jacobi-preconditioned single-reduction coarse solve changes the V-cycle, not the fixed point: converged
     FP64 and mixed solves agree with the reference's (cg!) FP64 solve to 1e-6."""
     from wavi_gb300.gpu import VelocitySolver
@@ -100,7 +102,7 @@ def test_srcg_jacobi_converged_solve_matches_reference(oracle, name):
     ost = om.stats()
     for prec in ("fp64", "mixed"):
         f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
-        s = VelocitySolver(g, sp, precision=prec, coarse_kernel="persistent", coarse_solver="srcg_jacobi")
+        s = VelocitySolver(g, sp, precision=prec, coarse_kernel=kernel, coarse_solver="srcg_jacobi")
         st = s.solve(p, f)
         assert st["status"] == 0, (prec, st)
         assert uv_err(f, om) < 1e-6, (prec, st, ost)

@@ -110,7 +110,8 @@ def test_haar_transforms_match_oracle(oracle, name):
 
 
 @pytest.mark.parametrize("mode", [(True, "persistent"), (True, "iterations"), (False, "persistent"),
-                                  (False, "iterations"), (True, "persistent", "streaming")])
+                                  (False, "iterations"), (True, "persistent", "streaming"),
+                                  (True, "persistent_global"), (False, "persistent_global")])
 @pytest.mark.parametrize("name", list(CASES))
 def test_one_vcycle_fixed_cg_count_matches_oracle(oracle, name, mode):
     """One Picard iteration whose coarse CG runs exactly 25 iterations (tol_coarse = 0): relinearisation,
@@ -154,7 +155,8 @@ def test_one_picard_iteration_matches_oracle(oracle, name):
     s.close()
 
 
-@pytest.mark.parametrize("mode", [(True, "persistent"), (True, "iterations"), (False, "persistent")])
+@pytest.mark.parametrize("mode", [(True, "persistent"), (True, "iterations"), (False, "persistent"),
+                                  (True, "persistent_global")])
 @pytest.mark.parametrize("name", list(CASES))
 def test_converged_solve_matches_oracle(oracle, name, mode):
     from wavi_gb300.gpu import VelocitySolver

@@ -516,6 +516,284 @@ __global__ void __launch_bounds__(TILE* TILE)
 }
 
 // ------------------------------------------------------------------------------------------------
+// Grids whose tiles outnumber the device's resident CTAs: the same two solvers with the CG vectors in
+// global memory (L2-resident up to ~10^7 unknowns), each CTA looping over tiles t = blockIdx.x + k·gridDim.x
+// in every phase.  The arithmetic and its order are those of the register-resident kernels above.
+// Vectors (full layout, N entries): xc (iterate, in place), gr (residual), gz (z = M⁻¹ r, or cg!'s
+// direction u), gp, gs (C-G recurrences, or cg!'s c = R A u in gp), gw (R A z), w (prolonged vector).
+// ------------------------------------------------------------------------------------------------
+template <typename T>
+struct GlobalCG {
+  T *gr, *gz, *gp, *gs, *gw;
+};
+
+template <typename T, int TILE>
+__global__ void __launch_bounds__(TILE* TILE)
+    k_srcg_global(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, const T* __restrict__ dcoarse,
+                  T* __restrict__ w, const T* __restrict__ bc, T* __restrict__ xc, GlobalCG<T> g,
+                  double* __restrict__ partials, DevState* st, const DevParams* __restrict__ P, GridBar* bar, int ntx,
+                  int nty) {
+  __shared__ CGShared<T, TILE> sm;
+  __shared__ SyncShared ss;
+  __shared__ CGScalars<T> sc;
+  const int ntiles = ntx * nty;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  unsigned epoch = 0;
+  int it = 0;
+  const int maxit = P->maxiter_coarse;
+  const double tol_coarse = P->tol_coarse;
+  auto minv = [&](int q) -> T {
+    if (!dcoarse) return (T)1;
+    const T dq = dcoarse[q];
+    return dq != (T)0 ? (T)1 / dq : (T)0;
+  };
+  // w = P xc
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+    const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+    prolong_store<T, TILE>(d, levels, cf.inner, inu ? xc[uidx(d, i, j)] : (T)0, inv ? xc[vidx(d, i, j)] : (T)0, i0,
+                           j0, sm, w);
+  }
+  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+  // r = b_c - R A w;  z = M⁻¹ r;  p = s = 0
+  T bb = 0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+    const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+    T cu, cv;
+    coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0, j0, sm, cu, cv);
+    if (inu) {
+      const int q = uidx(d, i, j);
+      const T bu = bc[q], ru = bu - cu;
+      g.gr[q] = ru;
+      g.gz[q] = minv(q) * ru;
+      g.gp[q] = g.gs[q] = (T)0;
+      bb += bu * bu;
+    }
+    if (inv) {
+      const int q = vidx(d, i, j);
+      const T bv = bc[q], rv = bv - cv;
+      g.gr[q] = rv;
+      g.gz[q] = minv(q) * rv;
+      g.gp[q] = g.gs[q] = (T)0;
+      bb += bv * bv;
+    }
+  }
+  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;  // every CTA has read w
+  bool first = true;
+  for (;;) {
+    // (after the first pass) p = z + β p;  s = R A z + β s;  x += α p;  r -= α s;  z = M⁻¹ r;  w = P z
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+      const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+      T zz[2] = {(T)0, (T)0};
+#pragma unroll
+      for (int comp = 0; comp < 2; ++comp) {
+        if (comp == 0 ? !inu : !inv) continue;
+        const int q = comp == 0 ? uidx(d, i, j) : vidx(d, i, j);
+        T z = g.gz[q];
+        if (!first) {
+          const T alpha = sc.alpha_t, beta = sc.beta_t;
+          const T p = fmul_add(beta, g.gp[q], z), s = fmul_add(beta, g.gs[q], g.gw[q]);
+          const T x = fmul_add(alpha, p, xc[q]), r = fmul_add(-alpha, s, g.gr[q]);
+          z = minv(q) * r;
+          g.gp[q] = p;
+          g.gs[q] = s;
+          xc[q] = x;
+          g.gr[q] = r;
+          g.gz[q] = z;
+        }
+        zz[comp] = z;
+      }
+      prolong_store<T, TILE>(d, levels, cf.inner, zz[0], zz[1], i0, j0, sm, w);
+    }
+    if (!first) ++it;
+    if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+    T a[4] = {T(0), T(0), T(0), first ? bb : T(0)};
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+      T wu, wv;
+      coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0, j0, sm, wu, wv);
+      if (i <= d.nx && j < d.ny) {
+        const int q = uidx(d, i, j);
+        const T r = g.gr[q], z = g.gz[q];
+        a[0] += r * z;
+        a[1] += wu * z;
+        a[2] += r * r;
+        g.gw[q] = wu;
+      }
+      if (i < d.nx && j <= d.ny) {
+        const int q = vidx(d, i, j);
+        const T r = g.gr[q], z = g.gz[q];
+        a[0] += r * z;
+        a[1] += wv * z;
+        a[2] += r * r;
+        g.gw[q] = wv;
+      }
+    }
+    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const double* tot) {
+          const double gamma = tot[0], delta = tot[1];
+          sc.res = sqrt(tot[2]);
+          int stop;
+          if (first) {
+            sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[3]));  // reltol = sqrt(eps)
+            sc.beta = 0.0;
+            sc.alpha = gamma / delta;
+            stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
+          } else {
+            stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
+            if (!stop) {
+              sc.beta = gamma / sc.gamma_prev;
+              sc.alpha = gamma / (delta - sc.beta * gamma / sc.alpha);
+            }
+          }
+          if (!stop && (!(sc.alpha == sc.alpha) || isinf(sc.alpha))) stop = 1;
+          sc.gamma_prev = gamma;
+          sc.alpha_t = (T)sc.alpha;
+          sc.beta_t = (T)sc.beta;
+          sc.stop = stop;
+        }))
+      return;
+    if (sc.stop) break;
+    first = false;
+  }
+  if (blockIdx.x == 0 && tx == 0 && ty == 0) {
+    st->cg_it = it;
+    st->cg_total += it;
+    st->cg_res = sc.res;
+    st->cg_tol = sc.tol;
+  }
+}
+
+// cg! with global vectors: gz holds the direction u, gp holds c = R A u.
+template <typename T, int TILE>
+__global__ void __launch_bounds__(TILE* TILE)
+    k_cg_global(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, T* __restrict__ w,
+                const T* __restrict__ bc, T* __restrict__ xc, GlobalCG<T> g, double* __restrict__ partials, DevState* st,
+                const DevParams* __restrict__ P, GridBar* bar, int ntx, int nty) {
+  __shared__ CGShared<T, TILE> sm;
+  __shared__ SyncShared ss;
+  __shared__ CGScalars<T> sc;
+  const int ntiles = ntx * nty;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  unsigned epoch = 0;
+  int it = 0;
+  const int maxit = P->maxiter_coarse;
+  const double tol_coarse = P->tol_coarse;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+    const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+    prolong_store<T, TILE>(d, levels, cf.inner, inu ? xc[uidx(d, i, j)] : (T)0, inv ? xc[vidx(d, i, j)] : (T)0, i0,
+                           j0, sm, w);
+  }
+  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+  {
+    T a[4] = {T(0), T(0), T(0), T(0)};
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+      T cu, cv;
+      coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0, j0, sm, cu, cv);
+      if (i <= d.nx && j < d.ny) {
+        const int q = uidx(d, i, j);
+        const T bu = bc[q], ru = bu - cu;
+        g.gr[q] = ru;
+        g.gz[q] = (T)0;
+        a[0] += ru * ru;
+        a[1] += bu * bu;
+      }
+      if (i < d.nx && j <= d.ny) {
+        const int q = vidx(d, i, j);
+        const T bv = bc[q], rv = bv - cv;
+        g.gr[q] = rv;
+        g.gz[q] = (T)0;
+        a[0] += rv * rv;
+        a[1] += bv * bv;
+      }
+    }
+    if (!grid_sync<2>(bar, partials, epoch, ss, a, [&](const double* tot) {
+          sc.res = sqrt(tot[0]);
+          sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[1]));  // reltol = sqrt(eps)
+          sc.alpha_prev = 1.0;  // prev
+          sc.stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
+          sc.beta = sc.res * sc.res;
+          sc.beta_t = (T)0;  // u = 0: the first direction is r
+        }))
+      return;
+  }
+  while (!sc.stop) {
+    const T beta = sc.beta_t;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+      const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+      T uu = 0, uv = 0;
+      if (inu) {
+        const int q = uidx(d, i, j);
+        uu = fmul_add(beta, g.gz[q], g.gr[q]);
+        g.gz[q] = uu;
+      }
+      if (inv) {
+        const int q = vidx(d, i, j);
+        uv = fmul_add(beta, g.gz[q], g.gr[q]);
+        g.gz[q] = uv;
+      }
+      prolong_store<T, TILE>(d, levels, cf.inner, uu, uv, i0, j0, sm, w);
+    }
+    if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+    T dot[4] = {T(0), T(0), T(0), T(0)};
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+      T cu, cv;
+      coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0, j0, sm, cu, cv);
+      if (i <= d.nx && j < d.ny) {
+        const int q = uidx(d, i, j);
+        dot[0] += g.gz[q] * cu;
+        g.gp[q] = cu;
+      }
+      if (i < d.nx && j <= d.ny) {
+        const int q = vidx(d, i, j);
+        dot[0] += g.gz[q] * cv;
+        g.gp[q] = cv;
+      }
+    }
+    if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const double* tot) {
+          sc.alpha = (sc.res * sc.res) / tot[0];
+          sc.alpha_t = (T)sc.alpha;
+        }))
+      return;
+    const T alpha = sc.alpha_t;
+    T rr[4] = {T(0), T(0), T(0), T(0)};
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+#pragma unroll
+      for (int comp = 0; comp < 2; ++comp) {
+        if (comp == 0 ? !(i <= d.nx && j < d.ny) : !(i < d.nx && j <= d.ny)) continue;
+        const int q = comp == 0 ? uidx(d, i, j) : vidx(d, i, j);
+        xc[q] = fmul_add(alpha, g.gz[q], xc[q]);
+        const T r = fmul_add(-alpha, g.gp[q], g.gr[q]);
+        g.gr[q] = r;
+        rr[0] += r * r;
+      }
+    }
+    ++it;
+    if (!grid_sync<1>(bar, partials, epoch, ss, rr, [&](const double* tot) {
+          sc.alpha_prev = sc.res;  // prev
+          sc.res = sqrt(tot[0]);
+          sc.stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
+          sc.beta = (sc.res * sc.res) / (sc.alpha_prev * sc.alpha_prev);
+          sc.beta_t = (T)sc.beta;
+        }))
+      return;
+  }
+  if (blockIdx.x == 0 && tx == 0 && ty == 0) {
+    st->cg_it = it;
+    st->cg_total += it;
+    st->cg_res = sc.res;
+    st->cg_prev = sc.alpha_prev;
+    st->cg_tol = sc.tol;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
 // Exact diagonal of the coarse operator R A P (a Jacobi preconditioner for the mixed-precision coarse
 // solve).  With P e_k = inner ⊙ (φ ⊗ ψ) a Haar basis function and A symmetric, summation by parts of the
 // operator's differences gives its quadratic form

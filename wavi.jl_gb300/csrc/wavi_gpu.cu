@@ -95,7 +95,8 @@ struct wavi_ctx {
   int ew_blocks = 0;
   // persistent coarse CG: grid barrier, launch shape, tiles per CTA (0 = per-iteration kernels)
   GridBar* bar = nullptr;
-  int pers_maxt = 0, pers_grid = 0, ntx = 0, nty = 0;
+  int pers_maxt = 0, pers_grid = 0, ntx = 0, nty = 0;  // pers_maxt -1: CG vectors in global memory
+  void *gz = nullptr, *gw = nullptr;                    // extra vectors of the global-memory variant
   int coarse_solver = WAVI_COARSE_CG;  // resolved coarse solver (never WAVI_COARSE_AUTO)
   void* dcoarse = nullptr;             // diag(R A P) for the Jacobi-preconditioned single-reduction CG
   // solve graph
@@ -354,6 +355,35 @@ int launch_cg_persistent(wavi_ctx* c) {
   return 0;
 }
 
+// The same with the CG vectors in global memory (grids with more tiles than resident CTAs).
+template <typename T, int TILE>
+int launch_cg_global(wavi_ctx* c) {
+  const Dims& d = c->d;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)c->pers_grid);
+  cfg.blockDim = dim3(TILE, TILE);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const GlobalCG<T> g{(T*)c->rc, (T*)c->gz, (T*)c->uc, (T*)c->cc, (T*)c->gw};
+  if (c->coarse_solver == WAVI_COARSE_CG) {
+    CK(cudaLaunchKernelEx(&cfg, k_cg_global<T, TILE>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv, (T*)c->w,
+                          (const T*)c->bc, (T*)c->xc, g, c->partials, c->S, (const DevParams*)c->P, c->bar, c->ntx,
+                          c->nty));
+  } else {
+    const T* dc = c->coarse_solver == WAVI_COARSE_SRCG_JACOBI ? (const T*)c->dcoarse : nullptr;
+    CK(cudaLaunchKernelEx(&cfg, k_srcg_global<T, TILE>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv, dc,
+                          (T*)c->w, (const T*)c->bc, (T*)c->xc, g, c->partials, c->S, (const DevParams*)c->P, c->bar,
+                          c->ntx, c->nty));
+  }
+  c->launches++;
+  return 0;
+}
+
 template <typename T, int TILE>
 int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& tc) {
   const Dims& d = c->d;
@@ -365,7 +395,9 @@ int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& t
   }
   k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar);
   CKL();
-  if (c->pers_maxt == 1)
+  if (c->pers_maxt < 0)
+    TRY((launch_cg_global<T, TILE>(c)));
+  else if (c->pers_maxt == 1)
     TRY((launch_cg_persistent<T, TILE, 1>(c)));
   else if (c->pers_maxt == 2)
     TRY((launch_cg_persistent<T, TILE, 2>(c)));
@@ -442,7 +474,7 @@ int enqueue_all_host_driven(wavi_ctx* c) {
     CK(cudaStreamSynchronize(c->st));
     c->host_syncs++;
     TRY(collect_coarse_time(c));
-    if (c->hS->vcycle_needed && c->pers_maxt > 0) {
+    if (c->hS->vcycle_needed && c->pers_maxt != 0) {
       TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
       CK(cudaEventRecord(c->evc0, c->st));
       TRY((enqueue_cg_persistent<T, TILE>(c, h, tv, tc)));
@@ -529,7 +561,7 @@ int build_graph(wavi_ctx* c) {
   TRY(enqueue_picard_head(c, h, tp));
   TRY(end_capture(c, pbody, sinks));
   TRY(add_conditional(c, pbody, sinks, h.vcycle, cudaGraphCondTypeIf, &vbody, &vnode));
-  if (c->pers_maxt > 0) {
+  if (c->pers_maxt != 0) {
     // V-cycle body: pre part, one persistent coarse-CG kernel, post part
     TRY(begin_capture(c, vbody, {}));
     TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
@@ -587,7 +619,7 @@ void choose_persistent(wavi_ctx* c) {
   const int caps[3] = {resident_ctas<1, T, TILE>(nsm, s), resident_ctas<2, T, TILE>(nsm, s),
                        resident_ctas<4, T, TILE>(nsm, s)};
   const int maxts[3] = {1, 2, 4};
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 3 && c->opt.coarse_kernel != 3; ++k) {
     const long g = (ntiles + maxts[k] - 1) / maxts[k];
     if (caps[k] > 0 && g <= caps[k]) {
       c->pers_maxt = maxts[k];
@@ -595,6 +627,14 @@ void choose_persistent(wavi_ctx* c) {
       return;
     }
   }
+  // global-memory vectors: one CTA per resident slot, looping over the tiles
+  int per_sm = 0;
+  cudaError_t e = s == WAVI_COARSE_CG
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_global<T, TILE>, TILE * TILE, 0)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_srcg_global<T, TILE>, TILE * TILE, 0);
+  if (e != cudaSuccess || per_sm <= 0) return;
+  c->pers_maxt = -1;
+  c->pers_grid = (int)std::min<long>(ntiles, (long)per_sm * nsm);
 }
 
 int ensure_graph(wavi_ctx* c) {
@@ -940,6 +980,8 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   const int want = opt->coarse_solver;
   if (want < WAVI_COARSE_AUTO || want > WAVI_COARSE_SRCG_JACOBI)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_solver %d", want));
+  if (opt->coarse_kernel < 0 || opt->coarse_kernel > 3)
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_kernel %d", opt->coarse_kernel));
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));
   c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) ? WAVI_COARSE_SRCG_JACOBI : WAVI_COARSE_CG) : want;
@@ -955,7 +997,7 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
       c->tile == 16 ? (mixed(c) ? choose_persistent<float, 16>(c) : choose_persistent<double, 16>(c))
                     : (mixed(c) ? choose_persistent<float, 32>(c) : choose_persistent<double, 32>(c));
     }
-    if (opt->coarse_kernel == 1 && c->pers_maxt == 0)
+    if ((opt->coarse_kernel == 1 || opt->coarse_kernel == 3) && c->pers_maxt == 0)
       return bail(fail(c, WAVI_ERR_ARGUMENT, "the persistent coarse CG does not fit this grid on this device"));
   } else {
     c->coarse_solver = WAVI_COARSE_CG;
@@ -970,6 +1012,12 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
     double* q = nullptr;
     if ((r = dalloc(c, &q, N))) return bail(r);
     c->dcoarse = q;
+    if (c->pers_maxt < 0) {
+      if ((r = dalloc(c, &q, N))) return bail(r);
+      c->gz = q;
+      if ((r = dalloc(c, &q, N))) return bail(r);
+      c->gw = q;
+    }
   }
   if ((r = dalloc(c, &c->P, 1))) return bail(r);
   if ((r = dalloc(c, &c->S, 1))) return bail(r);

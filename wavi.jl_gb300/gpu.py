@@ -35,7 +35,7 @@ ALL_FIELDS = abi.FIELD_INPUTS + abi.FIELD_STATE + ("wu_mask", "wv_mask", "wu_cor
 class VelocitySolver:
     """One GPU velocity-solve context (``wavi_ctx``) for a fixed grid and solver parameters."""
 
-    COARSE_KERNELS = {"auto": 0, "persistent": 1, "iterations": 2}
+    COARSE_KERNELS = {"auto": 0, "persistent": 1, "iterations": 2, "persistent_global": 3}
     STENCIL_KERNELS = {"auto": 0, "tiled": 1, "streaming": 2}
 
     def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0,
