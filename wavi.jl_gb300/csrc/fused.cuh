@@ -441,9 +441,9 @@ __global__ void __launch_bounds__(TX* TY)
 // the rows of its strip; lanes 1..30 write the outputs of columns ib .. ib+29.  The x-neighbours of a
 // point come from the adjacent lanes (warp shuffles) and its y-neighbours from the registers of the
 // previous row, so every array element is read once per strip, with whole-row coalesced loads, and no
-// shared memory or block barrier is involved.  Per row a lane loads u(i,j+2), v(i,j+2), h_v(i,j+2),
-// h_u(i,j+1) (the next rows, in flight while this row computes), hη_h, dimp, hη_c, β_u, β_v and the
-// interior masks of row j, and writes f_u(i,j), f_v(i,j).
+// shared memory or block barrier is involved.  While row j computes, a lane's loads for the next rows
+// are in flight: u, v, h_u, h_v of row j+2 and hη_h, dimp, hη_c, β_u, β_v and the interior masks of
+// row j+1.  It writes f_u(i,j), f_v(i,j).
 //   MODE 0: y = A x      MODE 2: smoother sweep: x_out = x_in + ω r_in / diag on colour `colour`,
 //                                r_out = b - A x_out on the interior (the fused k_smooth<UPDATE>)
 //   MODE 1: y = b - A x on the interior (k_smooth<!UPDATE>)
@@ -480,36 +480,62 @@ __global__ void __launch_bounds__(32 * ST_WARPS)
   };
   auto hu_at = [&](int jj) -> T { return (col_u && jj >= 0 && jj < d.ny) ? cf.h_m[uidx(d, i, jj)] : (T)0; };
   auto hv_at = [&](int jj) -> T { return (col_v && jj >= 0 && jj <= d.ny) ? cf.h_m[vidx(d, i, jj)] : (T)0; };
+  // per-row coefficients, loaded one row ahead of their use
+  struct RowCoef {
+    T heh, dm, hec, bu, bv;
+    uint8_t iu, iv;
+  };
+  auto coef_at = [&](int jj) -> RowCoef {
+    RowCoef r{(T)0, (T)0, (T)0, (T)0, (T)0, 0, 0};
+    if (col_v && jj >= 0 && jj < d.ny) {
+      r.heh = cf.heta_h[hidx(d, i, jj)];
+      r.dm = cf.dimp[hidx(d, i, jj)];
+    }
+    if (i >= 0 && i < d.nx - 1 && jj >= 0 && jj < d.ny - 1) r.hec = cf.heta_c[cidx(d, i, jj)];
+    if (jj >= j0 && out_lane) {
+      if (col_u && jj < d.ny) {
+        const int q = uidx(d, i, jj);
+        r.iu = cf.inner[q];
+        r.bu = cf.beta_m[q];
+      }
+      if (col_v && jj <= d.ny) {
+        const int q = vidx(d, i, jj);
+        r.iv = cf.inner[q];
+        r.bv = cf.beta_m[q];
+      }
+    }
+    return r;
+  };
   int j = j0 - 1;
   T u_c = xu_at(j), v_c = xv_at(j), hu_c = hu_at(j), hv_c = hv_at(j);
-  T u_n = xu_at(j + 1), v_n = xv_at(j + 1), hv_n = hv_at(j + 1);
+  T u_n = xu_at(j + 1), v_n = xv_at(j + 1), hv_n = hv_at(j + 1), hu_n = hu_at(j + 1);
+  RowCoef k_c = coef_at(j);
   T ryy_p = 0, e_p = 0, rxyc_p = 0, rxyc_pl = 0;
   for (; j < j1; ++j) {
     const bool hcell = col_v && j >= 0 && j < d.ny;
     const bool cpt = i >= 0 && i < d.nx - 1 && j >= 0 && j < d.ny - 1;
-    const T heh = hcell ? cf.heta_h[hidx(d, i, j)] : (T)0;
-    const T dm = hcell ? cf.dimp[hidx(d, i, j)] : (T)0;
-    const T hec = cpt ? cf.heta_c[cidx(d, i, j)] : (T)0;
-    const T u_nn = xu_at(j + 2), v_nn = xv_at(j + 2), hv_nn = hv_at(j + 2), hu_n = hu_at(j + 1);
+    // next rows' loads go out before this row's arithmetic
+    const RowCoef k_n = coef_at(j + 1);
+    const T u_nn = xu_at(j + 2), v_nn = xv_at(j + 2), hv_nn = hv_at(j + 2), hu_nn = hu_at(j + 2);
     const T uR = __shfl_down_sync(0xffffffffu, u_c, 1), huR = __shfl_down_sync(0xffffffffu, hu_c, 1);
     const T u_nR = __shfl_down_sync(0xffffffffu, u_n, 1), v_nR = __shfl_down_sync(0xffffffffu, v_n, 1);
     T rxx = 0, ryy = 0, e = 0, rxyc = 0;
     if (hcell) {
       const T ux = (uR - u_c) * rdx, vy = (v_n - v_c) * rdy;
-      const T he2 = (T)2 * heh;
+      const T he2 = (T)2 * k_c.heh;
       rxx = he2 * ((T)2 * ux + vy);
       ryy = he2 * ((T)2 * vy + ux);
-      if (dm != (T)0) e = dm * ((huR * uR - hu_c * u_c) * rdx + (hv_n * v_n - hv_c * v_c) * rdy);
+      if (k_c.dm != (T)0) e = k_c.dm * ((huR * uR - hu_c * u_c) * rdx + (hv_n * v_n - hv_c * v_c) * rdy);
     }
-    if (cpt && hec != (T)0) rxyc = hec * ((u_nR - uR) * rdy + (v_nR - v_n) * rdx);
+    if (cpt && k_c.hec != (T)0) rxyc = k_c.hec * ((u_nR - uR) * rdy + (v_nR - v_n) * rdx);
     const T rxx_l = __shfl_up_sync(0xffffffffu, rxx, 1), e_l = __shfl_up_sync(0xffffffffu, e, 1);
     const T rxyc_l = __shfl_up_sync(0xffffffffu, rxyc, 1);
     if (j >= j0 && out_lane) {
       if (col_u && j < d.ny) {
         const int q = uidx(d, i, j);
         T f = 0;
-        if (cf.inner[q]) {
-          f = (rxx - rxx_l) * rdx + (rxyc_l - rxyc_pl) * rdy - cf.beta_m[q] * u_c - hu_c * ((e - e_l) * rdx);
+        if (k_c.iu) {
+          f = (rxx - rxx_l) * rdx + (rxyc_l - rxyc_pl) * rdy - k_c.bu * u_c - hu_c * ((e - e_l) * rdx);
           if (MODE != 0) f = b[q] - f;
         }
         y[q] = f;
@@ -518,8 +544,8 @@ __global__ void __launch_bounds__(32 * ST_WARPS)
       if (col_v && j <= d.ny) {
         const int q = vidx(d, i, j);
         T f = 0;
-        if (cf.inner[q]) {
-          f = (ryy - ryy_p) * rdy + (rxyc_p - rxyc_pl) * rdx - cf.beta_m[q] * v_c - hv_c * ((e - e_p) * rdy);
+        if (k_c.iv) {
+          f = (ryy - ryy_p) * rdy + (rxyc_p - rxyc_pl) * rdx - k_c.bv * v_c - hv_c * ((e - e_p) * rdy);
           if (MODE != 0) f = b[q] - f;
         }
         y[q] = f;
@@ -536,7 +562,9 @@ __global__ void __launch_bounds__(32 * ST_WARPS)
     hv_c = hv_n;
     u_n = u_nn;
     v_n = v_nn;
+    hu_n = hu_nn;
     hv_n = hv_nn;
+    k_c = k_n;
   }
 }
 
