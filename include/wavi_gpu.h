@@ -110,7 +110,8 @@ typedef struct wavi_options {
  * compute both inner products of an iteration in one grid reduction, keep cg!'s stopping rule on the
  * unpreconditioned residual, and need the persistent coarse kernel. */
 typedef enum wavi_coarse_solver {
-  WAVI_COARSE_AUTO = 0,              /* FP64: cg!; mixed: SRCG_JACOBI when the persistent kernel fits */
+  WAVI_COARSE_AUTO = 0,              /* FP64: cg!; mixed: SRCG_JACOBI when the persistent kernel fits and
+                                        the ice mask covers the whole domain, else cg! */
   WAVI_COARSE_CG = 1,                /* the reference's cg! recurrence */
   WAVI_COARSE_SRCG = 2,              /* single-reduction CG, no preconditioner (same iterates as cg!) */
   WAVI_COARSE_SRCG_JACOBI = 3        /* single-reduction CG preconditioned by diag(R A P) */
@@ -283,6 +284,24 @@ typedef struct wavi_operator_desc {
  * different streams, or from different host threads — race and must be ordered by the caller. */
 int wavi_residual_noalloc(const wavi_operator_desc* op, const double* x_uv, const double* b_uv, double* r_uv,
                           double* rr_out, void* stream);
+
+/* ---- Ensembles ---------------------------------------------------------------------------------
+ * n independent domains (grids of different sizes) solved concurrently: one context per member (own
+ * stream, device buffers and solve graph), at most `concurrency` members in flight, each member's
+ * persistent coarse-CG kernel sized to 1/concurrency of the device's resident CTAs so that the
+ * concurrent cooperative launches always fit together.  The reference has no ensemble call; this is
+ * update_velocities! (update_velocities.jl:11-29) for each member, the role SharedMemorySpec's per-
+ * subdomain solves on threads play there (src/SharedMemorySpec.jl:101-125).
+ * options->use_graphs must be 1.  grids and solver_params are arrays of n. */
+typedef struct wavi_ensemble wavi_ensemble;
+int wavi_ensemble_create(int n, const wavi_grid_desc* grids, const wavi_solver_params* solver_params,
+                         const wavi_options* options, int concurrency, wavi_ensemble** out);
+/* update_velocities! for every member: params, fields (device pointers) and stats are arrays of n.
+ * Returns when every member's results are in its arrays; per-member convergence is in stats[k].status.
+ * A hard error returns the first failing member's status (message in wavi_ensemble_last_error). */
+int wavi_ensemble_solve_device(wavi_ensemble* ens, const wavi_params* params, wavi_fields* fields, wavi_stats* stats);
+int wavi_ensemble_destroy(wavi_ensemble* ens);
+const char* wavi_ensemble_last_error(const wavi_ensemble* ens);
 
 #ifdef __cplusplus
 }

@@ -130,6 +130,11 @@ def load_library(path=None):
         "wavi_time_operator_device": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.POINTER(C.c_double)]),
         "wavi_haar_device": (C.c_int, [vp, C.c_int, vp, vp, vp]),
         "wavi_residual_noalloc": (C.c_int, [C.POINTER(OperatorDesc), vp, vp, vp, vp, vp]),
+        "wavi_ensemble_create": (C.c_int, [C.c_int, C.POINTER(GridDesc), C.POINTER(SolverParams), C.POINTER(Options),
+                                           C.c_int, C.POINTER(vp)]),
+        "wavi_ensemble_solve_device": (C.c_int, [vp, C.POINTER(Params), C.POINTER(Fields), C.POINTER(Stats)]),
+        "wavi_ensemble_destroy": (C.c_int, [vp]),
+        "wavi_ensemble_last_error": (C.c_char_p, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -576,6 +576,90 @@ inline void stream_shape(const Dims& d, int nsm, dim3& grid, int& rows) {
   grid = dim3((unsigned)ncb, (unsigned)((d.ny + 1 + rows - 1) / rows));
 }
 
+// ------------------------------------------------------------------------------------------------
+// Compact <-> full coarse-correction cache on the device.  The reference stores the coarse correction
+// compactly, one entry per true wavelet-mask point in column-major order (UWavelets.jl:46,
+// get_correction_coarse / set_correction_coarse!, update_preconditioners.jl:195-216); the solver keeps
+// it on the full grid.  A point's compact index is the number of mask points before it: per-block
+// counts (k_mask_count), an exclusive scan of the counts (k_scan_counts, one block), then each block
+// ranks its points with warp ballots (k_mask_map).  One range (the u part or the v part) per launch.
+// ------------------------------------------------------------------------------------------------
+constexpr int MS_BLOCK = 1024;
+
+static __global__ void __launch_bounds__(MS_BLOCK) k_mask_count(const uint8_t* __restrict__ m, int n, int* __restrict__ counts) {
+  const int i = blockIdx.x * MS_BLOCK + threadIdx.x;
+  const int c = __syncthreads_count(i < n && m[i] != 0);
+  if (threadIdx.x == 0) counts[blockIdx.x] = c;
+}
+
+static __global__ void __launch_bounds__(MS_BLOCK) k_scan_counts(int* __restrict__ counts, int nblocks) {
+  __shared__ int warp_tot[32];
+  __shared__ int carry;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  if (t == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nblocks; base += MS_BLOCK) {
+    const int k = base + t;
+    const int v = k < nblocks ? counts[k] : 0;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+      int w = warp_tot[lane], wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, wi, o);
+        if (lane >= o) wi += y;
+      }
+      warp_tot[lane] = wi - w;  // exclusive warp offsets
+    }
+    __syncthreads();
+    const int excl = carry + warp_tot[wid] + incl - v;
+    __syncthreads();
+    if (k < nblocks) counts[k] = excl;
+    if (t == MS_BLOCK - 1) carry = excl + v;
+    __syncthreads();
+  }
+}
+
+// EXPAND: full[i] = m[i] ? compact[rank(i)] : 0 (and m01[i] = m[i] != 0); else compact[rank(i)] = full[i].
+template <bool EXPAND>
+__global__ void __launch_bounds__(MS_BLOCK)
+    k_mask_map(const uint8_t* __restrict__ m, int n, const int* __restrict__ offsets, double* __restrict__ full,
+               double* __restrict__ compact, uint8_t* __restrict__ m01) {
+  __shared__ int warp_off[32];
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int i = blockIdx.x * MS_BLOCK + t;
+  const bool on = i < n && m[i] != 0;
+  const unsigned bal = __ballot_sync(0xffffffffu, on);
+  if (lane == 0) warp_off[wid] = __popc(bal);
+  __syncthreads();
+  if (wid == 0) {
+    const int w = warp_off[lane];
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += y;
+    }
+    warp_off[lane] = wi - w;
+  }
+  __syncthreads();
+  if (i >= n) return;
+  const int pos = offsets[blockIdx.x] + warp_off[wid] + __popc(bal & ((1u << lane) - 1u));
+  if (EXPAND) {
+    full[i] = on ? compact[pos] : 0.0;
+    m01[i] = on ? 1 : 0;
+  } else if (on) {
+    compact[pos] = full[i];
+  }
+}
+
 // Haar restriction of a fine vector (KIND 1, masked by the wavelet mask) with |out|^2; the last block
 // stores |b_c| = sqrt(total) for the coarse CG's absolute tolerance (update_preconditioners.jl:65-70).
 template <typename T, int TILE>

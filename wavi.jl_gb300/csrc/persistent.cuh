@@ -542,8 +542,9 @@ __global__ void __launch_bounds__(TILE* TILE)
   int it = 0;
   const int maxit = P->maxiter_coarse;
   const double tol_coarse = P->tol_coarse;
+  const bool use_m = dcoarse != nullptr;
   auto minv = [&](int q) -> T {
-    if (!dcoarse) return (T)1;
+    if (!use_m) return (T)1;
     const T dq = dcoarse[q];
     return dq != (T)0 ? (T)1 / dq : (T)0;
   };

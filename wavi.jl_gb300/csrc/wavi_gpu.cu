@@ -51,6 +51,8 @@ struct wavi_ctx {
   double coarse_ms = 0.0;
   int coarse_launches = 0;
   bool coarse_pending = false;
+  bool skipped = false;  // the last enqueued solve had maxiter_picard <= 0
+  int pers_share = 1;    // persistent coarse kernels of this many contexts may run at once (ensembles)
   Dims d{};
   wavi_solver_params sp{};
   wavi_options opt{};
@@ -99,6 +101,13 @@ struct wavi_ctx {
   void *gz = nullptr, *gw = nullptr;                    // extra vectors of the global-memory variant
   int coarse_solver = WAVI_COARSE_CG;  // resolved coarse solver (never WAVI_COARSE_AUTO)
   void* dcoarse = nullptr;             // diag(R A P) for the Jacobi-preconditioned single-reduction CG
+  // coarse-correction cache mapping: block offsets of the mask scan (u part, then v part from
+  // mask_offsets_v), staging for host callers, and the host masks' counts
+  int* mask_offsets = nullptr;
+  int mask_offsets_v = 0;
+  uint8_t* wmask_in = nullptr;
+  double* comp_stage = nullptr;
+  long nwu = 0, nwv = 0;
   // solve graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -616,8 +625,9 @@ void choose_persistent(wavi_ctx* c) {
   if (!coop || nsm <= 0) return;
   const long ntiles = (long)c->ntx * c->nty;
   const int s = c->coarse_solver;
-  const int caps[3] = {resident_ctas<1, T, TILE>(nsm, s), resident_ctas<2, T, TILE>(nsm, s),
-                       resident_ctas<4, T, TILE>(nsm, s)};
+  const int share = std::max(1, c->pers_share);
+  const int caps[3] = {resident_ctas<1, T, TILE>(nsm, s) / share, resident_ctas<2, T, TILE>(nsm, s) / share,
+                       resident_ctas<4, T, TILE>(nsm, s) / share};
   const int maxts[3] = {1, 2, 4};
   for (int k = 0; k < 3 && c->opt.coarse_kernel != 3; ++k) {
     const long g = (ntiles + maxts[k] - 1) / maxts[k];
@@ -634,7 +644,7 @@ void choose_persistent(wavi_ctx* c) {
                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_srcg_global<T, TILE>, TILE * TILE, 0);
   if (e != cudaSuccess || per_sm <= 0) return;
   c->pers_maxt = -1;
-  c->pers_grid = (int)std::min<long>(ntiles, (long)per_sm * nsm);
+  c->pers_grid = (int)std::max<long>(1, std::min<long>(ntiles, (long)per_sm * nsm / share));
 }
 
 int ensure_graph(wavi_ctx* c) {
@@ -667,17 +677,17 @@ int set_params(wavi_ctx* c, const wavi_params* p) {
   return 0;
 }
 
-int solve_resident(wavi_ctx* c, const wavi_params* p, wavi_stats* st) {
+// A solve in two halves: solve_enqueue issues the whole solve on the context's stream (and, in graph
+// mode, returns at once); solve_finish waits for it and fills the statistics.
+int solve_enqueue(wavi_ctx* c, const wavi_params* p) {
   c->launches = 0;
   c->host_syncs = 0;
   c->coarse_ms = 0.0;
   c->coarse_launches = 0;
   c->coarse_pending = false;
   TRY(set_params(c, p));
-  if (c->sp.maxiter_picard <= 0) {
-    if (st) *st = wavi_stats{};
-    return 0;
-  }
+  c->skipped = c->sp.maxiter_picard <= 0;
+  if (c->skipped) return 0;
   CK(cudaEventRecord(c->ev0, c->st));
   if (c->opt.use_graphs) {
     TRY(ensure_graph(c));
@@ -689,6 +699,17 @@ int solve_resident(wavi_ctx* c, const wavi_params* p, wavi_stats* st) {
   }
   CK(cudaEventRecord(c->ev1, c->st));
   CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
+  return 0;
+}
+
+int solve_finish(wavi_ctx* c, wavi_stats* st) {
+  if (c->skipped) {
+    if (st) {
+      *st = wavi_stats{};
+      st->coarse_solver = c->coarse_solver;
+    }
+    return 0;
+  }
   CK(cudaStreamSynchronize(c->st));
   c->host_syncs++;
   float ms = 0.f;
@@ -719,6 +740,11 @@ int solve_resident(wavi_ctx* c, const wavi_params* p, wavi_stats* st) {
   return 0;  // not converging is reported through stats.status only, like the reference's silent stop
 }
 
+int solve_resident(wavi_ctx* c, const wavi_params* p, wavi_stats* st) {
+  TRY(solve_enqueue(c, p));
+  return solve_finish(c, st);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Upload / download between wavi_fields and the context
 // ---------------------------------------------------------------------------------------------
@@ -730,6 +756,24 @@ int copy_in(wavi_ctx* c, double* dst, const double* src, size_t n, cudaMemcpyKin
 int copy_out(wavi_ctx* c, double* dst, const double* src, size_t n, cudaMemcpyKind kind, const char* name) {
   if (!dst) return fail(c, WAVI_ERR_ARGUMENT, "field %s is null", name);
   CK(cudaMemcpyAsync(dst, src, n * sizeof(double), kind, c->st));
+  return 0;
+}
+
+// Full <-> compact coarse-correction cache for one part (u: base 0, n = Nu; v: base Nu, n = Nv).
+// EXPAND also writes the normalised wavelet mask and the part's block offsets, which the compaction
+// after the solve reuses (the solve does not change the mask).
+template <bool EXPAND>
+int map_coarse_cache(wavi_ctx* c, const uint8_t* mask, int n, int base, double* compact) {
+  const int nb = (n + MS_BLOCK - 1) / MS_BLOCK;
+  int* off = c->mask_offsets + (base == 0 ? 0 : c->mask_offsets_v);
+  if (EXPAND) {
+    k_mask_count<<<nb, MS_BLOCK, 0, c->st>>>(mask, n, off);
+    CKL();
+    k_scan_counts<<<1, MS_BLOCK, 0, c->st>>>(off, nb);
+    CKL();
+  }
+  k_mask_map<EXPAND><<<nb, MS_BLOCK, 0, c->st>>>(mask, n, off, c->xc_full64 + base, compact, c->wmask_uv + base);
+  CKL();
   return 0;
 }
 
@@ -749,29 +793,28 @@ int upload(wavi_ctx* c, const wavi_fields* f, bool host) {
   IN(c->beta_eff_uv, f->gu_beta_eff, d.Nu) IN(c->beta_eff_uv + d.Nu, f->gv_beta_eff, d.Nv)
   IN(c->resid_uv, f->gu_residual, d.Nu) IN(c->resid_uv + d.Nu, f->gv_residual, d.Nv)
 #undef IN
-  // adaptive coarse space and its compact correction cache -> full layout
+  // adaptive coarse space and its compact correction cache -> full layout, on the device
   if (!f->wu_mask || !f->wv_mask || !f->wu_correction_coarse || !f->wv_correction_coarse)
     return fail(c, WAVI_ERR_ARGUMENT, "wavelet masks / coarse corrections are null");
-  const cudaMemcpyKind kh = host ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost;
-  std::vector<uint8_t> wm((size_t)d.N);
-  CK(cudaMemcpyAsync(wm.data(), f->wu_mask, d.Nu, kh, c->st));
-  CK(cudaMemcpyAsync(wm.data() + d.Nu, f->wv_mask, d.Nv, kh, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  size_t nwu = 0, nwv = 0;
-  for (int i = 0; i < d.Nu; ++i) nwu += (wm[i] = wm[i] ? 1 : 0);
-  for (int i = d.Nu; i < d.N; ++i) nwv += (wm[i] = wm[i] ? 1 : 0);
-  std::vector<double> cu(nwu), cv(nwv), full((size_t)d.N, 0.0);
-  if (nwu) CK(cudaMemcpyAsync(cu.data(), f->wu_correction_coarse, nwu * sizeof(double), kh, c->st));
-  if (nwv) CK(cudaMemcpyAsync(cv.data(), f->wv_correction_coarse, nwv * sizeof(double), kh, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  size_t a = 0, b = 0;
-  for (int i = 0; i < d.Nu; ++i)
-    if (wm[i]) full[i] = cu[a++];
-  for (int i = d.Nu; i < d.N; ++i)
-    if (wm[i]) full[i] = cv[b++];
-  CK(cudaMemcpyAsync(c->wmask_uv, wm.data(), d.N, cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(c->xc_full64, full.data(), sizeof(double) * d.N, cudaMemcpyHostToDevice, c->st));
-  CK(cudaStreamSynchronize(c->st));
+  const uint8_t* mu = f->wu_mask;
+  const uint8_t* mv = f->wv_mask;
+  const double* cu = f->wu_correction_coarse;
+  const double* cv = f->wv_correction_coarse;
+  if (host) {  // stage the host arrays (the compact lengths are the host masks' counts)
+    c->nwu = c->nwv = 0;
+    for (int i = 0; i < d.Nu; ++i) c->nwu += f->wu_mask[i] != 0;
+    for (int i = 0; i < d.Nv; ++i) c->nwv += f->wv_mask[i] != 0;
+    CK(cudaMemcpyAsync(c->wmask_in, f->wu_mask, d.Nu, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->wmask_in + d.Nu, f->wv_mask, d.Nv, cudaMemcpyHostToDevice, c->st));
+    if (c->nwu) CK(cudaMemcpyAsync(c->comp_stage, f->wu_correction_coarse, sizeof(double) * c->nwu, cudaMemcpyHostToDevice, c->st));
+    if (c->nwv) CK(cudaMemcpyAsync(c->comp_stage + d.Nu, f->wv_correction_coarse, sizeof(double) * c->nwv, cudaMemcpyHostToDevice, c->st));
+    mu = c->wmask_in;
+    mv = c->wmask_in + d.Nu;
+    cu = c->comp_stage;
+    cv = c->comp_stage + d.Nu;
+  }
+  TRY(map_coarse_cache<true>(c, mu, d.Nu, 0, const_cast<double*>(cu)));
+  TRY(map_coarse_cache<true>(c, mv, d.Nv, d.Nu, const_cast<double*>(cv)));
   return 0;
 }
 
@@ -787,23 +830,17 @@ int download(wavi_ctx* c, wavi_fields* f, bool host) {
   OUT(f->gu_beta_eff, c->beta_eff_uv, d.Nu) OUT(f->gv_beta_eff, c->beta_eff_uv + d.Nu, d.Nv)
   OUT(f->gu_residual, c->resid_uv, d.Nu) OUT(f->gv_residual, c->resid_uv + d.Nu, d.Nv)
 #undef OUT
-  // coarse correction cache: full -> compact in mask order
-  std::vector<double> full((size_t)d.N);
-  std::vector<uint8_t> wm((size_t)d.N);
-  CK(cudaMemcpyAsync(full.data(), c->xc_full64, sizeof(double) * d.N, cudaMemcpyDeviceToHost, c->st));
-  CK(cudaMemcpyAsync(wm.data(), c->wmask_uv, d.N, cudaMemcpyDeviceToHost, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  std::vector<double> cu, cv;
-  cu.reserve(d.Nu);
-  cv.reserve(d.Nv);
-  for (int i = 0; i < d.Nu; ++i)
-    if (wm[i]) cu.push_back(full[i]);
-  for (int i = d.Nu; i < d.N; ++i)
-    if (wm[i]) cv.push_back(full[i]);
-  const cudaMemcpyKind hk = host ? cudaMemcpyHostToHost : cudaMemcpyHostToDevice;
-  if (!cu.empty()) CK(cudaMemcpyAsync(f->wu_correction_coarse, cu.data(), sizeof(double) * cu.size(), hk, c->st));
-  if (!cv.empty()) CK(cudaMemcpyAsync(f->wv_correction_coarse, cv.data(), sizeof(double) * cv.size(), hk, c->st));
-  CK(cudaStreamSynchronize(c->st));
+  // coarse correction cache: full -> compact in mask order, on the device
+  if (host) {
+    TRY(map_coarse_cache<false>(c, c->wmask_uv, d.Nu, 0, c->comp_stage));
+    TRY(map_coarse_cache<false>(c, c->wmask_uv + d.Nu, d.Nv, d.Nu, c->comp_stage + d.Nu));
+    if (c->nwu) CK(cudaMemcpyAsync(f->wu_correction_coarse, c->comp_stage, sizeof(double) * c->nwu, cudaMemcpyDeviceToHost, c->st));
+    if (c->nwv) CK(cudaMemcpyAsync(f->wv_correction_coarse, c->comp_stage + d.Nu, sizeof(double) * c->nwv, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  } else {
+    TRY(map_coarse_cache<false>(c, c->wmask_uv, d.Nu, 0, f->wu_correction_coarse));
+    TRY(map_coarse_cache<false>(c, c->wmask_uv + d.Nu, d.Nv, d.Nu, f->wv_correction_coarse));
+  }
   return 0;
 }
 
@@ -853,7 +890,8 @@ const char* wavi_last_error(const wavi_ctx* ctx) { return ctx ? ctx->err.c_str()
 
 void* wavi_ctx_stream(const wavi_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
 
-int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const wavi_options* opt, wavi_ctx** out) {
+static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, const wavi_options* opt, int share,
+                      wavi_ctx** out) {
   wavi_ctx* c = nullptr;
   if (!out) return fail(nullptr, WAVI_ERR_ARGUMENT, "out is null");
   *out = nullptr;
@@ -871,6 +909,7 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   if (opt->device < 0 || opt->device >= ndev) return fail(nullptr, WAVI_ERR_ARGUMENT, "device %d out of range", opt->device);
   if ((long)(g->nx + 1) * (g->ny + 1) > (1L << 30)) return fail(nullptr, WAVI_ERR_ARGUMENT, "grid too large");
   c = new wavi_ctx();
+  c->pers_share = std::max(1, share);
   c->dev = opt->device;
   c->sp = *sp;
   c->opt = *opt;
@@ -942,8 +981,10 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   A(beta_eff_uv, N) A(resid_uv, N) A(hn, Nh)
   A(heta_h64, Nh) A(heta_c64, Nc) A(dimp64, Nh) A(beta_m64, N) A(h_m64, N)
   A(heta_h32, Nh) A(heta_c32, Nc) A(dimp32, Nh) A(beta_m32, N) A(h_m32, N)
-  A(x64, N) A(b64, N) A(r64, N) A(xfix64, N)
+  A(x64, N) A(b64, N) A(r64, N) A(xfix64, N) A(wmask_in, N) A(comp_stage, N)
 #undef A
+  c->mask_offsets_v = (d.Nu + MS_BLOCK - 1) / MS_BLOCK;
+  if ((r = dalloc(c, &c->mask_offsets, (size_t)c->mask_offsets_v + (d.Nv + MS_BLOCK - 1) / MS_BLOCK))) return bail(r);
   for (void** p : {&c->rs, &c->corr[0], &c->corr[1], &c->rsm[0], &c->rsm[1], &c->diag, &c->xc, &c->rc, &c->uc, &c->cc,
                    &c->w, &c->bc}) {
     double* q = nullptr;
@@ -984,7 +1025,13 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_kernel %d", opt->coarse_kernel));
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));
-  c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) ? WAVI_COARSE_SRCG_JACOBI : WAVI_COARSE_CG) : want;
+  // auto: FP64 runs the reference's cg!; mixed runs the Jacobi single-reduction CG on domains whose ice
+  // mask is full, and cg! where the mask cuts the domain (calving fronts inside it): there the masked
+  // Haar functions can coincide on the interior, R A P turns singular, and the FP32 Jacobi iteration
+  // was seen to stall the Picard loop where the unpreconditioned recurrences converge
+  bool full_mask = true;
+  for (int i = 0; i < d.Nh && full_mask; ++i) full_mask = hm[i] != 0;
+  c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) && full_mask ? WAVI_COARSE_SRCG_JACOBI : WAVI_COARSE_CG) : want;
   if (opt->coarse_kernel != 2) {
     if (mixed(c))
       c->tile == 16 ? choose_persistent<float, 16>(c) : choose_persistent<float, 32>(c);
@@ -1038,6 +1085,10 @@ int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const
   return WAVI_OK;
 }
 
+int wavi_ctx_create(const wavi_grid_desc* g, const wavi_solver_params* sp, const wavi_options* opt, wavi_ctx** out) {
+  return create_ctx(g, sp, opt, 1, out);
+}
+
 int wavi_ctx_destroy(wavi_ctx* c) {
   if (!c) return WAVI_OK;
   cudaSetDevice(c->dev);
@@ -1071,7 +1122,9 @@ int wavi_solve_velocities_device(wavi_ctx* c, const wavi_params* p, wavi_fields*
   if (!f) return fail(c, WAVI_ERR_ARGUMENT, "fields is null");
   TRY(upload(c, f, false));
   TRY(solve_resident(c, p, st));
-  return download(c, f, false);
+  TRY(download(c, f, false));
+  CK(cudaStreamSynchronize(c->st));  // results are in the caller's arrays on return
+  return 0;
 }
 
 int wavi_relinearise_device(wavi_ctx* c, const wavi_params* p, wavi_fields* f) {
@@ -1096,8 +1149,9 @@ int wavi_relinearise_device(wavi_ctx* c, const wavi_params* p, wavi_fields* f) {
                   mixed(c) ? c->h_m32 : nullptr, mixed(c) ? c->heta_c32 : nullptr};
   k_relin_uv<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, uin, uout);
   CKL();
+  TRY(download(c, f, false));
   CK(cudaStreamSynchronize(c->st));
-  return download(c, f, false);
+  return 0;
 }
 
 int wavi_apply_operator_device(wavi_ctx* c, int precision, const void* in_uv, void* out_uv) {
@@ -1189,6 +1243,107 @@ int wavi_haar_device(wavi_ctx* c, int kind, const double* in_uv, double* out_uv,
   CKL();
   CK(cudaStreamSynchronize(c->st));
   return 0;
+}
+
+
+// ---------------------------------------------------------------------------------------------
+// Ensembles: independent domains solved concurrently, one context (stream, graph) per member
+// ---------------------------------------------------------------------------------------------
+}  // extern "C"
+
+struct wavi_ensemble {
+  std::vector<wavi_ctx*> m;
+  std::vector<cudaEvent_t> done;
+  int concurrency = 1;
+  std::string err;
+};
+
+namespace {
+int ens_fail(wavi_ensemble* e, int code, const std::string& msg) {
+  e->err = msg;
+  return code;
+}
+}  // namespace
+
+extern "C" {
+
+int wavi_ensemble_create(int n, const wavi_grid_desc* grids, const wavi_solver_params* sps, const wavi_options* opt,
+                         int concurrency, wavi_ensemble** out) {
+  if (!out) return fail(nullptr, WAVI_ERR_ARGUMENT, "out is null");
+  *out = nullptr;
+  if (n < 1 || !grids || !sps || !opt) return fail(nullptr, WAVI_ERR_ARGUMENT, "bad ensemble arguments");
+  if (!opt->use_graphs) return fail(nullptr, WAVI_ERR_ARGUMENT, "ensemble members run as CUDA graphs (use_graphs = 1)");
+  auto* e = new wavi_ensemble();
+  e->concurrency = std::max(1, std::min(concurrency, n));
+  for (int k = 0; k < n; ++k) {
+    wavi_ctx* c = nullptr;
+    const int r = create_ctx(&grids[k], &sps[k], opt, e->concurrency, &c);
+    cudaEvent_t ev = nullptr;
+    if (r == 0 && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+      wavi_ctx_destroy(c);
+      c = nullptr;
+    }
+    if (!c) {
+      const std::string msg = "member " + std::to_string(k) + ": " + (r ? g_create_error : std::string("event creation failed"));
+      wavi_ensemble_destroy(e);
+      return fail(nullptr, r ? r : WAVI_ERR_CUDA, "%s", msg.c_str());
+    }
+    e->m.push_back(c);
+    e->done.push_back(ev);
+  }
+  *out = e;
+  return WAVI_OK;
+}
+
+int wavi_ensemble_destroy(wavi_ensemble* e) {
+  if (!e) return WAVI_OK;
+  for (wavi_ctx* c : e->m) wavi_ctx_destroy(c);
+  for (cudaEvent_t ev : e->done)
+    if (ev) cudaEventDestroy(ev);
+  delete e;
+  return WAVI_OK;
+}
+
+const char* wavi_ensemble_last_error(const wavi_ensemble* e) { return e ? e->err.c_str() : g_create_error.c_str(); }
+
+int wavi_ensemble_solve_device(wavi_ensemble* e, const wavi_params* params, wavi_fields* fields, wavi_stats* stats) {
+  if (!e || !params || !fields) return WAVI_ERR_ARGUMENT;
+  const int n = (int)e->m.size(), S = e->concurrency;
+  int err = 0, err_k = -1;
+  int issued = 0;
+  // largest members first (longest-processing-time order), so that big domains do not form the tail
+  std::vector<int> order(n);
+  for (int k = 0; k < n; ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return e->m[a]->d.N > e->m[b]->d.N; });
+  for (int o = 0; o < n && !err; ++o) {
+    const int k = order[o];
+    wavi_ctx* c = e->m[k];
+    int r = check_ctx(c);
+    if (!r) r = check_params(c, &params[k]);
+    // at most S members in flight: the o-th member starts after the (o - S)-th has finished
+    if (!r && o >= S && cudaStreamWaitEvent(c->st, e->done[order[o - S]], 0) != cudaSuccess)
+      r = fail(c, WAVI_ERR_CUDA, "stream wait");
+    if (!r) r = upload(c, &fields[k], false);
+    if (!r) r = solve_enqueue(c, &params[k]);
+    if (!r) r = download(c, &fields[k], false);
+    if (!r && cudaEventRecord(e->done[k], c->st) != cudaSuccess) r = fail(c, WAVI_ERR_CUDA, "event record");
+    if (r) {
+      err = r;
+      err_k = k;
+    } else {
+      issued = o + 1;
+    }
+  }
+  for (int o = 0; o < issued; ++o) {
+    const int k = order[o];
+    const int r = solve_finish(e->m[k], stats ? &stats[k] : nullptr);
+    if (r && !err) {
+      err = r;
+      err_k = k;
+    }
+  }
+  if (err) return ens_fail(e, err, "member " + std::to_string(err_k) + ": " + e->m[err_k]->err);
+  return WAVI_OK;
 }
 
 }  // extern "C"

@@ -1,0 +1,84 @@
+"""Ensembles of independent domains solved at once (include/wavi_gpu.h, wavi_ensemble_*), and the
+autotuner that picks their launch configuration.
+
+An ensemble holds one solver context per member (grids of different sizes); a solve issues every
+member's whole Picard-converged solve (a CUDA graph) on the member's own stream, with at most
+``concurrency`` members in flight, and returns when all are done.  There is no CPU fallback.
+"""
+import ctypes as C
+import dataclasses
+import time
+
+from . import abi
+from .gpu import PRECISIONS, VelocitySolver, device_fields, stats_dict
+
+
+class EnsembleSolver:
+    """``wavi_ensemble``: one context per member grid, solved concurrently."""
+
+    def __init__(self, grids, solver_params, precision="mixed", device=0, concurrency=16, coarse_kernel="auto",
+                 coarse_solver="auto", stencil_kernel="auto"):
+        self.lib = abi.load_library()
+        self.n = n = len(grids)
+        if len(solver_params) != n:
+            raise ValueError("one SolverParams per member")
+        self.grids = grids
+        descs = [g.descriptor() for g in grids]  # keeps the mask arrays alive through the create call
+        garr = (abi.GridDesc * n)(*[d.desc for d in descs])
+        sparr = (abi.SolverParams * n)(*[sp.to_c() for sp in solver_params])
+        opt = abi.Options(int(device), PRECISIONS[precision], 1, 0, VelocitySolver.COARSE_KERNELS[coarse_kernel],
+                          abi.COARSE_SOLVERS[coarse_solver], VelocitySolver.STENCIL_KERNELS[stencil_kernel], 0)
+        ens = C.c_void_p()
+        st = self.lib.wavi_ensemble_create(n, garr, sparr, C.byref(opt), int(concurrency), C.byref(ens))
+        if st != 0:
+            raise abi.WaviError(st, self.lib.wavi_last_error(None).decode())
+        self.ens = ens
+        self.config = dict(concurrency=int(concurrency), coarse_kernel=coarse_kernel, coarse_solver=coarse_solver,
+                           stencil_kernel=stencil_kernel)
+
+    def close(self):
+        if getattr(self, "ens", None) and self.ens.value:
+            self.lib.wavi_ensemble_destroy(self.ens)
+            self.ens = C.c_void_p()
+
+    __del__ = close
+
+    def solve_device(self, params, tensors):
+        """update_velocities! for every member: params and tensors (dicts of device tensors, modified in
+        place) are lists of n.  Returns the members' stats dicts."""
+        n = self.n
+        parr = (abi.Params * n)(*[p.to_c() for p in params])
+        farr = (abi.Fields * n)(*[device_fields(t) for t in tensors])
+        starr = (abi.Stats * n)()
+        st = self.lib.wavi_ensemble_solve_device(self.ens, parr, farr, starr)
+        if st != 0:
+            raise abi.WaviError(st, self.lib.wavi_ensemble_last_error(self.ens).decode())
+        return [stats_dict(starr[k]) for k in range(n)]
+
+
+DEFAULT_CANDIDATES = tuple(dict(concurrency=s, coarse_kernel=ck) for s in (8, 16, 32, 64)
+                           for ck in ("auto", "iterations"))
+
+
+def autotune(grids, solver_params, params, make_tensors, precision="mixed", device=0, candidates=DEFAULT_CANDIDATES,
+             picard=2, sync=None):
+    """Pick the ensemble launch configuration: for each candidate (keyword arguments of EnsembleSolver:
+    members in flight, coarse-CG kernel, stencil kernel) time one ensemble solve capped at `picard`
+    Picard iterations, after one untimed solve that instantiates the graphs.  `make_tensors()` returns
+    fresh device copies of every member's fields.  Returns (best candidate, [(seconds, candidate), ...])."""
+    capped = [dataclasses.replace(sp, maxiter_picard=picard) for sp in solver_params]
+    timings = []
+    for cand in candidates:
+        ens = EnsembleSolver(grids, capped, precision=precision, device=device, **cand)
+        try:
+            ens.solve_device(params, make_tensors())
+            tensors = make_tensors()
+            if sync:
+                sync()
+            t0 = time.perf_counter()
+            ens.solve_device(params, tensors)
+            timings.append((time.perf_counter() - t0, cand))
+        finally:
+            ens.close()
+    best = min(timings, key=lambda tc: tc[0])[1]
+    return best, timings

@@ -109,15 +109,7 @@ class VelocitySolver:
 
     # -- device tensors ----------------------------------------------------------------------------
     def _device_fields(self, tensors):
-        f = abi.Fields()
-        for name in ALL_FIELDS:
-            t = tensors[name]
-            ptr = t.data_ptr()
-            if name in ("wu_mask", "wv_mask"):
-                setattr(f, name, C.cast(C.c_void_p(ptr), C.POINTER(C.c_uint8)))
-            else:
-                setattr(f, name, C.cast(C.c_void_p(ptr), C.POINTER(C.c_double)))
-        return f
+        return device_fields(tensors)
 
     def solve_device(self, params, tensors):
         """update_velocities! on device tensors (dict of name -> tensor with data_ptr()), in place."""
@@ -165,6 +157,18 @@ class VelocitySolver:
         st = self.lib.wavi_haar_device(self.ctx, int(kind), C.c_void_p(in_uv.data_ptr()), C.c_void_p(out_uv.data_ptr()), m)
         if st != 0:
             raise self._err(st)
+
+
+def device_fields(tensors):
+    """wavi_fields of device pointers from a dict of name -> tensor (anything with data_ptr())."""
+    f = abi.Fields()
+    for name in ALL_FIELDS:
+        ptr = tensors[name].data_ptr()
+        if name in ("wu_mask", "wv_mask"):
+            setattr(f, name, C.cast(C.c_void_p(ptr), C.POINTER(C.c_uint8)))
+        else:
+            setattr(f, name, C.cast(C.c_void_p(ptr), C.POINTER(C.c_double)))
+    return f
 
 
 def stats_dict(s):

@@ -133,6 +133,31 @@ def channel_c3(**kw):
     return channel_case(nx, ny, dx, ns, C=C, temperature=temp, **kw)
 
 
+def ensemble_members(n=256, seed=6, tol_picard=1e-6, maxiter_picard=100):
+    """The ragged ensemble: n independent channel domains at dx = dy = 2 km, nσ = 4, with nx ~ U{64..512},
+    ny ~ U{16..128}, C ~ log-U(3e3, 3e4) and accumulation ~ U(0.1, 0.5) drawn from `seed`.  Each member
+    is the MISMIP+ channel scaled to its own extent with its own roughness (seed 1000 + k) and thickness
+    noise (seed 2000 + k), both drawn on the 8 km template and refined, as for the 640 x 80 case.
+    Returns a list of (grid, bed, params, solver_params, initial_conditions)."""
+    rng = np.random.default_rng(seed)
+    nxs = rng.integers(64, 513, size=n)
+    nys = rng.integers(16, 129, size=n)
+    cs = np.exp(rng.uniform(np.log(3.0e3), np.log(3.0e4), size=n))
+    accs = rng.uniform(0.1, 0.5, size=n)
+    out = []
+    for k in range(n):
+        nx, ny = int(nxs[k]), int(nys[k])
+        g = _grid(nx, ny, 2000.0, 4)
+        bed = refined_channel_bed(g, seed=1000 + k)
+        p = Params(accumulation_rate=float(accs[k]), glen_a_ref=2.0e-17, weertman_c=float(cs[k]),
+                   default_temperature=263.15)
+        sp = SolverParams(tol_picard=tol_picard, maxiter_picard=maxiter_picard)
+        ic = InitialConditions(initial_thickness=np.asfortranarray(
+            300.0 * (1.0 + template_field((nx, ny), 2000 + k, "uniform"))))
+        out.append((g, bed, p, sp, ic))
+    return out
+
+
 def small_case(nx=24, ny=12, dx=4000.0, ns=4, seed=0, mask="full", fixed=False, **kw):
     """Small ragged test cases: masks 'full', 'disc' (a circular ice mask, calving fronts on all sides),
     optional Dirichlet lines (u_isfixed / v_isfixed) as in the reference's iceberg test."""
