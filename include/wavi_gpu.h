@@ -285,6 +285,29 @@ typedef struct wavi_operator_desc {
 int wavi_residual_noalloc(const wavi_operator_desc* op, const double* x_uv, const double* b_uv, double* r_uv,
                           double* rr_out, void* stream);
 
+/* ---- Adjoint and tangent linear of the converged solve ------------------------------------------
+ * Gradients with respect to per-cell log C (Weertman drag coefficient, update_state.jl:129-134) and
+ * log A (rate factor, all σ levels; B = A^(-1/n), utilities.jl:462-466) of a misfit J(u, v), by implicit
+ * differentiation of the Picard fixed point of the last solve on this context (update_velocities.jl
+ * :11-29 at convergence: A(coef) x = b together with the per-cell viscosity and drag fixed points
+ * :227-339): one linear solve with the transposed linearised operator J_Fᵀ (viscosity and drag
+ * derivatives included), by FGMRES preconditioned with one V-cycle of the solve's preconditioner.  The
+ * reference has no adjoint.  Preconditions: a float64 context, no u/v_isfixed points, a preceding solve
+ * converged tightly (the linearisation is exact at the fixed point).  Device pointers: dJ_du (nx+1)*ny,
+ * dJ_dv nx*(ny+1) in, dJ_dlogC and dJ_dlogA nx*ny out.  The solve's state is left unchanged. */
+typedef struct wavi_adjoint_stats {
+  int32_t status;                    /* 0, or WAVI_ERR_NOT_CONVERGED if the linear solve hit maxiter */
+  int32_t iterations;                /* FGMRES iterations (one preconditioned operator application each) */
+  double rel_residual;               /* final ||b - K x|| / ||b|| of the linear solve */
+  double elapsed_ms;                 /* host wall time of the call */
+} wavi_adjoint_stats;
+int wavi_adjoint_device(wavi_ctx* ctx, const wavi_params* params, const double* dJ_du, const double* dJ_dv,
+                        double* dJ_dlogC, double* dJ_dlogA, double tol, int maxiter, wavi_adjoint_stats* stats);
+/* The tangent linear: (du, dv) = d(u, v)/dθ · (dlogC, dlogA) (either direction may be NULL), from
+ * J_F (du, dv) = -∂F/∂θ · dθ.  Same preconditions; the pair satisfies <J v, w> = <v, Jᵀ w>. */
+int wavi_tangent_device(wavi_ctx* ctx, const wavi_params* params, const double* dlogC, const double* dlogA,
+                        double* du, double* dv, double tol, int maxiter, wavi_adjoint_stats* stats);
+
 /* ---- Ensembles ---------------------------------------------------------------------------------
  * n independent domains (grids of different sizes) solved concurrently: one context per member (own
  * stream, device buffers and solve graph), at most `concurrency` members in flight, each member's

@@ -89,6 +89,11 @@ class OperatorDesc(C.Structure):
                 ("h_m", C.c_void_p), ("inner", C.c_void_p)]
 
 
+class AdjointStats(C.Structure):
+    _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("rel_residual", C.c_double),
+                ("elapsed_ms", C.c_double)]
+
+
 NOALLOC_MAX_TILES = 16384
 
 
@@ -130,6 +135,10 @@ def load_library(path=None):
         "wavi_time_operator_device": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.POINTER(C.c_double)]),
         "wavi_haar_device": (C.c_int, [vp, C.c_int, vp, vp, vp]),
         "wavi_residual_noalloc": (C.c_int, [C.POINTER(OperatorDesc), vp, vp, vp, vp, vp]),
+        "wavi_adjoint_device": (C.c_int, [vp, C.POINTER(Params), vp, vp, vp, vp, C.c_double, C.c_int,
+                                          C.POINTER(AdjointStats)]),
+        "wavi_tangent_device": (C.c_int, [vp, C.POINTER(Params), vp, vp, vp, vp, C.c_double, C.c_int,
+                                          C.POINTER(AdjointStats)]),
         "wavi_ensemble_create": (C.c_int, [C.c_int, C.POINTER(GridDesc), C.POINTER(SolverParams), C.POINTER(Options),
                                            C.c_int, C.POINTER(vp)]),
         "wavi_ensemble_solve_device": (C.c_int, [vp, C.POINTER(Params), C.POINTER(Fields), C.POINTER(Stats)]),

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -31,6 +32,7 @@
 #include "kernels.cuh"
 #include "fused.cuh"
 #include "persistent.cuh"
+#include "adjoint.cuh"
 
 using namespace wavi;
 
@@ -53,6 +55,16 @@ struct wavi_ctx {
   bool coarse_pending = false;
   bool skipped = false;  // the last enqueued solve had maxiter_picard <= 0
   int pers_share = 1;    // persistent coarse kernels of this many contexts may run at once (ensembles)
+  bool solved = false;   // a solve has left its converged state in the buffers (the adjoint linearises it)
+  struct Adj {           // adjoint / tangent-linear buffers, allocated on first use
+    bool ready = false;
+    AdjCell cell{};
+    double *ebar = nullptr, *sbar = nullptr, *dheta_h = nullptr, *dhn = nullptr, *dbeff = nullptr, *dheta_c = nullptr,
+           *dbeta_m = nullptr, *zero_h = nullptr, *xstate = nullptr, *ta = nullptr, *tb = nullptr, *b = nullptr,
+           *x = nullptr, *uv_keep = nullptr, *xc_keep = nullptr, *dotv = nullptr;
+    unsigned* counter = nullptr;
+    std::vector<double*> V, Z;
+  } adj;
   Dims d{};
   wavi_solver_params sp{};
   wavi_options opt{};
@@ -712,6 +724,7 @@ int solve_finish(wavi_ctx* c, wavi_stats* st) {
   }
   CK(cudaStreamSynchronize(c->st));
   c->host_syncs++;
+  c->solved = true;
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   TRY(collect_coarse_time(c));
@@ -854,6 +867,217 @@ int check_ctx(wavi_ctx* c) {
 int check_params(wavi_ctx* c, const wavi_params* p) {
   if (!p) return fail(c, WAVI_ERR_ARGUMENT, "params is null");
   if (!(p->glen_n > 0) || !(p->weertman_m > 0)) return fail(c, WAVI_ERR_ARGUMENT, "glen_n and weertman_m must be positive");
+  return 0;
+}
+
+
+// ---------------------------------------------------------------------------------------------
+// Adjoint and tangent linear of the converged solve (adjoint.cuh): J_F v, J_Fᵀ w, one V-cycle as the
+// preconditioner, restarted right-preconditioned FGMRES (Saad 1993) for both linear systems.
+// ---------------------------------------------------------------------------------------------
+constexpr int ADJ_RESTART = 40;
+
+int adj_alloc(wavi_ctx* c) {
+  auto& a = c->adj;
+  if (a.ready) return 0;
+  const Dims& d = c->d;
+  const size_t Nh = d.Nh, N = d.N;
+  int r = 0;
+#define AA(p, n) \
+  if ((r = dalloc(c, &p, n))) return r;
+  AA(a.cell.ux, Nh) AA(a.cell.vy, Nh) AA(a.cell.sh, Nh) AA(a.cell.uc, Nh) AA(a.cell.vc, Nh) AA(a.cell.S, Nh)
+  AA(a.cell.L, 8 * Nh) AA(a.ebar, Nh) AA(a.sbar, Nh) AA(a.dheta_h, Nh) AA(a.dhn, Nh) AA(a.dbeff, Nh)
+  AA(a.dheta_c, std::max<size_t>(d.Nc, 1)) AA(a.dbeta_m, N) AA(a.zero_h, Nh) AA(a.xstate, N) AA(a.ta, N) AA(a.tb, N)
+  AA(a.b, N) AA(a.x, N) AA(a.uv_keep, N) AA(a.xc_keep, N) AA(a.dotv, 1) AA(a.counter, 1)
+#undef AA
+  a.V.assign(ADJ_RESTART + 1, nullptr);
+  a.Z.assign(ADJ_RESTART, nullptr);
+  for (auto& v : a.V)
+    if ((r = dalloc(c, &v, N))) return r;
+  for (auto& v : a.Z)
+    if ((r = dalloc(c, &v, N))) return r;
+  a.ready = true;
+  return 0;
+}
+
+AdjUV adj_uv(wavi_ctx* c) { return {c->mask_uv, c->h_mask, c->c_mask, c->gf, c->gf_uv, c->h}; }
+
+double adj_dot(wavi_ctx* c, const double* x, const double* y, int* err) {
+  k_dot<<<c->ew_blocks, EW_THREADS, 0, c->st>>>(c->d.N, x, y, c->partials, c->adj.counter, c->adj.dotv);
+  double v = 0.0;
+  if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&v, c->adj.dotv, sizeof(double), cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+      cudaStreamSynchronize(c->st) != cudaSuccess)
+    *err = fail(c, WAVI_ERR_CUDA, "adjoint dot product failed");
+  return v;
+}
+
+// out = J_F v (transpose = false) or J_Fᵀ v (transpose = true), interior vectors.
+int adj_apply(wavi_ctx* c, bool transpose, const double* v, double* out) {
+  const Dims& d = c->d;
+  auto& a = c->adj;
+  const OpCoef<double> cf = coef<double>(c);
+  if (!transpose) {
+    k_tlm_cell<<<(d.Nh + 127) / 128, 128, 0, c->st>>>(d, a.cell, adj_uv(c), v, nullptr, nullptr, a.dheta_h, a.dhn, a.dbeff);
+    CKL();
+    k_tlm_uv<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, adj_uv(c), a.dhn, a.dbeff, a.dbeta_m, a.dheta_c);
+    CKL();
+    TRY(launch_op<double>(c, v, a.ta));
+    const OpCoef<double> dcf{a.dheta_h, a.dheta_c, a.zero_h, a.dbeta_m, c->h_m64, c->inner_uv};
+    k_op<double, double, 0><<<c->op_grid, c->op_block, 0, c->st>>>(d, dcf, a.xstate, nullptr, a.tb, c->partials, nullptr);
+    CKL();
+    k_add_inner<<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, a.ta, a.tb, out);
+    CKL();
+  } else {
+    TRY(launch_op<double>(c, v, a.ta));  // the operator is symmetric
+    k_adj_cell<<<(d.Nh + 127) / 128, 128, 0, c->st>>>(d, a.cell, adj_uv(c), c->inner_uv, a.xstate, v, a.ebar, a.sbar,
+                                                     nullptr, nullptr);
+    CKL();
+    k_adj_uv<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, a.cell, adj_uv(c), c->inner_uv, a.ebar, a.sbar, a.ta, out);
+    CKL();
+  }
+  (void)cf;
+  return 0;
+}
+
+// out = one V-cycle of the solve's preconditioner applied to v (zero start, zero coarse warm start).
+template <typename T, int TILE>
+int adj_vcycle(wavi_ctx* c, const double* v, double* out) {
+  const size_t bytes = sizeof(double) * c->d.N;
+  CK(cudaMemcpyAsync(c->r64, v, bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemsetAsync(c->x64, 0, bytes, c->st));
+  CK(cudaMemsetAsync(c->xc_full64, 0, bytes, c->st));
+  CondHandles h{};
+  h.active = 0;
+  Tally tv, tc;
+  if (c->pers_maxt != 0) {
+    TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
+    TRY((enqueue_cg_persistent<T, TILE>(c, h, tv, tc)));
+    TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
+  } else {
+    TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv)));
+    CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    int* live = &c->S->cg_continue;
+    while (c->hS->cg_continue) {
+      for (int k = 0; k < CG_BATCH; ++k) TRY((enqueue_cg_iteration<T, TILE>(c, h, live, tc)));
+      CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+    }
+    TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
+  }
+  CK(cudaMemcpyAsync(out, c->x64, bytes, cudaMemcpyDeviceToDevice, c->st));
+  return 0;
+}
+
+int adj_precond(wavi_ctx* c, const double* v, double* out) {
+  return c->tile == 16 ? adj_vcycle<double, 16>(c, v, out) : adj_vcycle<double, 32>(c, v, out);
+}
+
+// Solve K x = b (K = J_F or J_Fᵀ) by FGMRES(ADJ_RESTART) to ||b - K x|| <= tol ||b||.
+int adj_fgmres(wavi_ctx* c, bool transpose, const double* b, double* x, double tol, int maxit, int* iters, double* relres) {
+  auto& a = c->adj;
+  const int n = c->d.N, m = ADJ_RESTART;
+  const int nb = c->ew_blocks;
+  int err = 0;
+  CK(cudaMemsetAsync(x, 0, sizeof(double) * n, c->st));
+  const double bnorm = std::sqrt(adj_dot(c, b, b, &err));
+  if (err) return err;
+  *iters = 0;
+  *relres = 0.0;
+  if (bnorm == 0.0) return 0;
+  double* r = a.V[0];
+  CK(cudaMemcpyAsync(r, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->st));
+  std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
+  auto Hij = [&](int i, int j) -> double& { return H[(size_t)i * m + j]; };
+  for (;;) {
+    double beta = std::sqrt(adj_dot(c, r, r, &err));
+    if (err) return err;
+    *relres = beta / bnorm;
+    if (*relres <= tol || *iters >= maxit) break;
+    k_scale<<<nb, EW_THREADS, 0, c->st>>>(n, 1.0 / beta, r, a.V[0]);
+    CKL();
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int k = 0;
+    for (; k < m && *iters < maxit; ++k) {
+      TRY(adj_precond(c, a.V[k], a.Z[k]));
+      TRY(adj_apply(c, transpose, a.Z[k], a.V[k + 1]));
+      for (int i = 0; i <= k; ++i) {
+        Hij(i, k) = adj_dot(c, a.V[k + 1], a.V[i], &err);
+        if (err) return err;
+        k_axpy<<<nb, EW_THREADS, 0, c->st>>>(n, -Hij(i, k), a.V[i], a.V[k + 1]);
+        CKL();
+      }
+      const double hn = std::sqrt(adj_dot(c, a.V[k + 1], a.V[k + 1], &err));
+      if (err) return err;
+      Hij(k + 1, k) = hn;
+      if (hn > 0.0) {
+        k_scale<<<nb, EW_THREADS, 0, c->st>>>(n, 1.0 / hn, a.V[k + 1], a.V[k + 1]);
+        CKL();
+      }
+      for (int i = 0; i < k; ++i) {  // previous Givens rotations
+        const double t = cs[i] * Hij(i, k) + sn[i] * Hij(i + 1, k);
+        Hij(i + 1, k) = -sn[i] * Hij(i, k) + cs[i] * Hij(i + 1, k);
+        Hij(i, k) = t;
+      }
+      const double den = std::hypot(Hij(k, k), Hij(k + 1, k));
+      cs[k] = den > 0.0 ? Hij(k, k) / den : 1.0;
+      sn[k] = den > 0.0 ? Hij(k + 1, k) / den : 0.0;
+      Hij(k, k) = den;
+      Hij(k + 1, k) = 0.0;
+      g[k + 1] = -sn[k] * g[k];
+      g[k] = cs[k] * g[k];
+      ++*iters;
+      if (std::fabs(g[k + 1]) <= tol * bnorm || hn == 0.0) {
+        ++k;
+        break;
+      }
+    }
+    for (int i = k - 1; i >= 0; --i) {  // H y = g
+      double v = g[i];
+      for (int j = i + 1; j < k; ++j) v -= Hij(i, j) * y[j];
+      y[i] = Hij(i, i) != 0.0 ? v / Hij(i, i) : 0.0;
+    }
+    for (int i = 0; i < k; ++i) {
+      k_axpy<<<nb, EW_THREADS, 0, c->st>>>(n, y[i], a.Z[i], x);
+      CKL();
+    }
+    // true residual r = b - K x
+    TRY(adj_apply(c, transpose, x, a.tb));
+    k_scale<<<nb, EW_THREADS, 0, c->st>>>(n, 1.0, b, r);
+    CKL();
+    k_axpy<<<nb, EW_THREADS, 0, c->st>>>(n, -1.0, a.tb, r);
+    CKL();
+  }
+  return 0;
+}
+
+// Linearisation point: the per-cell sensitivities of the converged state, its interior vector, and
+// copies of the state the V-cycle preconditioner overwrites.
+int adj_prepare(wavi_ctx* c, const wavi_params* p) {
+  if (mixed(c)) return fail(c, WAVI_ERR_ARGUMENT, "the adjoint needs a float64 context");
+  if (c->has_fixed) return fail(c, WAVI_ERR_ARGUMENT, "the adjoint does not support Dirichlet (isfixed) points");
+  if (!c->solved) return fail(c, WAVI_ERR_ARGUMENT, "no converged solve to linearise: call a solve first");
+  TRY(adj_alloc(c));
+  TRY(set_params(c, p));
+  auto& a = c->adj;
+  const Dims& d = c->d;
+  const size_t bytes = sizeof(double) * d.N;
+  AdjIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->eta, c->beta, c->quad_f2, c->wc, c->glen_b, c->h, c->zeta, c->qw, c->P};
+  k_adj_local<<<(d.Nh + 127) / 128, 128, 0, c->st>>>(d, in, a.cell);
+  CKL();
+  CK(cudaMemcpyAsync(a.xstate, c->x64, bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(a.uv_keep, c->uv, bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(a.xc_keep, c->xc_full64, bytes, cudaMemcpyDeviceToDevice, c->st));
+  return 0;
+}
+
+int adj_restore(wavi_ctx* c) {
+  const size_t bytes = sizeof(double) * c->d.N;
+  CK(cudaMemcpyAsync(c->uv, c->adj.uv_keep, bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(c->xc_full64, c->adj.xc_keep, bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(c->x64, c->adj.xstate, bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return 0;
 }
 
@@ -1221,6 +1445,78 @@ int wavi_coarse_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
   }
   CKL();
   CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+int wavi_adjoint_device(wavi_ctx* c, const wavi_params* p, const double* dJ_du, const double* dJ_dv, double* dJ_dlogC,
+                        double* dJ_dlogA, double tol, int maxiter, wavi_adjoint_stats* stats) {
+  TRY(check_ctx(c));
+  TRY(check_params(c, p));
+  if (!dJ_du || !dJ_dv || !dJ_dlogC || !dJ_dlogA) return fail(c, WAVI_ERR_ARGUMENT, "null adjoint argument");
+  if (!(tol > 0.0) || maxiter < 1) return fail(c, WAVI_ERR_ARGUMENT, "tol must be > 0 and maxiter >= 1");
+  const auto t0 = std::chrono::steady_clock::now();
+  TRY(adj_prepare(c, p));
+  auto& a = c->adj;
+  const Dims& d = c->d;
+  CK(cudaMemcpyAsync(a.b, dJ_du, sizeof(double) * d.Nu, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(a.b + d.Nu, dJ_dv, sizeof(double) * d.Nv, cudaMemcpyDeviceToDevice, c->st));
+  k_mask_inner<<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, a.b);
+  CKL();
+  int iters = 0;
+  double rr = 0.0;
+  int r = adj_fgmres(c, true, a.b, a.x, tol, maxiter, &iters, &rr);
+  if (!r) {
+    k_adj_cell<<<(d.Nh + 127) / 128, 128, 0, c->st>>>(d, a.cell, adj_uv(c), c->inner_uv, a.xstate, a.x, nullptr, nullptr,
+                                                     dJ_dlogC, dJ_dlogA);
+    if (cudaGetLastError() != cudaSuccess) r = fail(c, WAVI_ERR_CUDA, "adjoint gradient kernel");
+  }
+  const int rr2 = adj_restore(c);
+  if (r) return r;
+  if (rr2) return rr2;
+  if (stats) {
+    stats->status = rr <= tol ? WAVI_OK : WAVI_ERR_NOT_CONVERGED;
+    stats->iterations = iters;
+    stats->rel_residual = rr;
+    stats->elapsed_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return 0;
+}
+
+int wavi_tangent_device(wavi_ctx* c, const wavi_params* p, const double* dlogC, const double* dlogA, double* du,
+                        double* dv, double tol, int maxiter, wavi_adjoint_stats* stats) {
+  TRY(check_ctx(c));
+  TRY(check_params(c, p));
+  if (!du || !dv) return fail(c, WAVI_ERR_ARGUMENT, "null tangent output");
+  if (!(tol > 0.0) || maxiter < 1) return fail(c, WAVI_ERR_ARGUMENT, "tol must be > 0 and maxiter >= 1");
+  const auto t0 = std::chrono::steady_clock::now();
+  TRY(adj_prepare(c, p));
+  auto& a = c->adj;
+  const Dims& d = c->d;
+  // b = -A(∂coef/∂θ dθ) x
+  k_tlm_cell<<<(d.Nh + 127) / 128, 128, 0, c->st>>>(d, a.cell, adj_uv(c), nullptr, dlogC, dlogA, a.dheta_h, a.dhn, a.dbeff);
+  CKL();
+  k_tlm_uv<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, adj_uv(c), a.dhn, a.dbeff, a.dbeta_m, a.dheta_c);
+  CKL();
+  const OpCoef<double> dcf{a.dheta_h, a.dheta_c, a.zero_h, a.dbeta_m, c->h_m64, c->inner_uv};
+  k_op<double, double, 0><<<c->op_grid, c->op_block, 0, c->st>>>(d, dcf, a.xstate, nullptr, a.tb, c->partials, nullptr);
+  CKL();
+  k_scale<<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, -1.0, a.tb, a.b);
+  CKL();
+  int iters = 0;
+  double rr = 0.0;
+  int r = adj_fgmres(c, false, a.b, a.x, tol, maxiter, &iters, &rr);
+  if (!r && (cudaMemcpyAsync(du, a.x, sizeof(double) * d.Nu, cudaMemcpyDeviceToDevice, c->st) != cudaSuccess ||
+             cudaMemcpyAsync(dv, a.x + d.Nu, sizeof(double) * d.Nv, cudaMemcpyDeviceToDevice, c->st) != cudaSuccess))
+    r = fail(c, WAVI_ERR_CUDA, "tangent output copy");
+  const int rr2 = adj_restore(c);
+  if (r) return r;
+  if (rr2) return rr2;
+  if (stats) {
+    stats->status = rr <= tol ? WAVI_OK : WAVI_ERR_NOT_CONVERGED;
+    stats->iterations = iters;
+    stats->rel_residual = rr;
+    stats->elapsed_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
   return 0;
 }
 

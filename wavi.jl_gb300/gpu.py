@@ -146,6 +146,30 @@ class VelocitySolver:
         if st != 0:
             raise self._err(st)
 
+    # -- adjoint ---------------------------------------------------------------------------------
+    def adjoint_device(self, params, dJ_du, dJ_dv, grad_logC, grad_logA, tol=1e-10, maxiter=400):
+        """Gradient of J w.r.t. per-cell log C and log A at the last solve's fixed point, from dJ/du, dJ/dv
+        (device tensors in reference shapes, flattened column-major); writes grad_logC, grad_logA (nx*ny)."""
+        st = abi.AdjointStats()
+        r = self.lib.wavi_adjoint_device(self.ctx, C.byref(params.to_c()), C.c_void_p(dJ_du.data_ptr()),
+                                         C.c_void_p(dJ_dv.data_ptr()), C.c_void_p(grad_logC.data_ptr()),
+                                         C.c_void_p(grad_logA.data_ptr()), float(tol), int(maxiter), C.byref(st))
+        if r != 0:
+            raise self._err(r)
+        return {"status": st.status, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                "elapsed_ms": st.elapsed_ms}
+
+    def tangent_device(self, params, dlogC, dlogA, du, dv, tol=1e-10, maxiter=400):
+        """(du, dv) = d(u, v)/d(log C, log A) · (dlogC, dlogA) at the last solve's fixed point."""
+        st = abi.AdjointStats()
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+        r = self.lib.wavi_tangent_device(self.ctx, C.byref(params.to_c()), ptr(dlogC), ptr(dlogA), ptr(du), ptr(dv),
+                                         float(tol), int(maxiter), C.byref(st))
+        if r != 0:
+            raise self._err(r)
+        return {"status": st.status, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                "elapsed_ms": st.elapsed_ms}
+
     def coarse_diagonal_device(self, out_uv, precision="fp64"):
         """diag(R A P) for the current coefficients and wavelet mask, on the full wavelet grids."""
         st = self.lib.wavi_coarse_diagonal_device(self.ctx, PRECISIONS[precision], C.c_void_p(out_uv.data_ptr()))
