@@ -534,6 +534,108 @@ def ensemble_arm(args):
     return 0
 
 
+def adjoint_arm(args):
+    """The adjoint workload on the 640 x 80 channel: J = ½ Σ (|u| − u_obs)² with u_obs from a forward
+    solve at log C + 0.1 z (z ~ N(0, 1) per cell, seed 4) plus 2 % Gaussian noise (seed 5); the gradient
+    with respect to per-cell log C and log A at the unperturbed state by wavi_adjoint_device; checked by
+    the dot-product test against wavi_tangent_device and by central differences of tightly converged
+    forward solves along 20 seeded directions (seeds 100-119), with a step sweep on the first."""
+    import dataclasses
+    import torch
+    __graft_entry__.load_package()
+    from wavi_gb300 import build, synthetic
+    build.build_library()
+    from wavi_gb300.gpu import VelocitySolver
+    from wavi_gb300.misfit import misfit, misfit_gradient, speed
+    from wavi_gb300.model import GPUParallelSpec, Model, pre_solve, release_solver
+    g, bed, p, sp, ic = synthetic.channel_c2(tol_picard=1e-11, maxiter_picard=600)
+    solver = VelocitySolver(g, sp, precision="fp64")
+    c0 = np.full((g.nx, g.ny), float(p.weertman_c))
+    a0 = np.full((g.nx, g.ny), float(p.glen_a_ref))
+    state = {}
+
+    def solve(dlogc=None, dloga=None):
+        p2 = dataclasses.replace(p, weertman_c=np.asfortranarray(c0 * np.exp(dlogc if dlogc is not None else 0.0)),
+                                 glen_a_ref=np.asfortranarray(a0 * np.exp(dloga if dloga is not None else 0.0)))
+        m = Model(g, bed, p2, sp, ic, parallel_spec=GPUParallelSpec(precision="fp64"))
+        pre_solve(m)
+        f = {k: np.array(v, copy=True, order="F") for k, v in m.fields.items()}
+        release_solver(m)
+        st = solver.solve(m.params, f)
+        state["m"], state["params"] = m, m.params
+        return f, st
+
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64).ravel(order="F"))).cuda()
+    z = np.random.default_rng(4).standard_normal((g.nx, g.ny))
+    f_true, _ = solve(0.1 * z)
+    m = state["m"]
+    masks = (m.u_mask, m.v_mask, m.h_mask)
+    s_true, _, _ = speed(f_true["u"], f_true["v"], *masks)
+    s_obs = s_true * (1.0 + 0.02 * np.random.default_rng(5).standard_normal(s_true.shape))
+    f0, st0 = solve()
+    params = state["params"]
+    gu, gv = misfit_gradient(f0["u"], f0["v"], *masks, s_obs)
+    gc = torch.zeros(g.nx * g.ny, dtype=torch.float64, device="cuda")
+    ga = torch.zeros_like(gc)
+    times, ast = [], None
+    for it in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ast = solver.adjoint_device(params, dev(gu), dev(gv), gc, ga, tol=1e-12, maxiter=400)
+        if it >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    grad_c = gc.cpu().numpy().reshape((g.nx, g.ny), order="F")
+    grad_a = ga.cpu().numpy().reshape((g.nx, g.ny), order="F")
+    # dot-product test
+    rng = np.random.default_rng(6)
+    vc, va = rng.standard_normal((g.nx, g.ny)), rng.standard_normal((g.nx, g.ny))
+    wu = np.where(m.u_inner, rng.standard_normal((g.nx + 1, g.ny)), 0.0)
+    wv = np.where(m.v_inner, rng.standard_normal((g.nx, g.ny + 1)), 0.0)
+    du = torch.zeros((g.nx + 1) * g.ny, dtype=torch.float64, device="cuda")
+    dv = torch.zeros(g.nx * (g.ny + 1), dtype=torch.float64, device="cuda")
+    tst = solver.tangent_device(params, dev(vc), dev(va), du, dv, tol=1e-12, maxiter=400)
+    gc2, ga2 = torch.zeros_like(gc), torch.zeros_like(ga)
+    solver.adjoint_device(params, dev(wu), dev(wv), gc2, ga2, tol=1e-12, maxiter=400)
+    lhs = float(torch.dot(du, dev(wu)) + torch.dot(dv, dev(wv)))
+    rhs = float(torch.dot(gc2, dev(vc)) + torch.dot(ga2, dev(va)))
+    # central differences
+    def fd(vc, va, h):
+        fp, _ = solve(h * vc, h * va)
+        fm, _ = solve(-h * vc, -h * va)
+        return (misfit(fp["u"], fp["v"], *masks, s_obs) - misfit(fm["u"], fm["v"], *masks, s_obs)) / (2 * h)
+    dirs = [(np.random.default_rng(100 + k).standard_normal((g.nx, g.ny)),
+             np.random.default_rng(200 + k).standard_normal((g.nx, g.ny))) for k in range(args.directions)]
+    sweep = {}
+    ad0 = float(np.sum(grad_c * dirs[0][0]) + np.sum(grad_a * dirs[0][1]))
+    for h in (1e-2, 1e-3, 1e-4, 1e-5):
+        sweep[h] = abs(fd(*dirs[0], h) - ad0) / abs(ad0)
+    h_best = min(sweep, key=sweep.get)
+    errs = []
+    for k, (dc, da) in enumerate(dirs):
+        ad = float(np.sum(grad_c * dc) + np.sum(grad_a * da))
+        fdv = fd(dc, da, h_best)
+        errs.append(abs(ad - fdv) / abs(fdv))
+    line = {
+        "metric": "adjoint gradients/s (d misfit / d(log C, log A), 640x80 channel, converged FP64 state)",
+        "value": len(times) / sum(times), "unit": "gradients/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "J = 0.5 sum (|u| - u_obs)^2 on the 640x80 channel, u_obs from log C + 0.1 z "
+                               "(seed 4) plus 2% noise (seed 5); forward solves to rel. residual < 1e-11",
+                   "timing": "host wall clock around wavi_adjoint_device"},
+        "forward": {"picard_iterations": st0["picard_iterations"], "rel_residual": st0["rel_residual"],
+                    "status": st0["status_name"]},
+        "adjoint": {"fgmres_iterations": ast["iterations"], "rel_residual": ast["rel_residual"]},
+        "tangent": {"fgmres_iterations": tst["iterations"], "rel_residual": tst["rel_residual"]},
+        "dot_test_rel_err": abs(lhs - rhs) / max(abs(lhs), abs(rhs)),
+        "fd_step_sweep": {str(h): e for h, e in sweep.items()}, "fd_step": h_best,
+        "fd_directions": len(errs), "fd_max_rel_err": max(errs), "fd_median_rel_err": float(np.median(errs)),
+    }
+    print(json.dumps(line), flush=True)
+    solver.close()
+    return 0
+
+
 def profile_case(args):
     """One untimed case for ncu: the workload solved host-driven (every kernel a separate launch) and
     capped at --picard Picard iterations, or --op-launches operator launches on the stencil grid."""
@@ -574,13 +676,16 @@ def main():
     ap.add_argument("--picard", type=int, default=1, help="--profile solve: Picard iterations")
     ap.add_argument("--precision", default="mixed", choices=("mixed", "fp64"), help="--profile solve: precision")
     ap.add_argument("--op-launches", type=int, default=3, help="--profile op: operator launches")
-    ap.add_argument("--config", default="c2", choices=("c2", "c5"),
-                    help="c2: the 640x80 solve (default); c5: the ragged 256-member ensemble")
+    ap.add_argument("--config", default="c2", choices=("c2", "c4", "c5"),
+                    help="c2: the 640x80 solve (default); c4: the adjoint on 640x80; c5: the ragged 256-member ensemble")
+    ap.add_argument("--directions", type=int, default=20, help="--config c4: finite-difference directions")
     ap.add_argument("--members", type=int, default=256, help="--config c5: ensemble members")
     ap.add_argument("--no-tune", action="store_true", help="--config c5: skip the autotuner")
     args = ap.parse_args()
     if args.profile:
         return profile_case(args)
+    if args.config == "c4":
+        return adjoint_arm(args)
     if args.config == "c5":
         # more hardware work queues than the default 8, so that concurrent members do not serialise
         os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
