@@ -110,3 +110,27 @@ def test_adjoint_preconditions():
     with pytest.raises(WaviError, match="no converged solve"):
         s.adjoint_device(p, z, z, z, z)
     s.close()
+
+
+def test_autograd_function_backward_is_the_adjoint():
+    """torch.autograd through VelocityFunction: the gradient of <w, (u, v)> agrees with the tangent linear,
+    <∇, dθ> = <w, J dθ>."""
+    from wavi_gb300.autograd import Problem, VelocityFunction
+    case = Case(nx=40, ny=16, dx=4000.0, mask="full")
+    g = case.g
+    c0, a0 = float(case.p.weertman_c), float(case.p.glen_a_ref)
+    prob = Problem(case.solver, lambda C, A: case.solve(np.log(C / c0), np.log(A / a0)), tol=1e-12)
+    logC = torch.full((g.nx * g.ny,), np.log(c0), dtype=torch.float64, device="cuda", requires_grad=True)
+    logA = torch.full((g.nx * g.ny,), np.log(a0), dtype=torch.float64, device="cuda", requires_grad=True)
+    u, v = VelocityFunction.apply(logC, logA, prob)
+    rng = np.random.default_rng(21)
+    wu = _dev(np.where(case.m.u_inner, rng.standard_normal((g.nx + 1, g.ny)), 0.0))
+    wv = _dev(np.where(case.m.v_inner, rng.standard_normal((g.nx, g.ny + 1)), 0.0))
+    (torch.dot(wu, u) + torch.dot(wv, v)).backward()
+    vc, va = rng.standard_normal((g.nx, g.ny)), rng.standard_normal((g.nx, g.ny))
+    du = torch.zeros((g.nx + 1) * g.ny, dtype=torch.float64, device="cuda")
+    dv = torch.zeros(g.nx * (g.ny + 1), dtype=torch.float64, device="cuda")
+    case.solver.tangent_device(case.m.params, _dev(vc), _dev(va), du, dv, tol=1e-12)
+    lhs = float(torch.dot(wu, du) + torch.dot(wv, dv))
+    rhs = float(torch.dot(logC.grad, _dev(vc)) + torch.dot(logA.grad, _dev(va)))
+    assert abs(lhs - rhs) <= 1e-8 * max(abs(lhs), abs(rhs)), (lhs, rhs)
