@@ -308,6 +308,35 @@ int wavi_adjoint_device(wavi_ctx* ctx, const wavi_params* params, const double* 
 int wavi_tangent_device(wavi_ctx* ctx, const wavi_params* params, const double* dlogC, const double* dlogA,
                         double* du, double* dv, double tol, int maxiter, wavi_adjoint_stats* stats);
 
+/* ---- Device time stepping -------------------------------------------------------------------------
+ * nsteps time steps of dt with the model kept on the device (run_simulation.jl:6-42): per step,
+ * update_state! (update_state.jl:7-21: surface elevation, geometry on the u/v grids, height above
+ * floatation, grounded fraction by pos_fraction (utilities.jl:255-396), accumulation, uniform basal melt,
+ * C·grounded fraction, ds/dh; the velocity solve; velocities on the h grid, dh/dt, update_wavelets!) and
+ * then update_thickness! with evolve_shelves.  fields (device pointers) holds the model state at the start;
+ * on return every field of it holds the state after the last step, including those wavi_fields marks as
+ * inputs (update_state! overwrites them in the reference as well) and the wavelet masks.  The coarse-
+ * correction cache restarts at zero after every update_wavelets!, so the run leaves
+ * wu/wv_correction_coarse untouched: after it the caller's caches are zero vectors of lengths
+ * outputs->n_wu, n_wv.  stats sums the steps' counts and keeps the last step's status and residuals. */
+typedef struct wavi_step_inputs {
+  const double* bed;                 /* nx*ny bed elevation */
+  const double* weertman_c;          /* nx*ny Weertman C before the grounded-fraction factor (Params) */
+  const double* accumulation;        /* nx*ny accumulation rate (Params) */
+  const uint8_t* h_isfixed;          /* nx*ny cells whose thickness does not evolve */
+  double basal_melt_rate;            /* uniform basal melt rate (UniformMeltRate) */
+  double reserved0;
+} wavi_step_inputs;
+typedef struct wavi_step_outputs {
+  double* dhdt;                      /* nx*ny, or NULL; the other arrays likewise */
+  double *u_h, *v_h, *u_bed, *v_bed, *u_surf, *v_surf;  /* velocities on the h grid (:164-178) */
+  int32_t n_wu, n_wv;                /* coarse-space sizes after the last update_wavelets! */
+  int32_t steps;
+  int32_t reserved0;
+} wavi_step_outputs;
+int wavi_run_device(wavi_ctx* ctx, const wavi_params* params, double dt, int nsteps, const wavi_step_inputs* inputs,
+                    wavi_fields* fields, wavi_step_outputs* outputs, wavi_stats* stats);
+
 /* ---- Ensembles ---------------------------------------------------------------------------------
  * n independent domains (grids of different sizes) solved concurrently: one context per member (own
  * stream, device buffers and solve graph), at most `concurrency` members in flight, each member's

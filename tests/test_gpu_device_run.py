@@ -1,0 +1,100 @@
+"""Device-resident time stepping (wavi_run_device): update_state! and update_thickness! on the GPU around
+the solve, against the oracle's run_simulation! restatement and the reference's MISMIP+ golden file."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+torch = pytest.importorskip("torch")
+
+# the level a different coarse-CG summation order gives after many coupled steps (test_gpu_timestepping.py)
+TOL = {"h": 2e-5, "u": 2.5e-4, "v": 5e-5, "eta_av": 5e-4, "grounded_fraction": 5e-5, "bed_speed": 2.5e-4}
+GOLDEN = {"h": "h", "u": "u", "v": "v", "viscosity": "eta_av", "grounded_fraction": "grounded_fraction",
+          "bed_speed": "bed_speed"}
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def _dev(a, dtype=np.float64):
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=dtype).ravel(order="F"))).cuda()
+
+
+def _run(m, dt, nsteps):
+    """Run the host model's initial state on the device; returns the fields (reference shapes), the
+    stats and the coarse-space sizes."""
+    from wavi_gb300.gpu import ALL_FIELDS, VelocitySolver
+    s = VelocitySolver(m.grid, m.solver_params, precision="fp64")
+    f = m.fields
+    t = {k: _dev(f[k], np.uint8 if k in ("wu_mask", "wv_mask") else np.float64) for k in ALL_FIELDS}
+    outs = {"dhdt": torch.zeros(m.grid.nx * m.grid.ny, dtype=torch.float64, device="cuda")}
+    st, counts = s.run_device(m.params, dt, nsteps, _dev(f["b"]), _dev(m.weertman_c_param), _dev(m.accumulation_param),
+                              _dev(m.h_isfixed, np.uint8), m.melt_rate, t, outputs=outs)
+    s.close()
+    out = {}
+    for k in ALL_FIELDS:
+        if k in ("wu_correction_coarse", "wv_correction_coarse"):
+            continue
+        out[k] = t[k].cpu().numpy().reshape(np.asarray(f[k]).shape, order="F")
+    out["dhdt"] = outs["dhdt"].cpu().numpy().reshape((m.grid.nx, m.grid.ny), order="F")
+    return out, st, counts
+
+
+def test_channel_c1_200_steps_matches_oracle(oracle, pkg):
+    from wavi_gb300 import config, synthetic
+    from wavi_gb300.model import GPUParallelSpec, Model
+    g, bed, p, sp, ic = synthetic.channel_c1(maxiter_picard=1)
+    m = Model(g, bed, p, sp, ic, parallel_spec=GPUParallelSpec(precision="fp64"))
+    om = oracle.build_model(g, bed, p, sp, ic)
+    out, st, (nwu, nwv) = _run(m, 0.5, 200)
+    om.run(200, 0.5)
+    for key, tol in TOL.items():
+        assert _rel(out[key], om.field(key)) < tol, (key, _rel(out[key], om.field(key)))
+    assert _rel(out["dhdt"], om.field("dhdt")) < 1e-3
+    for name in ("wu_mask", "wv_mask"):
+        agree = np.mean(out[name].astype(bool) == om.mask(name).astype(bool))
+        assert agree > 0.995, (name, agree)
+    assert abs(nwu - int(om.mask("wu_mask").sum())) <= 0.005 * out["wu_mask"].size
+
+
+def test_mismip_golden_1000_steps_on_device(oracle, pkg):
+    from wavi_gb300 import config
+    from wavi_gb300.model import GPUParallelSpec, Model
+    from wavi_gb300.synthetic import mismip_plus_bed
+    g = config.Grid(nx=80, ny=10, nσ=4, x0=0.0, y0=-40000.0, dx=8000.0, dy=8000.0, u_iszero=["north"],
+                    v_iszero=["west", "east"])
+    p = config.Params(default_thickness=100.0, accumulation_rate=0.3, default_temperature=265.700709)
+    sp = config.SolverParams(maxiter_picard=1)
+    m = Model(g, lambda x, y: float(mismip_plus_bed(x, y)), p, sp, parallel_spec=GPUParallelSpec(precision="fp64"))
+    out, st, _ = _run(m, 0.1, 1000)
+    gold = np.load(os.path.join(HERE, "golden", "mismip_100yr_v1_8_3.npz"))
+    for name, key in GOLDEN.items():
+        tol = TOL[key if key in TOL else "eta_av"]
+        assert _rel(out[key], gold[name]) < tol, (name, _rel(out[key], gold[name]))
+    om = oracle.build_model(g, lambda x, y: float(mismip_plus_bed(x, y)), p, sp)
+    om.run(1000, 0.1)
+    for name, key in GOLDEN.items():
+        tol = TOL[key if key in TOL else "eta_av"]
+        assert _rel(out[key], om.field(key)) < tol, (key, _rel(out[key], om.field(key)))
+
+
+def test_run_simulation_device_run_matches_host_loop(oracle, pkg):
+    """The host mirror's run_simulation with GPUParallelSpec(device_run=True) (one wavi_run_device call)
+    against the oracle's run of the same 50 steps."""
+    from wavi_gb300 import config, synthetic
+    from wavi_gb300.model import GPUParallelSpec, Model, Simulation, release_solver, run_simulation
+    g, bed, p, sp, ic = synthetic.channel_c1(maxiter_picard=1)
+    m = Model(g, bed, p, sp, ic, parallel_spec=GPUParallelSpec(precision="fp64", device_run=True))
+    sim = Simulation(m, config.TimesteppingParams(dt=0.5, n_iter_total=50))
+    run_simulation(sim)
+    release_solver(m)
+    assert sim.n_iter == 50
+    om = oracle.build_model(g, bed, p, sp, ic)
+    om.run(50, 0.5)
+    for key, tol in TOL.items():
+        assert _rel(m.fields[key], om.field(key)) < tol, key
+    assert m.fields["wu_correction_coarse"].size == int(np.count_nonzero(m.fields["wu_mask"]))

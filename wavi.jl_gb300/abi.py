@@ -89,6 +89,16 @@ class OperatorDesc(C.Structure):
                 ("h_m", C.c_void_p), ("inner", C.c_void_p)]
 
 
+class StepInputs(C.Structure):
+    _fields_ = [("bed", C.c_void_p), ("weertman_c", C.c_void_p), ("accumulation", C.c_void_p),
+                ("h_isfixed", C.c_void_p), ("basal_melt_rate", C.c_double), ("reserved0", C.c_double)]
+
+
+class StepOutputs(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("dhdt", "u_h", "v_h", "u_bed", "v_bed", "u_surf", "v_surf")] + [
+        ("n_wu", C.c_int32), ("n_wv", C.c_int32), ("steps", C.c_int32), ("reserved0", C.c_int32)]
+
+
 class AdjointStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("rel_residual", C.c_double),
                 ("elapsed_ms", C.c_double)]
@@ -139,6 +149,8 @@ def load_library(path=None):
                                           C.POINTER(AdjointStats)]),
         "wavi_tangent_device": (C.c_int, [vp, C.POINTER(Params), vp, vp, vp, vp, C.c_double, C.c_int,
                                           C.POINTER(AdjointStats)]),
+        "wavi_run_device": (C.c_int, [vp, C.POINTER(Params), C.c_double, C.c_int, C.POINTER(StepInputs),
+                                      C.POINTER(Fields), C.POINTER(StepOutputs), C.POINTER(Stats)]),
         "wavi_ensemble_create": (C.c_int, [C.c_int, C.POINTER(GridDesc), C.POINTER(SolverParams), C.POINTER(Options),
                                            C.c_int, C.POINTER(vp)]),
         "wavi_ensemble_solve_device": (C.c_int, [vp, C.POINTER(Params), C.POINTER(Fields), C.POINTER(Stats)]),

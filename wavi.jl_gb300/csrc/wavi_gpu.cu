@@ -33,6 +33,7 @@
 #include "fused.cuh"
 #include "persistent.cuh"
 #include "adjoint.cuh"
+#include "timestep.cuh"
 
 using namespace wavi;
 
@@ -65,6 +66,12 @@ struct wavi_ctx {
     unsigned* counter = nullptr;
     std::vector<double*> V, Z;
   } adj;
+  struct Step {          // device time stepping buffers, allocated on first use
+    bool ready = false;
+    double *b = nullptr, *c_param = nullptr, *acc_param = nullptr, *haf = nullptr, *afq = nullptr, *dhdt = nullptr;
+    double *uh = nullptr, *vh = nullptr, *ub = nullptr, *vb = nullptr, *us = nullptr, *vs = nullptr, *wav = nullptr;
+    uint8_t* h_isfixed = nullptr;
+  } step;
   Dims d{};
   wavi_solver_params sp{};
   wavi_options opt{};
@@ -1081,6 +1088,65 @@ int adj_restore(wavi_ctx* c) {
   return 0;
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// Device time stepping (timestep.cuh): update_state! around the solve and update_thickness!
+// ---------------------------------------------------------------------------------------------
+int step_alloc(wavi_ctx* c) {
+  auto& t = c->step;
+  if (t.ready) return 0;
+  const size_t Nh = c->d.Nh, N = c->d.N;
+  int r = 0;
+#define SA(p, n) \
+  if ((r = dalloc(c, &p, n))) return r;
+  SA(t.b, Nh) SA(t.c_param, Nh) SA(t.acc_param, Nh) SA(t.haf, Nh) SA(t.afq, 4 * Nh) SA(t.dhdt, Nh) SA(t.uh, Nh)
+  SA(t.vh, Nh) SA(t.ub, Nh) SA(t.vb, Nh) SA(t.us, Nh) SA(t.vs, Nh) SA(t.wav, N) SA(t.h_isfixed, Nh)
+#undef SA
+  t.ready = true;
+  return 0;
+}
+
+StepState step_state(wavi_ctx* c) {
+  return {c->h_mask, c->mask_uv, c->h, c->s, c->dsdh, c->gf, c->wc, c->acc, c->melt, c->h_uv, c->s_uv, c->gf_uv, c->P};
+}
+StepBuf step_buf(wavi_ctx* c, double melt) {
+  auto& t = c->step;
+  return {t.b, t.c_param, t.acc_param, t.h_isfixed, melt, t.haf, t.afq, t.dhdt, t.uh, t.vh, t.ub, t.vb, t.us, t.vs};
+}
+
+// The update_state! steps before the solve (update_state.jl:51-147), into the solve's own buffers.
+int step_pre(wavi_ctx* c, double melt) {
+  const Dims& d = c->d;
+  const int hb = (d.Nh + 127) / 128;
+  k_step_pre_h<<<hb, 128, 0, c->st>>>(d, step_state(c), step_buf(c, melt));
+  CKL();
+  k_step_geom_uv<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, step_state(c));
+  CKL();
+  k_step_pos_quarters<<<hb, 128, 0, c->st>>>(d, c->h_mask, c->step.haf, c->step.afq);
+  CKL();
+  k_step_pos_gather<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, step_state(c), c->step.afq, c->step.c_param);
+  CKL();
+  return 0;
+}
+
+// After the solve: velocities on the h grid, dh/dt, the wavelet coarse space (update_state.jl:17-19),
+// then update_thickness!.
+int step_post(wavi_ctx* c, double melt, double dt, double h_min) {
+  const Dims& d = c->d;
+  const int hb = (d.Nh + 127) / 128;
+  k_step_post_h<<<hb, 128, 0, c->st>>>(d, step_state(c), step_buf(c, melt), c->uv, c->beta, c->quad_f1, c->quad_f2);
+  CKL();
+  k_haar<double, double, 2, false, false><<<c->haar_grid, c->haar_block, 0, c->st>>>(
+      d, c->sp.levels, c->uv, c->step.wav, nullptr, c->mask_uv, nullptr, c->partials, nullptr);
+  CKL();
+  k_step_wavelet_mask<<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->step.wav, c->sp.wavelet_threshold, c->wmask_uv,
+                                                               c->xc_full64);
+  CKL();
+  k_step_thickness<<<hb, 128, 0, c->st>>>(d, step_state(c), step_buf(c, melt), dt, h_min);
+  CKL();
+  return 0;
+}
+
 }  // namespace
 
 namespace wavi {
@@ -1517,6 +1583,82 @@ int wavi_tangent_device(wavi_ctx* c, const wavi_params* p, const double* dlogC, 
     stats->rel_residual = rr;
     stats->elapsed_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
+  return 0;
+}
+
+int wavi_run_device(wavi_ctx* c, const wavi_params* p, double dt, int nsteps, const wavi_step_inputs* in, wavi_fields* f,
+                    wavi_step_outputs* out, wavi_stats* st) {
+  TRY(check_ctx(c));
+  TRY(check_params(c, p));
+  if (!in || !f || !in->bed || !in->weertman_c || !in->accumulation || !in->h_isfixed)
+    return fail(c, WAVI_ERR_ARGUMENT, "null time-stepping argument");
+  if (nsteps < 0 || !(dt >= 0.0)) return fail(c, WAVI_ERR_ARGUMENT, "nsteps must be >= 0 and dt >= 0");
+  TRY(step_alloc(c));
+  const Dims& d = c->d;
+  auto& t = c->step;
+  wavi_params pp = *p;
+  pp.dt = dt;  // set_dt_in_model! (Simulation.jl:56-59)
+  TRY(upload(c, f, false));
+  CK(cudaMemcpyAsync(t.b, in->bed, sizeof(double) * d.Nh, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(t.c_param, in->weertman_c, sizeof(double) * d.Nh, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(t.acc_param, in->accumulation, sizeof(double) * d.Nh, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(t.h_isfixed, in->h_isfixed, d.Nh, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemsetAsync(t.dhdt, 0, sizeof(double) * d.Nh, c->st));
+  wavi_stats acc{}, one{};
+  for (int k = 0; k < nsteps; ++k) {
+    TRY(set_params(c, &pp));
+    TRY(step_pre(c, in->basal_melt_rate));
+    TRY(solve_enqueue(c, &pp));
+    TRY(solve_finish(c, &one));
+    acc.picard_iterations += one.picard_iterations;
+    acc.coarse_cg_iterations += one.coarse_cg_iterations;
+    acc.op_applications += one.op_applications;
+    acc.algorithmic_bytes += one.algorithmic_bytes;
+    acc.elapsed_ms += one.elapsed_ms;
+    acc.kernel_launches += one.kernel_launches;
+    acc.host_syncs += one.host_syncs;
+    acc.status = one.status;
+    acc.rel_residual = one.rel_residual;
+    acc.rel_update = one.rel_update;
+    acc.coarse_solver = one.coarse_solver;
+    TRY(step_post(c, in->basal_melt_rate, dt, p->minimum_thickness));
+  }
+  // the model state after the last step (update_state! overwrites these fields in the reference too)
+  const cudaMemcpyKind dd = cudaMemcpyDeviceToDevice;
+#define OUTD(dst, src, n) CK(cudaMemcpyAsync(const_cast<double*>(dst), src, sizeof(double) * (n), dd, c->st));
+  OUTD(f->h, c->h, d.Nh) OUTD(f->s, c->s, d.Nh) OUTD(f->dsdh, c->dsdh, d.Nh) OUTD(f->grounded_fraction, c->gf, d.Nh)
+  OUTD(f->weertman_c, c->wc, d.Nh) OUTD(f->accumulation, c->acc, d.Nh) OUTD(f->basal_melt, c->melt, d.Nh)
+  OUTD(f->gu_h, c->h_uv, d.Nu) OUTD(f->gv_h, c->h_uv + d.Nu, d.Nv) OUTD(f->gu_s, c->s_uv, d.Nu) OUTD(f->gv_s, c->s_uv + d.Nu, d.Nv)
+  OUTD(f->gu_grounded_fraction, c->gf_uv, d.Nu) OUTD(f->gv_grounded_fraction, c->gf_uv + d.Nu, d.Nv)
+  OUTD(f->u, c->uv, d.Nu) OUTD(f->v, c->uv + d.Nu, d.Nv) OUTD(f->eta, c->eta, (size_t)d.Nh * d.ns)
+  OUTD(f->beta, c->beta, d.Nh) OUTD(f->quad_f2, c->quad_f2, d.Nh) OUTD(f->shelf_strain_rate, c->shelf, d.Nh)
+  OUTD(f->av_speed, c->av_speed, d.Nh) OUTD(f->bed_speed, c->bed_speed, d.Nh) OUTD(f->tau_bed, c->tau, d.Nh)
+  OUTD(f->eta_av, c->eta_av, d.Nh) OUTD(f->quad_f1, c->quad_f1, d.Nh) OUTD(f->beta_eff, c->beta_eff, d.Nh)
+  OUTD(f->gu_beta_eff, c->beta_eff_uv, d.Nu) OUTD(f->gv_beta_eff, c->beta_eff_uv + d.Nu, d.Nv)
+  OUTD(f->gu_residual, c->resid_uv, d.Nu) OUTD(f->gv_residual, c->resid_uv + d.Nu, d.Nv)
+  if (out) {
+    if (out->dhdt) OUTD(out->dhdt, t.dhdt, d.Nh)
+    if (out->u_h) OUTD(out->u_h, t.uh, d.Nh)
+    if (out->v_h) OUTD(out->v_h, t.vh, d.Nh)
+    if (out->u_bed) OUTD(out->u_bed, t.ub, d.Nh)
+    if (out->v_bed) OUTD(out->v_bed, t.vb, d.Nh)
+    if (out->u_surf) OUTD(out->u_surf, t.us, d.Nh)
+    if (out->v_surf) OUTD(out->v_surf, t.vs, d.Nh)
+  }
+#undef OUTD
+  CK(cudaMemcpyAsync(const_cast<uint8_t*>(f->wu_mask), c->wmask_uv, d.Nu, dd, c->st));
+  CK(cudaMemcpyAsync(const_cast<uint8_t*>(f->wv_mask), c->wmask_uv + d.Nu, d.Nv, dd, c->st));
+  std::vector<uint8_t> wm((size_t)d.N);
+  CK(cudaMemcpyAsync(wm.data(), c->wmask_uv, d.N, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (out) {
+    out->n_wu = out->n_wv = 0;
+    for (int i = 0; i < d.Nu; ++i) out->n_wu += wm[i] != 0;
+    for (int i = d.Nu; i < d.N; ++i) out->n_wv += wm[i] != 0;
+    out->steps = nsteps;
+  }
+  c->solved = false;  // the state moved on after the last solve; the adjoint needs a fresh solve
+  if (st) *st = acc;
   return 0;
 }
 

@@ -146,6 +146,26 @@ class VelocitySolver:
         if st != 0:
             raise self._err(st)
 
+    # -- device time stepping --------------------------------------------------------------------
+    def run_device(self, params, dt, nsteps, bed, weertman_c, accumulation, h_isfixed, melt_rate, tensors,
+                   outputs=None):
+        """nsteps of update_state! + update_thickness! on the device (wavi_run_device).  bed, weertman_c,
+        accumulation (float64) and h_isfixed (uint8) are device tensors of nx*ny; tensors holds the model
+        fields (modified in place: the state after the last step); outputs optionally maps dhdt, u_h, v_h,
+        u_bed, v_bed, u_surf, v_surf to device tensors.  Returns (stats dict, (n_wu, n_wv))."""
+        ins = abi.StepInputs(bed.data_ptr(), weertman_c.data_ptr(), accumulation.data_ptr(), h_isfixed.data_ptr(),
+                             float(melt_rate), 0.0)
+        outs = abi.StepOutputs()
+        for k, t in (outputs or {}).items():
+            setattr(outs, k, t.data_ptr())
+        f = device_fields(tensors)
+        stats = abi.Stats()
+        st = self.lib.wavi_run_device(self.ctx, C.byref(params.to_c()), float(dt), int(nsteps), C.byref(ins),
+                                      C.byref(f), C.byref(outs), C.byref(stats))
+        if st != 0:
+            raise self._err(st)
+        return stats_dict(stats), (outs.n_wu, outs.n_wv)
+
     # -- adjoint ---------------------------------------------------------------------------------
     def adjoint_device(self, params, dJ_du, dJ_dv, grad_logC, grad_logA, tol=1e-10, maxiter=400):
         """Gradient of J w.r.t. per-cell log C and log A at the last solve's fixed point, from dJ/du, dJ/dv

@@ -32,6 +32,7 @@ class GPUParallelSpec:
     use_graphs: bool = True
     picard_test: int = 0
     coarse_solver: str = "auto"  # "auto", "cg" (reference), "srcg", "srcg_jacobi" (single-reduction CG)
+    device_run: bool = False     # run_simulation without a callback keeps the model on the device (wavi_run_device)
 
 
 _SOLVERS = {}
@@ -427,8 +428,46 @@ def timestep(sim):
 
 
 def run_simulation(sim, callback=None):
+    ps = sim.model.parallel_spec
+    n = sim.timestepping_params.n_iter_total - sim.n_iter
+    if (isinstance(ps, GPUParallelSpec) and ps.device_run and callback is None and n > 0
+            and sim.timestepping_params.step_thickness):
+        return _run_on_device(sim, n)
     for _ in range(sim.n_iter + 1, sim.timestepping_params.n_iter_total + 1):
         timestep(sim)
         if callback is not None:
             callback(sim)
+    return sim
+
+
+def _run_on_device(sim, n):
+    """n time steps of update_state! + update_thickness! in one wavi_run_device call: the fields go to the
+    device once and come back once."""
+    import torch
+    model, dt = sim.model, sim.timestepping_params.dt
+    if not model.params.evolveShelves:
+        raise NotImplementedError("evolveShelves = false is outside the velocity-solve path")
+    f = model.fields
+    dev = lambda a, t=np.float64: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=t).ravel(order="F"))).cuda()
+    t = {k: dev(f[k], np.uint8 if k in ("wu_mask", "wv_mask") else np.float64) for k in gpu.ALL_FIELDS}
+    outs = {k: torch.zeros(model.grid.nx * model.grid.ny, dtype=torch.float64, device="cuda")
+            for k in ("dhdt", "u_h", "v_h", "u_bed", "v_bed", "u_surf", "v_surf")}
+    stats, (nwu, nwv) = _solver_for(model).run_device(model.params, dt, n, dev(f["b"]), dev(model.weertman_c_param),
+                                                       dev(model.accumulation_param), dev(model.h_isfixed, np.uint8),
+                                                       model.melt_rate, t, outputs=outs)
+    for k in gpu.ALL_FIELDS:
+        if k in ("wu_correction_coarse", "wv_correction_coarse"):
+            continue
+        host = t[k].cpu().numpy().reshape(np.asarray(f[k]).shape, order="F")
+        f[k] = host
+    f["wu_correction_coarse"] = np.zeros(nwu)  # update_wavelets! restarts the coarse cache
+    f["wv_correction_coarse"] = np.zeros(nwv)
+    shape = (model.grid.nx, model.grid.ny)
+    f["dhdt"] = outs["dhdt"].cpu().numpy().reshape(shape, order="F")
+    for key, name in (("u_h", "uh"), ("v_h", "vh"), ("u_bed", "ub"), ("v_bed", "vb"), ("u_surf", "us"), ("v_surf", "vs")):
+        if name in f:
+            f[name] = outs[key].cpu().numpy().reshape(shape, order="F")
+    model.last_stats = stats
+    sim.n_iter += n
+    sim.time += n * dt
     return sim
