@@ -91,10 +91,14 @@ def test_single_reduction_fixed_cg_count_matches_oracle(oracle, reference_cg, na
 
 
 @pytest.mark.parametrize("kernel", ["persistent", "persistent_global"])
+@pytest.mark.parametrize("solver", ["srcg", "srcg_jacobi"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_srcg_jacobi_converged_solve_matches_reference(oracle, name, kernel):
-    """The Jacobi-preconditioned single-reduction coarse solve changes the V-cycle, not the fixed point: converged
-    FP64 and mixed solves agree with the reference's (cg!) FP64 solve to 1e-6."""
+def test_single_reduction_converged_solve_matches_reference(oracle, name, solver, kernel):
+    """The single-reduction coarse solves change the V-cycle, not the fixed point: converged FP64 and mixed
+    solves agree with the reference's (cg!) FP64 solve to 1e-6.  On the disc grids R A P is singular and the
+    FP32 coarse solves drift along its null space; the mixed solve converges because a coarse solve that
+    ends above its tolerance does not become the next warm start (without that rule these cases stall at
+    ~1e-6 with every coarse solve at maxiter_coarse)."""
     from wavi_gb300.gpu import VelocitySolver
     g, p, sp, om = _setup(oracle, name, maxiter_picard=80, tol_picard=1e-7)
     f0 = fields_from_oracle(om, g)
@@ -102,11 +106,11 @@ def test_srcg_jacobi_converged_solve_matches_reference(oracle, name, kernel):
     ost = om.stats()
     for prec in ("fp64", "mixed"):
         f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
-        s = VelocitySolver(g, sp, precision=prec, coarse_kernel=kernel, coarse_solver="srcg_jacobi")
+        s = VelocitySolver(g, sp, precision=prec, coarse_kernel=kernel, coarse_solver=solver)
         st = s.solve(p, f)
         assert st["status"] == 0, (prec, st)
         assert uv_err(f, om) < 1e-6, (prec, st, ost)
-        if name == "full":  # on ice-shelf discs the masked coarse space blunts the Jacobi gain
+        if name == "full" and solver == "srcg_jacobi":  # on ice-shelf discs the masked coarse space blunts the Jacobi gain
             assert st["coarse_cg_iterations"] < ost["coarse_cg_iterations"], (prec, st, ost)
         s.close()
 

@@ -835,19 +835,27 @@ __global__ void k_cg_update(int n, const T* __restrict__ u, const T* __restrict_
   }
 }
 
-// End of the V-cycle: x64 += corr; u/v = x at the interior; xc64 = xc; |corr|^2 and |x|^2 for the
-// relative update.
+// End of the V-cycle: x64 += corr; u/v = x at the interior; xc64 = xc (the next coarse solve's warm
+// start); |corr|^2 and |x|^2 for the relative update.
+//
+// In the FP32 coarse solve the warm start is dropped (xc64 = 0) when the coarse CG ended without meeting
+// its tolerance.  On a masked grid R A P is singular (Haar basis functions that coincide on the ice);
+// FP32 rounding leaves b slightly outside R A P's range, so each solve drifts along the null space, and
+// through the warm start the drift accumulates over V-cycles until every coarse solve runs to
+// maxiter_coarse and the Picard loop stalls near 1e-6.  A converged coarse solve keeps its warm start,
+// so solves that never hit maxiter_coarse are unchanged; the FP64 path keeps the reference's cache.
 template <typename T>
 __global__ void k_vcycle_finish(int n, const uint8_t* __restrict__ inner, const T* __restrict__ corr, const T* __restrict__ xc,
                                 double* __restrict__ x, double* __restrict__ uv, double* __restrict__ xc64,
                                 double* __restrict__ partials, DevState* st) {
+  const bool keep = sizeof(T) == sizeof(double) || st->cg_res <= st->cg_tol;
   double s0 = 0.0, s1 = 0.0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const double cv = (double)corr[k];
     const double v = x[k] + cv;
     x[k] = v;
     if (inner[k]) uv[k] = v;
-    xc64[k] = (double)xc[k];
+    xc64[k] = keep ? (double)xc[k] : 0.0;
     s0 += cv * cv;
     s1 += v * v;
   }

@@ -26,6 +26,8 @@
 // after the barrier every CTA adds all partials in the same fixed order.  Every wait is bounded: after
 // ~2^22 polls a CTA records WAVI_ERR_WATCHDOG and all CTAs leave the kernel.
 #pragma once
+#include <type_traits>
+
 #include "fused.cuh"
 
 namespace wavi {
@@ -83,13 +85,19 @@ __device__ __forceinline__ bool grid_sync(GridBar* bar, double* __restrict__ par
       for (int q = 0; q < NS; ++q) ss.warp[wid][q] = (double)x[q];
   }
   __syncthreads();  // the CTA's writes (halo vector, warp sums) precede the arrival
-  if (t == 0) {
+  if (wid == 0 && NS > 0) {
+    // lane l adds the sums of warps l/4, l/4 + 8, ... for quantity l%4, then a butterfly over the lanes
+    // of equal l%4: three dependent FP64 adds instead of nw sequential ones (same order in every CTA)
+    const int q = lane & 3;
+    double s = 0.0;
+    if (q < NS)
+      for (int k = lane >> 2; k < nw; k += 8) s += ss.warp[k][q];
 #pragma unroll
-    for (int q = 0; q < NS; ++q) {
-      double s = 0.0;
-      for (int k = 0; k < nw; ++k) s += ss.warp[k][q];
-      slot[q * nb + blockIdx.x] = s;
-    }
+    for (int o = 4; o < 32; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane < NS) slot[lane * nb + blockIdx.x] = s;
+    __syncwarp();
+  }
+  if (t == 0) {
     __threadfence();
     red_release_add_u32(&bar->count, 1u);
     const unsigned target = epoch * nb;
@@ -232,6 +240,7 @@ __device__ __forceinline__ void prolong_store(const Dims& d, int levels, const u
 template <typename T>
 struct CGScalars {
   double res, tol, alpha, beta, gamma_prev, alpha_prev;
+  double rr, tol2;  // squared residual norm and tolerance (the FP32 kernels' stopping test)
   T alpha_t, beta_t;
   int stop;
 };
@@ -243,6 +252,25 @@ __device__ __forceinline__ T fmul_add(T a, T b, T c) {
 template <>
 __device__ __forceinline__ float fmul_add<float>(float a, float b, float c) {
   return fmaf(a, b, c);
+}
+
+// a / b for the CG scalars.  The FP64 kernels divide exactly.  In the FP32 kernels one thread per CTA
+// computes the scalars while the CTA waits, and GB300's FP64 divide makes that the largest single cost
+// of an iteration (about 2 µs for the three divisions and the square root); there the quotient is a
+// float reciprocal refined by two Newton steps in FP64 (relative error ~1e-15; exact division outside
+// float's range).
+template <typename T>
+__device__ __forceinline__ double cg_div(double a, double b) {
+  return a / b;
+}
+template <>
+__device__ __forceinline__ double cg_div<float>(double a, double b) {
+  const double ab = fabs(b);
+  if (!(ab > 1e-30 && ab < 1e30)) return a / b;
+  double r = (double)(1.0f / (float)b);
+  r = r * (2.0 - b * r);
+  double q = a * r;
+  return q + r * (a - b * q);
 }
 
 // The whole coarse CG of one V-cycle with the reference's cg! recurrence: from the warm start xc and
@@ -298,7 +326,9 @@ __global__ void __launch_bounds__(TILE* TILE)
       }
     if (!grid_sync<2>(bar, partials, epoch, ss, a, [&](const double* tot) {
           sc.res = sqrt(tot[0]);
+          sc.rr = tot[0];
           sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[1]));  // reltol = sqrt(eps)
+          sc.tol2 = sc.tol * sc.tol;
           sc.alpha_prev = 1.0;  // prev
           sc.stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
           sc.beta = sc.res * sc.res;
@@ -324,7 +354,7 @@ __global__ void __launch_bounds__(TILE* TILE)
         dot[0] += uu[k] * cu[k] + uv[k] * cv[k];
       }
     if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const double* tot) {
-          sc.alpha = (sc.res * sc.res) / tot[0];
+          sc.alpha = std::is_same<T, float>::value ? cg_div<T>(sc.rr, tot[0]) : (sc.res * sc.res) / tot[0];
           sc.alpha_t = (T)sc.alpha;
         }))
       return;
@@ -341,10 +371,17 @@ __global__ void __launch_bounds__(TILE* TILE)
       }
     ++it;
     if (!grid_sync<1>(bar, partials, epoch, ss, rr, [&](const double* tot) {
-          sc.alpha_prev = sc.res;  // prev
-          sc.res = sqrt(tot[0]);
-          sc.stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
-          sc.beta = (sc.res * sc.res) / (sc.alpha_prev * sc.alpha_prev);
+          if (std::is_same<T, float>::value) {  // squared norms: no square root per iteration
+            const double rr_prev = sc.rr;
+            sc.rr = tot[0];
+            sc.stop = it >= maxit || sc.rr <= sc.tol2 || !(sc.rr == sc.rr);
+            sc.beta = cg_div<T>(sc.rr, rr_prev);
+          } else {
+            sc.alpha_prev = sc.res;  // prev
+            sc.res = sqrt(tot[0]);
+            sc.stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
+            sc.beta = (sc.res * sc.res) / (sc.alpha_prev * sc.alpha_prev);
+          }
           sc.beta_t = (T)sc.beta;
         }))
       return;
@@ -359,7 +396,7 @@ __global__ void __launch_bounds__(TILE* TILE)
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {
     st->cg_it = it;
     st->cg_total += it;
-    st->cg_res = sc.res;
+    st->cg_res = std::is_same<T, float>::value ? sqrt(sc.rr) : sc.res;
     st->cg_prev = sc.alpha_prev;
     st->cg_tol = sc.tol;
   }
@@ -466,19 +503,22 @@ __global__ void __launch_bounds__(TILE* TILE)
         a[2] += ru[k] * ru[k] + rv[k] * rv[k];
       }
     if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const double* tot) {
+          constexpr bool f32 = std::is_same<T, float>::value;
           const double gamma = tot[0], delta = tot[1];
-          sc.res = sqrt(tot[2]);
+          sc.rr = tot[2];
+          if (!f32 || first) sc.res = sqrt(tot[2]);
           int stop;
           if (first) {
             sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[3]));  // reltol = sqrt(eps)
+            sc.tol2 = sc.tol * sc.tol;
             sc.beta = 0.0;
-            sc.alpha = gamma / delta;
-            stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
+            sc.alpha = cg_div<T>(gamma, delta);
+            stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.rr == sc.rr);
           } else {
-            stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
+            stop = it >= maxit || (f32 ? sc.rr <= sc.tol2 : sc.res <= sc.tol) || !(sc.rr == sc.rr);
             if (!stop) {
-              sc.beta = gamma / sc.gamma_prev;
-              sc.alpha = gamma / (delta - sc.beta * gamma / sc.alpha);
+              sc.beta = cg_div<T>(gamma, sc.gamma_prev);
+              sc.alpha = cg_div<T>(gamma, delta - sc.beta * cg_div<T>(gamma, sc.alpha));
             }
           }
           if (!stop && (!(sc.alpha == sc.alpha) || isinf(sc.alpha))) stop = 1;
@@ -510,7 +550,7 @@ __global__ void __launch_bounds__(TILE* TILE)
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {
     st->cg_it = it;
     st->cg_total += it;
-    st->cg_res = sc.res;
+    st->cg_res = std::is_same<T, float>::value ? sqrt(sc.rr) : sc.res;
     st->cg_tol = sc.tol;
   }
 }
@@ -633,19 +673,22 @@ __global__ void __launch_bounds__(TILE* TILE)
       }
     }
     if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const double* tot) {
+          constexpr bool f32 = std::is_same<T, float>::value;
           const double gamma = tot[0], delta = tot[1];
-          sc.res = sqrt(tot[2]);
+          sc.rr = tot[2];
+          if (!f32 || first) sc.res = sqrt(tot[2]);
           int stop;
           if (first) {
             sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[3]));  // reltol = sqrt(eps)
+            sc.tol2 = sc.tol * sc.tol;
             sc.beta = 0.0;
-            sc.alpha = gamma / delta;
-            stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
+            sc.alpha = cg_div<T>(gamma, delta);
+            stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.rr == sc.rr);
           } else {
-            stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
+            stop = it >= maxit || (f32 ? sc.rr <= sc.tol2 : sc.res <= sc.tol) || !(sc.rr == sc.rr);
             if (!stop) {
-              sc.beta = gamma / sc.gamma_prev;
-              sc.alpha = gamma / (delta - sc.beta * gamma / sc.alpha);
+              sc.beta = cg_div<T>(gamma, sc.gamma_prev);
+              sc.alpha = cg_div<T>(gamma, delta - sc.beta * cg_div<T>(gamma, sc.alpha));
             }
           }
           if (!stop && (!(sc.alpha == sc.alpha) || isinf(sc.alpha))) stop = 1;
@@ -661,7 +704,7 @@ __global__ void __launch_bounds__(TILE* TILE)
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {
     st->cg_it = it;
     st->cg_total += it;
-    st->cg_res = sc.res;
+    st->cg_res = std::is_same<T, float>::value ? sqrt(sc.rr) : sc.res;
     st->cg_tol = sc.tol;
   }
 }
@@ -713,7 +756,9 @@ __global__ void __launch_bounds__(TILE* TILE)
     }
     if (!grid_sync<2>(bar, partials, epoch, ss, a, [&](const double* tot) {
           sc.res = sqrt(tot[0]);
+          sc.rr = tot[0];
           sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[1]));  // reltol = sqrt(eps)
+          sc.tol2 = sc.tol * sc.tol;
           sc.alpha_prev = 1.0;  // prev
           sc.stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
           sc.beta = sc.res * sc.res;
@@ -757,7 +802,7 @@ __global__ void __launch_bounds__(TILE* TILE)
       }
     }
     if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const double* tot) {
-          sc.alpha = (sc.res * sc.res) / tot[0];
+          sc.alpha = std::is_same<T, float>::value ? cg_div<T>(sc.rr, tot[0]) : (sc.res * sc.res) / tot[0];
           sc.alpha_t = (T)sc.alpha;
         }))
       return;
@@ -777,10 +822,17 @@ __global__ void __launch_bounds__(TILE* TILE)
     }
     ++it;
     if (!grid_sync<1>(bar, partials, epoch, ss, rr, [&](const double* tot) {
-          sc.alpha_prev = sc.res;  // prev
-          sc.res = sqrt(tot[0]);
-          sc.stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
-          sc.beta = (sc.res * sc.res) / (sc.alpha_prev * sc.alpha_prev);
+          if (std::is_same<T, float>::value) {  // squared norms: no square root per iteration
+            const double rr_prev = sc.rr;
+            sc.rr = tot[0];
+            sc.stop = it >= maxit || sc.rr <= sc.tol2 || !(sc.rr == sc.rr);
+            sc.beta = cg_div<T>(sc.rr, rr_prev);
+          } else {
+            sc.alpha_prev = sc.res;  // prev
+            sc.res = sqrt(tot[0]);
+            sc.stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
+            sc.beta = (sc.res * sc.res) / (sc.alpha_prev * sc.alpha_prev);
+          }
           sc.beta_t = (T)sc.beta;
         }))
       return;
@@ -788,7 +840,7 @@ __global__ void __launch_bounds__(TILE* TILE)
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {
     st->cg_it = it;
     st->cg_total += it;
-    st->cg_res = sc.res;
+    st->cg_res = std::is_same<T, float>::value ? sqrt(sc.rr) : sc.res;
     st->cg_prev = sc.alpha_prev;
     st->cg_tol = sc.tol;
   }
