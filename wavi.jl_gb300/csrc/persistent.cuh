@@ -51,27 +51,102 @@ __device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
 }
 
+// ------------------------------------------------------------------------------------------------
+// Float-float arithmetic for the FP32 kernels' reductions and CG scalars.  GB300 executes FP64 at a
+// small fraction of its FP32 rate (a warp's FP64 instruction costs tens of cycles, with one lane active
+// or all), and the grid sums and scalar recurrences are serial chains on every CG iteration's critical
+// path.  A value is the unevaluated sum hi + lo of two floats with |lo| <= ulp(hi)/2 (~48-bit
+// significand), built from Knuth's TwoSum and the FMA TwoProduct (Dekker 1971; the double-double
+// algorithms of Hida, Li & Bailey 2001 carried over to floats).  The __f*_rn intrinsics keep the
+// compiler from contracting the error terms into FMAs.  The range is float's, as for the FP32 kernels'
+// per-thread products.
+// ------------------------------------------------------------------------------------------------
+struct ff {
+  float hi, lo;
+};
+__device__ __forceinline__ ff ff_quick_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ ff operator+(ff x, ff y) {
+  ff s = ff_two_sum(x.hi, y.hi);
+  const ff t = ff_two_sum(x.lo, y.lo);
+  s = ff_quick_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return ff_quick_two_sum(s.hi, __fadd_rn(s.lo, t.lo));
+}
+__device__ __forceinline__ ff operator-(ff x) { return {-x.hi, -x.lo}; }
+__device__ __forceinline__ ff operator-(ff x, ff y) { return x + (-y); }
+__device__ __forceinline__ ff operator*(ff x, ff y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  const float e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)));
+  return ff_quick_two_sum(p, e);
+}
+__device__ __forceinline__ ff operator/(ff x, ff y) {
+  const float q1 = __fdiv_rn(x.hi, y.hi);
+  const ff r = x - y * ff{q1, 0.0f};
+  return ff_quick_two_sum(q1, __fdiv_rn(r.hi, y.hi));
+}
+__device__ __forceinline__ bool operator<=(ff x, ff y) { return x.hi < y.hi || (x.hi == y.hi && x.lo <= y.lo); }
+__device__ __forceinline__ ff ff_of(double v) {
+  const float h = __double2float_rn(v);
+  return {h, __double2float_rn(v - (double)h)};
+}
+__device__ __forceinline__ double dbl_of(ff v) { return (double)v.hi + (double)v.lo; }
+__device__ __forceinline__ double dbl_of(double v) { return v; }
+
+// The type in which a kernel of vector type T sums its grid reductions and keeps its CG scalars.
+template <typename T>
+struct CGReal {
+  using type = double;
+};
+template <>
+struct CGReal<float> {
+  using type = ff;
+};
+__device__ __forceinline__ double real_term(double x) { return x; }
+__device__ __forceinline__ ff real_term(float x) { return {x, 0.0f}; }
+__device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ ff shfl_xor(ff v, int o) {
+  return {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+__device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ ff ld_cg(const ff* p) {
+  const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+  return {v.x, v.y};
+}
+
 // Shared memory of the grid synchronisation.
 struct SyncShared {
-  double warp[32][4];  // FP64 warp sums
-  double tot[4];       // grid totals
+  double warp[32][4];  // warp sums (CGReal of the kernel's vector type: double, or ff in the same 8 bytes)
+  double tot[4];       // grid totals (the same type)
   int ok;
 };
 
 // Grid-wide barrier over gridDim.x CTAs.  v[0..NS) are this thread's terms (type A: float or double);
-// after the barrier tot[0..NS) in shared memory hold their grid sums (FP64) and `scalars(tot)` has run in
-// thread 0 (it derives the CG scalars once per CTA); the barrier ends with a __syncthreads, so its
-// results are visible to the whole CTA.  `epoch` counts this thread's barriers since the launch (the
-// same in every thread); partials holds 2 x 4 x gridDim.x doubles (the two parities of the epoch, so a
-// slot is rewritten only after every CTA has read it).  Returns false (in every thread of the CTA) if
-// the wait gave up or another CTA reported an error.
+// they are summed over the warp in A, over the CTA and the grid in S = CGReal<A> (double, or float-float
+// for float), and after the barrier tot[0..NS) (type S, in shared memory) hold the grid sums and
+// `scalars(tot)` has run in thread 0 (it derives the CG scalars once per CTA); the barrier ends with a
+// __syncthreads, so its results are visible to the whole CTA.  `epoch` counts this thread's barriers
+// since the launch (the same in every thread); partials holds 2 x 4 x gridDim.x 8-byte slots (the two
+// parities of the epoch, so a slot is rewritten only after every CTA has read it).  Arrival is a
+// red.release by thread 0 after the CTA barrier (release is cumulative: it publishes the CTA's stores
+// ordered before it by the __syncthreads); the wait is an ld.acquire poll followed by a __syncthreads.
+// Returns false (in every thread of the CTA) if the wait gave up or another CTA reported an error.
 template <int NS, typename A, typename F>
 __device__ __forceinline__ bool grid_sync(GridBar* bar, double* __restrict__ partials, unsigned& epoch, SyncShared& ss,
                                           const A (&v)[4], F&& scalars) {
+  using S = typename CGReal<A>::type;
+  static_assert(sizeof(S) == sizeof(double), "partial slots are 8 bytes");
   const int t = flat_tid(), lane = t & 31, wid = t >> 5, nw = (flat_nthreads() + 31) >> 5;
   const unsigned nb = gridDim.x;
   ++epoch;
-  double* slot = partials + (size_t)(epoch & 1u) * 4u * nb;
+  S* slot = reinterpret_cast<S*>(partials + (size_t)(epoch & 1u) * 4u * nb);
+  S(*wsum)[4] = reinterpret_cast<S(*)[4]>(ss.warp);
+  S* tot = reinterpret_cast<S*>(ss.tot);
   if (NS > 0) {
     A x[4];
 #pragma unroll
@@ -82,23 +157,22 @@ __device__ __forceinline__ bool grid_sync(GridBar* bar, double* __restrict__ par
     }
     if (lane == 0)
 #pragma unroll
-      for (int q = 0; q < NS; ++q) ss.warp[wid][q] = (double)x[q];
+      for (int q = 0; q < NS; ++q) wsum[wid][q] = real_term(x[q]);
   }
   __syncthreads();  // the CTA's writes (halo vector, warp sums) precede the arrival
   if (wid == 0 && NS > 0) {
     // lane l adds the sums of warps l/4, l/4 + 8, ... for quantity l%4, then a butterfly over the lanes
-    // of equal l%4: three dependent FP64 adds instead of nw sequential ones (same order in every CTA)
+    // of equal l%4 (the same order in every CTA)
     const int q = lane & 3;
-    double s = 0.0;
+    S s{};
     if (q < NS)
-      for (int k = lane >> 2; k < nw; k += 8) s += ss.warp[k][q];
+      for (int k = lane >> 2; k < nw; k += 8) s = s + wsum[k][q];
 #pragma unroll
-    for (int o = 4; o < 32; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    for (int o = 4; o < 32; o <<= 1) s = s + shfl_xor(s, o);
     if (lane < NS) slot[lane * nb + blockIdx.x] = s;
     __syncwarp();
   }
   if (t == 0) {
-    __threadfence();
     red_release_add_u32(&bar->count, 1u);
     const unsigned target = epoch * nb;
     int ok = 1;
@@ -116,26 +190,26 @@ __device__ __forceinline__ bool grid_sync(GridBar* bar, double* __restrict__ par
   __syncthreads();
   if (!ss.ok) return false;
   if (NS > 0) {
-    // warp q adds partial q of every CTA: lane-strided sequential sums, then a butterfly (fixed order)
+    // warp q adds partial q of every CTA: eight slots per lane and round, added as a tree, then a
+    // butterfly (a fixed order, so every CTA obtains the same bits)
     if (wid < NS) {
-      const double* src = slot + wid * nb;
-      double s = 0.0;
+      const S* src = slot + wid * nb;
+      S s{};
       for (unsigned k0 = 0; k0 < nb; k0 += 256) {
-        double b[8];
+        S b[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
           const unsigned k = k0 + lane + 32u * e;
-          b[e] = k < nb ? __ldcg(src + k) : 0.0;
+          b[e] = k < nb ? ld_cg(src + k) : S{};
         }
-#pragma unroll
-        for (int e = 0; e < 8; ++e) s += b[e];
+        s = s + (((b[0] + b[1]) + (b[2] + b[3])) + ((b[4] + b[5]) + (b[6] + b[7])));
       }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) ss.tot[wid] = s;
+      for (int o = 16; o > 0; o >>= 1) s = s + shfl_xor(s, o);
+      if (lane == 0) tot[wid] = s;
     }
     __syncthreads();
-    if (t == 0) scalars(ss.tot);
+    if (t == 0) scalars(static_cast<const S*>(tot));
     __syncthreads();
   }
   return true;
@@ -144,7 +218,7 @@ __device__ __forceinline__ bool grid_sync(GridBar* bar, double* __restrict__ par
 template <typename A>
 __device__ __forceinline__ bool grid_barrier(GridBar* bar, double* __restrict__ partials, unsigned& epoch, SyncShared& ss) {
   const A v[4] = {A(0), A(0), A(0), A(0)};
-  return grid_sync<0>(bar, partials, epoch, ss, v, [](const double*) {});
+  return grid_sync<0>(bar, partials, epoch, ss, v, [](const typename CGReal<A>::type*) {});
 }
 
 // One lifting pass along a 1-D line held one element per lane (lane bits below TILE select the
@@ -236,41 +310,120 @@ __device__ __forceinline__ void prolong_store(const Dims& d, int levels, const u
   }
 }
 
-// CG scalars broadcast to the CTA (written by thread 0 inside grid_sync).
+// CG scalars broadcast to the CTA (written by thread 0 inside grid_sync).  R = CGReal<T>: the FP64
+// kernels keep the reference's FP64 scalars; the FP32 kernels keep squared norms and the recurrence
+// scalars in float-float (no FP64 arithmetic per iteration; res and tol are FP64, set once per solve).
 template <typename T>
 struct CGScalars {
-  double res, tol, alpha, beta, gamma_prev, alpha_prev;
-  double rr, tol2;  // squared residual norm and tolerance (the FP32 kernels' stopping test)
+  using R = typename CGReal<T>::type;
+  double res, tol;   // |r| and the stopping tolerance
+  double alpha_prev; // cg!'s "prev" (FP64 kernels)
+  R rr, tol2;        // |r|^2 and tol^2
+  R alpha, beta, gamma_prev;
   T alpha_t, beta_t;
   int stop;
 };
 
 template <typename T>
 __device__ __forceinline__ T fmul_add(T a, T b, T c) {
-  return fma(a, b, c);
+  return a * b + c;
 }
 template <>
 __device__ __forceinline__ float fmul_add<float>(float a, float b, float c) {
   return fmaf(a, b, c);
 }
 
-// a / b for the CG scalars.  The FP64 kernels divide exactly.  In the FP32 kernels one thread per CTA
-// computes the scalars while the CTA waits, and GB300's FP64 divide makes that the largest single cost
-// of an iteration (about 2 µs for the three divisions and the square root); there the quotient is a
-// float reciprocal refined by two Newton steps in FP64 (relative error ~1e-15; exact division outside
-// float's range).
+__device__ __forceinline__ float to_vec(ff v) { return v.hi; }
+__device__ __forceinline__ double to_vec(double v) { return v; }
+__device__ __forceinline__ bool is_nan(ff v) { return !(v.hi == v.hi); }
+__device__ __forceinline__ bool is_nan(double v) { return !(v == v); }
+__device__ __forceinline__ bool not_finite(ff v) { return !(v.hi == v.hi) || isinf(v.hi); }
+__device__ __forceinline__ bool not_finite(double v) { return !(v == v) || isinf(v); }
+
+// cg! scalars (IterativeSolvers cg!, the reference's coarse solver).  Start: |r0|^2 and |b_c|^2 give the
+// tolerance max(sqrt(eps) |r0|, tol_coarse |b_c|); the first direction is r (β = 0).
 template <typename T>
-__device__ __forceinline__ double cg_div(double a, double b) {
-  return a / b;
+__device__ __forceinline__ void cg_start(CGScalars<T>& sc, const typename CGReal<T>::type* tot, int maxit,
+                                         double tol_coarse) {
+  sc.res = sqrt(dbl_of(tot[0]));
+  sc.rr = tot[0];
+  sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(dbl_of(tot[1])));  // reltol = sqrt(eps)
+  if constexpr (std::is_same<T, float>::value)
+    sc.tol2 = ff_of(sc.tol * sc.tol);
+  else
+    sc.tol2 = sc.tol * sc.tol;
+  sc.alpha_prev = 1.0;  // prev
+  sc.stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
+  sc.beta_t = (T)0;  // u = 0: the first direction is r
 }
-template <>
-__device__ __forceinline__ double cg_div<float>(double a, double b) {
-  const double ab = fabs(b);
-  if (!(ab > 1e-30 && ab < 1e30)) return a / b;
-  double r = (double)(1.0f / (float)b);
-  r = r * (2.0 - b * r);
-  double q = a * r;
-  return q + r * (a - b * q);
+// α = |r|^2 / (u, c) with c = R A P u
+template <typename T>
+__device__ __forceinline__ void cg_alpha(CGScalars<T>& sc, const typename CGReal<T>::type* tot) {
+  if constexpr (std::is_same<T, float>::value)
+    sc.alpha = sc.rr / tot[0];
+  else
+    sc.alpha = (sc.res * sc.res) / tot[0];
+  sc.alpha_t = (T)to_vec(sc.alpha);
+}
+// new |r|^2: stopping test and β = |r|^2 / |r_prev|^2
+template <typename T>
+__device__ __forceinline__ void cg_next(CGScalars<T>& sc, const typename CGReal<T>::type* tot, int it, int maxit) {
+  if constexpr (std::is_same<T, float>::value) {  // squared norms: no square root per iteration
+    const ff rr_prev = sc.rr;
+    sc.rr = tot[0];
+    sc.stop = it >= maxit || sc.rr <= sc.tol2 || is_nan(sc.rr);
+    sc.beta = sc.rr / rr_prev;
+  } else {
+    sc.alpha_prev = sc.res;  // prev
+    sc.res = sqrt(tot[0]);
+    sc.stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
+    sc.beta = (sc.res * sc.res) / (sc.alpha_prev * sc.alpha_prev);
+  }
+  sc.beta_t = (T)to_vec(sc.beta);
+}
+// Single-reduction CG scalars from γ = (r, z), δ = (w, z), |r|^2 (and |b_c|^2 in the first pass):
+// β = γ/γ',  α = γ / (δ - β γ / α')  (the oracle's coarse_srcg in FP64, the same order).
+template <typename T>
+__device__ __forceinline__ void srcg_scalars(CGScalars<T>& sc, const typename CGReal<T>::type* tot, bool first, int it,
+                                             int maxit, double tol_coarse) {
+  using R = typename CGReal<T>::type;
+  constexpr bool f32 = std::is_same<T, float>::value;
+  const R gamma = tot[0], delta = tot[1];
+  sc.rr = tot[2];
+  if (!f32 || first) sc.res = sqrt(dbl_of(tot[2]));
+  int stop;
+  if (first) {
+    sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(dbl_of(tot[3])));  // reltol = sqrt(eps)
+    if constexpr (f32)
+      sc.tol2 = ff_of(sc.tol * sc.tol);
+    else
+      sc.tol2 = sc.tol * sc.tol;
+    sc.beta = R{};
+    sc.alpha = gamma / delta;
+    stop = (0 >= maxit) || sc.res <= sc.tol || is_nan(sc.rr);
+  } else {
+    if constexpr (f32)
+      stop = it >= maxit || sc.rr <= sc.tol2 || is_nan(sc.rr);
+    else
+      stop = it >= maxit || sc.res <= sc.tol || is_nan(sc.rr);
+    if (!stop) {
+      sc.beta = gamma / sc.gamma_prev;
+      sc.alpha = gamma / (delta - sc.beta * gamma / sc.alpha);
+    }
+  }
+  if (!stop && not_finite(sc.alpha)) stop = 1;
+  sc.gamma_prev = gamma;
+  sc.alpha_t = (T)to_vec(sc.alpha);
+  sc.beta_t = (T)to_vec(sc.beta);
+  sc.stop = stop;
+}
+// |r| of the final iterate for the statistics
+template <typename T>
+__device__ __forceinline__ double cg_final_res(const CGScalars<T>& sc) {
+  if constexpr (std::is_same<T, float>::value)
+    return sqrt(dbl_of(sc.rr));
+  else
+    return sc.res;
 }
 
 // The whole coarse CG of one V-cycle with the reference's cg! recurrence: from the warm start xc and
@@ -324,16 +477,7 @@ __global__ void __launch_bounds__(TILE* TILE)
         a[0] += ru[k] * ru[k] + rv[k] * rv[k];
         a[1] += bu * bu + bv * bv;
       }
-    if (!grid_sync<2>(bar, partials, epoch, ss, a, [&](const double* tot) {
-          sc.res = sqrt(tot[0]);
-          sc.rr = tot[0];
-          sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[1]));  // reltol = sqrt(eps)
-          sc.tol2 = sc.tol * sc.tol;
-          sc.alpha_prev = 1.0;  // prev
-          sc.stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
-          sc.beta = sc.res * sc.res;
-          sc.beta_t = (T)0;  // u = 0: the first direction is r (and res^2 may not fit in T)
-        }))
+    if (!grid_sync<2>(bar, partials, epoch, ss, a, [&](const typename CGReal<T>::type* tot) { cg_start<T>(sc, tot, maxit, tol_coarse); }))
       return;
   }
   while (!sc.stop) {
@@ -353,10 +497,7 @@ __global__ void __launch_bounds__(TILE* TILE)
         coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, cu[k], cv[k]);
         dot[0] += uu[k] * cu[k] + uv[k] * cv[k];
       }
-    if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const double* tot) {
-          sc.alpha = std::is_same<T, float>::value ? cg_div<T>(sc.rr, tot[0]) : (sc.res * sc.res) / tot[0];
-          sc.alpha_t = (T)sc.alpha;
-        }))
+    if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const typename CGReal<T>::type* tot) { cg_alpha<T>(sc, tot); }))
       return;
     const T alpha = sc.alpha_t;
     T rr[4] = {T(0), T(0), T(0), T(0)};
@@ -370,20 +511,7 @@ __global__ void __launch_bounds__(TILE* TILE)
         rr[0] += ru[k] * ru[k] + rv[k] * rv[k];
       }
     ++it;
-    if (!grid_sync<1>(bar, partials, epoch, ss, rr, [&](const double* tot) {
-          if (std::is_same<T, float>::value) {  // squared norms: no square root per iteration
-            const double rr_prev = sc.rr;
-            sc.rr = tot[0];
-            sc.stop = it >= maxit || sc.rr <= sc.tol2 || !(sc.rr == sc.rr);
-            sc.beta = cg_div<T>(sc.rr, rr_prev);
-          } else {
-            sc.alpha_prev = sc.res;  // prev
-            sc.res = sqrt(tot[0]);
-            sc.stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
-            sc.beta = (sc.res * sc.res) / (sc.alpha_prev * sc.alpha_prev);
-          }
-          sc.beta_t = (T)sc.beta;
-        }))
+    if (!grid_sync<1>(bar, partials, epoch, ss, rr, [&](const typename CGReal<T>::type* tot) { cg_next<T>(sc, tot, it, maxit); }))
       return;
   }
 #pragma unroll
@@ -396,7 +524,7 @@ __global__ void __launch_bounds__(TILE* TILE)
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {
     st->cg_it = it;
     st->cg_total += it;
-    st->cg_res = std::is_same<T, float>::value ? sqrt(sc.rr) : sc.res;
+    st->cg_res = cg_final_res(sc);
     st->cg_prev = sc.alpha_prev;
     st->cg_tol = sc.tol;
   }
@@ -502,31 +630,7 @@ __global__ void __launch_bounds__(TILE* TILE)
         a[1] += wu[k] * zu[k] + wv[k] * zv[k];
         a[2] += ru[k] * ru[k] + rv[k] * rv[k];
       }
-    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const double* tot) {
-          constexpr bool f32 = std::is_same<T, float>::value;
-          const double gamma = tot[0], delta = tot[1];
-          sc.rr = tot[2];
-          if (!f32 || first) sc.res = sqrt(tot[2]);
-          int stop;
-          if (first) {
-            sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[3]));  // reltol = sqrt(eps)
-            sc.tol2 = sc.tol * sc.tol;
-            sc.beta = 0.0;
-            sc.alpha = cg_div<T>(gamma, delta);
-            stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.rr == sc.rr);
-          } else {
-            stop = it >= maxit || (f32 ? sc.rr <= sc.tol2 : sc.res <= sc.tol) || !(sc.rr == sc.rr);
-            if (!stop) {
-              sc.beta = cg_div<T>(gamma, sc.gamma_prev);
-              sc.alpha = cg_div<T>(gamma, delta - sc.beta * cg_div<T>(gamma, sc.alpha));
-            }
-          }
-          if (!stop && (!(sc.alpha == sc.alpha) || isinf(sc.alpha))) stop = 1;
-          sc.gamma_prev = gamma;
-          sc.alpha_t = (T)sc.alpha;
-          sc.beta_t = (T)sc.beta;
-          sc.stop = stop;
-        }))
+    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const typename CGReal<T>::type* tot) { srcg_scalars<T>(sc, tot, first, it, maxit, tol_coarse); }))
       return;
     if (sc.stop) break;
     const T beta = sc.beta_t;
@@ -550,7 +654,7 @@ __global__ void __launch_bounds__(TILE* TILE)
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {
     st->cg_it = it;
     st->cg_total += it;
-    st->cg_res = std::is_same<T, float>::value ? sqrt(sc.rr) : sc.res;
+    st->cg_res = cg_final_res(sc);
     st->cg_tol = sc.tol;
   }
 }
@@ -672,31 +776,7 @@ __global__ void __launch_bounds__(TILE* TILE)
         g.gw[q] = wv;
       }
     }
-    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const double* tot) {
-          constexpr bool f32 = std::is_same<T, float>::value;
-          const double gamma = tot[0], delta = tot[1];
-          sc.rr = tot[2];
-          if (!f32 || first) sc.res = sqrt(tot[2]);
-          int stop;
-          if (first) {
-            sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[3]));  // reltol = sqrt(eps)
-            sc.tol2 = sc.tol * sc.tol;
-            sc.beta = 0.0;
-            sc.alpha = cg_div<T>(gamma, delta);
-            stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.rr == sc.rr);
-          } else {
-            stop = it >= maxit || (f32 ? sc.rr <= sc.tol2 : sc.res <= sc.tol) || !(sc.rr == sc.rr);
-            if (!stop) {
-              sc.beta = cg_div<T>(gamma, sc.gamma_prev);
-              sc.alpha = cg_div<T>(gamma, delta - sc.beta * cg_div<T>(gamma, sc.alpha));
-            }
-          }
-          if (!stop && (!(sc.alpha == sc.alpha) || isinf(sc.alpha))) stop = 1;
-          sc.gamma_prev = gamma;
-          sc.alpha_t = (T)sc.alpha;
-          sc.beta_t = (T)sc.beta;
-          sc.stop = stop;
-        }))
+    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const typename CGReal<T>::type* tot) { srcg_scalars<T>(sc, tot, first, it, maxit, tol_coarse); }))
       return;
     if (sc.stop) break;
     first = false;
@@ -704,7 +784,7 @@ __global__ void __launch_bounds__(TILE* TILE)
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {
     st->cg_it = it;
     st->cg_total += it;
-    st->cg_res = std::is_same<T, float>::value ? sqrt(sc.rr) : sc.res;
+    st->cg_res = cg_final_res(sc);
     st->cg_tol = sc.tol;
   }
 }
@@ -754,16 +834,7 @@ __global__ void __launch_bounds__(TILE* TILE)
         a[1] += bv * bv;
       }
     }
-    if (!grid_sync<2>(bar, partials, epoch, ss, a, [&](const double* tot) {
-          sc.res = sqrt(tot[0]);
-          sc.rr = tot[0];
-          sc.tol = fmax(1.4901161193847656e-08 * sc.res, tol_coarse * sqrt(tot[1]));  // reltol = sqrt(eps)
-          sc.tol2 = sc.tol * sc.tol;
-          sc.alpha_prev = 1.0;  // prev
-          sc.stop = (0 >= maxit) || sc.res <= sc.tol || !(sc.res == sc.res);
-          sc.beta = sc.res * sc.res;
-          sc.beta_t = (T)0;  // u = 0: the first direction is r
-        }))
+    if (!grid_sync<2>(bar, partials, epoch, ss, a, [&](const typename CGReal<T>::type* tot) { cg_start<T>(sc, tot, maxit, tol_coarse); }))
       return;
   }
   while (!sc.stop) {
@@ -801,10 +872,7 @@ __global__ void __launch_bounds__(TILE* TILE)
         g.gp[q] = cv;
       }
     }
-    if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const double* tot) {
-          sc.alpha = std::is_same<T, float>::value ? cg_div<T>(sc.rr, tot[0]) : (sc.res * sc.res) / tot[0];
-          sc.alpha_t = (T)sc.alpha;
-        }))
+    if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const typename CGReal<T>::type* tot) { cg_alpha<T>(sc, tot); }))
       return;
     const T alpha = sc.alpha_t;
     T rr[4] = {T(0), T(0), T(0), T(0)};
@@ -821,26 +889,13 @@ __global__ void __launch_bounds__(TILE* TILE)
       }
     }
     ++it;
-    if (!grid_sync<1>(bar, partials, epoch, ss, rr, [&](const double* tot) {
-          if (std::is_same<T, float>::value) {  // squared norms: no square root per iteration
-            const double rr_prev = sc.rr;
-            sc.rr = tot[0];
-            sc.stop = it >= maxit || sc.rr <= sc.tol2 || !(sc.rr == sc.rr);
-            sc.beta = cg_div<T>(sc.rr, rr_prev);
-          } else {
-            sc.alpha_prev = sc.res;  // prev
-            sc.res = sqrt(tot[0]);
-            sc.stop = it >= maxit || sc.res <= sc.tol || !(sc.res == sc.res);
-            sc.beta = (sc.res * sc.res) / (sc.alpha_prev * sc.alpha_prev);
-          }
-          sc.beta_t = (T)sc.beta;
-        }))
+    if (!grid_sync<1>(bar, partials, epoch, ss, rr, [&](const typename CGReal<T>::type* tot) { cg_next<T>(sc, tot, it, maxit); }))
       return;
   }
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {
     st->cg_it = it;
     st->cg_total += it;
-    st->cg_res = std::is_same<T, float>::value ? sqrt(sc.rr) : sc.res;
+    st->cg_res = cg_final_res(sc);
     st->cg_prev = sc.alpha_prev;
     st->cg_tol = sc.tol;
   }
