@@ -310,6 +310,266 @@ __device__ __forceinline__ void prolong_store(const Dims& d, int levels, const u
   }
 }
 
+// ------------------------------------------------------------------------------------------------
+// The FP32 register-resident kernels (TILE = 16) keep the operator's coefficients on chip for the whole
+// launch and transform u and v together.
+//
+// CoefTile: the coefficients that the tile's stress stage reads (h cells and c points of the tile and
+// its one-cell halo, h_m at the u and v points around them), staged once per launch in shared memory;
+// PointCoef: the thread's own point (β, h_m and the inner / coarse-space flags) in registers.  Per CG
+// iteration the operator then reads only the prolonged vector from L2.
+// ------------------------------------------------------------------------------------------------
+template <typename T, int TILE>
+struct CoefTile {
+  T he2[TILE + 1][TILE + 1];  // 2 hη at h cell (i0 - 1 + a, j0 - 1 + b); 0 off the grid
+  T dm[TILE + 1][TILE + 1];   // dimp at the h cells
+  T hc[TILE + 1][TILE + 1];   // hη_c at c point (i0 - 1 + a, j0 - 1 + b)
+  T hmu[TILE + 1][TILE + 2];  // h_m at u point (i0 - 1 + a, j0 - 1 + b)
+  T hmv[TILE + 2][TILE + 1];  // h_m at v point (i0 - 1 + a, j0 - 1 + b)
+};
+template <typename T>
+struct PointCoef {
+  T beta_u, beta_v, hm_u, hm_v;
+  bool inu, inv, inner_u, inner_v, wm_u, wm_v;  // on the grid; interior; in the coarse space
+};
+
+template <typename T, int TILE>
+__device__ __forceinline__ void load_coef_tile(const Dims& d, const OpCoef<T>& cf, const uint8_t* __restrict__ wmask,
+                                               int i0, int j0, CoefTile<T, TILE>& ct, PointCoef<T>& pc) {
+  for (int p = flat_tid(); p < (TILE + 1) * (TILE + 1); p += flat_nthreads()) {
+    const int la = p % (TILE + 1), lb = p / (TILE + 1), a = i0 - 1 + la, b = j0 - 1 + lb;
+    const bool hin = a >= 0 && a < d.nx && b >= 0 && b < d.ny;
+    ct.he2[lb][la] = hin ? (T)2 * cf.heta_h[hidx(d, a, b)] : (T)0;
+    ct.dm[lb][la] = hin ? cf.dimp[hidx(d, a, b)] : (T)0;
+    ct.hc[lb][la] = (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) ? cf.heta_c[cidx(d, a, b)] : (T)0;
+  }
+  for (int p = flat_tid(); p < (TILE + 1) * (TILE + 2); p += flat_nthreads()) {
+    const int la = p % (TILE + 2), lb = p / (TILE + 2), a = i0 - 1 + la, b = j0 - 1 + lb;
+    ct.hmu[lb][la] = (a >= 0 && a <= d.nx && b >= 0 && b < d.ny) ? cf.h_m[uidx(d, a, b)] : (T)0;
+  }
+  for (int p = flat_tid(); p < (TILE + 2) * (TILE + 1); p += flat_nthreads()) {
+    const int la = p % (TILE + 1), lb = p / (TILE + 1), a = i0 - 1 + la, b = j0 - 1 + lb;
+    ct.hmv[lb][la] = (a >= 0 && a < d.nx && b >= 0 && b <= d.ny) ? cf.h_m[vidx(d, a, b)] : (T)0;
+  }
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  pc.inu = i <= d.nx && j < d.ny;
+  pc.inv = i < d.nx && j <= d.ny;
+  const int qu = pc.inu ? uidx(d, i, j) : 0, qv = pc.inv ? vidx(d, i, j) : 0;
+  pc.beta_u = pc.inu ? cf.beta_m[qu] : (T)0;
+  pc.hm_u = pc.inu ? cf.h_m[qu] : (T)0;
+  pc.inner_u = pc.inu && cf.inner[qu];
+  pc.wm_u = pc.inu && wmask[qu];
+  pc.beta_v = pc.inv ? cf.beta_m[qv] : (T)0;
+  pc.hm_v = pc.inv ? cf.h_m[qv] : (T)0;
+  pc.inner_v = pc.inv && cf.inner[qv];
+  pc.wm_v = pc.inv && wmask[qv];
+}
+
+// stage_stress with the coefficients from the CoefTile (the same operations).
+template <typename T, int TX, int TY, int TILE>
+__device__ __forceinline__ void stage_stress_ct(const Dims& d, const CoefTile<T, TILE>& ct, int i0, int j0,
+                                                OpTile<T, TX, TY>& s) {
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
+  for (int p = flat_tid(); p < (TX + 1) * (TY + 1); p += flat_nthreads()) {
+    const int la = p % (TX + 1), lb = p / (TX + 1);
+    const int a = i0 - 1 + la, b = j0 - 1 + lb;
+    T rxx = 0, ryy = 0, e = 0, rxy = 0;
+    if (a >= 0 && a < d.nx && b >= 0 && b < d.ny) {
+      const T u0 = s.xu[lb][la], u1 = s.xu[lb][la + 1], v0 = s.xv[lb][la], v1 = s.xv[lb + 1][la];
+      const T ux = (u1 - u0) * rdx, vy = (v1 - v0) * rdy;
+      const T he2 = ct.he2[lb][la];
+      rxx = he2 * ((T)2 * ux + vy);
+      ryy = he2 * ((T)2 * vy + ux);
+      const T dm = ct.dm[lb][la];
+      if (dm != (T)0) {
+        const T divq = (ct.hmu[lb][la + 1] * u1 - ct.hmu[lb][la] * u0) * rdx +
+                       (ct.hmv[lb + 1][la] * v1 - ct.hmv[lb][la] * v0) * rdy;
+        e = dm * divq;
+      }
+    }
+    if (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) {
+      const T hc = ct.hc[lb][la];
+      if (hc != (T)0) {
+        const T uy = (s.xu[lb + 1][la + 1] - s.xu[lb][la + 1]) * rdy;
+        const T vx = (s.xv[lb + 1][la + 1] - s.xv[lb + 1][la]) * rdx;
+        rxy = hc * (uy + vx);
+      }
+    }
+    s.rxx[lb][la] = rxx;
+    s.ryy[lb][la] = ryy;
+    s.e[lb][la] = e;
+    s.rxy[lb][la] = rxy;
+  }
+}
+
+// P on a TILE x TILE tile, u and v together: the idwt lifting (haar_tile KIND 0) along y, then along x,
+// written as a gather.  The output at in-block position j is the block's scaling coefficient plus, per
+// level l (half = B >> (l + 1)), minus or plus the detail coefficient at (j rounded down to 2 half) + half:
+// plus when j lies in the upper half of its pair.  These are the lifting's additions in the same order,
+// so the result is the lifting's; positions off the grid hold zeros, which stands for the steps the
+// lifting skips at a ragged edge.  Along y the terms come from shared memory, along x by shuffles within
+// the row's lanes.  One __syncthreads (after the shared-memory writes; a leading one protects the buffers).
+template <int TILE, typename TT>
+__device__ __forceinline__ void idwt2d_pair(TT& u, TT& v, TT (*su)[TILE + 1], TT (*sv)[TILE + 1], int levels) {
+  constexpr int MAXL = TILE == 16 ? 4 : 5;  // levels + 1 <= log2(TILE)
+  const int tx = threadIdx.x, ty = threadIdx.y, B = 1 << (levels + 1);
+  __syncthreads();
+  su[ty][tx] = u;
+  sv[ty][tx] = v;
+  __syncthreads();
+  TT au = su[ty & ~(B - 1)][tx], av = sv[ty & ~(B - 1)][tx];
+#pragma unroll
+  for (int l = 0; l < MAXL; ++l)
+    if (l <= levels) {
+      const int half = B >> (l + 1), q = (ty & ~(2 * half - 1)) + half;
+      const TT pu = su[q][tx], pv = sv[q][tx];
+      if (ty & half) {
+        au = pu + au;
+        av = pv + av;
+      } else {
+        au = au - pu;
+        av = av - pv;
+      }
+    }
+  const int row0 = ((tx + TILE * ty) & 31) - tx;  // lane of the row's element 0
+  TT bu = __shfl_sync(0xffffffffu, au, row0 + (tx & ~(B - 1)));
+  TT bv = __shfl_sync(0xffffffffu, av, row0 + (tx & ~(B - 1)));
+#pragma unroll
+  for (int l = 0; l < MAXL; ++l) {
+    const int half = B >> (l + 1), q = (tx & ~(2 * half - 1)) + half;
+    const TT pu = __shfl_sync(0xffffffffu, au, row0 + q), pv = __shfl_sync(0xffffffffu, av, row0 + q);
+    if (l <= levels) {
+      if (tx & half) {
+        bu = pu + bu;
+        bv = pv + bv;
+      } else {
+        bu = bu - pu;
+        bv = bv - pv;
+      }
+    }
+  }
+  u = bu;
+  v = bv;
+}
+
+// Sum of m (a power of two <= MAXM) consecutive entries of column col from row r0, as a pairwise tree
+// (the order in which the idwtᵀ lifting accumulates them); absent entries are zeros.
+template <int MAXM, int TILE, typename TT>
+__device__ __forceinline__ TT column_tree_sum(const TT (*s)[TILE + 1], int r0, int m, int col) {
+  TT a[MAXM];
+#pragma unroll
+  for (int k = 0; k < MAXM; ++k) a[k] = k < m ? s[r0 + k][col] : (TT)0;
+#pragma unroll
+  for (int w = 1; w < MAXM; w <<= 1)
+#pragma unroll
+    for (int k = 0; k < MAXM; k += 2 * w) a[k] = a[k] + a[k + w];
+  return a[0];
+}
+
+// Pᵀ (= R) on a TILE x TILE tile, u and v together: the idwtᵀ lifting (haar_tile KIND 1) along y, then
+// along x.  Along y each output is a difference of two tree sums of its column (upper half minus lower
+// half of its pair at its own level; the scaling coefficient is the sum of both halves of the block),
+// read from shared memory; along x the lifting runs on the row's lanes with shuffles.  Inputs off the
+// grid must be zero (they stand for the partners the lifting skips at a ragged edge).
+template <int TILE, typename TT>
+__device__ __forceinline__ void idwt2dT_pair(TT& u, TT& v, TT (*su)[TILE + 1], TT (*sv)[TILE + 1], int levels) {
+  constexpr int MAXL = TILE == 16 ? 4 : 5;
+  const int tx = threadIdx.x, ty = threadIdx.y, B = 1 << (levels + 1);
+  __syncthreads();
+  su[ty][tx] = u;
+  sv[ty][tx] = v;
+  __syncthreads();
+  const int jj = ty & (B - 1);
+  const int m = jj == 0 ? (B >> 1) : (jj & -jj);
+  const int r0 = jj == 0 ? ty : ty - m;
+  const TT fu = column_tree_sum<TILE / 2, TILE>(su, r0, m, tx), gu = column_tree_sum<TILE / 2, TILE>(su, r0 + m, m, tx);
+  const TT fv = column_tree_sum<TILE / 2, TILE>(sv, r0, m, tx), gv = column_tree_sum<TILE / 2, TILE>(sv, r0 + m, m, tx);
+  TT bu = jj == 0 ? fu + gu : gu - fu, bv = jj == 0 ? fv + gv : gv - fv;
+#pragma unroll
+  for (int l = 0; l < MAXL; ++l)
+    if (l <= levels) {
+      const int half = 1 << l;
+      const TT pu = __shfl_xor_sync(0xffffffffu, bu, half), pv = __shfl_xor_sync(0xffffffffu, bv, half);
+      const int r = tx & (2 * half - 1);
+      if (r == 0) {
+        bu = bu + pu;
+        bv = bv + pv;
+      } else if (r == half) {
+        bu = bu - pu;
+        bv = bv - pv;
+      }
+    }
+  u = bu;
+  v = bv;
+}
+
+// Shared memory of the FP32 fast path: the coefficient tiles and the second Haar buffer.
+template <typename T, int TILE, int MAXT>
+struct FastShared {
+  CoefTile<T, TILE> ct[MAXT];
+  T hs2[TILE][TILE + 1];
+};
+
+// coarse_apply with on-chip coefficients and the paired Haar transform.
+template <typename T, int TILE>
+__device__ __forceinline__ void coarse_apply_fast(const Dims& d, int levels, const CoefTile<T, TILE>& ct,
+                                                  const PointCoef<T>& pc, const T* __restrict__ w, int i0, int j0,
+                                                  CGShared<T, TILE>& sm, T (*hs2)[TILE + 1], T& cu, T& cv) {
+  __syncthreads();  // the previous use of the tile's shared memory is over
+  stage_x(d, i0, j0, sm.op, [&](int q) { return __ldcg(w + q); });
+  __syncthreads();
+  stage_stress_ct(d, ct, i0, j0, sm.op);
+  __syncthreads();
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
+  const OpTile<T, TILE, TILE>& s = sm.op;
+  const int li = tx + 1, lj = ty + 1;
+  T yu = 0, yv = 0;
+  if (pc.inner_u)
+    yu = (s.rxx[lj][li] - s.rxx[lj][li - 1]) * rdx + (s.rxy[lj][li - 1] - s.rxy[lj - 1][li - 1]) * rdy -
+         pc.beta_u * s.xu[lj][li] - pc.hm_u * ((s.e[lj][li] - s.e[lj][li - 1]) * rdx);
+  if (pc.inner_v)
+    yv = (s.ryy[lj][li] - s.ryy[lj - 1][li]) * rdy + (s.rxy[lj - 1][li] - s.rxy[lj - 1][li - 1]) * rdx -
+         pc.beta_v * s.xv[lj][li] - pc.hm_v * ((s.e[lj][li] - s.e[lj - 1][li]) * rdy);
+  idwt2dT_pair<TILE>(yu, yv, sm.hs, hs2, levels);
+  cu = pc.wm_u ? yu : (T)0;
+  cv = pc.wm_v ? yv : (T)0;
+}
+
+// prolong_store with the paired Haar transform and the flags from registers.
+template <typename T, int TILE>
+__device__ __forceinline__ void prolong_store_fast(const Dims& d, int levels, const PointCoef<T>& pc, T uu, T uv,
+                                                   int i0, int j0, CGShared<T, TILE>& sm, T (*hs2)[TILE + 1],
+                                                   T* __restrict__ w) {
+  T pu = pc.inu ? uu : (T)0, pv = pc.inv ? uv : (T)0;
+  idwt2d_pair<TILE>(pu, pv, sm.hs, hs2, levels);
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  if (pc.inu) __stcg(w + uidx(d, i, j), pc.inner_u ? pu : (T)0);
+  if (pc.inv) __stcg(w + vidx(d, i, j), pc.inner_v ? pv : (T)0);
+}
+
+// The register-resident kernels call these: the fast path for FP32 tiles of 16 (FS = FastShared), the
+// general one otherwise (FS = char).
+template <typename T, int TILE, typename FS>
+__device__ __forceinline__ void tile_apply(const Dims& d, int levels, const OpCoef<T>& cf, const uint8_t* __restrict__ wmask,
+                                           const T* __restrict__ w, int i0, int j0, CGShared<T, TILE>& sm, FS& fs, int k,
+                                           const PointCoef<T>& pc, T& cu, T& cv) {
+  if constexpr (std::is_same<FS, char>::value)
+    coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0, j0, sm, cu, cv);
+  else
+    coarse_apply_fast<T, TILE>(d, levels, fs.ct[k], pc, w, i0, j0, sm, fs.hs2, cu, cv);
+}
+template <typename T, int TILE, typename FS>
+__device__ __forceinline__ void tile_prolong(const Dims& d, int levels, const OpCoef<T>& cf, T uu, T uv, int i0, int j0,
+                                             CGShared<T, TILE>& sm, FS& fs, const PointCoef<T>& pc, T* __restrict__ w) {
+  if constexpr (std::is_same<FS, char>::value)
+    prolong_store<T, TILE>(d, levels, cf.inner, uu, uv, i0, j0, sm, w);
+  else
+    prolong_store_fast<T, TILE>(d, levels, pc, uu, uv, i0, j0, sm, fs.hs2, w);
+}
+template <typename T, int TILE, int MAXT>
+using FastSharedFor = typename std::conditional<std::is_same<T, float>::value && TILE == 16, FastShared<T, TILE, MAXT>, char>::type;
+
 // CG scalars broadcast to the CTA (written by thread 0 inside grid_sync).  R = CGReal<T>: the FP64
 // kernels keep the reference's FP64 scalars; the FP32 kernels keep squared norms and the recurrence
 // scalars in float-float (no FP64 arithmetic per iteration; res and tol are FP64, set once per solve).
@@ -437,6 +697,8 @@ __global__ void __launch_bounds__(TILE* TILE)
   __shared__ CGShared<T, TILE> sm;
   __shared__ SyncShared ss;
   __shared__ CGScalars<T> sc;
+  __shared__ FastSharedFor<T, TILE, MAXT> fs;
+  PointCoef<T> pc[MAXT] = {};
   const int ntiles = ntx * nty;
   const int tx = threadIdx.x, ty = threadIdx.y;
   T xu[MAXT], xv[MAXT], ru[MAXT], rv[MAXT], uu[MAXT], uv[MAXT], cu[MAXT], cv[MAXT];
@@ -453,6 +715,11 @@ __global__ void __launch_bounds__(TILE* TILE)
     xv[k] = (own[k] && i < d.nx && j <= d.ny) ? xc[vidx(d, i, j)] : (T)0;
     uu[k] = uv[k] = cu[k] = cv[k] = ru[k] = rv[k] = (T)0;
   }
+  if constexpr (!std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value) {
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) load_coef_tile<T, TILE>(d, cf, wmask, i0s[k], j0s[k], fs.ct[k], pc[k]);
+  }  // (the tiles are first read after a __syncthreads)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
@@ -460,7 +727,7 @@ __global__ void __launch_bounds__(TILE* TILE)
   // start: w = P xc
 #pragma unroll
   for (int k = 0; k < MAXT; ++k)
-    if (own[k]) prolong_store<T, TILE>(d, levels, cf.inner, xu[k], xv[k], i0s[k], j0s[k], sm, w);
+    if (own[k]) tile_prolong<T, TILE>(d, levels, cf, xu[k], xv[k], i0s[k], j0s[k], sm, fs, pc[k], w);
   if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
   // r = b_c - R A P xc, u = 0;  |r|^2 and |b_c|^2
   {
@@ -468,7 +735,7 @@ __global__ void __launch_bounds__(TILE* TILE)
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
-        coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, cu[k], cv[k]);
+        tile_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, fs, k, pc[k], cu[k], cv[k]);
         const int i = i0s[k] + tx, j = j0s[k] + ty;
         const T bu = (i <= d.nx && j < d.ny) ? bc[uidx(d, i, j)] : (T)0;
         const T bv = (i < d.nx && j <= d.ny) ? bc[vidx(d, i, j)] : (T)0;
@@ -487,14 +754,14 @@ __global__ void __launch_bounds__(TILE* TILE)
       if (own[k]) {
         uu[k] = fmul_add(beta, uu[k], ru[k]);
         uv[k] = fmul_add(beta, uv[k], rv[k]);
-        prolong_store<T, TILE>(d, levels, cf.inner, uu[k], uv[k], i0s[k], j0s[k], sm, w);
+        tile_prolong<T, TILE>(d, levels, cf, uu[k], uv[k], i0s[k], j0s[k], sm, fs, pc[k], w);
       }
     if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
     T dot[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
-        coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, cu[k], cv[k]);
+        tile_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, fs, k, pc[k], cu[k], cv[k]);
         dot[0] += uu[k] * cu[k] + uv[k] * cv[k];
       }
     if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const typename CGReal<T>::type* tot) { cg_alpha<T>(sc, tot); }))
@@ -549,6 +816,8 @@ __global__ void __launch_bounds__(TILE* TILE)
   __shared__ CGShared<T, TILE> sm;
   __shared__ SyncShared ss;
   __shared__ CGScalars<T> sc;
+  __shared__ FastSharedFor<T, TILE, MAXT> fs;
+  PointCoef<T> pc[MAXT] = {};
   const int ntiles = ntx * nty;
   const int tx = threadIdx.x, ty = threadIdx.y;
   T xu[MAXT], xv[MAXT], ru[MAXT], rv[MAXT], zu[MAXT], zv[MAXT], wu[MAXT], wv[MAXT];
@@ -574,6 +843,11 @@ __global__ void __launch_bounds__(TILE* TILE)
     }
     ru[k] = rv[k] = zu[k] = zv[k] = wu[k] = wv[k] = pu[k] = pv[k] = su[k] = sv[k] = (T)0;
   }
+  if constexpr (!std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value) {
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) load_coef_tile<T, TILE>(d, cf, wmask, i0s[k], j0s[k], fs.ct[k], pc[k]);
+  }  // (the tiles are first read after a __syncthreads)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
@@ -581,14 +855,14 @@ __global__ void __launch_bounds__(TILE* TILE)
   // r = b_c - R A P xc;  z = M⁻¹ r
 #pragma unroll
   for (int k = 0; k < MAXT; ++k)
-    if (own[k]) prolong_store<T, TILE>(d, levels, cf.inner, xu[k], xv[k], i0s[k], j0s[k], sm, w);
+    if (own[k]) tile_prolong<T, TILE>(d, levels, cf, xu[k], xv[k], i0s[k], j0s[k], sm, fs, pc[k], w);
   if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
   T bb = 0;
 #pragma unroll
   for (int k = 0; k < MAXT; ++k)
     if (own[k]) {
       T cu, cv;
-      coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, cu, cv);
+      tile_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, fs, k, pc[k], cu, cv);
       const int i = i0s[k] + tx, j = j0s[k] + ty;
       const T bu = (i <= d.nx && j < d.ny) ? bc[uidx(d, i, j)] : (T)0;
       const T bv = (i < d.nx && j <= d.ny) ? bc[vidx(d, i, j)] : (T)0;
@@ -619,13 +893,13 @@ __global__ void __launch_bounds__(TILE* TILE)
     // w = R A P z
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
-      if (own[k]) prolong_store<T, TILE>(d, levels, cf.inner, zu[k], zv[k], i0s[k], j0s[k], sm, w);
+      if (own[k]) tile_prolong<T, TILE>(d, levels, cf, zu[k], zv[k], i0s[k], j0s[k], sm, fs, pc[k], w);
     if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
     T a[4] = {T(0), T(0), T(0), first ? bb : T(0)};
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
-        coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, wu[k], wv[k]);
+        tile_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, fs, k, pc[k], wu[k], wv[k]);
         a[0] += ru[k] * zu[k] + rv[k] * zv[k];
         a[1] += wu[k] * zu[k] + wv[k] * zv[k];
         a[2] += ru[k] * ru[k] + rv[k] * rv[k];
