@@ -34,7 +34,7 @@ namespace wavi {
 
 struct GridBar {
   unsigned count;  // arrivals since the launch began (monotonic; epoch e is complete at e * gridDim.x)
-  unsigned gen;
+  unsigned gen;    // launch generation: the tags of the FP32 kernels' tagged words (advanced before each launch)
   int err;
   int pad;
   double sum[4];
@@ -50,6 +50,24 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 __device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
 }
+
+// Tagged words of the FP32 register-resident kernels: a 32-bit value and the 32-bit tag of the exchange
+// that wrote it, in one naturally aligned 64-bit word (single-copy atomic), so a reader that sees the
+// expected tag sees that exchange's value.  Writers store relaxed and need no fence: a word is rewritten
+// only after its readers have consumed it (the kernel's reductions order that).
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" : : "l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long tagged(unsigned tag, float x) {
+  return ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(x);
+}
+__device__ __forceinline__ unsigned tag_of(unsigned long long w) { return (unsigned)(w >> 32); }
+__device__ __forceinline__ float value_of(unsigned long long w) { return __uint_as_float((unsigned)w); }
 
 // ------------------------------------------------------------------------------------------------
 // Float-float arithmetic for the FP32 kernels' reductions and CG scalars.  GB300 executes FP64 at a
@@ -503,24 +521,118 @@ __device__ __forceinline__ void idwt2dT_pair(TT& u, TT& v, TT (*su)[TILE + 1], T
   v = bv;
 }
 
-// Shared memory of the FP32 fast path: the coefficient tiles and the second Haar buffer.
-template <typename T, int TILE, int MAXT>
-struct FastShared {
-  CoefTile<T, TILE> ct[MAXT];
-  T hs2[TILE][TILE + 1];
+// Tagged halo exchange of the FP32 register-resident kernels.  The prolonged vector of a tile never
+// leaves the chip except its boundary: each tile publishes its first/last column and row (u and v) as
+// tagged words in its halo box, and a tile's operator reads its one-point halo ring from the neighbours'
+// boxes, waiting (bounded) for the current exchange's tag.  No grid barrier and no fence separate the
+// prolongation from the operator, and a CTA waits only for its neighbours.  Ordering: a tile rewrites its
+// box only after the next grid reduction, which needs every CTA's partial, computed from the halo values
+// it read.  Tags are (gen << 21) + exchange, gen advanced by k_reset_barrier before each launch past the
+// previous launch's range, so no word left by an earlier launch carries a current tag.  (Tagged words
+// for the reductions as well, every CTA polling every CTA's partial, were measured slower than the
+// counter barrier: the polls crowd the few L2 lines that the partials occupy.)
+struct TagState {
+  unsigned long long* halo;  // [tile][u, v][west column, east column, south row, north row][TILE]
+  unsigned base;             // gen << 21
+  unsigned hx;               // exchanges so far in this launch
 };
 
-// coarse_apply with on-chip coefficients and the paired Haar transform.
+// Bounded wait for a tagged word.  On a timeout (or another CTA's error) sets fail and bar->err.
+__device__ __forceinline__ unsigned long long wait_tagged(const unsigned long long* p, unsigned tag, GridBar* bar,
+                                                          volatile int* fail) {
+  unsigned long long w = ld_relaxed_u64(p);
+  long polls = 0;
+  while (tag_of(w) != tag) {
+    if (++polls > kBarrierSpinLimit || ((polls & 255) == 0 && *(volatile int*)&bar->err)) {
+      *fail = 1;
+      atomicExch(&bar->err, 1);
+      break;
+    }
+    if (polls > 8) __nanosleep(32);
+    w = ld_relaxed_u64(p);
+  }
+  return w;
+}
+
+// P on the tile (paired Haar transform); the prolonged values stay in the thread's registers (hu, hv:
+// inner ⊙ P u, zero off the grid) and the tile's boundary is published for exchange ts.hx.
 template <typename T, int TILE>
-__device__ __forceinline__ void coarse_apply_fast(const Dims& d, int levels, const CoefTile<T, TILE>& ct,
-                                                  const PointCoef<T>& pc, const T* __restrict__ w, int i0, int j0,
-                                                  CGShared<T, TILE>& sm, T (*hs2)[TILE + 1], T& cu, T& cv) {
+__device__ __forceinline__ void prolong_publish(int levels, const PointCoef<T>& pc, T uu, T uv, int tile,
+                                                CGShared<T, TILE>& sm, T (*hs2)[TILE + 1], const TagState& ts, T& hu,
+                                                T& hv) {
+  T pu = pc.inu ? uu : (T)0, pv = pc.inv ? uv : (T)0;
+  idwt2d_pair<TILE>(pu, pv, sm.hs, hs2, levels);
+  hu = pc.inner_u ? pu : (T)0;
+  hv = pc.inner_v ? pv : (T)0;
+  const unsigned tag = ts.base + ts.hx;
+  unsigned long long* box = ts.halo + (size_t)tile * (8 * TILE);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  if (tx == 0) {
+    st_relaxed_u64(box + 0 * TILE + ty, tagged(tag, hu));
+    st_relaxed_u64(box + 4 * TILE + ty, tagged(tag, hv));
+  }
+  if (tx == TILE - 1) {
+    st_relaxed_u64(box + 1 * TILE + ty, tagged(tag, hu));
+    st_relaxed_u64(box + 5 * TILE + ty, tagged(tag, hv));
+  }
+  if (ty == 0) {
+    st_relaxed_u64(box + 2 * TILE + tx, tagged(tag, hu));
+    st_relaxed_u64(box + 6 * TILE + tx, tagged(tag, hv));
+  }
+  if (ty == TILE - 1) {
+    st_relaxed_u64(box + 3 * TILE + tx, tagged(tag, hu));
+    st_relaxed_u64(box + 7 * TILE + tx, tagged(tag, hv));
+  }
+}
+
+// coarse_apply of the fast path: the tile's interior from registers (hu, hv), its halo ring from the
+// neighbours' boxes (exchange ts.hx), the coefficients from the CoefTile, the paired Pᵀ.  Returns false
+// (in every thread) if a wait gave up.
+template <typename T, int TILE>
+__device__ __forceinline__ bool apply_tagged(const Dims& d, int levels, const CoefTile<T, TILE>& ct, const PointCoef<T>& pc,
+                                             T hu, T hv, int i0, int j0, int ntx, CGShared<T, TILE>& sm,
+                                             T (*hs2)[TILE + 1], const TagState& ts, GridBar* bar, volatile int* fail,
+                                             T& cu, T& cv) {
+  constexpr int RING = 4 * TILE + 4;
   __syncthreads();  // the previous use of the tile's shared memory is over
-  stage_x(d, i0, j0, sm.op, [&](int q) { return __ldcg(w + q); });
+  const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TILE * ty;
+  sm.op.xu[ty + 1][tx + 1] = hu;
+  sm.op.xv[ty + 1][tx + 1] = hv;
+  if (t < 2 * RING) {
+    // ring position p: the row below (lj = 0), the row above (lj = TILE + 1), then the two columns
+    const int c = t >= RING, p = t - c * RING;
+    int li, lj;
+    if (p < TILE + 2) {
+      li = p;
+      lj = 0;
+    } else if (p < 2 * (TILE + 2)) {
+      li = p - (TILE + 2);
+      lj = TILE + 1;
+    } else {
+      const int q = p - 2 * (TILE + 2);
+      li = (q & 1) ? TILE + 1 : 0;
+      lj = 1 + (q >> 1);
+    }
+    const int i = i0 - 1 + li, j = j0 - 1 + lj;
+    const bool on = c == 0 ? (i >= 0 && i <= d.nx && j >= 0 && j < d.ny) : (i >= 0 && i < d.nx && j >= 0 && j <= d.ny);
+    T val = 0;
+    if (on) {
+      // the owning tile and the edge of its box that holds (i, j)
+      const int ti = i / TILE, tj = j / TILE;
+      const int e = li == 0 ? 1 : li == TILE + 1 ? 0 : lj == 0 ? 3 : 2;
+      const int k = (li == 0 || li == TILE + 1) ? j - tj * TILE : i - ti * TILE;
+      const unsigned long long* src = ts.halo + (size_t)(tj * ntx + ti) * (8 * TILE) + (c * 4 + e) * TILE + k;
+      val = value_of(wait_tagged(src, ts.base + ts.hx, bar, fail));
+    }
+    if (c == 0)
+      sm.op.xu[lj][li] = val;
+    else
+      sm.op.xv[lj][li] = val;
+  }
   __syncthreads();
+  if (*fail) return false;
   stage_stress_ct(d, ct, i0, j0, sm.op);
   __syncthreads();
-  const int tx = threadIdx.x, ty = threadIdx.y;
   const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
   const OpTile<T, TILE, TILE>& s = sm.op;
   const int li = tx + 1, lj = ty + 1;
@@ -534,39 +646,16 @@ __device__ __forceinline__ void coarse_apply_fast(const Dims& d, int levels, con
   idwt2dT_pair<TILE>(yu, yv, sm.hs, hs2, levels);
   cu = pc.wm_u ? yu : (T)0;
   cv = pc.wm_v ? yv : (T)0;
+  return true;
 }
 
-// prolong_store with the paired Haar transform and the flags from registers.
-template <typename T, int TILE>
-__device__ __forceinline__ void prolong_store_fast(const Dims& d, int levels, const PointCoef<T>& pc, T uu, T uv,
-                                                   int i0, int j0, CGShared<T, TILE>& sm, T (*hs2)[TILE + 1],
-                                                   T* __restrict__ w) {
-  T pu = pc.inu ? uu : (T)0, pv = pc.inv ? uv : (T)0;
-  idwt2d_pair<TILE>(pu, pv, sm.hs, hs2, levels);
-  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-  if (pc.inu) __stcg(w + uidx(d, i, j), pc.inner_u ? pu : (T)0);
-  if (pc.inv) __stcg(w + vidx(d, i, j), pc.inner_v ? pv : (T)0);
-}
-
-// The register-resident kernels call these: the fast path for FP32 tiles of 16 (FS = FastShared), the
-// general one otherwise (FS = char).
-template <typename T, int TILE, typename FS>
-__device__ __forceinline__ void tile_apply(const Dims& d, int levels, const OpCoef<T>& cf, const uint8_t* __restrict__ wmask,
-                                           const T* __restrict__ w, int i0, int j0, CGShared<T, TILE>& sm, FS& fs, int k,
-                                           const PointCoef<T>& pc, T& cu, T& cv) {
-  if constexpr (std::is_same<FS, char>::value)
-    coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0, j0, sm, cu, cv);
-  else
-    coarse_apply_fast<T, TILE>(d, levels, fs.ct[k], pc, w, i0, j0, sm, fs.hs2, cu, cv);
-}
-template <typename T, int TILE, typename FS>
-__device__ __forceinline__ void tile_prolong(const Dims& d, int levels, const OpCoef<T>& cf, T uu, T uv, int i0, int j0,
-                                             CGShared<T, TILE>& sm, FS& fs, const PointCoef<T>& pc, T* __restrict__ w) {
-  if constexpr (std::is_same<FS, char>::value)
-    prolong_store<T, TILE>(d, levels, cf.inner, uu, uv, i0, j0, sm, w);
-  else
-    prolong_store_fast<T, TILE>(d, levels, pc, uu, uv, i0, j0, sm, fs.hs2, w);
-}
+// Shared memory of the FP32 fast path: the coefficient tiles, the second Haar buffer, the failure flag.
+template <typename T, int TILE, int MAXT>
+struct FastShared {
+  CoefTile<T, TILE> ct[MAXT];
+  T hs2[TILE][TILE + 1];
+  int fail;
+};
 template <typename T, int TILE, int MAXT>
 using FastSharedFor = typename std::conditional<std::is_same<T, float>::value && TILE == 16, FastShared<T, TILE, MAXT>, char>::type;
 
@@ -690,10 +779,11 @@ __device__ __forceinline__ double cg_final_res(const CGScalars<T>& sc) {
 // right-hand side bc (both global, full layout) to the final xc.  Writes the CG statistics into st (CTA 0).
 // Stopping rule of cg!: |r| <= max(sqrt(eps) |r0|, abstol) with abstol = tol_coarse |b_c|, or maxiter.
 template <typename T, int TILE, int MAXT>
-__global__ void __launch_bounds__(TILE* TILE)
+__global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
     k_cg_persistent(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, T* __restrict__ w,
                     const T* __restrict__ bc, T* __restrict__ xc, double* __restrict__ partials, DevState* st,
-                    const DevParams* __restrict__ P, GridBar* bar, int ntx, int nty) {
+                    const DevParams* __restrict__ P, GridBar* bar, unsigned long long* __restrict__ halo, int ntx,
+                    int nty) {
   __shared__ CGShared<T, TILE> sm;
   __shared__ SyncShared ss;
   __shared__ CGScalars<T> sc;
@@ -715,27 +805,60 @@ __global__ void __launch_bounds__(TILE* TILE)
     xv[k] = (own[k] && i < d.nx && j <= d.ny) ? xc[vidx(d, i, j)] : (T)0;
     uu[k] = uv[k] = cu[k] = cv[k] = ru[k] = rv[k] = (T)0;
   }
-  if constexpr (!std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value) {
-#pragma unroll
-    for (int k = 0; k < MAXT; ++k)
-      if (own[k]) load_coef_tile<T, TILE>(d, cf, wmask, i0s[k], j0s[k], fs.ct[k], pc[k]);
-  }  // (the tiles are first read after a __syncthreads)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
   const double tol_coarse = P->tol_coarse;
+  constexpr bool kFast = !std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value;
+  T hu[MAXT], hv[MAXT];  // fast path: the tiles' prolonged vectors (inner ⊙ P u)
+  TagState ts{halo, 0u, 0u};
+  volatile int* fail = nullptr;
+  if constexpr (kFast) {
+    ts.base = *(volatile unsigned*)&bar->gen << 21;
+    fail = &fs.fail;
+    if (tx == 0 && ty == 0) fs.fail = 0;
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) load_coef_tile<T, TILE>(d, cf, wmask, i0s[k], j0s[k], fs.ct[k], pc[k]);
+  }  // (all of it is read after a __syncthreads)
+  // w = inner ⊙ P (a, b) for tile k: published (fast path) or stored to w
+  auto prolong = [&](int k, T a, T b) {
+    if constexpr (kFast)
+      prolong_publish<T, TILE>(levels, pc[k], a, b, blockIdx.x + k * gridDim.x, sm, fs.hs2, ts, hu[k], hv[k]);
+    else
+      prolong_store<T, TILE>(d, levels, cf.inner, a, b, i0s[k], j0s[k], sm, w);
+  };
+  // between the prolongation and the operator: a grid barrier, except on the fast path, whose operator
+  // waits for its halo ring
+  auto halo_ready = [&]() -> bool {
+    if constexpr (kFast)
+      return true;
+    else
+      return grid_barrier<T>(bar, partials, epoch, ss);
+  };
+  // (c1, c2) = wmask ⊙ R A w on tile k
+  auto apply = [&](int k, T& c1, T& c2) -> bool {
+    if constexpr (kFast) {
+      return apply_tagged<T, TILE>(d, levels, fs.ct[k], pc[k], hu[k], hv[k], i0s[k], j0s[k], ntx, sm, fs.hs2, ts, bar,
+                                   fail, c1, c2);
+    } else {
+      coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, c1, c2);
+      return true;
+    }
+  };
   // start: w = P xc
+  ++ts.hx;  // a new exchange
 #pragma unroll
   for (int k = 0; k < MAXT; ++k)
-    if (own[k]) tile_prolong<T, TILE>(d, levels, cf, xu[k], xv[k], i0s[k], j0s[k], sm, fs, pc[k], w);
-  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+    if (own[k]) prolong(k, xu[k], xv[k]);
+  if (!halo_ready()) return;
   // r = b_c - R A P xc, u = 0;  |r|^2 and |b_c|^2
   {
     T a[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
-        tile_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, fs, k, pc[k], cu[k], cv[k]);
+        if (!apply(k, cu[k], cv[k])) return;
         const int i = i0s[k] + tx, j = j0s[k] + ty;
         const T bu = (i <= d.nx && j < d.ny) ? bc[uidx(d, i, j)] : (T)0;
         const T bv = (i < d.nx && j <= d.ny) ? bc[vidx(d, i, j)] : (T)0;
@@ -749,19 +872,20 @@ __global__ void __launch_bounds__(TILE* TILE)
   }
   while (!sc.stop) {
     const T beta = sc.beta_t;
+    ++ts.hx;  // a new exchange
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
         uu[k] = fmul_add(beta, uu[k], ru[k]);
         uv[k] = fmul_add(beta, uv[k], rv[k]);
-        tile_prolong<T, TILE>(d, levels, cf, uu[k], uv[k], i0s[k], j0s[k], sm, fs, pc[k], w);
+        prolong(k, uu[k], uv[k]);
       }
-    if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+    if (!halo_ready()) return;
     T dot[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
-        tile_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, fs, k, pc[k], cu[k], cv[k]);
+        if (!apply(k, cu[k], cv[k])) return;
         dot[0] += uu[k] * cu[k] + uv[k] * cv[k];
       }
     if (!grid_sync<1>(bar, partials, epoch, ss, dot, [&](const typename CGReal<T>::type* tot) { cg_alpha<T>(sc, tot); }))
@@ -809,10 +933,11 @@ __global__ void __launch_bounds__(TILE* TILE)
 // recursively updated residual drifts by ~1e-3 in FP32).  The oracle's coarse_srcg states the same
 // iteration in FP64.
 template <typename T, int TILE, int MAXT>
-__global__ void __launch_bounds__(TILE* TILE)
+__global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
     k_srcg_persistent(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, const T* __restrict__ dcoarse,
                       T* __restrict__ w, const T* __restrict__ bc, T* __restrict__ xc, double* __restrict__ partials,
-                      DevState* st, const DevParams* __restrict__ P, GridBar* bar, int ntx, int nty) {
+                      DevState* st, const DevParams* __restrict__ P, GridBar* bar, unsigned long long* __restrict__ halo, int ntx,
+                    int nty) {
   __shared__ CGShared<T, TILE> sm;
   __shared__ SyncShared ss;
   __shared__ CGScalars<T> sc;
@@ -843,26 +968,59 @@ __global__ void __launch_bounds__(TILE* TILE)
     }
     ru[k] = rv[k] = zu[k] = zv[k] = wu[k] = wv[k] = pu[k] = pv[k] = su[k] = sv[k] = (T)0;
   }
-  if constexpr (!std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value) {
-#pragma unroll
-    for (int k = 0; k < MAXT; ++k)
-      if (own[k]) load_coef_tile<T, TILE>(d, cf, wmask, i0s[k], j0s[k], fs.ct[k], pc[k]);
-  }  // (the tiles are first read after a __syncthreads)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
   const double tol_coarse = P->tol_coarse;
+  constexpr bool kFast = !std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value;
+  T hu[MAXT], hv[MAXT];  // fast path: the tiles' prolonged vectors (inner ⊙ P u)
+  TagState ts{halo, 0u, 0u};
+  volatile int* fail = nullptr;
+  if constexpr (kFast) {
+    ts.base = *(volatile unsigned*)&bar->gen << 21;
+    fail = &fs.fail;
+    if (tx == 0 && ty == 0) fs.fail = 0;
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) load_coef_tile<T, TILE>(d, cf, wmask, i0s[k], j0s[k], fs.ct[k], pc[k]);
+  }  // (all of it is read after a __syncthreads)
+  // w = inner ⊙ P (a, b) for tile k: published (fast path) or stored to w
+  auto prolong = [&](int k, T a, T b) {
+    if constexpr (kFast)
+      prolong_publish<T, TILE>(levels, pc[k], a, b, blockIdx.x + k * gridDim.x, sm, fs.hs2, ts, hu[k], hv[k]);
+    else
+      prolong_store<T, TILE>(d, levels, cf.inner, a, b, i0s[k], j0s[k], sm, w);
+  };
+  // between the prolongation and the operator: a grid barrier, except on the fast path, whose operator
+  // waits for its halo ring
+  auto halo_ready = [&]() -> bool {
+    if constexpr (kFast)
+      return true;
+    else
+      return grid_barrier<T>(bar, partials, epoch, ss);
+  };
+  // (c1, c2) = wmask ⊙ R A w on tile k
+  auto apply = [&](int k, T& c1, T& c2) -> bool {
+    if constexpr (kFast) {
+      return apply_tagged<T, TILE>(d, levels, fs.ct[k], pc[k], hu[k], hv[k], i0s[k], j0s[k], ntx, sm, fs.hs2, ts, bar,
+                                   fail, c1, c2);
+    } else {
+      coarse_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, c1, c2);
+      return true;
+    }
+  };
   // r = b_c - R A P xc;  z = M⁻¹ r
+  ++ts.hx;  // a new exchange
 #pragma unroll
   for (int k = 0; k < MAXT; ++k)
-    if (own[k]) tile_prolong<T, TILE>(d, levels, cf, xu[k], xv[k], i0s[k], j0s[k], sm, fs, pc[k], w);
-  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+    if (own[k]) prolong(k, xu[k], xv[k]);
+  if (!halo_ready()) return;
   T bb = 0;
 #pragma unroll
   for (int k = 0; k < MAXT; ++k)
     if (own[k]) {
       T cu, cv;
-      tile_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, fs, k, pc[k], cu, cv);
+      if (!apply(k, cu, cv)) return;
       const int i = i0s[k] + tx, j = j0s[k] + ty;
       const T bu = (i <= d.nx && j < d.ny) ? bc[uidx(d, i, j)] : (T)0;
       const T bv = (i < d.nx && j <= d.ny) ? bc[vidx(d, i, j)] : (T)0;
@@ -872,7 +1030,8 @@ __global__ void __launch_bounds__(TILE* TILE)
       zu[k] = iu[k] * ru[k];
       zv[k] = iv[k] * rv[k];
     }
-  // (every CTA has read w: the barrier below orders the rewrite)
+  // (every CTA has read the prolonged vector, from w or from the halo boxes: the barrier below orders the
+  // rewrite)
   if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
   bool first = true;
   for (;;) {
@@ -891,15 +1050,16 @@ __global__ void __launch_bounds__(TILE* TILE)
       ++it;
     }
     // w = R A P z
+    ++ts.hx;  // a new exchange
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
-      if (own[k]) tile_prolong<T, TILE>(d, levels, cf, zu[k], zv[k], i0s[k], j0s[k], sm, fs, pc[k], w);
-    if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+      if (own[k]) prolong(k, zu[k], zv[k]);
+    if (!halo_ready()) return;
     T a[4] = {T(0), T(0), T(0), first ? bb : T(0)};
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
-        tile_apply<T, TILE>(d, levels, cf, wmask, w, i0s[k], j0s[k], sm, fs, k, pc[k], wu[k], wv[k]);
+        if (!apply(k, wu[k], wv[k])) return;
         a[0] += ru[k] * zu[k] + rv[k] * zv[k];
         a[1] += wu[k] * zu[k] + wv[k] * zv[k];
         a[2] += ru[k] * ru[k] + rv[k] * rv[k];
@@ -1287,10 +1447,14 @@ __global__ void __launch_bounds__(TILE* TILE)
 }
 
 // Before a persistent CG: an idle barrier (count 0, no error).
-static __global__ void k_reset_barrier(GridBar* bar) {
+// Before each persistent launch: restart the arrival counter, clear the error, and advance the tag
+// generation past every tag the previous launch can have written (at most maxiter_coarse + 2 tagged
+// exchanges; 2^21 tags per generation step).
+static __global__ void k_reset_barrier(GridBar* bar, const DevParams* __restrict__ P) {
   if (threadIdx.x == 0) {
     bar->count = 0u;
     bar->err = 0;
+    bar->gen += 1u + ((unsigned)max(P->maxiter_coarse, 0) >> 20);
   }
 }
 

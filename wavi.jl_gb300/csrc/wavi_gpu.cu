@@ -116,6 +116,8 @@ struct wavi_ctx {
   int ew_blocks = 0;
   // persistent coarse CG: grid barrier, launch shape, tiles per CTA (0 = per-iteration kernels)
   GridBar* bar = nullptr;
+  // halo boxes of the FP32 register-resident coarse CG: 8 x tile tagged words per tile
+  unsigned long long* halo_box = nullptr;
   int pers_maxt = 0, pers_grid = 0, ntx = 0, nty = 0;  // pers_maxt -1: CG vectors in global memory
   void *gz = nullptr, *gw = nullptr;                    // extra vectors of the global-memory variant
   int coarse_solver = WAVI_COARSE_CG;  // resolved coarse solver (never WAVI_COARSE_AUTO)
@@ -371,13 +373,13 @@ int launch_cg_persistent(wavi_ctx* c) {
   cfg.numAttrs = 1;
   if (c->coarse_solver == WAVI_COARSE_CG) {
     CK(cudaLaunchKernelEx(&cfg, k_cg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
-                          (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar, c->ntx,
-                          c->nty));
+                          (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
+                          c->halo_box, c->ntx, c->nty));
   } else {
     const T* dc = c->coarse_solver == WAVI_COARSE_SRCG_JACOBI ? (const T*)c->dcoarse : nullptr;
     CK(cudaLaunchKernelEx(&cfg, k_srcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
                           dc, (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
-                          c->ntx, c->nty));
+                          c->halo_box, c->ntx, c->nty));
   }
   c->launches++;
   return 0;
@@ -421,7 +423,7 @@ int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& t
     CKL();
     tv.launches++;
   }
-  k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar);
+  k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar, (const DevParams*)c->P);
   CKL();
   if (c->pers_maxt < 0)
     TRY((launch_cg_global<T, TILE>(c)));
@@ -1345,6 +1347,9 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   c->max_partials = std::max(c->max_partials, 8 * std::max(c->pers_grid, 1));
   if ((r = dalloc(c, &c->partials, (size_t)c->max_partials))) return bail(r);
   if ((r = dalloc(c, &c->bar, 1))) return bail(r);
+  if (c->pers_maxt > 0) {
+    if ((r = dalloc(c, &c->halo_box, (size_t)c->ntx * c->nty * 8 * c->tile))) return bail(r);
+  }
   {
     double* q = nullptr;
     if ((r = dalloc(c, &q, N))) return bail(r);
