@@ -1446,6 +1446,124 @@ __global__ void __launch_bounds__(TILE* TILE)
   }
 }
 
+// k_coarse_diag for 16 x 16 tiles, separated.  A basis function is x = inner ⊙ (φ ⊗ ψ) on its block, so
+// a difference along x is ψ(r) (inner φ)(p) - ψ(r) (inner φ)(p-1) and one along y is φ(p) times the
+// difference of inner ψ; every term of the quadratic form is therefore ψ(r)² times a sum over the row r
+// that depends on φ alone, or φ(p)² times a sum over the column p that depends on ψ alone:
+//   diag(φ_kx ⊗ ψ_ky) = Σ_r ψ_ky(r)² X[kx][r] + Σ_p φ_kx(p)² Y[ky][p].
+// u: X holds the u_x, div q and β terms, Y the u_y term; v: Y holds v_y and div q, X the v_x and β terms.
+// Each thread builds one entry of X and one of Y (sums over 17 positions), then evaluates its own basis
+// function (32 terms): O(TILE) work per function instead of k_coarse_diag's O(support area), the same
+// terms added in another order.
+template <typename T, int TILE>
+__global__ void __launch_bounds__(TILE* TILE)
+    k_coarse_diag_sep(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, T* __restrict__ dc) {
+  __shared__ T s_heh[TILE + 1][TILE + 1], s_hec[TILE + 1][TILE + 1], s_dim[TILE + 1][TILE + 1];
+  __shared__ float s_basis[2][TILE][TILE + 1];  // [along x, along y][offset][position]
+  __shared__ T s_in[TILE][TILE + 1], s_hm[TILE][TILE + 1], s_beta[TILE][TILE + 1];  // [r][p] on the block
+  __shared__ T s_x[TILE][TILE + 1], s_y[TILE][TILE + 1];                           // X[kx][r], Y[ky][p]
+  const int bx0 = blockIdx.x * TILE, by0 = blockIdx.y * TILE, tx = threadIdx.x, ty = threadIdx.y;
+  for (int p = tx + TILE * ty; p < (TILE + 1) * (TILE + 1); p += TILE * TILE) {
+    const int la = p % (TILE + 1), lb = p / (TILE + 1), a = bx0 - 1 + la, b = by0 - 1 + lb;
+    const bool hv = a >= 0 && a < d.nx && b >= 0 && b < d.ny;
+    const bool cv = a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1;
+    s_heh[lb][la] = hv ? cf.heta_h[hidx(d, a, b)] : (T)0;
+    s_dim[lb][la] = hv ? cf.dimp[hidx(d, a, b)] : (T)0;
+    s_hec[lb][la] = cv ? cf.heta_c[cidx(d, a, b)] : (T)0;
+  }
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d), rdx2 = rdx * rdx, rdy2 = rdy * rdy;
+  for (int comp = 0; comp < 2; ++comp) {
+    const int nxg = comp == 0 ? d.nx + 1 : d.nx, nyg = comp == 0 ? d.ny : d.ny + 1;
+    const int lenx = min(TILE, nxg - bx0), leny = min(TILE, nyg - by0);
+    auto gq = [&](int gi, int gj) { return comp == 0 ? uidx(d, gi, gj) : vidx(d, gi, gj); };
+    __syncthreads();  // the previous component's tables are no longer read
+    if (ty < 2) {
+      float b[TILE];
+      basis_1d<TILE>(tx, ty == 0 ? lenx : leny, levels, b);
+#pragma unroll
+      for (int p = 0; p < TILE; ++p) s_basis[ty][tx][p] = b[p];
+    }
+    {
+      const bool on = tx < lenx && ty < leny;
+      const int q = on ? gq(bx0 + tx, by0 + ty) : 0;
+      s_in[ty][tx] = (on && cf.inner[q]) ? (T)1 : (T)0;
+      s_hm[ty][tx] = on ? cf.h_m[q] : (T)0;
+      s_beta[ty][tx] = on ? cf.beta_m[q] : (T)0;
+    }
+    __syncthreads();
+    // (inner φ_k)(p) in row r and (inner ψ_k)(r) in column p; zero off the block
+    auto ix = [&](int k, int p, int r) -> T {
+      return (p >= 0 && p < lenx && r >= 0 && r < leny) ? s_in[r][p] * (T)s_basis[0][k][p] : (T)0;
+    };
+    auto iy = [&](int k, int p, int r) -> T {
+      return (p >= 0 && p < lenx && r >= 0 && r < leny) ? s_in[r][p] * (T)s_basis[1][k][r] : (T)0;
+    };
+    auto hmb = [&](int p, int r) -> T { return (p >= 0 && p < lenx && r >= 0 && r < leny) ? s_hm[r][p] : (T)0; };
+    {
+      // thread (tx, ty): X[kx = tx][r = ty] and Y[ky = tx][p = ty]
+      const int k = tx;
+      T xs = 0, ys = 0;
+      if (comp == 0) {
+        const int r = ty;
+        T a = 0, bsum = 0;
+        for (int p = 0; p <= TILE; ++p) {  // h cell between u points p-1, p of row r
+          const T dxv = ix(k, p, r) - ix(k, p - 1, r);
+          const T dqv = hmb(p, r) * ix(k, p, r) - hmb(p - 1, r) * ix(k, p - 1, r);
+          a += s_dim[r + 1][p] * dqv * dqv - (T)4 * s_heh[r + 1][p] * dxv * dxv;
+        }
+        for (int p = 0; p < TILE; ++p) {
+          const T f = (T)s_basis[0][k][p];
+          bsum += (r < leny && p < lenx) ? s_beta[r][p] * s_in[r][p] * f * f : (T)0;
+        }
+        xs = rdx2 * a - bsum;
+        const int p = ty;
+        T c = 0;
+        for (int rr = 0; rr <= TILE; ++rr) {  // c point between u points (p, rr-1), (p, rr)
+          const T dyv = iy(k, p, rr) - iy(k, p, rr - 1);
+          c += s_hec[rr][p] * dyv * dyv;
+        }
+        ys = -rdy2 * c;
+      } else {
+        const int p = ty;
+        T a = 0;
+        for (int rr = 0; rr <= TILE; ++rr) {  // h cell between v points (p, rr-1), (p, rr)
+          const T dyv = iy(k, p, rr) - iy(k, p, rr - 1);
+          const T dqv = hmb(p, rr) * iy(k, p, rr) - hmb(p, rr - 1) * iy(k, p, rr - 1);
+          a += s_dim[rr][p + 1] * dqv * dqv - (T)4 * s_heh[rr][p + 1] * dyv * dyv;
+        }
+        ys = rdy2 * a;
+        const int r = ty;
+        T c = 0, bsum = 0;
+        for (int pp = 0; pp <= TILE; ++pp) {  // c point between v points (pp-1, r), (pp, r)
+          const T dxv = ix(k, pp, r) - ix(k, pp - 1, r);
+          c += s_hec[r][pp] * dxv * dxv;
+        }
+        for (int pp = 0; pp < TILE; ++pp) {
+          const T f = (T)s_basis[0][k][pp];
+          bsum += (r < leny && pp < lenx) ? s_beta[r][pp] * s_in[r][pp] * f * f : (T)0;
+        }
+        xs = -rdx2 * c - bsum;
+      }
+      s_x[k][ty] = xs;
+      s_y[k][ty] = ys;
+    }
+    __syncthreads();
+    const int i = bx0 + tx, j = by0 + ty;
+    if (i >= nxg || j >= nyg) continue;  // (no __syncthreads below in this component)
+    T e = 0;
+    for (int r = 0; r < TILE; ++r) {
+      const T ps = (T)s_basis[1][ty][r];
+      e += ps * ps * s_x[tx][r];
+    }
+    for (int p = 0; p < TILE; ++p) {
+      const T ph = (T)s_basis[0][tx][p];
+      e += ph * ph * s_y[ty][p];
+    }
+    const int q = gq(i, j);
+    dc[q] = wmask[q] ? e : (T)0;
+  }
+}
+
 // Before a persistent CG: an idle barrier (count 0, no error).
 // Before each persistent launch: restart the arrival counter, clear the error, and advance the tag
 // generation past every tag the previous launch can have written (at most maxiter_coarse + 2 tagged

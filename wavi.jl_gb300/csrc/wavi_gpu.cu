@@ -414,12 +414,20 @@ int launch_cg_global(wavi_ctx* c) {
   return 0;
 }
 
+// diag(R A P) into dst: the separated kernel for 16 x 16 tiles, the general one otherwise.
+template <typename T, int TILE>
+void launch_coarse_diag(wavi_ctx* c, T* dst) {
+  if constexpr (TILE == 16)
+    k_coarse_diag_sep<T, TILE><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, c->sp.levels, coef<T>(c), c->wmask_uv, dst);
+  else
+    k_coarse_diag<T, TILE><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, c->sp.levels, coef<T>(c), c->wmask_uv, dst);
+}
+
 template <typename T, int TILE>
 int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& tc) {
   const Dims& d = c->d;
   if (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI) {
-    k_coarse_diag<T, TILE><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, c->sp.levels, coef<T>(c), c->wmask_uv,
-                                                                      (T*)c->dcoarse);
+    launch_coarse_diag<T, TILE>(c, (T*)c->dcoarse);
     CKL();
     tv.launches++;
   }
@@ -1500,17 +1508,16 @@ int wavi_op_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
 int wavi_coarse_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
   TRY(check_ctx(c));
   if (!diag_uv) return fail(c, WAVI_ERR_ARGUMENT, "null vector");
-  const int L = c->sp.levels;
   if (precision == WAVI_PRECISION_FP64) {
     if (c->tile == 16)
-      k_coarse_diag<double, 16><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, L, coef<double>(c), c->wmask_uv, (double*)diag_uv);
+      launch_coarse_diag<double, 16>(c, (double*)diag_uv);
     else
-      k_coarse_diag<double, 32><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, L, coef<double>(c), c->wmask_uv, (double*)diag_uv);
+      launch_coarse_diag<double, 32>(c, (double*)diag_uv);
   } else if (precision == WAVI_PRECISION_MIXED && mixed(c)) {
     if (c->tile == 16)
-      k_coarse_diag<float, 16><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, L, coef<float>(c), c->wmask_uv, (float*)diag_uv);
+      launch_coarse_diag<float, 16>(c, (float*)diag_uv);
     else
-      k_coarse_diag<float, 32><<<c->tile_grid, c->tile_block, 0, c->st>>>(c->d, L, coef<float>(c), c->wmask_uv, (float*)diag_uv);
+      launch_coarse_diag<float, 32>(c, (float*)diag_uv);
   } else {
     return fail(c, WAVI_ERR_ARGUMENT, "float32 diagonal needs a mixed-precision context");
   }
