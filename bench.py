@@ -426,7 +426,8 @@ def gpu_arm(args):
                      "kernel": "k_srcg_persistent<float> (coarse CG, one launch per V-cycle, 640x80)",
                      "per": "CG iteration", "alg_bytes_per_iteration": cg_bytes, "us_per_iteration": sec_it * 1e6,
                      "cg_iterations": cg_its, "launches": cg_launches, "peak_source": "measured" if peaks else "fallback",
-                     "note": "L2-resident working set; bound by grid-barrier latency (2 barriers per iteration)"},
+                     "note": "on-chip/L2-resident working set; bound by the latency of one grid reduction and one "
+                             "neighbour halo exchange per iteration"},
         "roofline_stencil": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak,
                              "traffic": ncu_traffic("op_kernel_4096x1024.md", "traffic_bytes_per_launch"),
