@@ -355,6 +355,14 @@ int wavi_ensemble_solve_device(wavi_ensemble* ens, const wavi_params* params, wa
 int wavi_ensemble_destroy(wavi_ensemble* ens);
 const char* wavi_ensemble_last_error(const wavi_ensemble* ens);
 
+/* ---- Self-test of the bounded waits -------------------------------------------------------------
+ * Every wait of the persistent kernels (grid barriers, tagged halo words) gives up after a bounded
+ * number of polls, records WAVI_ERR_WATCHDOG and returns, so that the context stays usable.  This call
+ * exercises that path without a fault: one thread waits, with the kernels' own bounded wait, for a
+ * tagged word that nothing writes (about two seconds), then the error flag is cleared.  *fired = 1 if
+ * the wait gave up as designed.  Not part of the reference interface (a test hook). */
+int wavi_selftest_watchdog(wavi_ctx* ctx, int* fired);
+
 #ifdef __cplusplus
 }
 #endif

@@ -145,6 +145,7 @@ def load_library(path=None):
         "wavi_time_operator_device": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.POINTER(C.c_double)]),
         "wavi_haar_device": (C.c_int, [vp, C.c_int, vp, vp, vp]),
         "wavi_residual_noalloc": (C.c_int, [C.POINTER(OperatorDesc), vp, vp, vp, vp, vp]),
+        "wavi_selftest_watchdog": (C.c_int, [vp, C.POINTER(C.c_int)]),
         "wavi_adjoint_device": (C.c_int, [vp, C.POINTER(Params), vp, vp, vp, vp, C.c_double, C.c_int,
                                           C.POINTER(AdjointStats)]),
         "wavi_tangent_device": (C.c_int, [vp, C.POINTER(Params), vp, vp, vp, vp, C.c_double, C.c_int,

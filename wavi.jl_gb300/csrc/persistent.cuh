@@ -383,41 +383,38 @@ __device__ __forceinline__ void load_coef_tile(const Dims& d, const OpCoef<T>& c
   pc.wm_v = pc.inv && wmask[qv];
 }
 
-// stage_stress with the coefficients from the CoefTile (the same operations).
+// One stress cell (la, lb) of stage_stress with the coefficients from the CoefTile (the same operations).
 template <typename T, int TX, int TY, int TILE>
-__device__ __forceinline__ void stage_stress_ct(const Dims& d, const CoefTile<T, TILE>& ct, int i0, int j0,
-                                                OpTile<T, TX, TY>& s) {
+__device__ __forceinline__ void stress_cell_ct(const Dims& d, const CoefTile<T, TILE>& ct, int i0, int j0,
+                                               OpTile<T, TX, TY>& s, int la, int lb) {
   const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
-  for (int p = flat_tid(); p < (TX + 1) * (TY + 1); p += flat_nthreads()) {
-    const int la = p % (TX + 1), lb = p / (TX + 1);
-    const int a = i0 - 1 + la, b = j0 - 1 + lb;
-    T rxx = 0, ryy = 0, e = 0, rxy = 0;
-    if (a >= 0 && a < d.nx && b >= 0 && b < d.ny) {
-      const T u0 = s.xu[lb][la], u1 = s.xu[lb][la + 1], v0 = s.xv[lb][la], v1 = s.xv[lb + 1][la];
-      const T ux = (u1 - u0) * rdx, vy = (v1 - v0) * rdy;
-      const T he2 = ct.he2[lb][la];
-      rxx = he2 * ((T)2 * ux + vy);
-      ryy = he2 * ((T)2 * vy + ux);
-      const T dm = ct.dm[lb][la];
-      if (dm != (T)0) {
-        const T divq = (ct.hmu[lb][la + 1] * u1 - ct.hmu[lb][la] * u0) * rdx +
-                       (ct.hmv[lb + 1][la] * v1 - ct.hmv[lb][la] * v0) * rdy;
-        e = dm * divq;
-      }
+  const int a = i0 - 1 + la, b = j0 - 1 + lb;
+  T rxx = 0, ryy = 0, e = 0, rxy = 0;
+  if (a >= 0 && a < d.nx && b >= 0 && b < d.ny) {
+    const T u0 = s.xu[lb][la], u1 = s.xu[lb][la + 1], v0 = s.xv[lb][la], v1 = s.xv[lb + 1][la];
+    const T ux = (u1 - u0) * rdx, vy = (v1 - v0) * rdy;
+    const T he2 = ct.he2[lb][la];
+    rxx = he2 * ((T)2 * ux + vy);
+    ryy = he2 * ((T)2 * vy + ux);
+    const T dm = ct.dm[lb][la];
+    if (dm != (T)0) {
+      const T divq = (ct.hmu[lb][la + 1] * u1 - ct.hmu[lb][la] * u0) * rdx +
+                     (ct.hmv[lb + 1][la] * v1 - ct.hmv[lb][la] * v0) * rdy;
+      e = dm * divq;
     }
-    if (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) {
-      const T hc = ct.hc[lb][la];
-      if (hc != (T)0) {
-        const T uy = (s.xu[lb + 1][la + 1] - s.xu[lb][la + 1]) * rdy;
-        const T vx = (s.xv[lb + 1][la + 1] - s.xv[lb + 1][la]) * rdx;
-        rxy = hc * (uy + vx);
-      }
-    }
-    s.rxx[lb][la] = rxx;
-    s.ryy[lb][la] = ryy;
-    s.e[lb][la] = e;
-    s.rxy[lb][la] = rxy;
   }
+  if (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) {
+    const T hc = ct.hc[lb][la];
+    if (hc != (T)0) {
+      const T uy = (s.xu[lb + 1][la + 1] - s.xu[lb][la + 1]) * rdy;
+      const T vx = (s.xv[lb + 1][la + 1] - s.xv[lb + 1][la]) * rdx;
+      rxy = hc * (uy + vx);
+    }
+  }
+  s.rxx[lb][la] = rxx;
+  s.ryy[lb][la] = ryy;
+  s.e[lb][la] = e;
+  s.rxy[lb][la] = rxy;
 }
 
 // P on a TILE x TILE tile, u and v together: the idwt lifting (haar_tile KIND 0) along y, then along x,
@@ -598,40 +595,79 @@ __device__ __forceinline__ bool apply_tagged(const Dims& d, int levels, const Co
   const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TILE * ty;
   sm.op.xu[ty + 1][tx + 1] = hu;
   sm.op.xv[ty + 1][tx + 1] = hv;
+  // halo ring: thread t < 2 RING issues the load of its word now, and checks its tag after the interior
+  // stresses (which need no halo value) so that the L2 round trip overlaps them
+  const unsigned tag = ts.base + ts.hx;
+  const unsigned long long* src = nullptr;
+  int li_r = 0, lj_r = 0, c_r = 0;
+  unsigned long long w = 0;
   if (t < 2 * RING) {
     // ring position p: the row below (lj = 0), the row above (lj = TILE + 1), then the two columns
-    const int c = t >= RING, p = t - c * RING;
-    int li, lj;
+    c_r = t >= RING;
+    const int p = t - c_r * RING;
     if (p < TILE + 2) {
-      li = p;
-      lj = 0;
+      li_r = p;
+      lj_r = 0;
     } else if (p < 2 * (TILE + 2)) {
-      li = p - (TILE + 2);
-      lj = TILE + 1;
+      li_r = p - (TILE + 2);
+      lj_r = TILE + 1;
     } else {
       const int q = p - 2 * (TILE + 2);
-      li = (q & 1) ? TILE + 1 : 0;
-      lj = 1 + (q >> 1);
+      li_r = (q & 1) ? TILE + 1 : 0;
+      lj_r = 1 + (q >> 1);
     }
-    const int i = i0 - 1 + li, j = j0 - 1 + lj;
-    const bool on = c == 0 ? (i >= 0 && i <= d.nx && j >= 0 && j < d.ny) : (i >= 0 && i < d.nx && j >= 0 && j <= d.ny);
-    T val = 0;
+    const int i = i0 - 1 + li_r, j = j0 - 1 + lj_r;
+    const bool on = c_r == 0 ? (i >= 0 && i <= d.nx && j >= 0 && j < d.ny) : (i >= 0 && i < d.nx && j >= 0 && j <= d.ny);
     if (on) {
       // the owning tile and the edge of its box that holds (i, j)
       const int ti = i / TILE, tj = j / TILE;
-      const int e = li == 0 ? 1 : li == TILE + 1 ? 0 : lj == 0 ? 3 : 2;
-      const int k = (li == 0 || li == TILE + 1) ? j - tj * TILE : i - ti * TILE;
-      const unsigned long long* src = ts.halo + (size_t)(tj * ntx + ti) * (8 * TILE) + (c * 4 + e) * TILE + k;
-      val = value_of(wait_tagged(src, ts.base + ts.hx, bar, fail));
+      const int e = li_r == 0 ? 1 : li_r == TILE + 1 ? 0 : lj_r == 0 ? 3 : 2;
+      const int k = (li_r == 0 || li_r == TILE + 1) ? j - tj * TILE : i - ti * TILE;
+      src = ts.halo + (size_t)(tj * ntx + ti) * (8 * TILE) + (c_r * 4 + e) * TILE + k;
+      w = ld_relaxed_u64(src);
     }
-    if (c == 0)
-      sm.op.xu[lj][li] = val;
+  }
+  __syncthreads();  // the interior of x is in shared memory
+  for (int p = t; p < (TILE - 1) * (TILE - 1); p += TILE * TILE)
+    stress_cell_ct(d, ct, i0, j0, sm.op, 1 + p % (TILE - 1), 1 + p / (TILE - 1));
+  if (t < 2 * RING) {
+    T val = 0;
+    if (src) {
+      long polls = 0;
+      while (tag_of(w) != tag) {
+        if (++polls > kBarrierSpinLimit || ((polls & 255) == 0 && *(volatile int*)&bar->err)) {
+          *fail = 1;
+          atomicExch(&bar->err, 1);
+          break;
+        }
+        if (polls > 8) __nanosleep(32);
+        w = ld_relaxed_u64(src);
+      }
+      val = value_of(w);
+    }
+    if (c_r == 0)
+      sm.op.xu[lj_r][li_r] = val;
     else
-      sm.op.xv[lj][li] = val;
+      sm.op.xv[lj_r][li_r] = val;
   }
   __syncthreads();
   if (*fail) return false;
-  stage_stress_ct(d, ct, i0, j0, sm.op);
+  // the stress cells on the tile's boundary (17 x 17 - 15 x 15 = 4 TILE)
+  if (t < 4 * TILE) {
+    int la, lb;
+    if (t < TILE + 1) {
+      la = t;
+      lb = 0;
+    } else if (t < 2 * (TILE + 1)) {
+      la = t - (TILE + 1);
+      lb = TILE;
+    } else {
+      const int q = t - 2 * (TILE + 1);
+      la = (q & 1) ? TILE : 0;
+      lb = 1 + (q >> 1);
+    }
+    stress_cell_ct(d, ct, i0, j0, sm.op, la, lb);
+  }
   __syncthreads();
   const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
   const OpTile<T, TILE, TILE>& s = sm.op;
@@ -1561,6 +1597,17 @@ __global__ void __launch_bounds__(TILE* TILE)
     }
     const int q = gq(i, j);
     dc[q] = wmask[q] ? e : (T)0;
+  }
+}
+
+// Self-test of the bounded waits: one thread waits, with wait_tagged, for a word that nothing writes;
+// out = 1 if the wait gave up (it also sets bar->err, which the caller clears).
+static __global__ void k_selftest_wait(GridBar* bar, const unsigned long long* __restrict__ word, int* out) {
+  __shared__ int fail;
+  if (threadIdx.x == 0) {
+    fail = 0;
+    wait_tagged(word, 1u, bar, &fail);
+    *out = fail;
   }
 }
 

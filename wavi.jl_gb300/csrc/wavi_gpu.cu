@@ -118,6 +118,7 @@ struct wavi_ctx {
   GridBar* bar = nullptr;
   // halo boxes of the FP32 register-resident coarse CG: 8 x tile tagged words per tile
   unsigned long long* halo_box = nullptr;
+  unsigned long long* selftest = nullptr;  // [0]: a tagged word nothing writes, [1]: the self-test's result
   int pers_maxt = 0, pers_grid = 0, ntx = 0, nty = 0;  // pers_maxt -1: CG vectors in global memory
   void *gz = nullptr, *gw = nullptr;                    // extra vectors of the global-memory variant
   int coarse_solver = WAVI_COARSE_CG;  // resolved coarse solver (never WAVI_COARSE_AUTO)
@@ -1355,6 +1356,7 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   c->max_partials = std::max(c->max_partials, 8 * std::max(c->pers_grid, 1));
   if ((r = dalloc(c, &c->partials, (size_t)c->max_partials))) return bail(r);
   if ((r = dalloc(c, &c->bar, 1))) return bail(r);
+  if ((r = dalloc(c, &c->selftest, 2))) return bail(r);
   if (c->pers_maxt > 0) {
     if ((r = dalloc(c, &c->halo_box, (size_t)c->ntx * c->nty * 8 * c->tile))) return bail(r);
   }
@@ -1502,6 +1504,23 @@ int wavi_op_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
     return fail(c, WAVI_ERR_ARGUMENT, "float32 diagonal needs a mixed-precision context");
   CKL();
   CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+int wavi_selftest_watchdog(wavi_ctx* c, int* fired) {
+  TRY(check_ctx(c));
+  if (!fired) return fail(c, WAVI_ERR_ARGUMENT, "null pointer");
+  CK(cudaMemsetAsync(c->selftest, 0, 2 * sizeof(unsigned long long), c->st));
+  k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar, (const DevParams*)c->P);
+  CKL();
+  k_selftest_wait<<<1, 32, 0, c->st>>>(c->bar, c->selftest, (int*)(c->selftest + 1));
+  CKL();
+  int out = 0;
+  CK(cudaMemcpyAsync(&out, c->selftest + 1, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar, (const DevParams*)c->P);  // the barrier idle again (no error)
+  CKL();
+  CK(cudaStreamSynchronize(c->st));
+  *fired = out;
   return 0;
 }
 

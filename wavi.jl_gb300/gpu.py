@@ -196,6 +196,14 @@ class VelocitySolver:
         if st != 0:
             raise self._err(st)
 
+    def selftest_watchdog(self):
+        """Run the bounded-wait self-test (wavi_selftest_watchdog): True if the wait gave up as designed."""
+        fired = C.c_int(0)
+        st = self.lib.wavi_selftest_watchdog(self.ctx, C.byref(fired))
+        if st != 0:
+            raise self._err(st)
+        return bool(fired.value)
+
     def haar_device(self, kind, in_uv, out_uv, mask_uv=None):
         m = C.c_void_p(mask_uv.data_ptr()) if mask_uv is not None else None
         st = self.lib.wavi_haar_device(self.ctx, int(kind), C.c_void_p(in_uv.data_ptr()), C.c_void_p(out_uv.data_ptr()), m)
