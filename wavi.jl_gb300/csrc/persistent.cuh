@@ -277,146 +277,6 @@ __device__ __forceinline__ TT haar2d(TT v, TT (*sm)[TILE + 1], int bx0, int by0,
   return lift_lanes<KIND>(v, tx, bx0, nxg, (bx0 + tx) < nxg && (by0 + ty) < nyg, levels);
 }
 
-template <typename T, int TILE>
-struct CGShared {
-  OpTile<T, TILE, TILE> op;
-  T hs[TILE][TILE + 1];
-};
-
-// c = wmask ⊙ R (A w) at this thread's point of the tile with origin (i0, j0); w is read from global
-// memory (tile + halo).  Every thread of the CTA must call it.
-template <typename T, int TILE>
-__device__ __forceinline__ void coarse_apply(const Dims& d, int levels, const OpCoef<T>& cf, const uint8_t* __restrict__ wmask,
-                                             const T* __restrict__ w, int i0, int j0, CGShared<T, TILE>& sm, T& cu, T& cv) {
-  __syncthreads();  // the previous use of the tile's shared memory is over
-  stage_x(d, i0, j0, sm.op, [&](int q) { return __ldcg(w + q); });
-  __syncthreads();
-  stage_stress(d, cf, i0, j0, sm.op);
-  __syncthreads();
-  const int tx = threadIdx.x, ty = threadIdx.y, i = i0 + tx, j = j0 + ty;
-  const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
-  T yu = 0, yv = 0;
-  if (inu) {
-    const int q = uidx(d, i, j);
-    if (cf.inner[q]) yu = stage_out_u(d, cf, sm.op, tx + 1, ty + 1, q);
-  }
-  if (inv) {
-    const int q = vidx(d, i, j);
-    if (cf.inner[q]) yv = stage_out_v(d, cf, sm.op, tx + 1, ty + 1, q);
-  }
-  yu = haar2d<TILE, 1>(yu, sm.hs, i0, j0, d.nx + 1, d.ny, levels);
-  yv = haar2d<TILE, 1>(yv, sm.hs, i0, j0, d.nx, d.ny + 1, levels);
-  cu = (inu && wmask[uidx(d, i, j)]) ? yu : (T)0;
-  cv = (inv && wmask[vidx(d, i, j)]) ? yv : (T)0;
-}
-
-// w = inner ⊙ P u at this thread's point; written to global memory.
-template <typename T, int TILE>
-__device__ __forceinline__ void prolong_store(const Dims& d, int levels, const uint8_t* __restrict__ inner, T uu, T uv,
-                                              int i0, int j0, CGShared<T, TILE>& sm, T* __restrict__ w) {
-  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-  const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
-  const T pu = haar2d<TILE, 0>(uu, sm.hs, i0, j0, d.nx + 1, d.ny, levels);
-  const T pv = haar2d<TILE, 0>(uv, sm.hs, i0, j0, d.nx, d.ny + 1, levels);
-  if (inu) {
-    const int q = uidx(d, i, j);
-    __stcg(w + q, inner[q] ? pu : (T)0);
-  }
-  if (inv) {
-    const int q = vidx(d, i, j);
-    __stcg(w + q, inner[q] ? pv : (T)0);
-  }
-}
-
-// ------------------------------------------------------------------------------------------------
-// The FP32 register-resident kernels (TILE = 16) keep the operator's coefficients on chip for the whole
-// launch and transform u and v together.
-//
-// CoefTile: the coefficients that the tile's stress stage reads (h cells and c points of the tile and
-// its one-cell halo, h_m at the u and v points around them), staged once per launch in shared memory;
-// PointCoef: the thread's own point (β, h_m and the inner / coarse-space flags) in registers.  Per CG
-// iteration the operator then reads only the prolonged vector from L2.
-// ------------------------------------------------------------------------------------------------
-template <typename T, int TILE>
-struct CoefTile {
-  T he2[TILE + 1][TILE + 1];  // 2 hη at h cell (i0 - 1 + a, j0 - 1 + b); 0 off the grid
-  T dm[TILE + 1][TILE + 1];   // dimp at the h cells
-  T hc[TILE + 1][TILE + 1];   // hη_c at c point (i0 - 1 + a, j0 - 1 + b)
-  T hmu[TILE + 1][TILE + 2];  // h_m at u point (i0 - 1 + a, j0 - 1 + b)
-  T hmv[TILE + 2][TILE + 1];  // h_m at v point (i0 - 1 + a, j0 - 1 + b)
-};
-template <typename T>
-struct PointCoef {
-  T beta_u, beta_v, hm_u, hm_v;
-  bool inu, inv, inner_u, inner_v, wm_u, wm_v;  // on the grid; interior; in the coarse space
-};
-
-template <typename T, int TILE>
-__device__ __forceinline__ void load_coef_tile(const Dims& d, const OpCoef<T>& cf, const uint8_t* __restrict__ wmask,
-                                               int i0, int j0, CoefTile<T, TILE>& ct, PointCoef<T>& pc) {
-  for (int p = flat_tid(); p < (TILE + 1) * (TILE + 1); p += flat_nthreads()) {
-    const int la = p % (TILE + 1), lb = p / (TILE + 1), a = i0 - 1 + la, b = j0 - 1 + lb;
-    const bool hin = a >= 0 && a < d.nx && b >= 0 && b < d.ny;
-    ct.he2[lb][la] = hin ? (T)2 * cf.heta_h[hidx(d, a, b)] : (T)0;
-    ct.dm[lb][la] = hin ? cf.dimp[hidx(d, a, b)] : (T)0;
-    ct.hc[lb][la] = (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) ? cf.heta_c[cidx(d, a, b)] : (T)0;
-  }
-  for (int p = flat_tid(); p < (TILE + 1) * (TILE + 2); p += flat_nthreads()) {
-    const int la = p % (TILE + 2), lb = p / (TILE + 2), a = i0 - 1 + la, b = j0 - 1 + lb;
-    ct.hmu[lb][la] = (a >= 0 && a <= d.nx && b >= 0 && b < d.ny) ? cf.h_m[uidx(d, a, b)] : (T)0;
-  }
-  for (int p = flat_tid(); p < (TILE + 2) * (TILE + 1); p += flat_nthreads()) {
-    const int la = p % (TILE + 1), lb = p / (TILE + 1), a = i0 - 1 + la, b = j0 - 1 + lb;
-    ct.hmv[lb][la] = (a >= 0 && a < d.nx && b >= 0 && b <= d.ny) ? cf.h_m[vidx(d, a, b)] : (T)0;
-  }
-  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-  pc.inu = i <= d.nx && j < d.ny;
-  pc.inv = i < d.nx && j <= d.ny;
-  const int qu = pc.inu ? uidx(d, i, j) : 0, qv = pc.inv ? vidx(d, i, j) : 0;
-  pc.beta_u = pc.inu ? cf.beta_m[qu] : (T)0;
-  pc.hm_u = pc.inu ? cf.h_m[qu] : (T)0;
-  pc.inner_u = pc.inu && cf.inner[qu];
-  pc.wm_u = pc.inu && wmask[qu];
-  pc.beta_v = pc.inv ? cf.beta_m[qv] : (T)0;
-  pc.hm_v = pc.inv ? cf.h_m[qv] : (T)0;
-  pc.inner_v = pc.inv && cf.inner[qv];
-  pc.wm_v = pc.inv && wmask[qv];
-}
-
-// One stress cell (la, lb) of stage_stress with the coefficients from the CoefTile (the same operations).
-template <typename T, int TX, int TY, int TILE>
-__device__ __forceinline__ void stress_cell_ct(const Dims& d, const CoefTile<T, TILE>& ct, int i0, int j0,
-                                               OpTile<T, TX, TY>& s, int la, int lb) {
-  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
-  const int a = i0 - 1 + la, b = j0 - 1 + lb;
-  T rxx = 0, ryy = 0, e = 0, rxy = 0;
-  if (a >= 0 && a < d.nx && b >= 0 && b < d.ny) {
-    const T u0 = s.xu[lb][la], u1 = s.xu[lb][la + 1], v0 = s.xv[lb][la], v1 = s.xv[lb + 1][la];
-    const T ux = (u1 - u0) * rdx, vy = (v1 - v0) * rdy;
-    const T he2 = ct.he2[lb][la];
-    rxx = he2 * ((T)2 * ux + vy);
-    ryy = he2 * ((T)2 * vy + ux);
-    const T dm = ct.dm[lb][la];
-    if (dm != (T)0) {
-      const T divq = (ct.hmu[lb][la + 1] * u1 - ct.hmu[lb][la] * u0) * rdx +
-                     (ct.hmv[lb + 1][la] * v1 - ct.hmv[lb][la] * v0) * rdy;
-      e = dm * divq;
-    }
-  }
-  if (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) {
-    const T hc = ct.hc[lb][la];
-    if (hc != (T)0) {
-      const T uy = (s.xu[lb + 1][la + 1] - s.xu[lb][la + 1]) * rdy;
-      const T vx = (s.xv[lb + 1][la + 1] - s.xv[lb + 1][la]) * rdx;
-      rxy = hc * (uy + vx);
-    }
-  }
-  s.rxx[lb][la] = rxx;
-  s.ryy[lb][la] = ryy;
-  s.e[lb][la] = e;
-  s.rxy[lb][la] = rxy;
-}
-
 // P on a TILE x TILE tile, u and v together: the idwt lifting (haar_tile KIND 0) along y, then along x,
 // written as a gather.  The output at in-block position j is the block's scaling coefficient plus, per
 // level l (half = B >> (l + 1)), minus or plus the detail coefficient at (j rounded down to 2 half) + half:
@@ -516,6 +376,158 @@ __device__ __forceinline__ void idwt2dT_pair(TT& u, TT& v, TT (*su)[TILE + 1], T
     }
   u = bu;
   v = bv;
+}
+
+template <typename T, int TILE>
+struct CGShared {
+  OpTile<T, TILE, TILE> op;
+  T hs[TILE][TILE + 1];
+  T hs2[std::is_same<T, float>::value ? TILE : 1][TILE + 1];  // FP32: the second buffer of the paired transforms
+};
+
+// c = wmask ⊙ R (A w) at this thread's point of the tile with origin (i0, j0); w is read from global
+// memory (tile + halo).  Every thread of the CTA must call it.
+template <typename T, int TILE>
+__device__ __forceinline__ void coarse_apply(const Dims& d, int levels, const OpCoef<T>& cf, const uint8_t* __restrict__ wmask,
+                                             const T* __restrict__ w, int i0, int j0, CGShared<T, TILE>& sm, T& cu, T& cv) {
+  __syncthreads();  // the previous use of the tile's shared memory is over
+  stage_x(d, i0, j0, sm.op, [&](int q) { return __ldcg(w + q); });
+  __syncthreads();
+  stage_stress(d, cf, i0, j0, sm.op);
+  __syncthreads();
+  const int tx = threadIdx.x, ty = threadIdx.y, i = i0 + tx, j = j0 + ty;
+  const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+  T yu = 0, yv = 0;
+  if (inu) {
+    const int q = uidx(d, i, j);
+    if (cf.inner[q]) yu = stage_out_u(d, cf, sm.op, tx + 1, ty + 1, q);
+  }
+  if (inv) {
+    const int q = vidx(d, i, j);
+    if (cf.inner[q]) yv = stage_out_v(d, cf, sm.op, tx + 1, ty + 1, q);
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    idwt2dT_pair<TILE>(yu, yv, sm.hs, sm.hs2, levels);
+  } else {
+    yu = haar2d<TILE, 1>(yu, sm.hs, i0, j0, d.nx + 1, d.ny, levels);
+    yv = haar2d<TILE, 1>(yv, sm.hs, i0, j0, d.nx, d.ny + 1, levels);
+  }
+  cu = (inu && wmask[uidx(d, i, j)]) ? yu : (T)0;
+  cv = (inv && wmask[vidx(d, i, j)]) ? yv : (T)0;
+}
+
+// w = inner ⊙ P u at this thread's point; written to global memory.
+template <typename T, int TILE>
+__device__ __forceinline__ void prolong_store(const Dims& d, int levels, const uint8_t* __restrict__ inner, T uu, T uv,
+                                              int i0, int j0, CGShared<T, TILE>& sm, T* __restrict__ w) {
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+  T pu, pv;
+  if constexpr (std::is_same<T, float>::value) {
+    pu = inu ? uu : (T)0;
+    pv = inv ? uv : (T)0;
+    idwt2d_pair<TILE>(pu, pv, sm.hs, sm.hs2, levels);
+  } else {
+    pu = haar2d<TILE, 0>(uu, sm.hs, i0, j0, d.nx + 1, d.ny, levels);
+    pv = haar2d<TILE, 0>(uv, sm.hs, i0, j0, d.nx, d.ny + 1, levels);
+  }
+  if (inu) {
+    const int q = uidx(d, i, j);
+    __stcg(w + q, inner[q] ? pu : (T)0);
+  }
+  if (inv) {
+    const int q = vidx(d, i, j);
+    __stcg(w + q, inner[q] ? pv : (T)0);
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// The FP32 register-resident kernels (TILE = 16) keep the operator's coefficients on chip for the whole
+// launch and transform u and v together.
+//
+// CoefTile: the coefficients that the tile's stress stage reads (h cells and c points of the tile and
+// its one-cell halo, h_m at the u and v points around them), staged once per launch in shared memory;
+// PointCoef: the thread's own point (β, h_m and the inner / coarse-space flags) in registers.  Per CG
+// iteration the operator then reads only the prolonged vector from L2.
+// ------------------------------------------------------------------------------------------------
+template <typename T, int TILE>
+struct CoefTile {
+  T he2[TILE + 1][TILE + 1];  // 2 hη at h cell (i0 - 1 + a, j0 - 1 + b); 0 off the grid
+  T dm[TILE + 1][TILE + 1];   // dimp at the h cells
+  T hc[TILE + 1][TILE + 1];   // hη_c at c point (i0 - 1 + a, j0 - 1 + b)
+  T hmu[TILE + 1][TILE + 2];  // h_m at u point (i0 - 1 + a, j0 - 1 + b)
+  T hmv[TILE + 2][TILE + 1];  // h_m at v point (i0 - 1 + a, j0 - 1 + b)
+};
+template <typename T>
+struct PointCoef {
+  T beta_u, beta_v, hm_u, hm_v;
+  bool inu, inv, inner_u, inner_v, wm_u, wm_v;  // on the grid; interior; in the coarse space
+};
+
+template <typename T, int TILE>
+__device__ __forceinline__ void load_coef_tile(const Dims& d, const OpCoef<T>& cf, const uint8_t* __restrict__ wmask,
+                                               int i0, int j0, CoefTile<T, TILE>& ct, PointCoef<T>& pc) {
+  for (int p = flat_tid(); p < (TILE + 1) * (TILE + 1); p += flat_nthreads()) {
+    const int la = p % (TILE + 1), lb = p / (TILE + 1), a = i0 - 1 + la, b = j0 - 1 + lb;
+    const bool hin = a >= 0 && a < d.nx && b >= 0 && b < d.ny;
+    ct.he2[lb][la] = hin ? (T)2 * cf.heta_h[hidx(d, a, b)] : (T)0;
+    ct.dm[lb][la] = hin ? cf.dimp[hidx(d, a, b)] : (T)0;
+    ct.hc[lb][la] = (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) ? cf.heta_c[cidx(d, a, b)] : (T)0;
+  }
+  for (int p = flat_tid(); p < (TILE + 1) * (TILE + 2); p += flat_nthreads()) {
+    const int la = p % (TILE + 2), lb = p / (TILE + 2), a = i0 - 1 + la, b = j0 - 1 + lb;
+    ct.hmu[lb][la] = (a >= 0 && a <= d.nx && b >= 0 && b < d.ny) ? cf.h_m[uidx(d, a, b)] : (T)0;
+  }
+  for (int p = flat_tid(); p < (TILE + 2) * (TILE + 1); p += flat_nthreads()) {
+    const int la = p % (TILE + 1), lb = p / (TILE + 1), a = i0 - 1 + la, b = j0 - 1 + lb;
+    ct.hmv[lb][la] = (a >= 0 && a < d.nx && b >= 0 && b <= d.ny) ? cf.h_m[vidx(d, a, b)] : (T)0;
+  }
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  pc.inu = i <= d.nx && j < d.ny;
+  pc.inv = i < d.nx && j <= d.ny;
+  const int qu = pc.inu ? uidx(d, i, j) : 0, qv = pc.inv ? vidx(d, i, j) : 0;
+  pc.beta_u = pc.inu ? cf.beta_m[qu] : (T)0;
+  pc.hm_u = pc.inu ? cf.h_m[qu] : (T)0;
+  pc.inner_u = pc.inu && cf.inner[qu];
+  pc.wm_u = pc.inu && wmask[qu];
+  pc.beta_v = pc.inv ? cf.beta_m[qv] : (T)0;
+  pc.hm_v = pc.inv ? cf.h_m[qv] : (T)0;
+  pc.inner_v = pc.inv && cf.inner[qv];
+  pc.wm_v = pc.inv && wmask[qv];
+}
+
+// One stress cell (la, lb) of stage_stress with the coefficients from the CoefTile (the same operations).
+template <typename T, int TX, int TY, int TILE>
+__device__ __forceinline__ void stress_cell_ct(const Dims& d, const CoefTile<T, TILE>& ct, int i0, int j0,
+                                               OpTile<T, TX, TY>& s, int la, int lb) {
+  const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
+  const int a = i0 - 1 + la, b = j0 - 1 + lb;
+  T rxx = 0, ryy = 0, e = 0, rxy = 0;
+  if (a >= 0 && a < d.nx && b >= 0 && b < d.ny) {
+    const T u0 = s.xu[lb][la], u1 = s.xu[lb][la + 1], v0 = s.xv[lb][la], v1 = s.xv[lb + 1][la];
+    const T ux = (u1 - u0) * rdx, vy = (v1 - v0) * rdy;
+    const T he2 = ct.he2[lb][la];
+    rxx = he2 * ((T)2 * ux + vy);
+    ryy = he2 * ((T)2 * vy + ux);
+    const T dm = ct.dm[lb][la];
+    if (dm != (T)0) {
+      const T divq = (ct.hmu[lb][la + 1] * u1 - ct.hmu[lb][la] * u0) * rdx +
+                     (ct.hmv[lb + 1][la] * v1 - ct.hmv[lb][la] * v0) * rdy;
+      e = dm * divq;
+    }
+  }
+  if (a >= 0 && a < d.nx - 1 && b >= 0 && b < d.ny - 1) {
+    const T hc = ct.hc[lb][la];
+    if (hc != (T)0) {
+      const T uy = (s.xu[lb + 1][la + 1] - s.xu[lb][la + 1]) * rdy;
+      const T vx = (s.xv[lb + 1][la + 1] - s.xv[lb + 1][la]) * rdx;
+      rxy = hc * (uy + vx);
+    }
+  }
+  s.rxx[lb][la] = rxx;
+  s.ryy[lb][la] = ryy;
+  s.e[lb][la] = e;
+  s.rxy[lb][la] = rxy;
 }
 
 // Tagged halo exchange of the FP32 register-resident kernels.  The prolonged vector of a tile never
