@@ -541,9 +541,13 @@ __device__ __forceinline__ void stress_cell_ct(const Dims& d, const CoefTile<T, 
 // for the reductions as well, every CTA polling every CTA's partial, were measured slower than the
 // counter barrier: the polls crowd the few L2 lines that the partials occupy.)
 struct TagState {
-  unsigned long long* halo;  // [tile][u, v][west column, east column, south row, north row][TILE]
+  unsigned long long* halo;  // [parity][tile][u, v][west column, east column, south row, north row][TILE]
   unsigned base;             // gen << 21
   unsigned hx;               // exchanges so far in this launch
+  size_t parity_stride;      // words per parity (0: one box set, the coarse CG's; its reductions order the rewrites)
+  __device__ __forceinline__ unsigned long long* box(int tile, int TILE) const {
+    return halo + (size_t)(hx & 1u) * parity_stride + (size_t)tile * (8 * TILE);
+  }
 };
 
 // Bounded wait for a tagged word.  On a timeout (or another CTA's error) sets fail and bar->err.
@@ -563,18 +567,12 @@ __device__ __forceinline__ unsigned long long wait_tagged(const unsigned long lo
   return w;
 }
 
-// P on the tile (paired Haar transform); the prolonged values stay in the thread's registers (hu, hv:
-// inner ⊙ P u, zero off the grid) and the tile's boundary is published for exchange ts.hx.
+// The tile's boundary values (this thread's hu, hv if it lies on the first/last row or column) as
+// tagged words of exchange ts.hx.
 template <typename T, int TILE>
-__device__ __forceinline__ void prolong_publish(int levels, const PointCoef<T>& pc, T uu, T uv, int tile,
-                                                CGShared<T, TILE>& sm, T (*hs2)[TILE + 1], const TagState& ts, T& hu,
-                                                T& hv) {
-  T pu = pc.inu ? uu : (T)0, pv = pc.inv ? uv : (T)0;
-  idwt2d_pair<TILE>(pu, pv, sm.hs, hs2, levels);
-  hu = pc.inner_u ? pu : (T)0;
-  hv = pc.inner_v ? pv : (T)0;
+__device__ __forceinline__ void publish_boundary(T hu, T hv, int tile, const TagState& ts) {
   const unsigned tag = ts.base + ts.hx;
-  unsigned long long* box = ts.halo + (size_t)tile * (8 * TILE);
+  unsigned long long* box = ts.box(tile, TILE);
   const int tx = threadIdx.x, ty = threadIdx.y;
   if (tx == 0) {
     st_relaxed_u64(box + 0 * TILE + ty, tagged(tag, hu));
@@ -594,21 +592,33 @@ __device__ __forceinline__ void prolong_publish(int levels, const PointCoef<T>& 
   }
 }
 
-// coarse_apply of the fast path: the tile's interior from registers (hu, hv), its halo ring from the
-// neighbours' boxes (exchange ts.hx), the coefficients from the CoefTile, the paired Pᵀ.  Returns false
-// (in every thread) if a wait gave up.
+// P on the tile (paired Haar transform); the prolonged values stay in the thread's registers (hu, hv:
+// inner ⊙ P u, zero off the grid) and the tile's boundary is published for exchange ts.hx.
 template <typename T, int TILE>
-__device__ __forceinline__ bool apply_tagged(const Dims& d, int levels, const CoefTile<T, TILE>& ct, const PointCoef<T>& pc,
-                                             T hu, T hv, int i0, int j0, int ntx, CGShared<T, TILE>& sm,
-                                             T (*hs2)[TILE + 1], const TagState& ts, GridBar* bar, volatile int* fail,
-                                             T& cu, T& cv) {
+__device__ __forceinline__ void prolong_publish(int levels, const PointCoef<T>& pc, T uu, T uv, int tile,
+                                                CGShared<T, TILE>& sm, T (*hs2)[TILE + 1], const TagState& ts, T& hu,
+                                                T& hv) {
+  T pu = pc.inu ? uu : (T)0, pv = pc.inv ? uv : (T)0;
+  idwt2d_pair<TILE>(pu, pv, sm.hs, hs2, levels);
+  hu = pc.inner_u ? pu : (T)0;
+  hv = pc.inner_v ? pv : (T)0;
+  publish_boundary<T, TILE>(hu, hv, tile, ts);
+}
+
+// The operator's staging on the fast path: the tile's x (this thread's hu, hv) into shared memory, its
+// one-point halo ring from the neighbours' boxes of exchange ts.hx, and the stresses.  The ring loads are
+// issued first and their tags checked after the 15 x 15 interior stress cells (which need no halo value),
+// so that the L2 round trip overlaps them; then the 4 TILE boundary cells.  Returns false (in every
+// thread) if a wait gave up.
+template <typename T, int TILE>
+__device__ __forceinline__ bool stage_tagged(const Dims& d, const CoefTile<T, TILE>& ct, T hu, T hv, int i0, int j0, int ntx,
+                                             OpTile<T, TILE, TILE>& op, const TagState& ts, GridBar* bar,
+                                             volatile int* fail) {
   constexpr int RING = 4 * TILE + 4;
   __syncthreads();  // the previous use of the tile's shared memory is over
   const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TILE * ty;
-  sm.op.xu[ty + 1][tx + 1] = hu;
-  sm.op.xv[ty + 1][tx + 1] = hv;
-  // halo ring: thread t < 2 RING issues the load of its word now, and checks its tag after the interior
-  // stresses (which need no halo value) so that the L2 round trip overlaps them
+  op.xu[ty + 1][tx + 1] = hu;
+  op.xv[ty + 1][tx + 1] = hv;
   const unsigned tag = ts.base + ts.hx;
   const unsigned long long* src = nullptr;
   int li_r = 0, lj_r = 0, c_r = 0;
@@ -635,13 +645,13 @@ __device__ __forceinline__ bool apply_tagged(const Dims& d, int levels, const Co
       const int ti = i / TILE, tj = j / TILE;
       const int e = li_r == 0 ? 1 : li_r == TILE + 1 ? 0 : lj_r == 0 ? 3 : 2;
       const int k = (li_r == 0 || li_r == TILE + 1) ? j - tj * TILE : i - ti * TILE;
-      src = ts.halo + (size_t)(tj * ntx + ti) * (8 * TILE) + (c_r * 4 + e) * TILE + k;
+      src = ts.box(tj * ntx + ti, TILE) + (c_r * 4 + e) * TILE + k;
       w = ld_relaxed_u64(src);
     }
   }
   __syncthreads();  // the interior of x is in shared memory
   for (int p = t; p < (TILE - 1) * (TILE - 1); p += TILE * TILE)
-    stress_cell_ct(d, ct, i0, j0, sm.op, 1 + p % (TILE - 1), 1 + p / (TILE - 1));
+    stress_cell_ct(d, ct, i0, j0, op, 1 + p % (TILE - 1), 1 + p / (TILE - 1));
   if (t < 2 * RING) {
     T val = 0;
     if (src) {
@@ -658,9 +668,9 @@ __device__ __forceinline__ bool apply_tagged(const Dims& d, int levels, const Co
       val = value_of(w);
     }
     if (c_r == 0)
-      sm.op.xu[lj_r][li_r] = val;
+      op.xu[lj_r][li_r] = val;
     else
-      sm.op.xv[lj_r][li_r] = val;
+      op.xv[lj_r][li_r] = val;
   }
   __syncthreads();
   if (*fail) return false;
@@ -678,23 +688,142 @@ __device__ __forceinline__ bool apply_tagged(const Dims& d, int levels, const Co
       la = (q & 1) ? TILE : 0;
       lb = 1 + (q >> 1);
     }
-    stress_cell_ct(d, ct, i0, j0, sm.op, la, lb);
+    stress_cell_ct(d, ct, i0, j0, op, la, lb);
   }
   __syncthreads();
+  return true;
+}
+
+// (A x) at this thread's u and v points from the staged stresses (stage_out_u / stage_out_v with the
+// coefficients from registers); zero off the interior.
+template <typename T, int TILE>
+__device__ __forceinline__ void out_tagged(const Dims& d, const PointCoef<T>& pc, const OpTile<T, TILE, TILE>& s, T& yu,
+                                           T& yv) {
   const T rdx = rdx_of<T>(d), rdy = rdy_of<T>(d);
-  const OpTile<T, TILE, TILE>& s = sm.op;
-  const int li = tx + 1, lj = ty + 1;
-  T yu = 0, yv = 0;
+  const int li = threadIdx.x + 1, lj = threadIdx.y + 1;
+  yu = 0;
+  yv = 0;
   if (pc.inner_u)
     yu = (s.rxx[lj][li] - s.rxx[lj][li - 1]) * rdx + (s.rxy[lj][li - 1] - s.rxy[lj - 1][li - 1]) * rdy -
          pc.beta_u * s.xu[lj][li] - pc.hm_u * ((s.e[lj][li] - s.e[lj][li - 1]) * rdx);
   if (pc.inner_v)
     yv = (s.ryy[lj][li] - s.ryy[lj - 1][li]) * rdy + (s.rxy[lj - 1][li] - s.rxy[lj - 1][li - 1]) * rdx -
          pc.beta_v * s.xv[lj][li] - pc.hm_v * ((s.e[lj][li] - s.e[lj - 1][li]) * rdy);
+}
+
+// coarse_apply of the fast path: stage_tagged, the operator, the paired Pᵀ.  Returns false (in every
+// thread) if a wait gave up.
+template <typename T, int TILE>
+__device__ __forceinline__ bool apply_tagged(const Dims& d, int levels, const CoefTile<T, TILE>& ct, const PointCoef<T>& pc,
+                                             T hu, T hv, int i0, int j0, int ntx, CGShared<T, TILE>& sm,
+                                             T (*hs2)[TILE + 1], const TagState& ts, GridBar* bar, volatile int* fail,
+                                             T& cu, T& cv) {
+  if (!stage_tagged<T, TILE>(d, ct, hu, hv, i0, j0, ntx, sm.op, ts, bar, fail)) return false;
+  T yu, yv;
+  out_tagged<T, TILE>(d, pc, sm.op, yu, yv);
   idwt2dT_pair<TILE>(yu, yv, sm.hs, hs2, levels);
   cu = pc.wm_u ? yu : (T)0;
   cv = pc.wm_v ? yv : (T)0;
   return true;
+}
+
+// ------------------------------------------------------------------------------------------------
+// The smoother as one persistent launch per pass (FP32, 16 x 16 tiles): gauss_seidel_smoother!
+// (update_preconditioners.jl:133-150), nsweeps sweeps over the four colours, each colour step the Jacobi
+// update x += ω r / diag of that colour's interior points followed by r = b - A x, as the per-step
+// k_smooth launches compute it (the same arithmetic in the same order).  A tile keeps x, r, b and diag
+// in registers and its coefficients in shared memory; after each update it publishes its boundary as
+// tagged words and the operator waits for its neighbours' ring only.  The boxes alternate parity by
+// step: a tile rewrites parity p two steps later, after computing r of the step in between, which needs
+// every neighbour's values of that step, which each neighbour publishes only after it has read this
+// tile's parity-p words.  residual_first: a first step without update (r = b - A x of the input x; r
+// is not read).  order: the four colours of a sweep, 3 bits each.
+// ------------------------------------------------------------------------------------------------
+template <int MAXT>
+struct SmoothShared {
+  OpTile<float, 16, 16> op;
+  CoefTile<float, 16> ct[MAXT];
+  int fail;
+};
+
+template <int MAXT>
+__global__ void __launch_bounds__(256, MAXT <= 2 ? 2 : 1)
+    k_smooth_persistent(Dims d, OpCoef<float> cf, const DevParams* __restrict__ P, const float* __restrict__ b,
+                        const float* __restrict__ diag, float* __restrict__ x, float* __restrict__ r, int residual_first,
+                        int nsweeps, int order, GridBar* bar, unsigned long long* __restrict__ halo, int ntx, int nty) {
+  constexpr int TILE = 16;
+  __shared__ SmoothShared<MAXT> sh;
+  const int ntiles = ntx * nty;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  float xu[MAXT], xv[MAXT], ru[MAXT], rv[MAXT], bu[MAXT], bv[MAXT], du[MAXT], dv[MAXT];
+  int colu[MAXT], colv[MAXT], i0s[MAXT], j0s[MAXT];
+  bool own[MAXT];
+  PointCoef<float> pc[MAXT] = {};
+  TagState ts{halo, 0u, 0u, (size_t)ntiles * 8 * TILE};
+  ts.base = *(volatile unsigned*)&bar->gen << 21;
+  if (tx == 0 && ty == 0) sh.fail = 0;
+  const float omega = (float)P->omega;
+#pragma unroll
+  for (int k = 0; k < MAXT; ++k) {
+    const int t = blockIdx.x + k * gridDim.x;
+    own[k] = t < ntiles;
+    i0s[k] = own[k] ? (t % ntx) * TILE : 0;
+    j0s[k] = own[k] ? (t / ntx) * TILE : 0;
+    if (own[k]) load_coef_tile<float, TILE>(d, cf, cf.inner, i0s[k], j0s[k], sh.ct[k], pc[k]);
+    const int i = i0s[k] + tx, j = j0s[k] + ty;
+    const bool inu = own[k] && pc[k].inu, inv = own[k] && pc[k].inv;
+    const int qu = inu ? uidx(d, i, j) : 0, qv = inv ? vidx(d, i, j) : 0;
+    xu[k] = inu ? x[qu] : 0.f;
+    xv[k] = inv ? x[qv] : 0.f;
+    ru[k] = (inu && !residual_first) ? r[qu] : 0.f;
+    rv[k] = (inv && !residual_first) ? r[qv] : 0.f;
+    bu[k] = inu ? b[qu] : 0.f;
+    bv[k] = inv ? b[qv] : 0.f;
+    du[k] = inu ? diag[qu] : 1.f;
+    dv[k] = inv ? diag[qv] : 1.f;
+    const int par = ((i - j) % 2 + 2) % 2;
+    colu[k] = 1 + par;
+    colv[k] = 3 + par;
+  }
+  const int nsteps = (residual_first ? 1 : 0) + 4 * nsweeps;
+  for (int step = 0; step < nsteps; ++step) {
+    const int sw = step - residual_first;
+    const int colour = sw < 0 ? 0 : (order >> (3 * (sw & 3))) & 7;
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k] && colour) {
+        if (pc[k].inner_u && colu[k] == colour) xu[k] = xu[k] + omega * ru[k] / du[k];
+        if (pc[k].inner_v && colv[k] == colour) xv[k] = xv[k] + omega * rv[k] / dv[k];
+      }
+    ++ts.hx;
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) publish_boundary<float, TILE>(xu[k], xv[k], blockIdx.x + k * gridDim.x, ts);
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        if (!stage_tagged<float, TILE>(d, sh.ct[k], xu[k], xv[k], i0s[k], j0s[k], ntx, sh.op, ts, bar, &sh.fail)) return;
+        float yu, yv;
+        out_tagged<float, TILE>(d, pc[k], sh.op, yu, yv);
+        ru[k] = pc[k].inner_u ? bu[k] - yu : 0.f;
+        rv[k] = pc[k].inner_v ? bv[k] - yv : 0.f;
+      }
+  }
+#pragma unroll
+  for (int k = 0; k < MAXT; ++k)
+    if (own[k]) {
+      const int i = i0s[k] + tx, j = j0s[k] + ty;
+      if (pc[k].inu) {
+        const int q = uidx(d, i, j);
+        x[q] = xu[k];
+        r[q] = ru[k];
+      }
+      if (pc[k].inv) {
+        const int q = vidx(d, i, j);
+        x[q] = xv[k];
+        r[q] = rv[k];
+      }
+    }
 }
 
 // Shared memory of the FP32 fast path: the coefficient tiles, the second Haar buffer, the failure flag.

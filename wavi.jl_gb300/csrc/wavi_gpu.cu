@@ -118,6 +118,9 @@ struct wavi_ctx {
   GridBar* bar = nullptr;
   // halo boxes of the FP32 register-resident coarse CG: 8 x tile tagged words per tile
   unsigned long long* halo_box = nullptr;
+  // the FP32 persistent smoother (one launch per pass): usable here, and its halo boxes (2 parities)
+  bool fused_smooth = false;
+  unsigned long long* smooth_box = nullptr;
   unsigned long long* selftest = nullptr;  // [0]: a tagged word nothing writes, [1]: the self-test's result
   int pers_maxt = 0, pers_grid = 0, ntx = 0, nty = 0;  // pers_maxt -1: CG vectors in global memory
   void *gz = nullptr, *gw = nullptr;                    // extra vectors of the global-memory variant
@@ -292,6 +295,55 @@ int launch_op(wavi_ctx* c, const T* x, T* y) {
   return 0;
 }
 
+// The persistent smoother runs on the coarse CG's cooperative grid (pers_grid CTAs of pers_maxt tiles):
+// it is used where that grid is resident for it too.
+bool smoother_fits(wavi_ctx* c) {
+  if (c->pers_maxt <= 0) return false;
+  int nsm = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
+  cudaError_t e = c->pers_maxt == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_persistent<1>, 256, 0)
+                  : c->pers_maxt == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_persistent<2>, 256, 0)
+                                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_smooth_persistent<4>, 256, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return (long)per_sm * nsm / std::max(1, c->pers_share) >= c->pers_grid;
+}
+
+// One smoother pass as one cooperative launch (k_smooth_persistent): a fresh tag generation, the pass,
+// and the watchdog check.  x and r in place; residual_first: r = b - A x before the sweeps.
+int launch_smooth_fused(wavi_ctx* c, const CondHandles& h, bool residual_first, int order, const float* b,
+                        const float* diag, float* x, float* r) {
+  k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar, (const DevParams*)c->P);
+  CKL();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)c->pers_grid);
+  cfg.blockDim = dim3(16, 16);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c->st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const int rf = residual_first ? 1 : 0, ns = c->sp.nsmooth;
+  const DevParams* P = (const DevParams*)c->P;
+  if (c->pers_maxt == 1)
+    CK(cudaLaunchKernelEx(&cfg, k_smooth_persistent<1>, c->d, coef<float>(c), P, b, diag, x, r, rf, ns, order, c->bar,
+                          c->smooth_box, c->ntx, c->nty));
+  else if (c->pers_maxt == 2)
+    CK(cudaLaunchKernelEx(&cfg, k_smooth_persistent<2>, c->d, coef<float>(c), P, b, diag, x, r, rf, ns, order, c->bar,
+                          c->smooth_box, c->ntx, c->nty));
+  else
+    CK(cudaLaunchKernelEx(&cfg, k_smooth_persistent<4>, c->d, coef<float>(c), P, b, diag, x, r, rf, ns, order, c->bar,
+                          c->smooth_box, c->ntx, c->nty));
+  c->launches++;
+  k_check_barrier<<<1, 32, 0, c->st>>>(c->bar, c->S, h);
+  CKL();
+  return 0;
+}
+
 template <typename T, int TILE>
 int enqueue_vcycle_pre(wavi_ctx* c, const CondHandles& h, Tally& t, bool cg_start = true) {
   const Dims& d = c->d;
@@ -306,14 +358,23 @@ int enqueue_vcycle_pre(wavi_ctx* c, const CondHandles& h, Tally& t, bool cg_star
   t.launches++;
   static const int fwd[4] = {1, 3, 2, 4};
   int cur = 0;
-  for (int it = 0; it < c->sp.nsmooth; ++it)
-    for (int oc = 0; oc < 4; ++oc) {
-      TRY(launch_smooth<T>(c, true, fwd[oc], rs, diag, corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]));
-      cur = 1 - cur;
-      t.launches++;
-      t.ops++;
-      t.bytes += op_bytes(d, sizeof(T), true) + 4.0 * sizeof(T) * d.N;
+  if constexpr (std::is_same<T, float>::value && TILE == 16) {
+    if (c->fused_smooth) {  // the whole pass in one cooperative launch, in place in corr[0], rsm[0]
+      TRY(launch_smooth_fused(c, h, false, fwd[0] | fwd[1] << 3 | fwd[2] << 6 | fwd[3] << 9, rs, diag, corr[0], rsm[0]));
+      t.launches += 3;
+      t.ops += 4 * c->sp.nsmooth;
+      t.bytes += 4.0 * c->sp.nsmooth * (op_bytes(d, sizeof(T), true) + 4.0 * sizeof(T) * d.N);
     }
+  }
+  if (!(std::is_same<T, float>::value && TILE == 16 && c->fused_smooth))
+    for (int it = 0; it < c->sp.nsmooth; ++it)
+      for (int oc = 0; oc < 4; ++oc) {
+        TRY(launch_smooth<T>(c, true, fwd[oc], rs, diag, corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]));
+        cur = 1 - cur;
+        t.launches++;
+        t.ops++;
+        t.bytes += op_bytes(d, sizeof(T), true) + 4.0 * sizeof(T) * d.N;
+      }
   // b_c = R r  and |b_c|
   k_restrict_norm<T, TILE><<<c->tile_grid, c->tile_block, 0, c->st>>>(d, L, rsm[cur], c->wmask_uv, (T*)c->bc,
                                                                       c->partials, c->S);
@@ -465,20 +526,33 @@ int enqueue_vcycle_post(wavi_ctx* c, const CondHandles& h, Tally& t) {
                                                                    nullptr, c->S, nullptr);
   CKL();
   // r = b - A corr, then the sweeps in reversed colour order
-  TRY(launch_smooth<T>(c, false, 0, rs, diag, corr[0], nullptr, nullptr, rsm[0]));
-  t.launches += 2;
-  t.ops++;
-  t.bytes += op_bytes(d, sizeof(T), true) + 3.0 * sizeof(T) * d.N;
   static const int bwd[4] = {4, 2, 3, 1};
   int cur = 0;
-  for (int it = 0; it < c->sp.nsmooth; ++it)
-    for (int oc = 0; oc < 4; ++oc) {
-      TRY(launch_smooth<T>(c, true, bwd[oc], rs, diag, corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]));
-      cur = 1 - cur;
-      t.launches++;
-      t.ops++;
-      t.bytes += op_bytes(d, sizeof(T), true) + 4.0 * sizeof(T) * d.N;
+  bool fused = false;
+  if constexpr (std::is_same<T, float>::value && TILE == 16) {
+    if (c->fused_smooth) {  // the residual and the whole pass in one cooperative launch, in place
+      TRY(launch_smooth_fused(c, h, true, bwd[0] | bwd[1] << 3 | bwd[2] << 6 | bwd[3] << 9, rs, diag, corr[0], rsm[0]));
+      t.launches += 4;
+      t.ops += 1 + 4 * c->sp.nsmooth;
+      t.bytes += op_bytes(d, sizeof(T), true) + 3.0 * sizeof(T) * d.N +
+                 4.0 * c->sp.nsmooth * (op_bytes(d, sizeof(T), true) + 4.0 * sizeof(T) * d.N);
+      fused = true;
     }
+  }
+  if (!fused) {
+    TRY(launch_smooth<T>(c, false, 0, rs, diag, corr[0], nullptr, nullptr, rsm[0]));
+    t.launches += 2;
+    t.ops++;
+    t.bytes += op_bytes(d, sizeof(T), true) + 3.0 * sizeof(T) * d.N;
+    for (int it = 0; it < c->sp.nsmooth; ++it)
+      for (int oc = 0; oc < 4; ++oc) {
+        TRY(launch_smooth<T>(c, true, bwd[oc], rs, diag, corr[cur], rsm[cur], corr[1 - cur], rsm[1 - cur]));
+        cur = 1 - cur;
+        t.launches++;
+        t.ops++;
+        t.bytes += op_bytes(d, sizeof(T), true) + 4.0 * sizeof(T) * d.N;
+      }
+  }
   k_vcycle_finish<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, corr[cur], (const T*)c->xc, c->x64, c->uv,
                                                              c->xc_full64, c->partials, c->S);
   CKL();
@@ -1359,6 +1433,10 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   if ((r = dalloc(c, &c->selftest, 2))) return bail(r);
   if (c->pers_maxt > 0) {
     if ((r = dalloc(c, &c->halo_box, (size_t)c->ntx * c->nty * 8 * c->tile))) return bail(r);
+    if (mixed(c) && c->tile == 16 && !c->stream_op && smoother_fits(c)) {
+      if ((r = dalloc(c, &c->smooth_box, (size_t)2 * c->ntx * c->nty * 8 * 16))) return bail(r);
+      c->fused_smooth = true;
+    }
   }
   {
     double* q = nullptr;
