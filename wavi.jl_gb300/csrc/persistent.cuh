@@ -145,7 +145,7 @@ struct SyncShared {
 };
 
 // Grid-wide barrier over gridDim.x CTAs.  v[0..NS) are this thread's terms (type A: float or double);
-// they are summed over the warp in A, over the CTA and the grid in S = CGReal<A> (double, or float-float
+// they are summed over the warp and the CTA in A, over the grid in S = CGReal<A> (double, or float-float
 // for float), and after the barrier tot[0..NS) (type S, in shared memory) hold the grid sums and
 // `scalars(tot)` has run in thread 0 (it derives the CG scalars once per CTA); the barrier ends with a
 // __syncthreads, so its results are visible to the whole CTA.  `epoch` counts this thread's barriers
@@ -183,10 +183,21 @@ __device__ __forceinline__ bool grid_sync(GridBar* bar, double* __restrict__ par
     // of equal l%4 (the same order in every CTA)
     const int q = lane & 3;
     S s{};
-    if (q < NS)
-      for (int k = lane >> 2; k < nw; k += 8) s = s + wsum[k][q];
+    if constexpr (std::is_same<A, float>::value) {
+      // FP32 kernels: the CTA's eight warp sums in FP32 as well (float-float from the CTA partials on;
+      // measured 1.7 % faster per solve than a float-float CTA sum)
+      float f = 0.f;
+      if (q < NS)
+        for (int k = lane >> 2; k < nw; k += 8) f += wsum[k][q].hi;
 #pragma unroll
-    for (int o = 4; o < 32; o <<= 1) s = s + shfl_xor(s, o);
+      for (int o = 4; o < 32; o <<= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
+      s = real_term(f);
+    } else {
+      if (q < NS)
+        for (int k = lane >> 2; k < nw; k += 8) s = s + wsum[k][q];
+#pragma unroll
+      for (int o = 4; o < 32; o <<= 1) s = s + shfl_xor(s, o);
+    }
     if (lane < NS) slot[lane * nb + blockIdx.x] = s;
     __syncwarp();
   }
