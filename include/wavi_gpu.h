@@ -110,11 +110,16 @@ typedef struct wavi_options {
  * compute both inner products of an iteration in one grid reduction, keep cg!'s stopping rule on the
  * unpreconditioned residual, and need the persistent coarse kernel. */
 typedef enum wavi_coarse_solver {
-  WAVI_COARSE_AUTO = 0,              /* FP64: cg!; mixed: SRCG_JACOBI when the persistent kernel fits and
-                                        the ice mask covers the whole domain, else cg! */
+  WAVI_COARSE_AUTO = 0,              /* FP64: cg!; mixed: SRCG_CHEBYSHEV when the ice mask covers the whole
+                                        domain (SRCG_JACOBI where only the global-memory persistent kernel
+                                        fits), else cg! */
   WAVI_COARSE_CG = 1,                /* the reference's cg! recurrence */
   WAVI_COARSE_SRCG = 2,              /* single-reduction CG, no preconditioner (same iterates as cg!) */
-  WAVI_COARSE_SRCG_JACOBI = 3        /* single-reduction CG preconditioned by diag(R A P) */
+  WAVI_COARSE_SRCG_JACOBI = 3,       /* single-reduction CG preconditioned by diag(R A P) */
+  WAVI_COARSE_SRCG_CHEBYSHEV = 4     /* single-reduction CG preconditioned by 3 Chebyshev-accelerated Jacobi
+                                        steps on [b/120, b], b = 1.15 lambda_max(diag(R A P)^-1 R A P) from
+                                        power steps each V-cycle (12 in a solve's first, then 4, warm-
+                                        started); register-resident persistent kernel only */
 } wavi_coarse_solver;
 
 /* The model fields the velocity solve reads and writes (src/Models/update_velocities.jl:202-383,

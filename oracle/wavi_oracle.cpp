@@ -301,6 +301,8 @@ struct Model {
   long last_cg_iters = 0;
   long op_applies = 0;
   std::vector<int> cg_iter_history;
+  Vec cheb_eig;           // coarse variant 4: the power vector (full wavelet layout, u then v), per solve
+  int cheb_vcycles = 0;   // coarse variant 4: V-cycles so far in this solve
   std::string err;
 };
 
@@ -831,6 +833,7 @@ int coarse_cg(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, doubl
 //      systems", J. Comput. Appl. Math. 25 (1989)): the same Krylov iterates in exact arithmetic, with
 //      the two inner products of an iteration computed together after its operator application
 //   3  the same, preconditioned by the Jacobi diagonal of R A P
+//   4  the same, preconditioned by Chebyshev-accelerated Jacobi steps (coarse_srcg_chebyshev)
 // ---------------------------------------------------------------------------------------------
 int g_coarse_variant = 0;
 
@@ -909,6 +912,91 @@ int coarse_srcg(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, dou
   return it;
 }
 
+// Variant 4: coarse_srcg with M⁻¹ r replaced by CHEB_STEPS steps of the Chebyshev-accelerated Jacobi
+// iteration on D⁻¹ R A P z = D⁻¹ r from z = 0 (D = diag(R A P)), on the interval [b / CHEB_RATIO, b],
+// b = 1.15 λmax(D⁻¹ R A P).  λmax by power steps (12 in a solve's first V-cycle, then 4) from the
+// previous V-cycle's vector (zero at a solve's start) plus 1e-3 times a fixed hash of the full index.
+// The GPU library's WAVI_COARSE_SRCG_CHEBYSHEV with its constants, in the same order of operations.
+constexpr int CHEB_STEPS = 3;
+constexpr double CHEB_RATIO = 120.0;
+static float cheb_start(int q) {  // in [-1, 1)
+  const unsigned h = (unsigned)q * 2654435761u;
+  return (float)((h >> 8) & 0xffffu) * (1.0f / 32768.0f) - 1.0f;
+}
+int coarse_srcg_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, double abstol, int maxiter) {
+  const size_t n = b.size(), nu = p.wu_idx.size();
+  Vec d = coarse_diag(m, w, p), minv(n);
+  for (size_t i = 0; i < n; ++i) minv[i] = d[i] != 0.0 ? 1.0 / d[i] : 0.0;
+  auto full = [&](size_t k) { return k < nu ? p.wu_idx[k] : m.Nu + p.wv_idx[k - nu]; };
+  Vec v(n), t;
+  for (size_t k = 0; k < n; ++k) v[k] = minv[k] != 0.0 ? m.cheb_eig[full(k)] + 1e-3 * (double)cheb_start(full(k)) : 0.0;
+  ++m.cheb_vcycles;
+  const int npow = m.cheb_vcycles <= 1 ? 12 : 4;
+  double th = 1.0, de = 1.0, sg = 1.0;
+  for (int ps = 0; ps < npow; ++ps) {
+    op_coarse(m, w, p, v, t);
+    for (size_t k = 0; k < n; ++k) t[k] = minv[k] * t[k];
+    const double tt = dotp(t, t), vv = dotp(v, v);
+    const double lam = (vv > 0.0 && tt > 0.0) ? std::sqrt(tt / vv) : 1.0;
+    const double bmax = 1.15 * lam, amin = bmax / CHEB_RATIO;
+    th = 0.5 * (bmax + amin);
+    de = 0.5 * (bmax - amin);
+    sg = (bmax + amin) / (bmax - amin);
+    const double nrm = tt > 0.0 ? 1.0 / std::sqrt(tt) : 0.0;
+    for (size_t k = 0; k < n; ++k) v[k] = t[k] * nrm;
+  }
+  for (size_t k = 0; k < n; ++k) m.cheb_eig[full(k)] = v[k];
+  auto prec = [&](const Vec& r, Vec& z) {
+    z.resize(n);
+    Vec dd(n), tt2;
+    for (size_t k = 0; k < n; ++k) {
+      z[k] = minv[k] * r[k];
+      z[k] = z[k] / th;
+      dd[k] = z[k];
+    }
+    double rho = 1.0 / sg;
+    for (int st = 1; st < CHEB_STEPS; ++st) {
+      op_coarse(m, w, p, z, tt2);
+      const double rn = 1.0 / (2.0 * sg - rho), c1 = rn * rho, c2 = 2.0 * rn / de;
+      for (size_t k = 0; k < n; ++k) {
+        dd[k] = c1 * dd[k] + c2 * (minv[k] * (r[k] - tt2[k]));
+        z[k] = z[k] + dd[k];
+      }
+      rho = rn;
+    }
+  };
+  Vec c, r = b, z, wv;
+  op_coarse(m, w, p, x, c);
+  for (size_t i = 0; i < n; ++i) r[i] -= c[i];
+  prec(r, z);
+  op_coarse(m, w, p, z, wv);
+  double gamma = dotp(r, z), delta = dotp(wv, z), res = norm2(r);
+  const double reltol = std::sqrt(2.220446049250313e-16);
+  const double tol = std::max(reltol * res, abstol);
+  Vec pp = z, s = wv;
+  double alpha = gamma / delta;
+  int it = 0;
+  bool stop = it >= maxiter || res <= tol || !(res == res) || !(alpha == alpha) || std::isinf(alpha);
+  while (!stop) {
+    for (size_t i = 0; i < n; ++i) x[i] += alpha * pp[i];
+    for (size_t i = 0; i < n; ++i) r[i] -= alpha * s[i];
+    prec(r, z);
+    op_coarse(m, w, p, z, wv);
+    ++it;
+    const double g2 = dotp(r, z), d2 = dotp(wv, z);
+    res = norm2(r);
+    stop = it >= maxiter || res <= tol || !(res == res);
+    if (stop) break;
+    const double beta = g2 / gamma;
+    alpha = g2 / (d2 - beta * g2 / alpha);
+    gamma = g2;
+    if (!(alpha == alpha) || std::isinf(alpha)) break;
+    for (size_t i = 0; i < n; ++i) pp[i] = z[i] + beta * pp[i];
+    for (size_t i = 0; i < n; ++i) s[i] = wv[i] + beta * s[i];
+  }
+  return it;
+}
+
 // gauss_seidel_smoother! (4-colour Jacobi with a full residual after each colour)   :133-150
 void smoother(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, const int* order) {
   Vec r;
@@ -932,9 +1020,9 @@ void vcycle(Model& m, OpWork& w, Precond& p, Vec& x, const Vec& b) {
   Vec bc;
   restrict_vec(m, p, r, bc);
   double abstol = m.S.tol_coarse * norm2(bc);
-  p.last_cg = g_coarse_variant == 0
-                  ? coarse_cg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
-                  : coarse_srcg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse, g_coarse_variant == 3);
+  p.last_cg = g_coarse_variant == 0   ? coarse_cg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
+              : g_coarse_variant == 4 ? coarse_srcg_chebyshev(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
+                                      : coarse_srcg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse, g_coarse_variant == 3);
   Vec pc;
   prolong_vec(m, p, p.corr, pc);
   for (size_t i = 0; i < x.size(); ++i) x[i] = x[i] + pc[i];
@@ -995,6 +1083,8 @@ void update_velocities(Model& m) {
   double rel = INFINITY;
   m.last_cg_iters = 0;
   m.cg_iter_history.clear();
+  m.cheb_eig.assign((size_t)(m.Nu + m.Nv), 0.0);
+  m.cheb_vcycles = 0;
   while (!converged && it < m.S.maxiter_picard) {
     ++it;
     inner_update(m);

@@ -64,8 +64,11 @@ def test_coarse_diagonal_matches_oracle(oracle, name):
         s.close()
 
 
-@pytest.mark.parametrize("kernel", ["persistent", "persistent_global"])
-@pytest.mark.parametrize("solver", ["srcg", "srcg_jacobi"])
+KERNEL_SOLVERS = [("persistent", "srcg"), ("persistent", "srcg_jacobi"), ("persistent", "srcg_chebyshev"),
+                  ("persistent_global", "srcg"), ("persistent_global", "srcg_jacobi")]
+
+
+@pytest.mark.parametrize("kernel,solver", KERNEL_SOLVERS)
 @pytest.mark.parametrize("name", list(CASES))
 def test_single_reduction_fixed_cg_count_matches_oracle(oracle, reference_cg, name, solver, kernel):
     """One Picard iteration whose coarse solve runs exactly 10 single-reduction iterations (tol_coarse = 0),
@@ -90,8 +93,7 @@ def test_single_reduction_fixed_cg_count_matches_oracle(oracle, reference_cg, na
     s.close()
 
 
-@pytest.mark.parametrize("kernel", ["persistent", "persistent_global"])
-@pytest.mark.parametrize("solver", ["srcg", "srcg_jacobi"])
+@pytest.mark.parametrize("kernel,solver", KERNEL_SOLVERS)
 @pytest.mark.parametrize("name", list(CASES))
 def test_single_reduction_converged_solve_matches_reference(oracle, name, solver, kernel):
     """The single-reduction coarse solves change the V-cycle, not the fixed point: converged FP64 and mixed
@@ -110,8 +112,27 @@ def test_single_reduction_converged_solve_matches_reference(oracle, name, solver
         st = s.solve(p, f)
         assert st["status"] == 0, (prec, st)
         assert uv_err(f, om) < 1e-6, (prec, st, ost)
-        if name == "full" and solver == "srcg_jacobi":  # on ice-shelf discs the masked coarse space blunts the Jacobi gain
+        if name == "full" and solver in ("srcg_jacobi", "srcg_chebyshev"):  # (masked coarse spaces blunt the gain)
             assert st["coarse_cg_iterations"] < ost["coarse_cg_iterations"], (prec, st, ost)
+        s.close()
+
+
+def test_chebyshev_needs_the_register_resident_kernel(oracle):
+    from wavi_gb300.abi import WaviError
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, "full")
+    with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):
+        VelocitySolver(g, sp, precision="mixed", coarse_kernel="persistent_global", coarse_solver="srcg_chebyshev")
+
+
+def test_mixed_default_is_chebyshev_on_full_masks(oracle):
+    from wavi_gb300.gpu import VelocitySolver
+    for name, want in (("full", "srcg_chebyshev"), ("disc", "cg")):
+        g, p, sp, om = _setup(oracle, name, maxiter_picard=2)
+        f = fields_from_oracle(om, g)
+        s = VelocitySolver(g, sp, precision="mixed")
+        st = s.solve(p, f)
+        assert st["coarse_solver"] == want, (name, st)
         s.close()
 
 
@@ -119,7 +140,7 @@ def test_single_reduction_solvers_need_the_persistent_kernel(oracle):
     from wavi_gb300.abi import WaviError
     from wavi_gb300.gpu import VelocitySolver
     g, p, sp, om = _setup(oracle, "full")
-    for solver in ("srcg", "srcg_jacobi"):
+    for solver in ("srcg", "srcg_jacobi", "srcg_chebyshev"):
         with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):
             VelocitySolver(g, sp, precision="mixed", coarse_kernel="iterations", coarse_solver=solver)
     # auto falls back to the reference recurrence with per-iteration kernels

@@ -67,7 +67,7 @@ def test_probed_coarse_diagonal_is_exact(oracle, shape):
     assert np.all(d[off] == 0.0)
 
 
-@pytest.mark.parametrize("variant", ["srcg", "srcg_jacobi"])
+@pytest.mark.parametrize("variant", ["srcg", "srcg_jacobi", "srcg_chebyshev"])
 def test_single_reduction_coarse_solves_reach_the_reference_fixed_point(oracle, reference_cg, variant):
     from wavi_gb300 import synthetic
     sols = {}
@@ -85,3 +85,5 @@ def test_single_reduction_coarse_solves_reach_the_reference_fixed_point(oracle, 
     assert err < 1e-6
     if variant == "srcg_jacobi":  # the preconditioner must pay for itself
         assert s1["coarse_cg_iterations"] < 0.75 * s0["coarse_cg_iterations"]
+    if variant == "srcg_chebyshev":  # two more operator applications per iteration: at least 3x fewer iterations
+        assert s1["coarse_cg_iterations"] < s0["coarse_cg_iterations"] / 3

@@ -847,6 +847,13 @@ struct FastShared {
 template <typename T, int TILE, int MAXT>
 using FastSharedFor = typename std::conditional<std::is_same<T, float>::value && TILE == 16, FastShared<T, TILE, MAXT>, char>::type;
 
+// The fixed perturbation of the power iteration's start vector at full-layout index q: a value in [-1, 1)
+// from a multiplicative hash (the oracle's coarse_srcg_chebyshev uses the same).
+__device__ __forceinline__ float cheb_start(int q) {
+  const unsigned h = (unsigned)q * 2654435761u;
+  return (float)((h >> 8) & 0xffffu) * (1.0f / 32768.0f) - 1.0f;
+}
+
 // CG scalars broadcast to the CTA (written by thread 0 inside grid_sync).  R = CGReal<T>: the FP64
 // kernels keep the reference's FP64 scalars; the FP32 kernels keep squared norms and the recurrence
 // scalars in float-float (no FP64 arithmetic per iteration; res and tol are FP64, set once per solve).
@@ -1119,13 +1126,15 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
 //   β = γ/γ';  α = γ/(δ - β γ/α');  p = z + β p;  s = w + β s
 // In FP32 this form keeps the attainable accuracy of standard CG (unlike the pipelined variants, whose
 // recursively updated residual drifts by ~1e-3 in FP32).  The oracle's coarse_srcg states the same
-// iteration in FP64.
+// iteration in FP64.  cheb > 1 replaces M⁻¹ by the Chebyshev-accelerated Jacobi iteration (precond
+// below): cheb - 1 more operator applications per iteration and ~0.4 of the iterations (and grid
+// reductions) for cheb = 3 on the channel workloads.
 template <typename T, int TILE, int MAXT>
 __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
     k_srcg_persistent(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, const T* __restrict__ dcoarse,
                       T* __restrict__ w, const T* __restrict__ bc, T* __restrict__ xc, double* __restrict__ partials,
-                      DevState* st, const DevParams* __restrict__ P, GridBar* bar, unsigned long long* __restrict__ halo, int ntx,
-                    int nty) {
+                      DevState* st, const DevParams* __restrict__ P, GridBar* bar, unsigned long long* __restrict__ halo,
+                      int cheb, float cheb_ratio, T* __restrict__ eig, int ntx, int nty) {
   __shared__ CGShared<T, TILE> sm;
   __shared__ SyncShared ss;
   __shared__ CGScalars<T> sc;
@@ -1135,6 +1144,8 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
   const int tx = threadIdx.x, ty = threadIdx.y;
   T xu[MAXT], xv[MAXT], ru[MAXT], rv[MAXT], zu[MAXT], zv[MAXT], wu[MAXT], wv[MAXT];
   T pu[MAXT], pv[MAXT], su[MAXT], sv[MAXT], iu[MAXT], iv[MAXT];  // iu, iv: M⁻¹ (0 off the coarse space)
+  T cdu[MAXT], cdv[MAXT];  // Chebyshev direction (cheb > 1)
+  __shared__ T cheb_s[3];  // θ, δ, σ of the Chebyshev interval
   int i0s[MAXT], j0s[MAXT];
   bool own[MAXT];
 #pragma unroll
@@ -1154,7 +1165,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
     } else {
       iu[k] = iv[k] = (T)1;
     }
-    ru[k] = rv[k] = zu[k] = zv[k] = wu[k] = wv[k] = pu[k] = pv[k] = su[k] = sv[k] = (T)0;
+    ru[k] = rv[k] = zu[k] = zv[k] = wu[k] = wv[k] = pu[k] = pv[k] = su[k] = sv[k] = cdu[k] = cdv[k] = (T)0;
   }
   unsigned epoch = 0;
   int it = 0;
@@ -1162,7 +1173,8 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
   const double tol_coarse = P->tol_coarse;
   constexpr bool kFast = !std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value;
   T hu[MAXT], hv[MAXT];  // fast path: the tiles' prolonged vectors (inner ⊙ P u)
-  TagState ts{halo, 0u, 0u};
+  // two box sets (by exchange parity): the Chebyshev steps exchange without a grid reduction in between
+  TagState ts{halo, 0u, 0u, (size_t)ntiles * 8 * TILE};
   volatile int* fail = nullptr;
   if constexpr (kFast) {
     ts.base = *(volatile unsigned*)&bar->gen << 21;
@@ -1197,6 +1209,104 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
       return true;
     }
   };
+  // z = M⁻¹ r: Jacobi, or (cheb > 1) the Jacobi-preconditioned Chebyshev iteration of cheb steps on
+  // D⁻¹ R A P z = D⁻¹ r from z = 0 (a fixed polynomial in D⁻¹ R A P times D⁻¹, symmetric positive
+  // definite for any interval when cheb is odd), cheb - 1 operator applications and no reduction
+  auto precond = [&]() -> bool {
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k) {
+      zu[k] = iu[k] * ru[k];
+      zv[k] = iv[k] * rv[k];
+    }
+    if (cheb <= 1) return true;
+    const T th = cheb_s[0], de = cheb_s[1], sg = cheb_s[2];
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k) {
+      zu[k] = zu[k] / th;
+      zv[k] = zv[k] / th;
+      cdu[k] = zu[k];
+      cdv[k] = zv[k];
+    }
+    T rho = (T)1 / sg;
+    for (int stp = 1; stp < cheb; ++stp) {
+      ++ts.hx;  // a new exchange
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k)
+        if (own[k]) prolong(k, zu[k], zv[k]);
+      if (!halo_ready()) return false;
+      const T rn = (T)1 / ((T)2 * sg - rho), c1 = rn * rho, c2 = (T)2 * rn / de;
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k)
+        if (own[k]) {
+          T tu, tv;
+          if (!apply(k, tu, tv)) return false;
+          cdu[k] = c1 * cdu[k] + c2 * (iu[k] * (ru[k] - tu));
+          cdv[k] = c1 * cdv[k] + c2 * (iv[k] * (rv[k] - tv));
+          zu[k] = zu[k] + cdu[k];
+          zv[k] = zv[k] + cdv[k];
+        }
+      rho = rn;
+    }
+    return true;
+  };
+  if (cheb > 1) {
+    // λmax of D⁻¹ R A P by power steps from the previous V-cycle's vector (eig, zeroed at each solve's
+    // start) plus a small fixed perturbation: 12 in a solve's first V-cycle, 4 after it; the interval
+    // [b / cheb_ratio, b], b = 1.15 λmax
+    T eu[MAXT], ev[MAXT];
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k) {
+      const int i = i0s[k] + tx, j = j0s[k] + ty;
+      const bool inu = own[k] && i <= d.nx && j < d.ny, inv = own[k] && i < d.nx && j <= d.ny;
+      const int qu = inu ? uidx(d, i, j) : 0, qv = inv ? vidx(d, i, j) : 0;
+      eu[k] = iu[k] != (T)0 ? eig[qu] + (T)1e-3 * cheb_start(qu) : (T)0;
+      ev[k] = iv[k] != (T)0 ? eig[qv] + (T)1e-3 * cheb_start(qv) : (T)0;
+    }
+    const int npow = st->picard_it <= 1 ? 12 : 4;
+    for (int pstep = 0; pstep < npow; ++pstep) {
+      ++ts.hx;  // a new exchange
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k)
+        if (own[k]) prolong(k, eu[k], ev[k]);
+      if (!halo_ready()) return;
+      T a2[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k)
+        if (own[k]) {
+          T tu, tv;
+          if (!apply(k, tu, tv)) return;
+          tu = iu[k] * tu;
+          tv = iv[k] * tv;
+          a2[0] += tu * tu + tv * tv;
+          a2[1] += eu[k] * eu[k] + ev[k] * ev[k];
+          eu[k] = tu;
+          ev[k] = tv;
+        }
+      if (!grid_sync<2>(bar, partials, epoch, ss, a2, [&](const typename CGReal<T>::type* tot) {
+            const double tt = dbl_of(tot[0]), vv = dbl_of(tot[1]);
+            const double lam = (vv > 0.0 && tt > 0.0) ? sqrt(tt / vv) : 1.0;
+            const double bmax = 1.15 * lam, amin = bmax / (double)cheb_ratio;
+            cheb_s[0] = (T)(0.5 * (bmax + amin));
+            cheb_s[1] = (T)(0.5 * (bmax - amin));
+            cheb_s[2] = (T)((bmax + amin) / (bmax - amin));
+            sc.alpha_t = (T)(tt > 0.0 ? 1.0 / sqrt(tt) : 0.0);  // the normalisation of the power vector
+          }))
+        return;
+      const T nrm = sc.alpha_t;
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k) {
+        eu[k] = eu[k] * nrm;
+        ev[k] = ev[k] * nrm;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        const int i = i0s[k] + tx, j = j0s[k] + ty;
+        if (i <= d.nx && j < d.ny) eig[uidx(d, i, j)] = eu[k];
+        if (i < d.nx && j <= d.ny) eig[vidx(d, i, j)] = ev[k];
+      }
+  }
   // r = b_c - R A P xc;  z = M⁻¹ r
   ++ts.hx;  // a new exchange
 #pragma unroll
@@ -1215,9 +1325,8 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
       ru[k] = bu - cu;
       rv[k] = bv - cv;
       bb += bu * bu + bv * bv;
-      zu[k] = iu[k] * ru[k];
-      zv[k] = iv[k] * rv[k];
     }
+  if (!precond()) return;
   // (every CTA has read the prolonged vector, from w or from the halo boxes: the barrier below orders the
   // rewrite)
   if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
@@ -1232,9 +1341,8 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
           xv[k] = fmul_add(alpha, pv[k], xv[k]);
           ru[k] = fmul_add(-alpha, su[k], ru[k]);
           rv[k] = fmul_add(-alpha, sv[k], rv[k]);
-          zu[k] = iu[k] * ru[k];
-          zv[k] = iv[k] * rv[k];
         }
+      if (!precond()) return;
       ++it;
     }
     // w = R A P z
@@ -1765,13 +1873,13 @@ static __global__ void k_selftest_wait(GridBar* bar, const unsigned long long* _
 
 // Before a persistent CG: an idle barrier (count 0, no error).
 // Before each persistent launch: restart the arrival counter, clear the error, and advance the tag
-// generation past every tag the previous launch can have written (at most maxiter_coarse + 2 tagged
-// exchanges; 2^21 tags per generation step).
+// generation past every tag the previous launch can have written (at most ~cheb (maxiter_coarse + 1) + 5
+// tagged exchanges, cheb <= 8; 2^21 tags per generation step).
 static __global__ void k_reset_barrier(GridBar* bar, const DevParams* __restrict__ P) {
   if (threadIdx.x == 0) {
     bar->count = 0u;
     bar->err = 0;
-    bar->gen += 1u + ((unsigned)max(P->maxiter_coarse, 0) >> 20);
+    bar->gen += 1u + ((unsigned)max(P->maxiter_coarse, 0) >> 16);
   }
 }
 

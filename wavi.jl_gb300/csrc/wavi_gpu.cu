@@ -126,6 +126,7 @@ struct wavi_ctx {
   void *gz = nullptr, *gw = nullptr;                    // extra vectors of the global-memory variant
   int coarse_solver = WAVI_COARSE_CG;  // resolved coarse solver (never WAVI_COARSE_AUTO)
   void* dcoarse = nullptr;             // diag(R A P) for the Jacobi-preconditioned single-reduction CG
+  void* cheb_eig = nullptr;            // the Chebyshev coarse solve's power vector (kept across V-cycles)
   // coarse-correction cache mapping: block offsets of the mask scan (u part, then v part from
   // mask_offsets_v), staging for host callers, and the host masks' counts
   int* mask_offsets = nullptr;
@@ -420,6 +421,12 @@ int enqueue_cg_iteration(wavi_ctx* c, const CondHandles& h, int* live, Tally& t)
 }
 
 // The whole coarse CG as one cooperative persistent kernel (persistent.cuh), then the watchdog check.
+// The Chebyshev coarse solve: steps of the Chebyshev-accelerated Jacobi iteration per preconditioner
+// application (odd: the preconditioner stays positive definite if λmax is underestimated) and the ratio
+// of the interval's ends.
+constexpr int kChebSteps = 3;
+constexpr float kChebRatio = 120.0f;
+
 template <typename T, int TILE, int MAXT>
 int launch_cg_persistent(wavi_ctx* c) {
   const Dims& d = c->d;
@@ -438,10 +445,11 @@ int launch_cg_persistent(wavi_ctx* c) {
                           (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
                           c->halo_box, c->ntx, c->nty));
   } else {
-    const T* dc = c->coarse_solver == WAVI_COARSE_SRCG_JACOBI ? (const T*)c->dcoarse : nullptr;
+    const bool cheb = c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV;
+    const T* dc = (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI || cheb) ? (const T*)c->dcoarse : nullptr;
     CK(cudaLaunchKernelEx(&cfg, k_srcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
                           dc, (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
-                          c->halo_box, c->ntx, c->nty));
+                          c->halo_box, cheb ? kChebSteps : 1, kChebRatio, (T*)c->cheb_eig, c->ntx, c->nty));
   }
   c->launches++;
   return 0;
@@ -488,7 +496,7 @@ void launch_coarse_diag(wavi_ctx* c, T* dst) {
 template <typename T, int TILE>
 int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& tc) {
   const Dims& d = c->d;
-  if (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI) {
+  if (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI || c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV) {
     launch_coarse_diag<T, TILE>(c, (T*)c->dcoarse);
     CKL();
     tv.launches++;
@@ -581,6 +589,7 @@ int enqueue_all_host_driven(wavi_ctx* c) {
   Tally tp, tv, tc;
   k_state_init<<<1, 32, 0, c->st>>>(c->S);
   CKL();
+  if (c->cheb_eig) CK(cudaMemsetAsync(c->cheb_eig, 0, c->d.N * sizeof(T), c->st));  // every solve starts cold
   for (;;) {
     TRY(enqueue_picard_head(c, h, tp));
     CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
@@ -664,6 +673,7 @@ int build_graph(wavi_ctx* c) {
   TRY(begin_capture(c, top, {}));
   k_state_init<<<1, 32, 0, c->st>>>(c->S);
   CKL();
+  if (c->cheb_eig) CK(cudaMemsetAsync(c->cheb_eig, 0, c->d.N * sizeof(T), c->st));  // every solve starts cold
   TRY(end_capture(c, top, sinks));
   cudaGraph_t pbody = nullptr, vbody = nullptr, cbody = nullptr;
   cudaGraphNode_t pnode, vnode, cnode;
@@ -1394,19 +1404,19 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   c->nty = (int)c->tile_grid.y;
   // coarse solver: the reference's cg! recurrence, or (persistent kernel only) single-reduction CG
   const int want = opt->coarse_solver;
-  if (want < WAVI_COARSE_AUTO || want > WAVI_COARSE_SRCG_JACOBI)
+  if (want < WAVI_COARSE_AUTO || want > WAVI_COARSE_SRCG_CHEBYSHEV)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_solver %d", want));
   if (opt->coarse_kernel < 0 || opt->coarse_kernel > 3)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_kernel %d", opt->coarse_kernel));
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));
-  // auto: FP64 runs the reference's cg!; mixed runs the Jacobi single-reduction CG on domains whose ice
-  // mask is full, and cg! where the mask cuts the domain (calving fronts inside it): there the masked
-  // Haar functions can coincide on the interior, R A P turns singular, and the FP32 Jacobi iteration
-  // was seen to stall the Picard loop where the unpreconditioned recurrences converge
+  // auto: FP64 runs the reference's cg!; mixed runs the Chebyshev-Jacobi single-reduction CG on domains
+  // whose ice mask is full (the Jacobi one where only the global-memory kernel fits), and cg! where the
+  // mask cuts the domain (calving fronts inside it): there the masked Haar functions can coincide on the
+  // interior and R A P turns singular
   bool full_mask = true;
   for (int i = 0; i < d.Nh && full_mask; ++i) full_mask = hm[i] != 0;
-  c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) && full_mask ? WAVI_COARSE_SRCG_JACOBI : WAVI_COARSE_CG) : want;
+  c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) && full_mask ? WAVI_COARSE_SRCG_CHEBYSHEV : WAVI_COARSE_CG) : want;
   if (opt->coarse_kernel != 2) {
     if (mixed(c))
       c->tile == 16 ? choose_persistent<float, 16>(c) : choose_persistent<float, 32>(c);
@@ -1421,6 +1431,11 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     }
     if ((opt->coarse_kernel == 1 || opt->coarse_kernel == 3) && c->pers_maxt == 0)
       return bail(fail(c, WAVI_ERR_ARGUMENT, "the persistent coarse CG does not fit this grid on this device"));
+    if (c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV && c->pers_maxt < 0) {
+      if (want != WAVI_COARSE_AUTO)
+        return bail(fail(c, WAVI_ERR_ARGUMENT, "the Chebyshev coarse solve needs the register-resident persistent kernel"));
+      c->coarse_solver = WAVI_COARSE_SRCG_JACOBI;
+    }
   } else {
     c->coarse_solver = WAVI_COARSE_CG;
   }
@@ -1432,7 +1447,7 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   if ((r = dalloc(c, &c->bar, 1))) return bail(r);
   if ((r = dalloc(c, &c->selftest, 2))) return bail(r);
   if (c->pers_maxt > 0) {
-    if ((r = dalloc(c, &c->halo_box, (size_t)c->ntx * c->nty * 8 * c->tile))) return bail(r);
+    if ((r = dalloc(c, &c->halo_box, (size_t)2 * c->ntx * c->nty * 8 * c->tile))) return bail(r);
     if (mixed(c) && c->tile == 16 && !c->stream_op && smoother_fits(c)) {
       if ((r = dalloc(c, &c->smooth_box, (size_t)2 * c->ntx * c->nty * 8 * 16))) return bail(r);
       c->fused_smooth = true;
@@ -1442,6 +1457,10 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     double* q = nullptr;
     if ((r = dalloc(c, &q, N))) return bail(r);
     c->dcoarse = q;
+    if (c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV) {
+      if ((r = dalloc(c, &q, N))) return bail(r);
+      c->cheb_eig = q;
+    }
     if (c->pers_maxt < 0) {
       if ((r = dalloc(c, &q, N))) return bail(r);
       c->gz = q;

@@ -31,7 +31,7 @@ class GPUParallelSpec:
     precision: str = "fp64"     # "fp64" (reference algorithm) or "mixed"
     use_graphs: bool = True
     picard_test: int = 0
-    coarse_solver: str = "auto"  # "auto", "cg" (reference), "srcg", "srcg_jacobi" (single-reduction CG)
+    coarse_solver: str = "auto"  # "auto", "cg" (reference), "srcg", "srcg_jacobi", "srcg_chebyshev" (single-reduction CG)
     device_run: bool = False     # run_simulation without a callback keeps the model on the device (wavi_run_device)
 
 
