@@ -15,7 +15,8 @@ reference's other solver parameters).
   roofline the dominant kernel of the step, the persistent coarse CG (k_srcg_persistent<float>), timed
            with CUDA events around each launch in a host-driven solve of the same state; per CG
            iteration: algorithmic bytes / duration against the measured HBM peak (the kernel's working
-           set, ~3 MB, is L2-resident: it is bound by grid-barrier latency, not by HBM)
+           set, ~3 MB, is on chip or in L2: it is bound by the latency of its grid reduction and of the
+           neighbour halo exchanges of its operator applications, not by HBM)
   roofline_stencil the fused operator kernel (float32) on a 4096 x 1024 grid (~190 MB per application,
            larger than L2), back-to-back launches timed with CUDA events: the HBM-bound stencil figure
   cpu_baseline the CPU oracle (the FP64 restatement of the reference) on a bounded sample

@@ -1,30 +1,29 @@
-// persistent.cuh — the coarse conjugate-gradient solve of one V-cycle as a single persistent kernel.
+// persistent.cuh — the coarse conjugate-gradient solve of one V-cycle as a single persistent kernel,
+// and the smoother pass as another.
 //
 // The coarse solve (IterativeSolvers cg! on R A P, update_preconditioners.jl:54-83) is a long chain of
 // small dependent steps: at 640 x 80 one iteration moves ~1 MB, far below what a launch costs.  Here one
 // cooperative launch runs every iteration.  Each CTA owns up to MAXT tiles of TILE x TILE points (a tile
 // holds whole Haar blocks of both velocity components); each thread keeps, in registers, the CG vectors
-// of its own point of every owned tile for the whole solve.  Per iteration only a prolonged vector
-// w = P u crosses L2 (the operator needs a one-point halo of it), separated from its readers by a grid
-// barrier.  Two kernels:
+// of its own point of every owned tile for the whole solve.  Per operator application only a prolonged
+// vector w = P u crosses L2 (the operator needs a one-point halo of it).  Two kernels:
 //
-//   k_cg_persistent   the reference's cg! recurrence: three barriers per iteration
-//                       1. u = r + β u;  w = P u                                   -> barrier
-//                       2. c = R A w (operator on tile + halo, Haar analysis, wavelet mask);
-//                          partial <u, c>                                          -> barrier + sum
-//                       3. α = |r|^2/<u,c>;  x += α u;  r -= α c;  partial |r|^2   -> barrier + sum
-//   k_srcg_persistent single-reduction CG (Chronopoulos & Gear 1989), optionally Jacobi-preconditioned:
-//                     both inner products of an iteration follow its operator application, so an
-//                     iteration costs one halo barrier and one reduction barrier.
+//   k_cg_persistent   the reference's cg! recurrence: u = r + β u; w = P u; c = R A w; <u, c>;
+//                     α; x, r; |r|^2 — two grid reductions per iteration
+//   k_srcg_persistent single-reduction CG (Chronopoulos & Gear 1989), preconditioned by nothing, by
+//                     the Jacobi diagonal, or by Chebyshev-accelerated Jacobi steps: both inner products
+//                     of an iteration follow its operator application, one grid reduction per iteration
 //
-// GB300 executes FP64 at a small fraction of its FP32 rate, so the per-point work of the FP32 (mixed)
-// instantiations stays in FP32: vector updates are FP32 FMAs with the scalars rounded once per CTA,
-// per-thread dot-product terms are FP32, and the FP64 accumulation starts at the warp sums (CTA sums,
-// grid sums and every CG scalar are FP64).  Scalars are computed by one thread per CTA.
+// The FP64 and global-memory instantiations separate the prolongation from the operator by a grid
+// barrier.  The FP32 instantiations on 16 x 16 tiles (the fast path) keep the tiles' coefficients in
+// shared memory, transform u and v together (idwt2d_pair, idwt2dT_pair), exchange only tile boundaries
+// through tagged words that the neighbours wait for (stage_tagged), and carry the grid reductions and
+// CG scalars in float-float arithmetic (GB300 executes FP64 at a small fraction of its FP32 rate).
+// k_smooth_persistent runs a smoother pass on the same machinery.
 //
-// Grid sums are deterministic and identical in every CTA: each CTA publishes its FP64 partials, and
-// after the barrier every CTA adds all partials in the same fixed order.  Every wait is bounded: after
-// ~2^22 polls a CTA records WAVI_ERR_WATCHDOG and all CTAs leave the kernel.
+// Grid sums are deterministic and identical in every CTA: each CTA publishes its partials, and after
+// the barrier every CTA adds all partials in the same fixed order.  Every wait is bounded: after ~2^22
+// polls a CTA records WAVI_ERR_WATCHDOG and all CTAs leave the kernel.
 #pragma once
 #include <type_traits>
 
@@ -1120,7 +1119,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
 // J. Comput. Appl. Math. 25 (1989)) on R A P x = b_c, an opt-in alternative to the reference's cg!, with
 // M = diag(R A P) (dcoarse) or M = I (dcoarse == nullptr), and cg!'s stopping rule on the
 // unpreconditioned residual.  Both inner products of an iteration follow its one operator application,
-// so an iteration costs one halo barrier and one reduction barrier (cg! needs two reductions):
+// so an iteration costs one reduction barrier (cg! needs two reductions) besides its operator application:
 //   x += α p;  r -= α s;  z = M⁻¹ r;  w = P z                                       -> barrier
 //   w = R A w;  partial (r,z), (w,z), |r|^2                                         -> barrier + sums
 //   β = γ/γ';  α = γ/(δ - β γ/α');  p = z + β p;  s = w + β s
