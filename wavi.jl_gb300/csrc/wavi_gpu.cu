@@ -105,6 +105,7 @@ struct wavi_ctx {
   double* partials = nullptr;
   int max_partials = 0;
   DevParams* P = nullptr;     // device
+  DevParams* P_adj = nullptr; // device: the adjoint's preconditioner V-cycle (capped coarse iterations)
   DevParams* hP = nullptr;    // pinned host staging
   DevState* S = nullptr;      // device
   DevState* hS = nullptr;     // pinned host copy
@@ -978,6 +979,7 @@ int check_params(wavi_ctx* c, const wavi_params* p) {
 // preconditioner, restarted right-preconditioned FGMRES (Saad 1993) for both linear systems.
 // ---------------------------------------------------------------------------------------------
 constexpr int ADJ_RESTART = 40;
+constexpr int kAdjCoarseIters = 100;  // coarse-CG iterations of the adjoint's preconditioner V-cycle
 
 int adj_alloc(wavi_ctx* c) {
   auto& a = c->adj;
@@ -991,6 +993,7 @@ int adj_alloc(wavi_ctx* c) {
   AA(a.cell.L, 8 * Nh) AA(a.ebar, Nh) AA(a.sbar, Nh) AA(a.dheta_h, Nh) AA(a.dhn, Nh) AA(a.dbeff, Nh)
   AA(a.dheta_c, std::max<size_t>(d.Nc, 1)) AA(a.dbeta_m, N) AA(a.zero_h, Nh) AA(a.xstate, N) AA(a.ta, N) AA(a.tb, N)
   AA(a.b, N) AA(a.x, N) AA(a.uv_keep, N) AA(a.xc_keep, N) AA(a.dotv, 1) AA(a.counter, 1)
+  AA(c->P_adj, 1)
 #undef AA
   a.V.assign(ADJ_RESTART + 1, nullptr);
   a.Z.assign(ADJ_RESTART, nullptr);
@@ -1041,9 +1044,22 @@ int adj_apply(wavi_ctx* c, bool transpose, const double* v, double* out) {
   return 0;
 }
 
-// out = one V-cycle of the solve's preconditioner applied to v (zero start, zero coarse warm start).
+template <typename T, int TILE>
+int adj_vcycle_body(wavi_ctx* c, const double* v, double* out);
+
+// out = one V-cycle of the solve's preconditioner applied to v (zero start, zero coarse warm start), its
+// coarse CG capped at kAdjCoarseIters iterations (P_adj): FGMRES takes any fixed preconditioner, and the
+// cold coarse solve would otherwise run towards maxiter_coarse in every application.
 template <typename T, int TILE>
 int adj_vcycle(wavi_ctx* c, const double* v, double* out) {
+  DevParams* const P_solve = c->P;
+  c->P = c->P_adj;
+  const int r = adj_vcycle_body<T, TILE>(c, v, out);
+  c->P = P_solve;
+  return r;
+}
+template <typename T, int TILE>
+int adj_vcycle_body(wavi_ctx* c, const double* v, double* out) {
   const size_t bytes = sizeof(double) * c->d.N;
   CK(cudaMemcpyAsync(c->r64, v, bytes, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaMemsetAsync(c->x64, 0, bytes, c->st));
@@ -1162,6 +1178,12 @@ int adj_prepare(wavi_ctx* c, const wavi_params* p) {
   if (!c->solved) return fail(c, WAVI_ERR_ARGUMENT, "no converged solve to linearise: call a solve first");
   TRY(adj_alloc(c));
   TRY(set_params(c, p));
+  {
+    DevParams pa = *c->hP;
+    pa.maxiter_coarse = std::min(pa.maxiter_coarse, kAdjCoarseIters);
+    CK(cudaMemcpyAsync(c->P_adj, &pa, sizeof(DevParams), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));  // (pa lives on this stack frame)
+  }
   auto& a = c->adj;
   const Dims& d = c->d;
   const size_t bytes = sizeof(double) * d.N;
