@@ -47,3 +47,14 @@ def test_no_device_is_an_error_not_a_crash(lib, pkg):
     assert st in (-7, -2)
     assert lib.wavi_last_error(None)
     assert lib.wavi_ctx_destroy(None) == 0
+
+
+def test_coarse_solver_names_match_the_header_enum(pkg):
+    """abi.COARSE_SOLVERS (the names the Python host and the tests use) against wavi_coarse_solver."""
+    import re
+    from wavi_gb300 import abi
+    here = os.path.dirname(os.path.abspath(__file__))
+    text = open(os.path.join(os.path.dirname(here), "include", "wavi_gpu.h")).read()
+    body = text[text.index("typedef enum wavi_coarse_solver"):text.index("} wavi_coarse_solver;")]
+    enum = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"WAVI_COARSE_(\w+)\s*=\s*(\d+)", body)}
+    assert enum == {k: v for k, v in abi.COARSE_SOLVERS.items()}, (enum, abi.COARSE_SOLVERS)
