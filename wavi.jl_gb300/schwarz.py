@@ -1,0 +1,179 @@
+"""Restricted additive Schwarz (RAS) over overlapping subdomains: the decomposition of the reference's
+SharedMemorySpec (src/SharedMemorySpec.jl).
+
+The reference's precondition!(model, ::SharedMemorySpec) (:78-158) tests the global residual and then, for
+niterations, copies the global velocities into every subdomain model (schwarzRestrictVelocities!), runs
+update_state! on each subdomain (a nested solve with the subdomain's halo velocities held fixed), scales the
+global velocities by `damping` and adds (1 - damping) times each subdomain's velocities weighted by a
+partition of unity (schwarzProlongVelocities!).  This module restates the pieces of that loop that live on
+the host — subdomain ranges, subdomain problems, restriction, prolongation and the partition of unity —
+with the reference's 1-based index arithmetic written 0-based — and the sweep loop, whose subdomain solve
+is a callable (by default update_state on a host Model, i.e. one velocity-solver context per subdomain).
+
+Because a subdomain's edge cells miss the shear-strain corners beyond the cut, their viscosity differs from
+the global model's, so a sweep of the converged global solution moves it by the order of the Picard
+tolerance times the ramp weights — in the reference as here; the sweeps are a preconditioner, not a solver.
+"""
+from dataclasses import dataclass, replace
+
+import numpy as np
+
+from .config import Grid, InitialConditions
+
+
+@dataclass
+class SchwarzSpec:
+    """SharedMemorySpec's parameters (src/SharedMemorySpec.jl:5-12): ngridsx x ngridsy subdomains,
+    `overlap` h cells of overlap on each side, niterations Schwarz iterations per Picard iteration, and
+    the damping of the prolongation."""
+    ngridsx: int = 1
+    ngridsy: int = 1
+    overlap: int = 1
+    niterations: int = 0
+    damping: float = 0.0
+
+
+def subdomain_range(nx, ny, igrid, jgrid, spec):
+    """The h cells of subdomain (igrid, jgrid) (1-based, as in the reference) as 0-based half-open ranges
+    (i0, i1, j0, j1): the subdomain's block of nx/ngridsx x ny/ngridsy cells and `overlap` more cells on
+    each side, clipped to the domain (schwarzModel, :181-201)."""
+    if nx % spec.ngridsx or ny % spec.ngridsy:
+        raise ValueError("Model domain is not an integer number of subdomains")
+    if not (1 <= igrid <= spec.ngridsx and 1 <= jgrid <= spec.ngridsy):
+        raise IndexError((igrid, jgrid))
+    nxd, nyd = nx // spec.ngridsx, ny // spec.ngridsy
+    i_start = (igrid - 1) * nxd + 1
+    i_stop = igrid * nxd
+    j_start = (jgrid - 1) * nyd + 1
+    j_stop = jgrid * nyd
+    i_start_g = max(i_start - spec.overlap, 1)
+    i_stop_g = min(i_stop + spec.overlap, nx)
+    j_start_g = max(j_start - spec.overlap, 1)
+    j_stop_g = min(j_stop + spec.overlap, ny)
+    return i_start_g - 1, i_stop_g, j_start_g - 1, j_stop_g
+
+
+def partition_of_unity(m, n, leavei1, leaveim, leavej1, leavejn, overlapi, overlapj):
+    """The m x n weights of schwarzPartitionOfUnity (:398-407): 1 inside, ramping linearly to 0 over
+    `overlapi` (`overlapj`) points towards each edge whose flag is not set.  The ramps of two neighbouring
+    subdomains add to 1 across their overlap."""
+    if not m > (0 if leavei1 else overlapi) + (0 if leaveim else overlapi):
+        raise ValueError("partition of unity: too few points in i for the ramps")
+    if not n > (0 if leavej1 else overlapj) + (0 if leavejn else overlapj):
+        raise ValueError("partition of unity: too few points in j for the ramps")
+    i = np.arange(1, m + 1, dtype=np.float64)
+    j = np.arange(1, n + 1, dtype=np.float64)
+    fi = np.ones(m)
+    if not leavei1:
+        fi = np.minimum(fi, (i - 1) / overlapi)
+    if not leaveim:
+        fi = np.minimum(fi, (m - i) / overlapi)
+    fj = np.ones(n)
+    if not leavej1:
+        fj = np.minimum(fj, (j - 1) / overlapj)
+    if not leavejn:
+        fj = np.minimum(fj, (n - j) / overlapj)
+    return np.asfortranarray(fi[:, None] * fj[None, :])
+
+
+def subdomain_problem(model, igrid, jgrid, spec):
+    """The inputs of subdomain (igrid, jgrid)'s model, taken from the global model's grid, parameters and
+    current fields (schwarzModel, :180-287): (grid, bed, params, initial conditions).  The subdomain's
+    velocity points on its cut boundaries (not the domain's own boundary) are fixed (:218-225): the global
+    solution enters there as Dirichlet values."""
+    g = model.grid
+    i0, i1, j0, j1 = subdomain_range(g.nx, g.ny, igrid, jgrid, spec)
+    nxg, nyg = i1 - i0, j1 - j0
+    u_isfixed = g.u_isfixed[i0:i1 + 1, j0:j1].copy(order="F")
+    v_isfixed = g.v_isfixed[i0:i1, j0:j1 + 1].copy(order="F")
+    if igrid != 1:
+        u_isfixed[0, :] = True
+        v_isfixed[0, :] = True
+    if igrid != spec.ngridsx:
+        u_isfixed[nxg, :] = True
+        v_isfixed[nxg - 1, :] = True
+    if jgrid != 1:
+        v_isfixed[:, 0] = True
+        u_isfixed[:, 0] = True
+    if jgrid != spec.ngridsy:
+        v_isfixed[:, nyg] = True
+        u_isfixed[:, nyg - 1] = True
+    grid = Grid(nx=nxg, ny=nyg, dx=g.dx, dy=g.dy, nσ=g.nσ, x0=g.x0 + i0 * g.dx, y0=g.y0 + j0 * g.dy,
+                h_mask=g.h_mask[i0:i1, j0:j1].copy(order="F"), h_isfixed=g.h_isfixed[i0:i1, j0:j1].copy(order="F"),
+                u_iszero=g.u_iszero[i0:i1 + 1, j0:j1].copy(order="F"),
+                v_iszero=g.v_iszero[i0:i1, j0:j1 + 1].copy(order="F"), u_isfixed=u_isfixed, v_isfixed=v_isfixed,
+                quadrature_weights=g.quadrature_weights, σ=g.σ)
+    f = model.fields
+    crop = lambda a: np.asfortranarray(np.asarray(a)[i0:i1, j0:j1]).copy(order="F")
+    glen_a_ref = np.broadcast_to(np.asarray(model.params.glen_a_ref, np.float64), (g.nx, g.ny))
+    params = replace(model.params, weertman_c=crop(model.weertman_c_param),
+                     accumulation_rate=crop(model.accumulation_param), glen_a_ref=crop(glen_a_ref))
+    ic = InitialConditions(initial_thickness=crop(f["h"]), initial_grounded_fraction=crop(f["grounded_fraction"]),
+                           initial_u_veloc=np.asfortranarray(f["u"][i0:i1 + 1, j0:j1]).copy(order="F"),
+                           initial_v_veloc=np.asfortranarray(f["v"][i0:i1, j0:j1 + 1]).copy(order="F"),
+                           initial_viscosity=np.asfortranarray(f["eta"][i0:i1, j0:j1, :]).copy(order="F"),
+                           initial_temperature=np.asfortranarray(f["temperature"][i0:i1, j0:j1, :]).copy(order="F"),
+                           initial_damage=np.asfortranarray(f["damage"][i0:i1, j0:j1, :]).copy(order="F"))
+    return grid, crop(f["b"]), params, ic
+
+
+def restrict_velocities(model_g, model, igrid, jgrid, spec):
+    """schwarzRestrictVelocities! (:306-330): the global velocities on the subdomain's points."""
+    g = model.grid
+    i0, i1, j0, j1 = subdomain_range(g.nx, g.ny, igrid, jgrid, spec)
+    model_g.fields["u"][...] = model.fields["u"][i0:i1 + 1, j0:j1]
+    model_g.fields["v"][...] = model.fields["v"][i0:i1, j0:j1 + 1]
+
+
+def prolong_velocities(model, model_g, igrid, jgrid, spec):
+    """schwarzProlongVelocities! (:350-380): add (1 - damping) times the subdomain's velocities, weighted
+    by its partition of unity (ramps over 2 overlap u points and 2 overlap - 1 v points across x, and the
+    reverse across y), to the global velocities.  The caller has scaled the global velocities by damping
+    before the first subdomain is added (precondition!, :124-125)."""
+    g = model.grid
+    i0, i1, j0, j1 = subdomain_range(g.nx, g.ny, igrid, jgrid, spec)
+    nxg, nyg = i1 - i0, j1 - j0
+    edges = (igrid == 1, igrid == spec.ngridsx, jgrid == 1, jgrid == spec.ngridsy)
+    upou = partition_of_unity(nxg + 1, nyg, *edges, 2 * spec.overlap, 2 * spec.overlap - 1)
+    vpou = partition_of_unity(nxg, nyg + 1, *edges, 2 * spec.overlap - 1, 2 * spec.overlap)
+    w = 1.0 - spec.damping
+    model.fields["u"][i0:i1 + 1, j0:j1] += w * upou * model_g.fields["u"]
+    model.fields["v"][i0:i1, j0:j1 + 1] += w * vpou * model_g.fields["v"]
+
+
+def build_subdomains(model, spec, make=None):
+    """update_preconditioner!(model, ::SharedMemorySpec) (:53-69): one subdomain model per (igrid, jgrid)
+    from the global model's current state.  ``make(grid, bed, params, solver_params, initial_conditions)``
+    builds each one; by default a host Model with the global model's solver and parallel specs (so each
+    subdomain solves through its own velocity-solver context)."""
+    if make is None:
+        from .model import Model
+        make = lambda grid, bed, params, solver_params, ic: Model(grid, bed, params, solver_params, ic,
+                                                                   parallel_spec=model.parallel_spec)
+    subs = {}
+    for igrid in range(1, spec.ngridsx + 1):
+        for jgrid in range(1, spec.ngridsy + 1):
+            grid, bed, params, ic = subdomain_problem(model, igrid, jgrid, spec)
+            subs[igrid, jgrid] = make(grid, bed, params, model.solver_params, ic)
+    return subs
+
+
+def ras_sweeps(model, spec, subdomains, solve=None):
+    """The Schwarz iterations of precondition!(model, ::SharedMemorySpec) (:98-155), run spec.niterations
+    times: restrict the global velocities into every subdomain, solve every subdomain (by default
+    update_state on a host Model), scale the global velocities by damping and add every subdomain's
+    velocities back through its partition of unity.  The residual test that precedes the sweeps in the
+    reference belongs to the caller's Picard loop."""
+    if solve is None:
+        from .model import update_state
+        solve = update_state
+    for _ in range(spec.niterations):
+        for (igrid, jgrid), sub in subdomains.items():
+            restrict_velocities(sub, model, igrid, jgrid, spec)
+        for sub in subdomains.values():
+            solve(sub)
+        model.fields["u"] *= spec.damping
+        model.fields["v"] *= spec.damping
+        for (igrid, jgrid), sub in subdomains.items():
+            prolong_velocities(model, sub, igrid, jgrid, spec)
+    return model
