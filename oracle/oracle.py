@@ -1,6 +1,6 @@
 """ctypes binding of the FP64 CPU oracle (oracle/wavi_oracle.cpp).
 
-TEST INFRASTRUCTURE ONLY.  Imported by tests/, by ``__graft_entry__.smoke()`` as the checker and by
+TEST INFRASTRUCTURE ONLY.  Imported by tests/, by ``__graft_entry__.smoke()`` to check its result and by
 ``bench.py`` for the CPU-baseline leg.  The product (the package and libwavi_gpu.so) never imports it.
 
 Parity of the oracle itself is pinned against the reference's golden files (tests/golden/*.npz, made

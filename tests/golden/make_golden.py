@@ -6,7 +6,7 @@ four JLD2 files, ``test/version_update_test_verification/v1_*_MISMIP_100yr_outpu
 files; every dataset there is a little-endian float64 array stored compact or contiguous.  This script reads them with
 the package's minimal HDF5 reader (``wavi_gb300.io.read_jld2``) and writes ``mismip_100yr_<julia version>.npz`` next to
 itself.  It reads the reference checkout and is run by hand
-in a container that has it; the GPU machine only sees the ``.npz`` files.
+on a machine that has it; the tests elsewhere only need the ``.npz`` files.
 
 Usage:  python tests/golden/make_golden.py [path-to-reference-checkout]
 """

@@ -208,7 +208,7 @@ OpCoef<float> coef<float>(const wavi_ctx* c) {
   return {c->heta_h32, c->heta_c32, c->dimp32, c->beta_m32, c->h_m32, c->inner_uv};
 }
 
-// Algorithmic bytes of one operator application (see the design doc's byte model): read x, write y,
+// Algorithmic bytes of one operator application: read x, write y,
 // coefficients heta_h, dimp (Nh), heta_c (Nc), beta_m, h_m (N), the interior mask (N bytes), plus the
 // right-hand side for the residual form.
 double op_bytes(const Dims& d, int w, bool resid) {
