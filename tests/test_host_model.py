@@ -57,3 +57,38 @@ def test_grid_boundary_strings(pkg):
         pkg.Grid(nx=5, ny=4, h_mask=np.ones((4, 4), bool))
     with pytest.raises(AssertionError):
         pkg.SolverParams(n_iter_viscosity=3)
+
+
+@pytest.mark.parametrize("mask", ["full", "disc"])
+def test_post_solve_and_thickness_step_match_oracle(oracle, pkg, mask):
+    """The host mirror's steps after the velocity solve — h-grid, bed and surface velocities, dh/dt, the
+    wavelet coarse space (update_state.jl:17-19) — and update_thickness! (run_simulation.jl:24-42) give the
+    oracle's values on the same velocities and relinearised fields."""
+    from wavi_gb300 import synthetic
+    from wavi_gb300.model import Model, Simulation, post_solve_steps, pre_solve, update_thickness
+    from wavi_gb300.config import TimesteppingParams
+    g, bed, p, sp, ic = synthetic.small_case(nx=26, ny=14, mask=mask)
+    m = Model(g, bed, p, sp, ic)
+    om = oracle.build_model(g, bed, p, sp, ic)
+    rng = np.random.default_rng(5)
+    u = 50 * rng.standard_normal((g.nx + 1, g.ny))
+    v = 20 * rng.standard_normal((g.nx, g.ny + 1))
+    om.field("u")[...] = u
+    om.field("v")[...] = v
+    om.pre_solve()
+    om.inner_update()
+    pre_solve(m)
+    m.fields["u"][...] = u
+    m.fields["v"][...] = v
+    for k in ("beta", "quad_f1", "quad_f2"):
+        m.fields[k][...] = om.field(k)
+    post_solve_steps(m)
+    om.post_solve()
+    for k in ("uh", "vh", "ub", "vb", "us", "vs", "dhdt"):
+        assert np.allclose(m.fields[k], om.field(k), rtol=1e-13, atol=1e-12), k
+    assert np.array_equal(m.fields["wu_mask"].astype(bool), om.mask("wu_mask").astype(bool))
+    assert np.array_equal(m.fields["wv_mask"].astype(bool), om.mask("wv_mask").astype(bool))
+    dt = 0.5
+    update_thickness(Simulation(m, TimesteppingParams(dt=dt, end_time=dt)))
+    om.update_thickness(dt)
+    assert np.allclose(m.fields["h"], om.field("h"), rtol=1e-14, atol=1e-12)

@@ -262,12 +262,13 @@ def pos_fraction(z1, mask=None):
                 b = np.where(~flip, -2 * a1_ / (a3_ - a1_), -2 * a1_ / (a2_ - a1_))
                 A1 = 0.5 * (b ** 2) / a
                 A2 = 0.5 * ((1.0 - b) ** 2) / a
-            A3 = 0.5 * a + b
-            t1 = (b > 0.0).astype(int) + (b > 1.0)
-            t2 = ((a + b) > 0.0).astype(int) + ((a + b) > 1.0)
-            ix = 1 + t1 + 3 * t2
-            area = np.select([ix == 1, ix == 2, ix == 3, ix == 4, ix == 5, ix == 6, ix == 7, ix == 8],
-                             [0.0 * a, -A1, A2 - A1, A1 + A3, A3, A2 + A3, 1.0 - A2 + A1, 1.0 - A2], 1.0)
+                A3 = 0.5 * a + b
+                t1 = (b > 0.0).astype(int) + (b > 1.0)
+                t2 = ((a + b) > 0.0).astype(int) + ((a + b) > 1.0)
+                ix = 1 + t1 + 3 * t2
+                # every candidate is evaluated; the ones a cell does not select may be inf or NaN
+                area = np.select([ix == 1, ix == 2, ix == 3, ix == 4, ix == 5, ix == 6, ix == 7, ix == 8],
+                                 [0.0 * a, -A1, A2 - A1, A1 + A3, A3, A2 + A3, 1.0 - A2 + A1, 1.0 - A2], 1.0)
             area = np.where(b < 0.0, 1.0 - area, area)
             area = np.where(a1_ < 0.0, 1.0 - area, area)
             afq[sc] = area
