@@ -12,7 +12,7 @@ The package directory is ``wavi.jl_gb300/``; it is imported under the module nam
   build.py      nvcc build of the library
 """
 from . import abi, config, synthetic  # noqa: F401
-from .config import Grid, InitialConditions, Params, SolverParams, TimesteppingParams  # noqa: F401
+from .config import Grid, InitialConditions, OutputParams, Params, SolverParams, TimesteppingParams  # noqa: F401
 
 
 def __getattr__(name):

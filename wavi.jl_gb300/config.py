@@ -236,6 +236,45 @@ class TimesteppingParams:
 
 
 @dataclass
+class OutputParams:
+    """Mirror of WAVI.OutputParams (src/OutputParams/OutputParams.jl:2-12, constructor :34-70).
+
+    ``outputs`` maps each output name to the array written under it (a reference to a model field, read
+    when the output is written, as the reference's named tuple of field references is); ``n_iter_out`` is
+    set by the Simulation from the time step (set_n_iter_out!, Simulation.jl:62-66).  NetCDF zipping
+    (zip_format "nc", zip_output) is not provided."""
+    outputs: dict = field(default_factory=dict)
+    output_freq: float = math.inf
+    output_format: str = "jld2"
+    prefix: str = "outfile"
+    output_path: str = "./"
+    dump_vel: bool = False
+    zip_format: str = "none"
+    output_start: bool = False
+    n_iter_out: int = -1
+
+    def __post_init__(self):
+        import os
+        if not (self.output_freq == math.inf or self.output_freq > 0):
+            raise ValueError("output frequency must be positive or Inf")
+        if not os.path.isdir(self.output_path):
+            os.makedirs(self.output_path)
+        if not self.output_path.endswith("/"):
+            self.output_path = self.output_path + "/"
+        if self.output_format not in ("jld2", "mat"):
+            raise ValueError("Output format must be `jld2` or `mat`")
+        if self.zip_format not in ("none", "nc"):
+            self.zip_format = "none"
+        if self.zip_format == "nc":
+            raise NotImplementedError("zipping the output to NetCDF is not provided")
+
+    def set_n_iter_out(self, dt, n_iter_total):
+        """set_n_iter_out! (src/Simulations/Simulation.jl:62-66)."""
+        self.n_iter_out = n_iter_total + 1 if self.output_freq == math.inf else int(round(self.output_freq / dt))
+        return self
+
+
+@dataclass
 class InitialConditions:
     """Mirror of WAVI.InitialConditions (src/InitialConditions.jl:27-34); None means 'use the default'."""
     initial_thickness: Optional[np.ndarray] = None

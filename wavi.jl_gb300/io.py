@@ -11,6 +11,19 @@ read_jld2
     version-2 object headers, link messages, compact or contiguous data layouts), as Julia-shaped arrays.
     Enough for the reference's golden and output files, which store each field as a plain float64 array;
     chunked or compressed datasets, and JLD2's serialised Julia structs, are not read.
+
+write_jld2
+    The inverse for float64 arrays: the file JLD2's ``@save`` writes for a set of Float64 arrays (the
+    reference's output and golden files, ``test/version_update_test_verification/*.jld2``).  The layout is
+    the 512-byte JLD2 header, an HDF5 version-2 superblock, one version-2 object header per array (fill
+    value, dataspace, IEEE float64 datatype and a compact or contiguous data layout) in link order, and
+    the root group's object header (link info, group info, one link per array, and a 16-byte NIL message
+    that keeps room for a header continuation) last.  Every object header and the superblock end in the
+    HDF5 lookup3 checksum.  Rebuilding the reference's four golden JLD2 files from their arrays gives them
+    byte for byte.
+
+write_output
+    run_simulation!'s periodic output files (src/OutputParams/output_writing.jl:7-27) in JLD2 (or MAT).
 """
 import struct
 
@@ -42,6 +55,10 @@ def read_vel(prefix, nx, ny):
     return tuple(out)
 
 
+class ChecksumError(ValueError):
+    """An HDF5 superblock or object header whose stored lookup3 checksum does not match its bytes."""
+
+
 class HDF5Reader:
     """Just enough HDF5 to walk a JLD2 root group and pull out contiguous float64 datasets."""
 
@@ -54,6 +71,8 @@ class HDF5Reader:
         if ver not in (2, 3):
             raise ValueError(f"unsupported superblock version {ver}")
         self.so, self.sl = data[sb + 9], data[sb + 10]
+        if struct.unpack_from("<I", data, sb + 44)[0] != lookup3(data[sb:sb + 44]):
+            raise ChecksumError("superblock checksum mismatch")
         p = sb + 12
         self.base, = struct.unpack_from("<Q", data, p)
         root_rel, = struct.unpack_from("<Q", data, p + 24)
@@ -73,6 +92,8 @@ class HDF5Reader:
         chunk = int.from_bytes(d[p:p + nsz], "little")
         p += nsz
         end = p + chunk
+        if struct.unpack_from("<I", d, end)[0] != lookup3(d[addr:end]):
+            raise ChecksumError(f"object header checksum mismatch at {addr}")
         while p + 4 <= end:
             mtype = d[p]
             msize, = struct.unpack_from("<H", d, p + 1)
@@ -137,10 +158,120 @@ class HDF5Reader:
 
 
 
+def lookup3(data: bytes, initval: int = 0) -> int:
+    """Bob Jenkins' lookup3 ``hashlittle`` (2006, public domain), the checksum of HDF5's version-2
+    metadata: 12-byte little-endian blocks mixed into three 32-bit words, the last (partial, zero-padded)
+    block followed by the final avalanche; an empty tail after full blocks skips the final step."""
+    M = 0xFFFFFFFF
+
+    def rot(x, k):
+        return ((x << k) | (x >> (32 - k))) & M
+
+    n = len(data)
+    a = b = c = (0xDEADBEEF + n + initval) & M
+    p = 0
+    while n - p > 12:
+        x, y, z = struct.unpack_from("<III", data, p)
+        a = (a + x) & M
+        b = (b + y) & M
+        c = (c + z) & M
+        a = (a - c) & M; a ^= rot(c, 4); c = (c + b) & M
+        b = (b - a) & M; b ^= rot(a, 6); a = (a + c) & M
+        c = (c - b) & M; c ^= rot(b, 8); b = (b + a) & M
+        a = (a - c) & M; a ^= rot(c, 16); c = (c + b) & M
+        b = (b - a) & M; b ^= rot(a, 19); a = (a + c) & M
+        c = (c - b) & M; c ^= rot(b, 4); b = (b + a) & M
+        p += 12
+    if n - p == 0:
+        return c
+    x, y, z = struct.unpack("<III", data[p:] + bytes(12 - (n - p)))
+    a = (a + x) & M
+    b = (b + y) & M
+    c = (c + z) & M
+    c ^= b; c = (c - rot(b, 14)) & M
+    a ^= c; a = (a - rot(c, 11)) & M
+    b ^= a; b = (b - rot(a, 25)) & M
+    c ^= b; c = (c - rot(b, 16)) & M
+    a ^= c; a = (a - rot(c, 4)) & M
+    b ^= a; b = (b - rot(a, 14)) & M
+    c ^= b; c = (c - rot(b, 24)) & M
+    return c
+
+
+_JLD2_BASE = 512          # the HDF5 base address: the superblock follows the 512-byte JLD2 header
+_UNDEF = b"\xff" * 8      # HDF5's undefined address
+# IEEE little-endian float64: class 1 version 3, byte order LE, padding 0, mantissa normalised (implied
+# leading 1), sign at bit 63; size 8; bit offset 0, precision 64, exponent at bit 52 of 11 bits, mantissa at
+# bit 0 of 52 bits, exponent bias 1023
+_F64_TYPE = bytes([0x31, 0x20, 0x3F, 0x00]) + struct.pack("<IHHBBBBI", 8, 0, 64, 52, 11, 0, 52, 1023)
+_FILL_VALUE = bytes([3, 0x09])    # fill value message v3: allocation early, fill never written, undefined
+COMPACT_LIMIT = 8192              # arrays up to this many bytes are stored inside their object header
+
+
+def _object_header(messages):
+    """A version-2 object header ("OHDR", no times or attribute phases) holding ``messages`` (type, flags,
+    body), with the chunk-size field of the fewest bytes that fit, and its lookup3 checksum."""
+    chunk = b"".join(bytes([t]) + struct.pack("<H", len(body)) + bytes([fl]) + body for t, fl, body in messages)
+    for code, width in ((0, 1), (1, 2), (2, 4), (3, 8)):
+        if len(chunk) < (1 << (8 * width)):
+            break
+    head = b"OHDR" + bytes([2, code]) + len(chunk).to_bytes(width, "little")
+    out = head + chunk
+    return out + struct.pack("<I", lookup3(out))
+
+
+def write_jld2(path, arrays, julia_version="1.8.3"):
+    """Write the float64 arrays (and float64 scalars) of ``arrays`` (a name -> value mapping, in the order
+    the links are to be listed) as JLD2's ``@save`` does: each array's dimensions reversed into HDF5 order, its column-major
+    bytes stored compact (up to COMPACT_LIMIT bytes) or contiguous right after its object header.
+    ``julia_version`` only fills the header's informational "(Julia x.y.z 64-bit LE)" field."""
+    header = b"HDF5-based Julia Data Format, version 0.1.1\x00 (Julia " + julia_version.encode() + b" 64-bit LE)\x00"
+    if len(header) > _JLD2_BASE:
+        raise ValueError("julia_version too long")
+    body = bytearray()            # everything after the superblock, addressed from the base
+    pos = 48                      # the version-2 superblock is 48 bytes
+    links = []
+    for name, a in arrays.items():
+        a = np.asarray(a)
+        if a.dtype != np.float64 or a.size == 0:
+            raise ValueError(f"{name}: only non-empty float64 arrays and float64 scalars are written")
+        raw = np.ascontiguousarray(a.ravel(order="F")).astype("<f8").tobytes()
+        dims = tuple(reversed(a.shape))
+        # dataspace v2: a simple space of the reversed dimensions, or the scalar space of a 0-d value
+        space = bytes([2, len(dims), 0, 1 if dims else 0]) + struct.pack("<" + "Q" * len(dims), *dims)
+        msgs = [(5, 0, _FILL_VALUE), (1, 0, space), (3, 1, _F64_TYPE)]
+        if len(raw) <= COMPACT_LIMIT:
+            obj = _object_header(msgs + [(8, 0, bytes([4, 0]) + struct.pack("<H", len(raw)) + raw)])
+        else:
+            probe = _object_header(msgs + [(8, 0, bytes([4, 1]) + bytes(16))])
+            obj = _object_header(msgs + [(8, 0, bytes([4, 1]) + struct.pack("<QQ", pos + len(probe), len(raw)))])
+            obj += raw
+        links.append((name, pos))
+        body += obj
+        pos += len(obj)
+    root_msgs = [(2, 0, bytes([0, 0]) + _UNDEF + _UNDEF), (10, 0, bytes([0, 0]))]
+    for name, addr in links:
+        nb = name.encode()
+        if len(nb) > 255:
+            raise ValueError(f"{name}: link names up to 255 bytes")
+        root_msgs.append((6, 0, bytes([1, 0x10, 1, len(nb)]) + nb + struct.pack("<Q", addr)))
+    root_msgs.append((0, 0, bytes(16)))
+    root = _object_header(root_msgs)
+    root_addr = pos
+    body += root
+    eof = _JLD2_BASE + 48 + len(body)
+    sb = b"\x89HDF\r\n\x1a\n" + bytes([2, 8, 8, 0]) + struct.pack("<Q", _JLD2_BASE) + _UNDEF + \
+        struct.pack("<QQ", eof, root_addr)
+    sb += struct.pack("<I", lookup3(sb))
+    with open(path, "wb") as f:
+        f.write(header + bytes(_JLD2_BASE - len(header)) + sb + bytes(body))
+    return eof
+
+
 def read_jld2(path, names=None):
     """The float64 datasets of the JLD2 file's root group (or those in ``names``) as a dict of arrays in
     Julia's shape and column-major order.  Datasets that are not plain float64 arrays are skipped unless
-    named, in which case they raise."""
+    named, in which case they raise; a checksum mismatch always raises (ChecksumError)."""
     with open(path, "rb") as f:
         rd = HDF5Reader(f.read())
     links = rd.links()
@@ -150,9 +281,33 @@ def read_jld2(path, names=None):
             raise KeyError(name)
         try:
             arr, shape = rd.dataset(links[name])
+        except ChecksumError:
+            raise
         except ValueError:
             if names is not None:
                 raise
             continue
         out[name] = arr.reshape(shape, order="F")
     return out
+
+
+def write_output(sim):
+    """write_output (src/OutputParams/output_writing.jl:7-27): the Simulation's outputs, plus the time
+    rounded to 3 decimals ("t") and the h-grid coordinates ("x", "y") unless an output of that name
+    exists, to ``<output_path><prefix><n_iter, 10 digits>.jld2`` (or ``.mat``).  The "mat" format is
+    written by scipy.io.savemat (MAT version 5).  Returns the file name."""
+    op, model = sim.output_params, sim.model
+    out = {str(k): np.array(v, dtype=np.float64) for k, v in op.outputs.items()}
+    out.setdefault("t", np.float64(round(sim.time, 3)))
+    out.setdefault("x", np.asarray(model.grid.xxh, np.float64))
+    out.setdefault("y", np.asarray(model.grid.yyh, np.float64))
+    fname = f"{op.output_path}{op.prefix}{sim.n_iter:010d}"
+    if op.output_format == "jld2":
+        fname += ".jld2"
+        write_jld2(fname, out)
+    else:
+        from scipy.io import savemat
+        fname += ".mat"
+        savemat(fname, out)
+    print(f"outputting at timestep number {sim.n_iter}")
+    return fname

@@ -19,7 +19,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .config import Grid, InitialConditions, Params, SolverParams, TimesteppingParams
+from .config import Grid, InitialConditions, OutputParams, Params, SolverParams, TimesteppingParams
 from . import gpu
 
 
@@ -398,11 +398,15 @@ def update_state(model):
 
 
 class Simulation:
-    """Mirror of WAVI.Simulation (src/Simulations/Simulation.jl:24-52) without output or pickup files."""
+    """Mirror of WAVI.Simulation (src/Simulations/Simulation.jl:24-52) with its output files but without
+    checkpoints or pickup."""
 
-    def __init__(self, model: Model, timestepping_params: TimesteppingParams):
+    def __init__(self, model: Model, timestepping_params: TimesteppingParams, output_params: OutputParams = None):
         self.model = model
         self.timestepping_params = timestepping_params
+        self.output_params = output_params
+        if output_params is not None:
+            output_params.set_n_iter_out(timestepping_params.dt, timestepping_params.n_iter_total)
         self.n_iter = 0
         self.time = 0.0
         model.params.dt = timestepping_params.dt  # set_dt_in_model! (Simulation.jl:56-59)
@@ -428,17 +432,50 @@ def timestep(sim):
     sim.time += sim.timestepping_params.dt
 
 
+def _write_due_output(sim):
+    """The output steps of run_simulation! after time step sim.n_iter (run_simulation.jl:85-94)."""
+    from .io import write_output, write_vel
+    op = sim.output_params
+    if op is None:
+        return
+    if sim.n_iter % op.n_iter_out == 0:
+        write_output(sim)
+    if sim.n_iter == sim.timestepping_params.n_iter_total and op.dump_vel:
+        write_vel(op.prefix, sim.model.fields["u"], sim.model.fields["v"])
+
+
 def run_simulation(sim, callback=None):
+    """run_simulation! (src/Simulations/run_simulation.jl:61-100) without checkpoints: the initial output
+    when output_start is set, then each time step followed by its due outputs.  With a device-resident
+    GPU spec and no callback, the steps between two outputs run as one wavi_run_device call."""
+    tp, op = sim.timestepping_params, sim.output_params
+    if op is not None and op.output_start and sim.n_iter == 0:
+        from .io import write_output
+        write_output(sim)
     ps = sim.model.parallel_spec
-    n = sim.timestepping_params.n_iter_total - sim.n_iter
-    if (isinstance(ps, GPUParallelSpec) and ps.device_run and callback is None and n > 0
-            and sim.timestepping_params.step_thickness):
-        return _run_on_device(sim, n)
-    for _ in range(sim.n_iter + 1, sim.timestepping_params.n_iter_total + 1):
-        timestep(sim)
-        if callback is not None:
-            callback(sim)
+    on_device = (isinstance(ps, GPUParallelSpec) and ps.device_run and callback is None and tp.step_thickness)
+    while sim.n_iter < tp.n_iter_total:
+        if on_device:
+            n = tp.n_iter_total - sim.n_iter
+            if op is not None:
+                n = min(n, op.n_iter_out - sim.n_iter % op.n_iter_out)
+            _run_on_device(sim, n)
+        else:
+            timestep(sim)
+            if callback is not None:
+                callback(sim)
+        _write_due_output(sim)
     return sim
+
+
+def _assign_field(f, name, host):
+    """Put a host copy of a field back into the model in place, so references to the field (such as an
+    OutputParams output) stay valid; a field of another shape, or a new one, is replaced."""
+    cur = f.get(name)
+    if isinstance(cur, np.ndarray) and cur.shape == host.shape and cur.flags.writeable:
+        cur[...] = host
+    else:
+        f[name] = host
 
 
 def _run_on_device(sim, n):
@@ -459,15 +496,14 @@ def _run_on_device(sim, n):
     for k in gpu.ALL_FIELDS:
         if k in ("wu_correction_coarse", "wv_correction_coarse"):
             continue
-        host = t[k].cpu().numpy().reshape(np.asarray(f[k]).shape, order="F")
-        f[k] = host
+        _assign_field(f, k, t[k].cpu().numpy().reshape(np.asarray(f[k]).shape, order="F"))
     f["wu_correction_coarse"] = np.zeros(nwu)  # update_wavelets! restarts the coarse cache
     f["wv_correction_coarse"] = np.zeros(nwv)
     shape = (model.grid.nx, model.grid.ny)
-    f["dhdt"] = outs["dhdt"].cpu().numpy().reshape(shape, order="F")
+    _assign_field(f, "dhdt", outs["dhdt"].cpu().numpy().reshape(shape, order="F"))
     for key, name in (("u_h", "uh"), ("v_h", "vh"), ("u_bed", "ub"), ("v_bed", "vb"), ("u_surf", "us"), ("v_surf", "vs")):
         if name in f:
-            f[name] = outs[key].cpu().numpy().reshape(shape, order="F")
+            _assign_field(f, name, outs[key].cpu().numpy().reshape(shape, order="F"))
     model.last_stats = stats
     sim.n_iter += n
     sim.time += n * dt
