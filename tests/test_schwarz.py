@@ -4,6 +4,8 @@ of unity, and restriction followed by damped prolongation.  Host logic only (no 
 import numpy as np
 import pytest
 
+from helpers import SOLVE_FIELDS, fields_from_oracle
+
 
 def _model(nx=32, ny=8):
     from wavi_gb300 import synthetic
@@ -173,3 +175,61 @@ def test_ras_sweep_of_the_solution_moves_it_by_the_edge_viscosity_only(oracle, c
         subs = build_subdomains(m, spec, make=lambda *a: _OracleSubdomain(oracle.build_model(*a)))
         ras_sweeps(m, spec, subs, solve=lambda s: s.om.update_state())
         assert _uv_dist(m, u, v) < 3e-3 * (1 - damping) + 1e-12
+
+
+class _OracleEnsemble:
+    """A stand-in with EnsembleSolver.solve_device's contract (lists of params and of member field dicts of
+    flat column-major tensors, solved in place) whose members the oracle solves, on CPU tensors."""
+
+    def __init__(self, oracle, subs):
+        self.oracle, self.subs = oracle, list(subs)
+
+    def solve_device(self, params, tensors):
+        import torch
+        stats = []
+        for sub, p, t in zip(self.subs, params, tensors):
+            g = sub.grid
+            om = self.oracle.build_model(g, sub.fields["b"], p, sub.solver_params)
+            for name in SOLVE_FIELDS + ("gu_residual", "gv_residual"):
+                om.field(name)[...] = t[name].numpy().reshape(om.field(name).shape, order="F")
+            for w in ("wu", "wv"):
+                mask = t[f"{w}_mask"].numpy().reshape(om.mask(f"{w}_mask").shape, order="F")
+                om.mask(f"{w}_mask")[...] = mask
+                full = np.zeros(mask.shape, order="F")
+                full.ravel(order="F")[mask.ravel(order="F") != 0] = t[f"{w}_correction_coarse"].numpy()
+                om.field(f"{w}_correction_full")[...] = full
+            om.update_velocities()
+            for name, a in fields_from_oracle(om, g).items():
+                t[name] = torch.from_numpy(np.ascontiguousarray(np.asarray(a).ravel(order="F")))
+            stats.append({"status": 0})
+        return stats
+
+
+def test_ensemble_batched_sweep_matches_per_subdomain_sweep(oracle, converged):
+    """The sweep with the subdomains' velocity solves batched as ensemble members (host Models; their
+    pre- and post-solve steps on the host) gives the global velocities of the per-subdomain sweep (the
+    oracle's whole update_state per subdomain), with the oracle solving in both, for two sweeps."""
+    from wavi_gb300.model import Model
+    from wavi_gb300.schwarz import EnsembleSubdomainSolver, SchwarzSpec, build_subdomains, ras_sweeps
+    m, u, v = converged
+    rng = np.random.default_rng(3)
+    pu = u * (1 + 0.1 * rng.standard_normal(u.shape))
+    pv = v * (1 + 0.1 * rng.standard_normal(v.shape))
+    spec = SchwarzSpec(ngridsx=2, ngridsy=2, overlap=2, niterations=2, damping=0.2)
+    out = []
+    for batched in (False, True):
+        m.fields["u"][...] = pu
+        m.fields["v"][...] = pv
+        if batched:
+            subs = build_subdomains(m, spec, make=lambda *a: Model(*a))
+            solver = EnsembleSubdomainSolver(subs, ensemble=_OracleEnsemble(oracle, subs.values()), device="cpu")
+            ras_sweeps(m, spec, subs, solve_all=solver)
+        else:
+            subs = build_subdomains(m, spec, make=lambda *a: _OracleSubdomain(oracle.build_model(*a)))
+            ras_sweeps(m, spec, subs, solve=lambda s: s.om.update_state())
+        out.append((m.fields["u"].copy(), m.fields["v"].copy()))
+    (ua, va), (ub, vb) = out
+    m.fields["u"][...], m.fields["v"][...] = pu, pv
+    assert _uv_dist(m, ua, va) > 1e-2  # the sweeps moved the velocities
+    m.fields["u"][...], m.fields["v"][...] = ub, vb
+    assert _uv_dist(m, ua, va) < 1e-10

@@ -158,22 +158,89 @@ def build_subdomains(model, spec, make=None):
     return subs
 
 
-def ras_sweeps(model, spec, subdomains, solve=None):
+def ras_sweeps(model, spec, subdomains, solve=None, solve_all=None):
     """The Schwarz iterations of precondition!(model, ::SharedMemorySpec) (:98-155), run spec.niterations
-    times: restrict the global velocities into every subdomain, solve every subdomain (by default
-    update_state on a host Model), scale the global velocities by damping and add every subdomain's
-    velocities back through its partition of unity.  The residual test that precedes the sweeps in the
-    reference belongs to the caller's Picard loop."""
-    if solve is None:
+    times: restrict the global velocities into every subdomain, solve every subdomain (``solve_all`` on
+    all of them at once, e.g. an EnsembleSubdomainSolver; else ``solve`` on each, by default update_state
+    on a host Model), scale the global velocities by damping and add every subdomain's velocities back
+    through its partition of unity.  The residual test that precedes the sweeps in the reference belongs
+    to the caller's Picard loop."""
+    if solve is None and solve_all is None:
         from .model import update_state
         solve = update_state
     for _ in range(spec.niterations):
         for (igrid, jgrid), sub in subdomains.items():
             restrict_velocities(sub, model, igrid, jgrid, spec)
-        for sub in subdomains.values():
-            solve(sub)
+        if solve_all is not None:
+            solve_all(subdomains)
+        else:
+            for sub in subdomains.values():
+                solve(sub)
         model.fields["u"] *= spec.damping
         model.fields["v"] *= spec.damping
         for (igrid, jgrid), sub in subdomains.items():
             prolong_velocities(model, sub, igrid, jgrid, spec)
     return model
+
+
+class EnsembleSubdomainSolver:
+    """update_state on every subdomain with the velocity solves batched: the host steps before and after
+    the solve (pre_solve, post_solve_steps) run per subdomain, and the subdomains' velocity solves run as
+    the members of one ensemble (wavi_ensemble_solve_device: one context and stream per member, members of
+    different sizes), the way the reference runs them on threads (:112-120).
+
+    The ensemble is made once from the subdomains' grids and serves every sweep, and every set of
+    subdomain models built later from the same decomposition (build_subdomains after each Picard
+    relinearisation).  ``ensemble`` replaces it with any object that has the same solve_device, and
+    ``device`` names the torch device the member fields are staged on."""
+
+    def __init__(self, subdomains, precision="fp64", device=0, concurrency=16, ensemble=None):
+        subs = list(subdomains.values())
+        if ensemble is None:
+            from .ensemble import EnsembleSolver
+            ensemble = EnsembleSolver([s.grid for s in subs], [s.solver_params for s in subs], precision=precision,
+                                      device=device, concurrency=concurrency)
+            device = f"cuda:{device}"
+        self.ensemble = ensemble
+        self.device = device
+        self.shapes = [(s.grid.nx, s.grid.ny) for s in subs]
+
+    def __call__(self, subdomains):
+        from .model import post_solve_steps, pre_solve
+        subs = list(subdomains.values())
+        if [(s.grid.nx, s.grid.ny) for s in subs] != self.shapes:
+            raise ValueError("the subdomains do not match the ensemble's members")
+        for s in subs:
+            pre_solve(s)
+        tensors = [_member_tensors(s.fields, self.device) for s in subs]
+        stats = self.ensemble.solve_device([s.params for s in subs], tensors)
+        for s, t, st in zip(subs, tensors, stats):
+            _member_fields_back(s.fields, t)
+            s.last_stats = st
+        for s in subs:
+            post_solve_steps(s)
+        return stats
+
+
+def _member_tensors(fields, device):
+    """The velocity solve's fields (column-major, masks as bytes) as flat tensors on ``device``."""
+    import torch
+    from .gpu import ALL_FIELDS
+    out = {}
+    for name in ALL_FIELDS:
+        a = np.asarray(fields[name])
+        dt = np.uint8 if name in ("wu_mask", "wv_mask") else np.float64
+        out[name] = torch.from_numpy(np.ascontiguousarray(a.astype(dt).ravel(order="F"))).to(device)
+    return out
+
+
+def _member_fields_back(fields, tensors):
+    """The solved member's fields back into the host model, in place where the shape is unchanged."""
+    from .gpu import ALL_FIELDS
+    for name in ALL_FIELDS:
+        host = tensors[name].cpu().numpy()
+        cur = fields[name]
+        if name in ("wu_correction_coarse", "wv_correction_coarse"):
+            fields[name] = host.copy()
+        else:
+            cur[...] = host.reshape(cur.shape, order="F")
