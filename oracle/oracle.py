@@ -4,8 +4,8 @@ TEST INFRASTRUCTURE ONLY.  Imported by tests/, by ``__graft_entry__.smoke()`` to
 ``bench.py`` for the CPU-baseline leg.  The product (the package and libwavi_gpu.so) never imports it.
 
 Parity of the oracle itself is pinned against the reference's golden files (tests/golden/*.npz, made
-from test/version_update_test_verification/*.jld2) and its known-answer tests (pos_fraction, Kronecker
-products, sigma quadrature).
+from test/version_update_test_verification/*.jld2), its known-answer tests (pos_fraction, Kronecker
+products, sigma quadrature) and its analytic iceberg steady state (test/verification_tests/iceberg_test.jl).
 """
 import ctypes as C
 import os

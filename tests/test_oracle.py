@@ -124,3 +124,19 @@ def test_converged_solve_reaches_tolerance(oracle, pkg):
     st = m.stats()
     assert st["rel_residual"] < 1e-6
     assert 1 < st["picard_iterations"] < 60
+
+
+def test_iceberg_reaches_the_analytic_steady_state(oracle, pkg):
+    """The reference's iceberg verification (test/verification_tests.jl:3-10, iceberg_test.jl): 1000 yr of
+    dt = 0.1 time steps with one Picard iteration each reach the closed-form steady state to the
+    reference's tolerances (h 1e-4, u and v 3e-4, relative)."""
+    from wavi_gb300 import synthetic
+    g, bed, p, sp, ic = synthetic.iceberg_case()
+    om = oracle.build_model(g, bed, p, sp, ic)
+    om.run(10000, 0.1)
+    h0, u0, v0 = synthetic.iceberg_analytic(g)
+    hm = np.asarray(g.h_mask, bool)
+    um, vm = om.mask("u_mask").astype(bool), om.mask("v_mask").astype(bool)
+    assert synthetic.relative_error(om.field("h"), h0, hm) < 1.0e-4
+    assert synthetic.relative_error(om.field("u"), u0, um) < 3.0e-4
+    assert synthetic.relative_error(om.field("v"), v0, vm) < 3.0e-4
