@@ -207,7 +207,7 @@ class OracleModel:
         return du, dv
 
 
-COARSE_VARIANTS = {"cg": 0, "srcg": 2, "srcg_jacobi": 3, "srcg_chebyshev": 4}
+COARSE_VARIANTS = {"cg": 0, "srcg": 2, "srcg_jacobi": 3, "srcg_chebyshev": 4, "pipelined_chebyshev": 5}
 
 
 def set_coarse_variant(name):

@@ -301,8 +301,8 @@ struct Model {
   long last_cg_iters = 0;
   long op_applies = 0;
   std::vector<int> cg_iter_history;
-  Vec cheb_eig;           // coarse variant 4: the power vector (full wavelet layout, u then v), per solve
-  int cheb_vcycles = 0;   // coarse variant 4: V-cycles so far in this solve
+  Vec cheb_eig;           // coarse variants 4, 5: the power vector (full wavelet layout, u then v), per solve
+  int cheb_vcycles = 0;   // coarse variants 4, 5: V-cycles so far in this solve
   std::string err;
 };
 
@@ -834,6 +834,8 @@ int coarse_cg(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, doubl
 //      the two inner products of an iteration computed together after its operator application
 //   3  the same, preconditioned by the Jacobi diagonal of R A P
 //   4  the same, preconditioned by Chebyshev-accelerated Jacobi steps (coarse_srcg_chebyshev)
+//   5  pipelined CG with variant 4's preconditioner (coarse_pipelined_chebyshev): the restatement a GPU
+//      kernel that overlaps its reduction will be checked against; the GPU library does not have it yet
 // ---------------------------------------------------------------------------------------------
 int g_coarse_variant = 0;
 
@@ -923,52 +925,67 @@ static float cheb_start(int q) {  // in [-1, 1)
   const unsigned h = (unsigned)q * 2654435761u;
   return (float)((h >> 8) & 0xffffu) * (1.0f / 32768.0f) - 1.0f;
 }
-int coarse_srcg_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, double abstol, int maxiter) {
-  const size_t n = b.size(), nu = p.wu_idx.size();
-  Vec d = coarse_diag(m, w, p), minv(n);
-  for (size_t i = 0; i < n; ++i) minv[i] = d[i] != 0.0 ? 1.0 / d[i] : 0.0;
+// The preconditioner of variants 4 and 5: D⁻¹ and the Chebyshev interval from the power steps.
+struct ChebPrec {
+  Vec minv;
+  double th = 1.0, de = 1.0, sg = 1.0;
+};
+ChebPrec cheb_setup(Model& m, OpWork& w, const Precond& p) {
+  const size_t n = p.wu_idx.size() + p.wv_idx.size(), nu = p.wu_idx.size();
+  ChebPrec c;
+  Vec d = coarse_diag(m, w, p);
+  c.minv.resize(n);
+  for (size_t i = 0; i < n; ++i) c.minv[i] = d[i] != 0.0 ? 1.0 / d[i] : 0.0;
   auto full = [&](size_t k) { return k < nu ? p.wu_idx[k] : m.Nu + p.wv_idx[k - nu]; };
   Vec v(n), t;
-  for (size_t k = 0; k < n; ++k) v[k] = minv[k] != 0.0 ? m.cheb_eig[full(k)] + 1e-3 * (double)cheb_start(full(k)) : 0.0;
+  for (size_t k = 0; k < n; ++k)
+    v[k] = c.minv[k] != 0.0 ? m.cheb_eig[full(k)] + 1e-3 * (double)cheb_start(full(k)) : 0.0;
   ++m.cheb_vcycles;
   const int npow = m.cheb_vcycles <= 1 ? 12 : 4;
-  double th = 1.0, de = 1.0, sg = 1.0;
   for (int ps = 0; ps < npow; ++ps) {
     op_coarse(m, w, p, v, t);
-    for (size_t k = 0; k < n; ++k) t[k] = minv[k] * t[k];
+    for (size_t k = 0; k < n; ++k) t[k] = c.minv[k] * t[k];
     const double tt = dotp(t, t), vv = dotp(v, v);
     const double lam = (vv > 0.0 && tt > 0.0) ? std::sqrt(tt / vv) : 1.0;
     const double bmax = 1.15 * lam, amin = bmax / CHEB_RATIO;
-    th = 0.5 * (bmax + amin);
-    de = 0.5 * (bmax - amin);
-    sg = (bmax + amin) / (bmax - amin);
+    c.th = 0.5 * (bmax + amin);
+    c.de = 0.5 * (bmax - amin);
+    c.sg = (bmax + amin) / (bmax - amin);
     const double nrm = tt > 0.0 ? 1.0 / std::sqrt(tt) : 0.0;
     for (size_t k = 0; k < n; ++k) v[k] = t[k] * nrm;
   }
   for (size_t k = 0; k < n; ++k) m.cheb_eig[full(k)] = v[k];
-  auto prec = [&](const Vec& r, Vec& z) {
-    z.resize(n);
-    Vec dd(n), tt2;
+  return c;
+}
+// z = CHEB_STEPS Chebyshev steps on D⁻¹ R A P z = D⁻¹ r from z = 0
+void cheb_apply(Model& m, OpWork& w, const Precond& p, const ChebPrec& c, const Vec& r, Vec& z) {
+  const size_t n = r.size();
+  z.resize(n);
+  Vec dd(n), tt2;
+  for (size_t k = 0; k < n; ++k) {
+    z[k] = c.minv[k] * r[k];
+    z[k] = z[k] / c.th;
+    dd[k] = z[k];
+  }
+  double rho = 1.0 / c.sg;
+  for (int st = 1; st < CHEB_STEPS; ++st) {
+    op_coarse(m, w, p, z, tt2);
+    const double rn = 1.0 / (2.0 * c.sg - rho), c1 = rn * rho, c2 = 2.0 * rn / c.de;
     for (size_t k = 0; k < n; ++k) {
-      z[k] = minv[k] * r[k];
-      z[k] = z[k] / th;
-      dd[k] = z[k];
+      dd[k] = c1 * dd[k] + c2 * (c.minv[k] * (r[k] - tt2[k]));
+      z[k] = z[k] + dd[k];
     }
-    double rho = 1.0 / sg;
-    for (int st = 1; st < CHEB_STEPS; ++st) {
-      op_coarse(m, w, p, z, tt2);
-      const double rn = 1.0 / (2.0 * sg - rho), c1 = rn * rho, c2 = 2.0 * rn / de;
-      for (size_t k = 0; k < n; ++k) {
-        dd[k] = c1 * dd[k] + c2 * (minv[k] * (r[k] - tt2[k]));
-        z[k] = z[k] + dd[k];
-      }
-      rho = rn;
-    }
-  };
+    rho = rn;
+  }
+}
+
+int coarse_srcg_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, double abstol, int maxiter) {
+  const size_t n = b.size();
+  const ChebPrec cp = cheb_setup(m, w, p);
   Vec c, r = b, z, wv;
   op_coarse(m, w, p, x, c);
   for (size_t i = 0; i < n; ++i) r[i] -= c[i];
-  prec(r, z);
+  cheb_apply(m, w, p, cp, r, z);
   op_coarse(m, w, p, z, wv);
   double gamma = dotp(r, z), delta = dotp(wv, z), res = norm2(r);
   const double reltol = std::sqrt(2.220446049250313e-16);
@@ -980,7 +997,7 @@ int coarse_srcg_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const V
   while (!stop) {
     for (size_t i = 0; i < n; ++i) x[i] += alpha * pp[i];
     for (size_t i = 0; i < n; ++i) r[i] -= alpha * s[i];
-    prec(r, z);
+    cheb_apply(m, w, p, cp, r, z);
     op_coarse(m, w, p, z, wv);
     ++it;
     const double g2 = dotp(r, z), d2 = dotp(wv, z);
@@ -993,6 +1010,62 @@ int coarse_srcg_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const V
     if (!(alpha == alpha) || std::isinf(alpha)) break;
     for (size_t i = 0; i < n; ++i) pp[i] = z[i] + beta * pp[i];
     for (size_t i = 0; i < n; ++i) s[i] = wv[i] + beta * s[i];
+  }
+  return it;
+}
+
+// Variant 5: pipelined CG (Ghysels & Vanroose, "Hiding global synchronization latency in the
+// preconditioned Conjugate Gradient algorithm", Parallel Computing 40 (2014) 224-238) with variant 4's
+// preconditioner and cg!'s stopping rule.  The same iterates as variant 4 in exact arithmetic; each
+// iteration's one reduction depends on nothing that iteration's preconditioner and operator produce, so a
+// GPU kernel can run them while the reduction completes.  Per iteration:
+//   γ = (r,u), δ = (w,u), |r|;  m = M⁻¹ w;  n = A m;  stop?
+//   β = γ/γ', α = γ/(δ − β γ/α')   (β = 0, α = γ/δ in the first iteration)
+//   z = n + β z;  q = m + β q;  s = w + β s;  p = u + β p
+//   x += α p;  r −= α s;  u −= α q;  w −= α z
+// started from r = b − A x, u = M⁻¹ r, w = A u.  The last iteration's m and n are computed and unused,
+// as they would be on the GPU, where they run before the reduction that stops the loop is known.
+int coarse_pipelined_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, double abstol,
+                               int maxiter) {
+  const size_t n = b.size();
+  const ChebPrec cp = cheb_setup(m, w, p);
+  Vec c, r = b, u, wv, mm, nn;
+  op_coarse(m, w, p, x, c);
+  for (size_t i = 0; i < n; ++i) r[i] -= c[i];
+  cheb_apply(m, w, p, cp, r, u);
+  op_coarse(m, w, p, u, wv);
+  Vec z(n, 0.0), q(n, 0.0), s(n, 0.0), pp(n, 0.0);
+  const double reltol = std::sqrt(2.220446049250313e-16);
+  double tol = 0.0, gamma_prev = 0.0, alpha = 0.0;
+  int it = 0;
+  for (;;) {
+    const double gamma = dotp(r, u), delta = dotp(wv, u), res = norm2(r);
+    if (it == 0) tol = std::max(reltol * res, abstol);
+    cheb_apply(m, w, p, cp, wv, mm);
+    op_coarse(m, w, p, mm, nn);
+    if (it >= maxiter || res <= tol || !(res == res)) break;
+    double beta = 0.0;
+    if (it == 0) {
+      alpha = gamma / delta;
+    } else {
+      beta = gamma / gamma_prev;
+      alpha = gamma / (delta - beta * gamma / alpha);
+    }
+    if (!(alpha == alpha) || std::isinf(alpha)) break;
+    gamma_prev = gamma;
+    for (size_t i = 0; i < n; ++i) {
+      z[i] = nn[i] + beta * z[i];
+      q[i] = mm[i] + beta * q[i];
+      s[i] = wv[i] + beta * s[i];
+      pp[i] = u[i] + beta * pp[i];
+    }
+    for (size_t i = 0; i < n; ++i) {
+      x[i] += alpha * pp[i];
+      r[i] -= alpha * s[i];
+      u[i] -= alpha * q[i];
+      wv[i] -= alpha * z[i];
+    }
+    ++it;
   }
   return it;
 }
@@ -1022,6 +1095,7 @@ void vcycle(Model& m, OpWork& w, Precond& p, Vec& x, const Vec& b) {
   double abstol = m.S.tol_coarse * norm2(bc);
   p.last_cg = g_coarse_variant == 0   ? coarse_cg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
               : g_coarse_variant == 4 ? coarse_srcg_chebyshev(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
+              : g_coarse_variant == 5 ? coarse_pipelined_chebyshev(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
                                       : coarse_srcg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse, g_coarse_variant == 3);
   Vec pc;
   prolong_vec(m, p, p.corr, pc);

@@ -4,6 +4,9 @@
   Kronecker product vs kron    test/test_kronecker.jl:3-35
   σ-quadrature identities      test/test_fields.jl:71-76
   MISMIP+ 100-year golden      test/version_update_test_verification/test_version_updates.jl:6-97
+  iceberg analytic state       test/verification_tests/iceberg_test.jl, test/verification_tests.jl:3-10
+  MISMIP+ Ice0 grounding line  test/verification_tests/MISMIP_PLUS_Ice0.jl, test/verification_tests.jl:14-36
+                               (opt-in: WAVI_SLOW_TESTS=1)
 """
 import os
 
@@ -140,3 +143,31 @@ def test_iceberg_reaches_the_analytic_steady_state(oracle, pkg):
     assert synthetic.relative_error(om.field("h"), h0, hm) < 1.0e-4
     assert synthetic.relative_error(om.field("u"), u0, um) < 3.0e-4
     assert synthetic.relative_error(om.field("v"), v0, vm) < 3.0e-4
+
+
+def _grounding_line_x(haf, xxh):
+    """get_glx (src/utilities.jl:417-426): per row of cells along y, the x where the height above
+    floatation changes from positive to negative, linearly interpolated between the two cells; in the
+    reference's column-major order."""
+    glm = (np.diff(np.sign(haf), axis=0) == -2).T
+    x1, x2 = xxh[:-1, :].T[glm], xxh[1:, :].T[glm]
+    h1, h2 = haf[:-1, :].T[glm], haf[1:, :].T[glm]
+    return x1 + (x2 - x1) * (0.0 - h1) / (h2 - h1)
+
+
+@pytest.mark.skipif(not os.environ.get("WAVI_SLOW_TESTS"), reason="20 000 oracle time steps (~4.5 min); WAVI_SLOW_TESTS=1")
+def test_mismip_plus_ice0_grounding_line(oracle, pkg):
+    """The reference's MISMIP+ Ice0 verification (test/verification_tests.jl:14-36,
+    verification_tests/MISMIP_PLUS_Ice0.jl): 10 000 yr of dt = 0.5 from a 100 m slab on the 8 km channel.
+    The grounding line crosses every row, is symmetric about the centre line to 1e-4, and lies in the
+    reference's loose bands (the tight bands are marked broken there at this resolution)."""
+    m = _mismip_golden_model(oracle, pkg)
+    m.run(20000, 0.5)
+    g = pkg.Grid(nx=80, ny=10, nσ=4, x0=0.0, y0=-40000.0, dx=8000.0, dy=8000.0)
+    glx = _grounding_line_x(np.asarray(m.field("haf")), g.xxh)
+    ny = 10
+    assert glx.size == ny
+    t = glx[[0, ny // 2 - 1, ny // 2, ny - 1]]
+    assert (t[3] - t[0]) / (t[3] + t[0]) < 1e-4 and (t[1] - t[2]) / (t[1] + t[2]) < 1e-4
+    assert 480000 < t[0] < 550000 and 480000 < t[3] < 550000
+    assert 430000 < t[1] < 490000 and 430000 < t[2] < 490000

@@ -1,6 +1,7 @@
 """The oracle's restatements of the GPU library's opt-in coarse solvers (single-reduction CG, Jacobi on
-diag(R A P)), checked on the CPU against first principles: the probed diagonal against the explicitly
-assembled coarse matrix, and the single-reduction solves against the reference's cg! on the same problem."""
+diag(R A P), Chebyshev steps) and of the pipelined CG a GPU kernel is to follow, checked on the CPU against
+first principles: the probed diagonal against the explicitly assembled coarse matrix, and the
+single-reduction and pipelined solves against the reference's cg! on the same problem."""
 import numpy as np
 import pytest
 
@@ -67,7 +68,7 @@ def test_probed_coarse_diagonal_is_exact(oracle, shape):
     assert np.all(d[off] == 0.0)
 
 
-@pytest.mark.parametrize("variant", ["srcg", "srcg_jacobi", "srcg_chebyshev"])
+@pytest.mark.parametrize("variant", ["srcg", "srcg_jacobi", "srcg_chebyshev", "pipelined_chebyshev"])
 def test_single_reduction_coarse_solves_reach_the_reference_fixed_point(oracle, reference_cg, variant):
     from wavi_gb300 import synthetic
     sols = {}
@@ -85,5 +86,26 @@ def test_single_reduction_coarse_solves_reach_the_reference_fixed_point(oracle, 
     assert err < 1e-6
     if variant == "srcg_jacobi":  # the preconditioner must pay for itself
         assert s1["coarse_cg_iterations"] < 0.75 * s0["coarse_cg_iterations"]
-    if variant == "srcg_chebyshev":  # two more operator applications per iteration: at least 3x fewer iterations
+    if variant in ("srcg_chebyshev", "pipelined_chebyshev"):  # two more operator applications per iteration
         assert s1["coarse_cg_iterations"] < s0["coarse_cg_iterations"] / 3
+
+
+@pytest.mark.parametrize("mask", ["full", "disc"])
+def test_pipelined_cg_follows_the_single_reduction_iterates(oracle, reference_cg, mask):
+    """Pipelined CG (variant 5) and single-reduction CG (variant 4) with the same Chebyshev preconditioner
+    produce the same Krylov iterates in exact arithmetic: in FP64 their Picard and coarse iteration counts
+    agree (to 1 %) and their converged velocities to the Picard tolerance."""
+    from wavi_gb300 import synthetic
+    sols = {}
+    for v in ("srcg_chebyshev", "pipelined_chebyshev"):
+        oracle.set_coarse_variant(v)
+        g, bed, p, sp, ic = synthetic.small_case(nx=40, ny=16, mask=mask, maxiter_picard=60, tol_picard=1e-7)
+        om = oracle.build_model(g, bed, p, sp, ic)
+        om.pre_solve()
+        om.update_velocities()
+        sols[v] = (np.array(om.field("u")), np.array(om.field("v")), om.stats())
+    (u0, v0, s0), (u1, v1, s1) = sols["srcg_chebyshev"], sols["pipelined_chebyshev"]
+    assert s1["picard_iterations"] == s0["picard_iterations"]
+    assert abs(s1["coarse_cg_iterations"] - s0["coarse_cg_iterations"]) <= 0.01 * s0["coarse_cg_iterations"]
+    err = np.sqrt(np.sum((u1 - u0) ** 2) + np.sum((v1 - v0) ** 2)) / np.sqrt(np.sum(u0 ** 2) + np.sum(v0 ** 2))
+    assert err < 1e-9
