@@ -1024,7 +1024,9 @@ int coarse_srcg_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const V
 //   z = n + β z;  q = m + β q;  s = w + β s;  p = u + β p
 //   x += α p;  r −= α s;  u −= α q;  w −= α z
 // started from r = b − A x, u = M⁻¹ r, w = A u.  The last iteration's m and n are computed and unused,
-// as they would be on the GPU, where they run before the reduction that stops the loop is known.
+// as they would be on the GPU, where they run before the reduction that stops the loop is known.  In FP64
+// the recurrences hold; in FP32 the recursively updated residual drifts away from b − A x (by ~1e-4 of
+// ‖b‖ on the coarse systems here), so an FP32 kernel needs periodic residual replacement.
 int coarse_pipelined_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, double abstol,
                                int maxiter) {
   const size_t n = b.size();
