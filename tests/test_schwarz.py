@@ -28,6 +28,9 @@ def test_subdomain_ranges():
         subdomain_range(30, 8, 1, 1, spec)
     with pytest.raises(IndexError):
         subdomain_range(32, 8, 5, 1, spec)
+    for bad in (dict(overlap=0), dict(ngridsx=0), dict(niterations=-1)):
+        with pytest.raises(ValueError):
+            SchwarzSpec(**bad)
 
 
 @pytest.mark.parametrize("ngx,ngy,overlap", [(4, 2, 2), (2, 2, 1), (8, 1, 2), (2, 4, 1), (1, 1, 3)])

@@ -32,6 +32,16 @@ class SchwarzSpec:
     niterations: int = 0
     damping: float = 0.0
 
+    def __post_init__(self):
+        # the reference does not check these; overlap 0 gives its partition of unity ramps of length 0 and
+        # -1, and NaN weights
+        if self.ngridsx < 1 or self.ngridsy < 1:
+            raise ValueError("ngridsx and ngridsy must be >= 1")
+        if self.overlap < 1:
+            raise ValueError("overlap must be >= 1")
+        if self.niterations < 0:
+            raise ValueError("niterations must be >= 0")
+
 
 def subdomain_range(nx, ny, igrid, jgrid, spec):
     """The h cells of subdomain (igrid, jgrid) (1-based, as in the reference) as 0-based half-open ranges
