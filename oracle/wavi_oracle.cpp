@@ -834,8 +834,8 @@ int coarse_cg(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, doubl
 //      the two inner products of an iteration computed together after its operator application
 //   3  the same, preconditioned by the Jacobi diagonal of R A P
 //   4  the same, preconditioned by Chebyshev-accelerated Jacobi steps (coarse_srcg_chebyshev)
-//   5  pipelined CG with variant 4's preconditioner (coarse_pipelined_chebyshev): the restatement a GPU
-//      kernel that overlaps its reduction will be checked against; the GPU library does not have it yet
+//   5  pipelined CG with variant 4's preconditioner and residual replacement (coarse_pipelined_chebyshev),
+//      the GPU library's opt-in WAVI_COARSE_PIPELINED_CHEBYSHEV
 // ---------------------------------------------------------------------------------------------
 int g_coarse_variant = 0;
 
@@ -1024,9 +1024,11 @@ int coarse_srcg_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const V
 //   z = n + β z;  q = m + β q;  s = w + β s;  p = u + β p
 //   x += α p;  r −= α s;  u −= α q;  w −= α z
 // started from r = b − A x, u = M⁻¹ r, w = A u.  The last iteration's m and n are computed and unused,
-// as they would be on the GPU, where they run before the reduction that stops the loop is known.  In FP64
-// the recurrences hold; in FP32 the recursively updated residual drifts away from b − A x (by ~1e-4 of
-// ‖b‖ on the coarse systems here), so an FP32 kernel needs periodic residual replacement.
+// as they are on the GPU, where they run before the reduction that stops the loop is known.  In FP32 the
+// recursively updated residual drifts from b − A x (by ~1e-4 of ‖b‖ on the coarse systems here), so every
+// PCG_REPLACE iterations r, u, w are recomputed from x, and s = A p, q = M⁻¹ s, z = A q from p (residual
+// replacement), as the GPU library's k_pcg_persistent does; in FP64 that changes the iterates by rounding.
+constexpr int PCG_REPLACE = 25;
 int coarse_pipelined_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, double abstol,
                                int maxiter) {
   const size_t n = b.size();
@@ -1041,6 +1043,15 @@ int coarse_pipelined_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, co
   double tol = 0.0, gamma_prev = 0.0, alpha = 0.0;
   int it = 0;
   for (;;) {
+    if (it > 0 && it % PCG_REPLACE == 0) {
+      op_coarse(m, w, p, x, c);
+      for (size_t i = 0; i < n; ++i) r[i] = b[i] - c[i];
+      cheb_apply(m, w, p, cp, r, u);
+      op_coarse(m, w, p, u, wv);
+      op_coarse(m, w, p, pp, s);
+      cheb_apply(m, w, p, cp, s, q);
+      op_coarse(m, w, p, q, z);
+    }
     const double gamma = dotp(r, u), delta = dotp(wv, u), res = norm2(r);
     if (it == 0) tol = std::max(reltol * res, abstol);
     cheb_apply(m, w, p, cp, wv, mm);

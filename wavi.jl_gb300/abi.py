@@ -22,7 +22,7 @@ SOFT_STATUS = (-4, -5)  # results are written; mirrors the reference's silent st
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
-COARSE_SOLVERS = {"auto": 0, "cg": 1, "srcg": 2, "srcg_jacobi": 3, "srcg_chebyshev": 4}  # wavi_coarse_solver
+COARSE_SOLVERS = {"auto": 0, "cg": 1, "srcg": 2, "srcg_jacobi": 3, "srcg_chebyshev": 4, "pipelined_chebyshev": 5}  # wavi_coarse_solver
 COARSE_SOLVER_NAMES = {v: k for k, v in COARSE_SOLVERS.items()}
 
 _dp = C.POINTER(C.c_double)

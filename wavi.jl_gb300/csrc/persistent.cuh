@@ -13,6 +13,8 @@
 //   k_srcg_persistent single-reduction CG (Chronopoulos & Gear 1989), preconditioned by nothing, by
 //                     the Jacobi diagonal, or by Chebyshev-accelerated Jacobi steps: both inner products
 //                     of an iteration follow its operator application, one grid reduction per iteration
+//   k_pcg_persistent  pipelined CG with the Chebyshev preconditioner (FP32 fast path only; opt-in): the
+//                     grid reduction of an iteration completes while its preconditioner and operator run
 //
 // The FP64 and global-memory instantiations separate the prolongation from the operator by a grid
 // barrier.  The FP32 instantiations on 16 x 16 tiles (the fast path) keep the tiles' coefficients in
@@ -220,6 +222,105 @@ __device__ __forceinline__ bool grid_sync(GridBar* bar, double* __restrict__ par
   if (NS > 0) {
     // warp q adds partial q of every CTA: eight slots per lane and round, added as a tree, then a
     // butterfly (a fixed order, so every CTA obtains the same bits)
+    if (wid < NS) {
+      const S* src = slot + wid * nb;
+      S s{};
+      for (unsigned k0 = 0; k0 < nb; k0 += 256) {
+        S b[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const unsigned k = k0 + lane + 32u * e;
+          b[e] = k < nb ? ld_cg(src + k) : S{};
+        }
+        s = s + (((b[0] + b[1]) + (b[2] + b[3])) + ((b[4] + b[5]) + (b[6] + b[7])));
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s = s + shfl_xor(s, o);
+      if (lane == 0) tot[wid] = s;
+    }
+    __syncthreads();
+    if (t == 0) scalars(static_cast<const S*>(tot));
+    __syncthreads();
+  }
+  return true;
+}
+
+// grid_sync in two halves, for a kernel with work to do while the grid sum completes (k_pcg_persistent):
+// grid_arrive publishes this CTA's partials and arrives, as the first half of grid_sync does; grid_wait
+// waits for every CTA's arrival, adds the partials and runs `scalars` in thread 0, as the second half
+// does, and ends with a __syncthreads.  Between the halves a CTA may exchange tagged words with its
+// neighbours, but it starts no other grid reduction or barrier and leaves ss alone.  The parity argument
+// of grid_sync holds unchanged: a CTA reaches the arrival of epoch e + 2 only after the wait of e + 1,
+// which needs every CTA's arrival at e + 1, which each CTA makes after its own wait of e.
+template <int NS, typename A>
+__device__ __forceinline__ void grid_arrive(GridBar* bar, double* __restrict__ partials, unsigned& epoch, SyncShared& ss,
+                                            const A (&v)[4]) {
+  using S = typename CGReal<A>::type;
+  static_assert(sizeof(S) == sizeof(double), "partial slots are 8 bytes");
+  const int t = flat_tid(), lane = t & 31, wid = t >> 5, nw = (flat_nthreads() + 31) >> 5;
+  const unsigned nb = gridDim.x;
+  ++epoch;
+  S* slot = reinterpret_cast<S*>(partials + (size_t)(epoch & 1u) * 4u * nb);
+  S(*wsum)[4] = reinterpret_cast<S(*)[4]>(ss.warp);
+  if (NS > 0) {
+    A x[4];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+      x[q] = v[q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x[q] += __shfl_xor_sync(0xffffffffu, x[q], o);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int q = 0; q < NS; ++q) wsum[wid][q] = real_term(x[q]);
+  }
+  __syncthreads();
+  if (wid == 0 && NS > 0) {
+    const int q = lane & 3;
+    S s{};
+    if constexpr (std::is_same<A, float>::value) {
+      float f = 0.f;
+      if (q < NS)
+        for (int k = lane >> 2; k < nw; k += 8) f += wsum[k][q].hi;
+#pragma unroll
+      for (int o = 4; o < 32; o <<= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
+      s = real_term(f);
+    } else {
+      if (q < NS)
+        for (int k = lane >> 2; k < nw; k += 8) s = s + wsum[k][q];
+#pragma unroll
+      for (int o = 4; o < 32; o <<= 1) s = s + shfl_xor(s, o);
+    }
+    if (lane < NS) slot[lane * nb + blockIdx.x] = s;
+    __syncwarp();
+  }
+  if (t == 0) red_release_add_u32(&bar->count, 1u);
+}
+template <int NS, typename A, typename F>
+__device__ __forceinline__ bool grid_wait(GridBar* bar, double* __restrict__ partials, unsigned epoch, SyncShared& ss,
+                                          F&& scalars) {
+  using S = typename CGReal<A>::type;
+  const int t = flat_tid(), lane = t & 31, wid = t >> 5;
+  const unsigned nb = gridDim.x;
+  const S* slot = reinterpret_cast<const S*>(partials + (size_t)(epoch & 1u) * 4u * nb);
+  S* tot = reinterpret_cast<S*>(ss.tot);
+  if (t == 0) {
+    const unsigned target = epoch * nb;
+    int ok = 1;
+    long polls = 0;
+    while ((int)(ld_acquire_u32(&bar->count) - target) < 0) {
+      if (++polls > kBarrierSpinLimit || ((polls & 255) == 0 && *(volatile int*)&bar->err)) {
+        ok = 0;
+        break;
+      }
+      if (polls > 8) __nanosleep(32);
+    }
+    if (!ok) atomicExch(&bar->err, 1);
+    ss.ok = ok;
+  }
+  __syncthreads();
+  if (!ss.ok) return false;
+  if (NS > 0) {
     if (wid < NS) {
       const S* src = slot + wid * nb;
       S s{};
@@ -1371,6 +1472,299 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
         su[k] = fmul_add(beta, su[k], wu[k]);
         sv[k] = fmul_add(beta, sv[k], wv[k]);
       }
+    first = false;
+  }
+#pragma unroll
+  for (int k = 0; k < MAXT; ++k)
+    if (own[k]) {
+      const int i = i0s[k] + tx, j = j0s[k] + ty;
+      if (i <= d.nx && j < d.ny) xc[uidx(d, i, j)] = xu[k];
+      if (i < d.nx && j <= d.ny) xc[vidx(d, i, j)] = xv[k];
+    }
+  if (blockIdx.x == 0 && tx == 0 && ty == 0) {
+    st->cg_it = it;
+    st->cg_total += it;
+    st->cg_res = cg_final_res(sc);
+    st->cg_tol = sc.tol;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Pipelined CG (Ghysels & Vanroose, "Hiding global synchronization latency in the preconditioned
+// Conjugate Gradient algorithm", Parallel Computing 40 (2014) 224-238) on the FP32 fast path, with
+// k_srcg_persistent's Chebyshev-accelerated Jacobi preconditioner M and cg!'s stopping rule.  The same
+// iterates as k_srcg_persistent in exact arithmetic; each iteration's one grid reduction (arrived at by
+// grid_arrive) completes while the CTA applies M and A, which need only neighbour exchanges:
+//   γ = (r,u), δ = (w,u), |r|²  → arrive;  m = M⁻¹ w;  n = A m;  wait;  stop?
+//   z = n + β z;  q = m + β q;  s = w + β s;  p = u + β p;  x += α p;  r −= α s;  u −= α q;  w −= α z
+// from r = b − A x, u = M⁻¹ r, w = A u.  In FP32 the recursively updated r, u, w drift from b − A x, so
+// every kPcgReplace iterations they are recomputed (residual replacement), with s = A p, q = M⁻¹ s and
+// z = A q.  The oracle's coarse_pipelined_chebyshev states the same iteration, replacement included, in
+// FP64.  x, r, u, w and the preconditioner's vectors stay in registers; p, s, q, z live in shared memory
+// (each thread touches only its own points of them).
+constexpr int kPcgReplace = 25;
+
+template <typename T, int TILE, int MAXT>
+struct PcgShared {
+  T v[4][MAXT][2][TILE * TILE];  // p, s, q, z: [vector][tile][u, v][thread]
+};
+
+template <typename T, int TILE, int MAXT>
+__global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
+    k_pcg_persistent(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, const T* __restrict__ dcoarse,
+                     const T* __restrict__ bc, T* __restrict__ xc, double* __restrict__ partials, DevState* st,
+                     const DevParams* __restrict__ P, GridBar* bar, unsigned long long* __restrict__ halo, int cheb,
+                     float cheb_ratio, T* __restrict__ eig, int ntx, int nty) {
+  static_assert(!std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value, "the pipelined CG needs the FP32 fast path");
+  __shared__ CGShared<T, TILE> sm;
+  __shared__ SyncShared ss;
+  __shared__ CGScalars<T> sc;
+  __shared__ FastSharedFor<T, TILE, MAXT> fs;
+  __shared__ PcgShared<T, TILE, MAXT> pv;
+  __shared__ T cheb_s[3];  // θ, δ, σ of the Chebyshev interval
+  enum { VP = 0, VS = 1, VQ = 2, VZ = 3 };
+  PointCoef<T> pc[MAXT] = {};
+  const int ntiles = ntx * nty;
+  const int tx = threadIdx.x, ty = threadIdx.y, lin = ty * TILE + tx;
+  T xu[MAXT], xv[MAXT], ru[MAXT], rv[MAXT], uu[MAXT], uv[MAXT], wu[MAXT], wv[MAXT];
+  T mu[MAXT], mv[MAXT], nu[MAXT], nv[MAXT], iu[MAXT], iv[MAXT];  // iu, iv: D⁻¹ (0 off the coarse space)
+  T cdu[MAXT], cdv[MAXT];                                        // Chebyshev direction
+  T hu[MAXT], hv[MAXT];                                          // the tiles' prolonged vectors
+  int i0s[MAXT], j0s[MAXT];
+  bool own[MAXT];
+#pragma unroll
+  for (int k = 0; k < MAXT; ++k) {
+    const int t = blockIdx.x + k * gridDim.x;
+    own[k] = t < ntiles;
+    i0s[k] = own[k] ? (t % ntx) * TILE : 0;
+    j0s[k] = own[k] ? (t / ntx) * TILE : 0;
+    const int i = i0s[k] + tx, j = j0s[k] + ty;
+    const bool inu = own[k] && i <= d.nx && j < d.ny, inv = own[k] && i < d.nx && j <= d.ny;
+    xu[k] = inu ? xc[uidx(d, i, j)] : (T)0;
+    xv[k] = inv ? xc[vidx(d, i, j)] : (T)0;
+    const T du = inu ? dcoarse[uidx(d, i, j)] : (T)0, dv = inv ? dcoarse[vidx(d, i, j)] : (T)0;
+    iu[k] = du != (T)0 ? (T)1 / du : (T)0;
+    iv[k] = dv != (T)0 ? (T)1 / dv : (T)0;
+    ru[k] = rv[k] = uu[k] = uv[k] = wu[k] = wv[k] = mu[k] = mv[k] = nu[k] = nv[k] = cdu[k] = cdv[k] = (T)0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) pv.v[q][k][0][lin] = pv.v[q][k][1][lin] = (T)0;
+  }
+  unsigned epoch = 0;
+  int it = 0;
+  const int maxit = P->maxiter_coarse;
+  const double tol_coarse = P->tol_coarse;
+  TagState ts{halo, 0u, 0u, (size_t)ntiles * 8 * TILE};
+  ts.base = *(volatile unsigned*)&bar->gen << 21;
+  volatile int* fail = &fs.fail;
+  if (tx == 0 && ty == 0) fs.fail = 0;
+#pragma unroll
+  for (int k = 0; k < MAXT; ++k)
+    if (own[k]) load_coef_tile<T, TILE>(d, cf, wmask, i0s[k], j0s[k], fs.ct[k], pc[k]);
+  // (all of it is read after a __syncthreads)
+  auto prolong = [&](int k, T a, T b) {
+    prolong_publish<T, TILE>(levels, pc[k], a, b, blockIdx.x + k * gridDim.x, sm, fs.hs2, ts, hu[k], hv[k]);
+  };
+  auto apply = [&](int k, T& c1, T& c2) -> bool {
+    return apply_tagged<T, TILE>(d, levels, fs.ct[k], pc[k], hu[k], hv[k], i0s[k], j0s[k], ntx, sm, fs.hs2, ts, bar,
+                                 fail, c1, c2);
+  };
+  // (ou, ov) = R A P (au, av): one neighbour exchange
+  auto op = [&](const T (&au)[MAXT], const T (&av)[MAXT], T (&ou)[MAXT], T (&ov)[MAXT]) -> bool {
+    ++ts.hx;  // a new exchange
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) prolong(k, au[k], av[k]);
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k] && !apply(k, ou[k], ov[k])) return false;
+    return true;
+  };
+  // (ou, ov) = M⁻¹ (au, av): cheb steps of the Chebyshev iteration on D⁻¹ R A P z = D⁻¹ a from z = 0, as
+  // k_srcg_persistent's precond (cheb - 1 exchanges, no reduction)
+  auto precond = [&](const T (&au)[MAXT], const T (&av)[MAXT], T (&ou)[MAXT], T (&ov)[MAXT]) -> bool {
+    const T th = cheb_s[0], de = cheb_s[1], sg = cheb_s[2];
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k) {
+      ou[k] = iu[k] * au[k];
+      ov[k] = iv[k] * av[k];
+      ou[k] = ou[k] / th;
+      ov[k] = ov[k] / th;
+      cdu[k] = ou[k];
+      cdv[k] = ov[k];
+    }
+    T rho = (T)1 / sg;
+    for (int stp = 1; stp < cheb; ++stp) {
+      ++ts.hx;  // a new exchange
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k)
+        if (own[k]) prolong(k, ou[k], ov[k]);
+      const T rn = (T)1 / ((T)2 * sg - rho), c1 = rn * rho, c2 = (T)2 * rn / de;
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k)
+        if (own[k]) {
+          T tu, tv;
+          if (!apply(k, tu, tv)) return false;
+          cdu[k] = c1 * cdu[k] + c2 * (iu[k] * (au[k] - tu));
+          cdv[k] = c1 * cdv[k] + c2 * (iv[k] * (av[k] - tv));
+          ou[k] = ou[k] + cdu[k];
+          ov[k] = ov[k] + cdv[k];
+        }
+      rho = rn;
+    }
+    return true;
+  };
+  // λmax of D⁻¹ R A P by power steps, as in k_srcg_persistent
+  {
+    T eu[MAXT], ev[MAXT];
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k) {
+      const int i = i0s[k] + tx, j = j0s[k] + ty;
+      const bool inu = own[k] && i <= d.nx && j < d.ny, inv = own[k] && i < d.nx && j <= d.ny;
+      const int qu = inu ? uidx(d, i, j) : 0, qv = inv ? vidx(d, i, j) : 0;
+      eu[k] = iu[k] != (T)0 ? eig[qu] + (T)1e-3 * cheb_start(qu) : (T)0;
+      ev[k] = iv[k] != (T)0 ? eig[qv] + (T)1e-3 * cheb_start(qv) : (T)0;
+    }
+    const int npow = st->picard_it <= 1 ? 12 : 4;
+    for (int pstep = 0; pstep < npow; ++pstep) {
+      ++ts.hx;  // a new exchange
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k)
+        if (own[k]) prolong(k, eu[k], ev[k]);
+      T a2[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k)
+        if (own[k]) {
+          T tu, tv;
+          if (!apply(k, tu, tv)) return;
+          tu = iu[k] * tu;
+          tv = iv[k] * tv;
+          a2[0] += tu * tu + tv * tv;
+          a2[1] += eu[k] * eu[k] + ev[k] * ev[k];
+          eu[k] = tu;
+          ev[k] = tv;
+        }
+      if (!grid_sync<2>(bar, partials, epoch, ss, a2, [&](const typename CGReal<T>::type* tot) {
+            const double tt = dbl_of(tot[0]), vv = dbl_of(tot[1]);
+            const double lam = (vv > 0.0 && tt > 0.0) ? sqrt(tt / vv) : 1.0;
+            const double bmax = 1.15 * lam, amin = bmax / (double)cheb_ratio;
+            cheb_s[0] = (T)(0.5 * (bmax + amin));
+            cheb_s[1] = (T)(0.5 * (bmax - amin));
+            cheb_s[2] = (T)((bmax + amin) / (bmax - amin));
+            sc.alpha_t = (T)(tt > 0.0 ? 1.0 / sqrt(tt) : 0.0);  // the normalisation of the power vector
+          }))
+        return;
+      const T nrm = sc.alpha_t;
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k) {
+        eu[k] = eu[k] * nrm;
+        ev[k] = ev[k] * nrm;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        const int i = i0s[k] + tx, j = j0s[k] + ty;
+        if (i <= d.nx && j < d.ny) eig[uidx(d, i, j)] = eu[k];
+        if (i < d.nx && j <= d.ny) eig[vidx(d, i, j)] = ev[k];
+      }
+  }
+  // r = b_c − R A P x (and |b_c|² for the tolerance); u = M⁻¹ r; w = R A P u
+  T bb = 0;
+  auto residual = [&]() -> bool {
+    if (!op(xu, xv, nu, nv)) return false;
+    bb = 0;
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        const int i = i0s[k] + tx, j = j0s[k] + ty;
+        const T bu = (i <= d.nx && j < d.ny) ? bc[uidx(d, i, j)] : (T)0;
+        const T bv = (i < d.nx && j <= d.ny) ? bc[vidx(d, i, j)] : (T)0;
+        ru[k] = bu - nu[k];
+        rv[k] = bv - nv[k];
+        bb += bu * bu + bv * bv;
+      }
+    if (!precond(ru, rv, uu, uv)) return false;
+    return op(uu, uv, wu, wv);
+  };
+  if (!residual()) return;
+  bool first = true;
+  for (;;) {
+    if (!first && it % kPcgReplace == 0) {
+      // residual replacement: r, u, w from x; s = A p, q = M⁻¹ s, z = A q from p
+      if (!residual()) return;
+      T tu[MAXT], tv[MAXT], su_[MAXT], sv_[MAXT];
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k) {
+        tu[k] = pv.v[VP][k][0][lin];
+        tv[k] = pv.v[VP][k][1][lin];
+      }
+      if (!op(tu, tv, su_, sv_)) return;
+      if (!precond(su_, sv_, tu, tv)) return;
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k) {
+        pv.v[VS][k][0][lin] = su_[k];
+        pv.v[VS][k][1][lin] = sv_[k];
+        pv.v[VQ][k][0][lin] = tu[k];
+        pv.v[VQ][k][1][lin] = tv[k];
+      }
+      if (!op(tu, tv, su_, sv_)) return;
+#pragma unroll
+      for (int k = 0; k < MAXT; ++k) {
+        pv.v[VZ][k][0][lin] = su_[k];
+        pv.v[VZ][k][1][lin] = sv_[k];
+      }
+    }
+    T a[4] = {T(0), T(0), T(0), first ? bb : T(0)};
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        a[0] += ru[k] * uu[k] + rv[k] * uv[k];
+        a[1] += wu[k] * uu[k] + wv[k] * uv[k];
+        a[2] += ru[k] * ru[k] + rv[k] * rv[k];
+      }
+    grid_arrive<4>(bar, partials, epoch, ss, a);
+    // m = M⁻¹ w and n = R A P m while the grid sum completes
+    if (!precond(wu, wv, mu, mv)) return;
+    if (!op(mu, mv, nu, nv)) return;
+    if (!grid_wait<4, T>(bar, partials, epoch, ss, [&](const typename CGReal<T>::type* tot) {
+          srcg_scalars<T>(sc, tot, first, it, maxit, tol_coarse);
+        }))
+      return;
+    if (sc.stop) break;
+    const T alpha = sc.alpha_t, beta = sc.beta_t;
+#pragma unroll
+    for (int k = 0; k < MAXT; ++k)
+      if (own[k]) {
+        T z0 = pv.v[VZ][k][0][lin], z1 = pv.v[VZ][k][1][lin];
+        T q0 = pv.v[VQ][k][0][lin], q1 = pv.v[VQ][k][1][lin];
+        T s0 = pv.v[VS][k][0][lin], s1 = pv.v[VS][k][1][lin];
+        T p0 = pv.v[VP][k][0][lin], p1 = pv.v[VP][k][1][lin];
+        z0 = fmul_add(beta, z0, nu[k]);
+        z1 = fmul_add(beta, z1, nv[k]);
+        q0 = fmul_add(beta, q0, mu[k]);
+        q1 = fmul_add(beta, q1, mv[k]);
+        s0 = fmul_add(beta, s0, wu[k]);
+        s1 = fmul_add(beta, s1, wv[k]);
+        p0 = fmul_add(beta, p0, uu[k]);
+        p1 = fmul_add(beta, p1, uv[k]);
+        xu[k] = fmul_add(alpha, p0, xu[k]);
+        xv[k] = fmul_add(alpha, p1, xv[k]);
+        ru[k] = fmul_add(-alpha, s0, ru[k]);
+        rv[k] = fmul_add(-alpha, s1, rv[k]);
+        uu[k] = fmul_add(-alpha, q0, uu[k]);
+        uv[k] = fmul_add(-alpha, q1, uv[k]);
+        wu[k] = fmul_add(-alpha, z0, wu[k]);
+        wv[k] = fmul_add(-alpha, z1, wv[k]);
+        pv.v[VZ][k][0][lin] = z0;
+        pv.v[VZ][k][1][lin] = z1;
+        pv.v[VQ][k][0][lin] = q0;
+        pv.v[VQ][k][1][lin] = q1;
+        pv.v[VS][k][0][lin] = s0;
+        pv.v[VS][k][1][lin] = s1;
+        pv.v[VP][k][0][lin] = p0;
+        pv.v[VP][k][1][lin] = p1;
+      }
+    ++it;
     first = false;
   }
 #pragma unroll

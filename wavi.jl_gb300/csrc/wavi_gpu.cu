@@ -445,6 +445,15 @@ int launch_cg_persistent(wavi_ctx* c) {
     CK(cudaLaunchKernelEx(&cfg, k_cg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
                           (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
                           c->halo_box, c->ntx, c->nty));
+  } else if (c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV) {
+    if constexpr (std::is_same<T, float>::value && TILE == 16 && MAXT <= 2) {
+      CK(cudaLaunchKernelEx(&cfg, k_pcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c),
+                            (const uint8_t*)c->wmask_uv, (const T*)c->dcoarse, (const T*)c->bc, (T*)c->xc, c->partials,
+                            c->S, (const DevParams*)c->P, c->bar, c->halo_box, kChebSteps, kChebRatio,
+                            (T*)c->cheb_eig, c->ntx, c->nty));
+    } else {
+      return fail(c, WAVI_ERR_ARGUMENT, "the pipelined coarse CG has no kernel for this precision and tiling");
+    }
   } else {
     const bool cheb = c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV;
     const T* dc = (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI || cheb) ? (const T*)c->dcoarse : nullptr;
@@ -497,7 +506,8 @@ void launch_coarse_diag(wavi_ctx* c, T* dst) {
 template <typename T, int TILE>
 int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& tc) {
   const Dims& d = c->d;
-  if (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI || c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV) {
+  if (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI || c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV ||
+      c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV) {
     launch_coarse_diag<T, TILE>(c, (T*)c->dcoarse);
     CKL();
     tv.launches++;
@@ -725,6 +735,15 @@ int build_graph(wavi_ctx* c) {
 template <int MAXT, typename T, int TILE>
 int resident_ctas(int nsm, int solver) {
   int per_sm = 0;
+  if (solver == WAVI_COARSE_PIPELINED_CHEBYSHEV) {
+    if constexpr (std::is_same<T, float>::value && TILE == 16 && MAXT <= 2) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent<T, TILE, MAXT>, TILE * TILE, 0) !=
+          cudaSuccess)
+        return 0;
+      return per_sm * nsm;
+    }
+    return 0;
+  }
   cudaError_t e = solver == WAVI_COARSE_CG
                       ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_persistent<T, TILE, MAXT>, TILE * TILE, 0)
                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_srcg_persistent<T, TILE, MAXT>, TILE * TILE, 0);
@@ -1426,7 +1445,7 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   c->nty = (int)c->tile_grid.y;
   // coarse solver: the reference's cg! recurrence, or (persistent kernel only) single-reduction CG
   const int want = opt->coarse_solver;
-  if (want < WAVI_COARSE_AUTO || want > WAVI_COARSE_SRCG_CHEBYSHEV)
+  if (want < WAVI_COARSE_AUTO || want > WAVI_COARSE_PIPELINED_CHEBYSHEV)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_solver %d", want));
   if (opt->coarse_kernel < 0 || opt->coarse_kernel > 3)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_kernel %d", opt->coarse_kernel));
@@ -1458,6 +1477,9 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
         return bail(fail(c, WAVI_ERR_ARGUMENT, "the Chebyshev coarse solve needs the register-resident persistent kernel"));
       c->coarse_solver = WAVI_COARSE_SRCG_JACOBI;
     }
+    if (c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV && (!mixed(c) || c->tile != 16 || c->pers_maxt <= 0))
+      return bail(fail(c, WAVI_ERR_ARGUMENT,
+                       "the pipelined coarse CG needs mixed precision, 16 x 16 tiles and the register-resident kernel"));
   } else {
     c->coarse_solver = WAVI_COARSE_CG;
   }
@@ -1479,7 +1501,7 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     double* q = nullptr;
     if ((r = dalloc(c, &q, N))) return bail(r);
     c->dcoarse = q;
-    if (c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV) {
+    if (c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV || c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV) {
       if ((r = dalloc(c, &q, N))) return bail(r);
       c->cheb_eig = q;
     }

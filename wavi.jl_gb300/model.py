@@ -31,7 +31,8 @@ class GPUParallelSpec:
     precision: str = "fp64"     # "fp64" (reference algorithm) or "mixed"
     use_graphs: bool = True
     picard_test: int = 0
-    coarse_solver: str = "auto"  # "auto", "cg" (reference), "srcg", "srcg_jacobi", "srcg_chebyshev" (single-reduction CG)
+    coarse_solver: str = "auto"  # "auto", "cg" (reference), "srcg", "srcg_jacobi", "srcg_chebyshev" (single-reduction
+    #                              CG), "pipelined_chebyshev" (opt-in)
     device_run: bool = False     # run_simulation without a callback keeps the model on the device (wavi_run_device)
 
 
