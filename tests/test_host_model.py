@@ -92,3 +92,28 @@ def test_post_solve_and_thickness_step_match_oracle(oracle, pkg, mask):
     update_thickness(Simulation(m, TimesteppingParams(dt=dt, end_time=dt)))
     om.update_thickness(dt)
     assert np.allclose(m.fields["h"], om.field("h"), rtol=1e-14, atol=1e-12)
+
+
+def test_volume_above_floatation_closed_form(pkg):
+    """The reference's known answer (test/test_utils.jl:33-42): 500 m of ice on a bed 200 m below sea level
+    over 20 x 25 cells of 1 km²."""
+    from wavi_gb300.model import Model, volume_above_floatation
+    g = pkg.Grid(nx=20, ny=25, dx=1000.0, dy=1000.0)
+    m = Model(g, -200.0 * np.ones((20, 25)), initial_conditions=pkg.InitialConditions(
+        initial_thickness=500.0 * np.ones((20, 25))))
+    vaf = volume_above_floatation(m.fields["h"], m.fields["b"], m.params, m.grid)
+    assert np.isclose(vaf, (500.0 - (1028.0 / 918.0) * 200.0) * 25 * 20 * 1000.0 ** 2, rtol=1e-14)
+
+
+def test_grounding_line_x_interpolates_the_sign_change(pkg):
+    """get_glx (src/utilities.jl:417-426) on a height above floatation that falls linearly along x and
+    crosses zero at a known x in each row, plus a row crossing twice (both crossings, in x order)."""
+    from wavi_gb300.model import grounding_line_x
+    nx, ny, dx = 10, 3, 1000.0
+    xxh = np.repeat(((np.arange(nx) + 0.5) * dx)[:, None], ny, axis=1)
+    x0 = np.array([3200.0, 5600.0, 7100.0])
+    haf = (x0[None, :] - xxh) * 0.01
+    haf[8, 2] = 5.0  # row 3 grounds again at cell 9 and floats at cell 10
+    glx = grounding_line_x(haf, xxh)
+    assert np.allclose(glx[:2], x0[:2]) and np.isclose(glx[2], x0[2]) and glx.size == 4
+    assert 8500.0 < glx[3] < 9500.0

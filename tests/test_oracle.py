@@ -145,16 +145,6 @@ def test_iceberg_reaches_the_analytic_steady_state(oracle, pkg):
     assert synthetic.relative_error(om.field("v"), v0, vm) < 3.0e-4
 
 
-def _grounding_line_x(haf, xxh):
-    """get_glx (src/utilities.jl:417-426): per row of cells along y, the x where the height above
-    floatation changes from positive to negative, linearly interpolated between the two cells; in the
-    reference's column-major order."""
-    glm = (np.diff(np.sign(haf), axis=0) == -2).T
-    x1, x2 = xxh[:-1, :].T[glm], xxh[1:, :].T[glm]
-    h1, h2 = haf[:-1, :].T[glm], haf[1:, :].T[glm]
-    return x1 + (x2 - x1) * (0.0 - h1) / (h2 - h1)
-
-
 @pytest.mark.skipif(not os.environ.get("WAVI_SLOW_TESTS"), reason="20 000 oracle time steps (~4.5 min); WAVI_SLOW_TESTS=1")
 def test_mismip_plus_ice0_grounding_line(oracle, pkg):
     """The reference's MISMIP+ Ice0 verification (test/verification_tests.jl:14-36,
@@ -164,7 +154,8 @@ def test_mismip_plus_ice0_grounding_line(oracle, pkg):
     m = _mismip_golden_model(oracle, pkg)
     m.run(20000, 0.5)
     g = pkg.Grid(nx=80, ny=10, nσ=4, x0=0.0, y0=-40000.0, dx=8000.0, dy=8000.0)
-    glx = _grounding_line_x(np.asarray(m.field("haf")), g.xxh)
+    from wavi_gb300.model import grounding_line_x
+    glx = grounding_line_x(np.asarray(m.field("haf")), g.xxh)
     ny = 10
     assert glx.size == ny
     t = glx[[0, ny // 2 - 1, ny // 2, ny - 1]]

@@ -220,9 +220,36 @@ def update_geometry_on_uv_grids(model):
     f["gv_s"][model.v_mask] = sv[model.v_mask]
 
 
+def height_above_floatation(h, b, params):
+    """height_above_floatation (src/utilities.jl:445)."""
+    return h - (params.density_ocean / params.density_ice) * (params.sea_level_wrt_geoid - b)
+
+
 def update_height_above_floatation(model):
-    p, f = model.params, model.fields
-    f["haf"][...] = f["h"] - (p.density_ocean / p.density_ice) * (p.sea_level_wrt_geoid - f["b"])
+    f = model.fields
+    f["haf"][...] = height_above_floatation(f["h"], f["b"], model.params)
+
+
+def volume_above_floatation(h, b, params, grid):
+    """volume_above_floatation (src/utilities.jl:453): the positive heights above floatation times the
+    cell area."""
+    haf = height_above_floatation(np.asarray(h, np.float64), np.asarray(b, np.float64), params)
+    return float(np.sum(haf[haf > 0])) * grid.dx * grid.dy
+
+
+def grounding_line_x(haf, xxh):
+    """The x of the grounding line in each row of cells along y (get_glx, src/utilities.jl:417-426): where
+    the height above floatation changes from positive to negative along x, interpolated linearly between
+    the two cells; in the reference's column-major order (by row, then by x)."""
+    glm = (np.diff(np.sign(haf), axis=0) == -2).T
+    x1, x2 = xxh[:-1, :].T[glm], xxh[1:, :].T[glm]
+    h1, h2 = haf[:-1, :].T[glm], haf[1:, :].T[glm]
+    return x1 + (x2 - x1) * (0.0 - h1) / (h2 - h1)
+
+
+def get_glx(model):
+    """get_glx(model) (src/utilities.jl:417-426) on the model's current height above floatation."""
+    return grounding_line_x(model.fields["haf"], model.grid.xxh)
 
 
 def pos_fraction(z1, mask=None):
