@@ -359,7 +359,7 @@ def gpu_arm(args):
     release_solver(m)
     g, p, sp = m.grid, m.params, m.solver_params
 
-    mixed = VelocitySolver(g, sp, precision="mixed", device=local)
+    mixed = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=args.coarse_solver)
     fp64 = VelocitySolver(g, sp, precision="fp64", device=local)
 
     # float64 reference algorithm on the GPU
@@ -380,12 +380,12 @@ def gpu_arm(args):
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     # dominant kernel: the persistent coarse CG, per CG iteration
-    prof = VelocitySolver(g, sp, precision="mixed", device=local, use_graphs=False)
+    prof = VelocitySolver(g, sp, precision="mixed", device=local, use_graphs=False, coarse_solver=args.coarse_solver)
     sec_it, cg_its, cg_launches = coarse_roofline(torch, prof, p, snapshot)
     prof.close()
     # operator applications per CG iteration: 1, or CHEB_STEPS with the Chebyshev preconditioner (the
     # library's default mixed coarse solver on full ice masks: CHEB_STEPS - 1 in the preconditioner)
-    apps = CHEB_STEPS if stmix[-1]["coarse_solver"] == "srcg_chebyshev" else 1
+    apps = CHEB_STEPS if stmix[-1]["coarse_solver"] in ("srcg_chebyshev", "pipelined_chebyshev") else 1
     cg_bytes = apps * cg_iteration_bytes(g.nx, g.ny, 4)
     cg_achieved = cg_bytes / sec_it / 1e9
     # the fused operator on a grid larger than L2
@@ -662,7 +662,8 @@ def profile_case(args):
     snapshot = {k: np.array(v, copy=True) for k, v in m.fields.items()}
     release_solver(m)
     sp = SolverParams(**{**m.solver_params.__dict__, "maxiter_picard": args.picard})
-    s = VelocitySolver(m.grid, sp, precision=args.precision, use_graphs=False)
+    s = VelocitySolver(m.grid, sp, precision=args.precision, use_graphs=False,
+                       coarse_solver=args.coarse_solver if args.precision == "mixed" else "auto")
     dev = {k: torch.from_numpy(np.ascontiguousarray(np.asarray(snapshot[k]).ravel(order="F"))).cuda()
            for k in solve_field_names()}
     st = s.solve_device(m.params, dev)
@@ -683,6 +684,9 @@ def main():
     ap.add_argument("--picard", type=int, default=1, help="--profile solve: Picard iterations")
     ap.add_argument("--precision", default="mixed", choices=("mixed", "fp64"), help="--profile solve: precision")
     ap.add_argument("--op-launches", type=int, default=3, help="--profile op: operator launches")
+    ap.add_argument("--coarse-solver", default="auto",
+                    choices=("auto", "cg", "srcg", "srcg_jacobi", "srcg_chebyshev", "pipelined_chebyshev"),
+                    help="coarse solver of the mixed-precision solves (the FP64 solve keeps the reference's)")
     ap.add_argument("--config", default="c2", choices=("c2", "c4", "c5"),
                     help="c2: the 640x80 solve (default); c4: the adjoint on 640x80; c5: the ragged 256-member ensemble")
     ap.add_argument("--directions", type=int, default=20, help="--config c4: finite-difference directions")
