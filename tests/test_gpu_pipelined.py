@@ -1,0 +1,68 @@
+"""The opt-in pipelined coarse CG (WAVI_COARSE_PIPELINED_CHEBYSHEV, k_pcg_persistent): its requirements are
+checked when a context is made; its solves are checked against the reference's FP64 solve and against the
+single-reduction Chebyshev solver it pipelines.  The kernel has not yet run on a GPU, so the tests that
+launch it are skipped unless WAVI_RUN_PIPELINED=1; the FP64 oracle states its iteration (coarse variant 5,
+tests/test_oracle_coarse.py)."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import fields_from_oracle, uv_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+launches = pytest.mark.skipif(not os.environ.get("WAVI_RUN_PIPELINED"),
+                              reason="launches k_pcg_persistent, not yet run on a GPU (WAVI_RUN_PIPELINED=1)")
+
+CASES = {
+    "full": dict(nx=40, ny=16, dx=4000.0, mask="full"),
+    "ragged": dict(nx=37, ny=13, dx=3000.0, mask="full"),
+    "channel": dict(nx=96, ny=32, dx=2000.0, mask="full"),
+}
+
+
+def _setup(oracle, name, **kw):
+    from wavi_gb300 import synthetic
+    g, bed, p, sp, ic = synthetic.small_case(**{**CASES[name], **kw})
+    om = oracle.build_model(g, bed, p, sp, ic)
+    om.pre_solve()
+    return g, p, sp, om
+
+
+def test_pipelined_needs_mixed_precision_and_16x16_tiles(oracle):
+    """Rejected, without a launch, in FP64 and with 32 x 32 tiles (levels 4)."""
+    from wavi_gb300.abi import WaviError
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, "full")
+    with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):
+        VelocitySolver(g, sp, precision="fp64", coarse_solver="pipelined_chebyshev")
+    from wavi_gb300.config import SolverParams
+    with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):
+        VelocitySolver(g, SolverParams(levels=4), precision="mixed", coarse_solver="pipelined_chebyshev")
+
+
+@launches
+@pytest.mark.parametrize("name", list(CASES))
+def test_pipelined_converged_solve_matches_reference(oracle, name):
+    """The pipelined coarse solve changes the V-cycle, not the fixed point: the converged mixed solve agrees
+    with the reference's FP64 solve to 1e-6, and needs no more than 10 % more coarse iterations than the
+    single-reduction Chebyshev solve (the same iterates in exact arithmetic)."""
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, name, maxiter_picard=80, tol_picard=1e-7)
+    f0 = fields_from_oracle(om, g)
+    om.update_velocities()
+    stats = {}
+    for solver in ("srcg_chebyshev", "pipelined_chebyshev"):
+        f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
+        s = VelocitySolver(g, sp, precision="mixed", coarse_solver=solver)
+        st = s.solve(p, f)
+        s.close()
+        assert st["status"] == 0, (solver, st)
+        assert st["coarse_solver"] == solver
+        assert uv_err(f, om) < 1e-6, (solver, st)
+        stats[solver] = st
+    a, b = stats["srcg_chebyshev"], stats["pipelined_chebyshev"]
+    assert b["coarse_cg_iterations"] <= 1.1 * a["coarse_cg_iterations"], (a, b)
