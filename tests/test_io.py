@@ -106,8 +106,6 @@ def test_output_params_mirror_the_reference_constructor(tmp_path, pkg):
     for bad in (dict(output_freq=0.0), dict(output_freq=-1.0), dict(output_format="nc")):
         with pytest.raises(ValueError):
             OutputParams(output_path=str(tmp_path), **bad)
-    with pytest.raises(NotImplementedError):
-        OutputParams(output_path=str(tmp_path), zip_format="nc")
 
 
 def _sim(tmp_path, fmt="jld2", **kw):
@@ -179,3 +177,34 @@ def test_device_copy_back_keeps_field_references(pkg):
     _assign_field(f, "dhdt", np.full((3, 2), 2.0))
     assert f["h"] is ref_h and (ref_h == 1).all() and f["wu_mask"] is ref_m and ref_m.all()
     assert (f["dhdt"] == 2).all()
+
+
+@pytest.mark.parametrize("fmt", ["jld2", "mat"])
+@pytest.mark.filterwarnings("ignore:found an output variable")
+def test_zip_output_merges_the_output_files_into_netcdf(tmp_path, pkg, monkeypatch, fmt):
+    """zip_output (src/OutputParams/zipping_output.jl): after the run the output files become one NetCDF
+    file with dimensions x, y, TIME, the coordinate variables and their attributes, and each nx x ny output
+    over (x, y, TIME) — stored (TIME, y, x) — with the values of every output step."""
+    from scipy.io import netcdf_file
+    from wavi_gb300 import model as M
+
+    def fake_timestep(sim):
+        sim.model.fields["h"][...] += 1.0
+        sim.n_iter += 1
+        sim.time += sim.timestepping_params.dt
+
+    monkeypatch.setattr(M, "timestep", fake_timestep)
+    sim = _sim(tmp_path, fmt, output_freq=0.5, output_start=True, zip_format="nc")
+    h0 = sim.model.fields["h"].copy()
+    M.run_simulation(sim)
+    g = sim.model.grid
+    with netcdf_file(str(tmp_path / "run.nc"), "r", mmap=False) as ds:
+        assert (ds.dimensions["x"], ds.dimensions["y"], ds.dimensions["TIME"]) == (g.nx, g.ny, 4)
+        assert np.array_equal(ds.variables["x"][:], g.xxh[:, 0]) and np.array_equal(ds.variables["y"][:], g.yyh[0, :])
+        assert np.allclose(ds.variables["TIME"][:], [0.0, 0.5, 1.0, 1.5])
+        assert ds.variables["TIME"].units == b"years" and ds.variables["x"].units == b"m"
+        assert ds.variables["h"].dimensions == ("TIME", "y", "x")
+        h = ds.variables["h"][:].copy()
+        assert "u" not in ds.variables  # (nx + 1) x ny: not on the h grid, skipped as in the reference
+    for i in range(4):
+        assert np.array_equal(h[i].T, h0 + 2 * i)

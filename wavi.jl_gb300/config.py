@@ -241,8 +241,8 @@ class OutputParams:
 
     ``outputs`` maps each output name to the array written under it (a reference to a model field, read
     when the output is written, as the reference's named tuple of field references is); ``n_iter_out`` is
-    set by the Simulation from the time step (set_n_iter_out!, Simulation.jl:62-66).  NetCDF zipping
-    (zip_format "nc", zip_output) is not provided."""
+    set by the Simulation from the time step (set_n_iter_out!, Simulation.jl:62-66).  zip_format "nc"
+    merges the output files into one NetCDF file at the end of run_simulation (io.zip_output)."""
     outputs: dict = field(default_factory=dict)
     output_freq: float = math.inf
     output_format: str = "jld2"
@@ -265,8 +265,6 @@ class OutputParams:
             raise ValueError("Output format must be `jld2` or `mat`")
         if self.zip_format not in ("none", "nc"):
             self.zip_format = "none"
-        if self.zip_format == "nc":
-            raise NotImplementedError("zipping the output to NetCDF is not provided")
 
     def set_n_iter_out(self, dt, n_iter_total):
         """set_n_iter_out! (src/Simulations/Simulation.jl:62-66)."""

@@ -22,8 +22,11 @@ write_jld2
     HDF5 lookup3 checksum.  Rebuilding the reference's four golden JLD2 files from their arrays gives them
     byte for byte.
 
-write_output
-    run_simulation!'s periodic output files (src/OutputParams/output_writing.jl:7-27) in JLD2 (or MAT).
+write_output, zip_output
+    run_simulation!'s periodic output files (src/OutputParams/output_writing.jl:7-27) in JLD2 (or MAT), and
+    their merge into one NetCDF file (src/OutputParams/zipping_output.jl), written in the classic NetCDF
+    format (64-bit offsets) by scipy where the reference's NCDatasets writes NetCDF-4: the same dimensions,
+    variables, attributes and values, readable by any NetCDF library.
 """
 import struct
 
@@ -301,7 +304,7 @@ def write_output(sim):
     out.setdefault("t", np.float64(round(sim.time, 3)))
     out.setdefault("x", np.asarray(model.grid.xxh, np.float64))
     out.setdefault("y", np.asarray(model.grid.yyh, np.float64))
-    fname = f"{op.output_path}{op.prefix}{sim.n_iter:010d}"
+    fname = f"{op.output_path}{op.prefix}{sim.n_iter:010d}"  # (Bool or integer outputs are written as float64)
     if op.output_format == "jld2":
         fname += ".jld2"
         write_jld2(fname, out)
@@ -311,3 +314,69 @@ def write_output(sim):
         savemat(fname, out)
     print(f"outputting at timestep number {sim.n_iter}")
     return fname
+
+
+def _read_output(fname):
+    """An output file as a dict (get_output_as_dict, zipping_output.jl:58-66)."""
+    if fname.endswith(".mat"):
+        from scipy.io import loadmat
+        return {k: v for k, v in loadmat(fname).items() if not k.startswith("__")}
+    return read_jld2(fname)
+
+
+def make_ncfile(output_format, folder, nc_name, prefix):
+    """make_ncfile and make_ncfile_from_filenames (zipping_output.jl:82-158): the files of ``folder`` named
+    <prefix>*.<output_format>, in name order (so in time step order), merged into ``nc_name``.  Dimensions
+    x and y (the first column of the h-grid x and the first row of its y) and TIME (each file's t), their
+    coordinate variables with the reference's attributes, and every output of size nx x ny as a variable
+    over (x, y, TIME) in Julia's order, which the file stores slowest first as (TIME, y, x).  Outputs of
+    another size are skipped with a warning, as in the reference.  Returns the file name, or None when
+    there are no files."""
+    import os
+    import warnings
+    from scipy.io import netcdf_file
+    names = sorted(f for f in os.listdir(folder) if f.endswith(output_format) and f.startswith(prefix))
+    if not names:
+        print("attempted to zip the outputs to nc format, but did not find any files...")
+        return None
+    files = [os.path.join(folder, f) for f in names]
+    first = _read_output(files[0])
+    x = np.asarray(first["x"], np.float64)[:, 0]
+    y = np.asarray(first["y"], np.float64)[0, :]
+    t = np.array([float(np.squeeze(_read_output(f)["t"])) for f in files])
+    if os.path.isfile(nc_name):
+        os.remove(nc_name)
+    with netcdf_file(nc_name, "w", version=2) as ds:
+        ds.createDimension("x", x.size)
+        ds.createDimension("y", y.size)
+        ds.createDimension("TIME", t.size)
+        for name, dim, vals, longname, units in (("x", "x", x, "x co-ordinates of ice grid points (h grid)", "m"),
+                                                 ("y", "y", y, "y co-ordinates of ice grid points (h grid)", "m"),
+                                                 ("TIME", "TIME", t, "Time", "years")):
+            v = ds.createVariable(name, "d", (dim,))
+            v[:] = vals
+            v.longname = longname
+            v.units = units
+        for key in first:
+            if key in ("x", "y", "t"):
+                continue
+            a = np.asarray(first[key])
+            if a.shape != (x.size, y.size):
+                warnings.warn(f"found an output variable ({key}) whose spatial dimensions ({a.shape}) do not match "
+                              "the co-ordinates. Skipping this variable from the nc output...")
+                continue
+            dtype = "b" if a.dtype == np.bool_ else a.dtype.char
+            v = ds.createVariable(key, dtype, ("TIME", "y", "x"))
+            for i, f in enumerate(files):
+                d = np.asarray(_read_output(f)[key])
+                v[i, :, :] = (d.astype(np.int8) if d.dtype == np.bool_ else d).T
+    return nc_name
+
+
+def zip_output(sim):
+    """zip_output (zipping_output.jl:162-169): with zip_format "nc", the run's output files merged into
+    <output_path><prefix>.nc."""
+    op = sim.output_params
+    if op is None or op.zip_format != "nc":
+        return None
+    return make_ncfile(op.output_format, op.output_path, f"{op.output_path}{op.prefix}.nc", op.prefix)

@@ -493,6 +493,9 @@ def run_simulation(sim, callback=None):
             if callback is not None:
                 callback(sim)
         _write_due_output(sim)
+    if sim.output_params is not None:
+        from .io import zip_output
+        zip_output(sim)  # (zipping_output.jl:162-169; after the last step, run_simulation.jl:96-97)
     return sim
 
 
