@@ -8,7 +8,12 @@ The package directory is ``wavi.jl_gb300/``; it is imported under the module nam
   gpu.py        VelocitySolver: one wavi_ctx per grid; host (e2e) and device entry points
   config.py     Grid / Params / SolverParams / TimesteppingParams / InitialConditions mirrors
   model.py      Model, update_state!, Simulation, run_simulation! with the GPU velocity solve plugged in
-  synthetic.py  seeded synthetic channel geometries of the benchmark configurations
+  ensemble.py   ensembles of independent domains solved at once, and their launch autotuner
+  autograd.py   the adjoint behind a torch.autograd.Function
+  misfit.py     the speed misfit (the adjoint workload's objective) and its velocity gradient
+  schwarz.py    SharedMemorySpec's restricted additive Schwarz decomposition and sweeps
+  io.py         file formats: the MITgcm velocity dump, JLD2 read/write, output files, their NetCDF merge
+  synthetic.py  seeded synthetic geometries: the benchmark channels, small test cases, the iceberg
   build.py      nvcc build of the library
 """
 from . import abi, config, synthetic  # noqa: F401
