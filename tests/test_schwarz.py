@@ -335,3 +335,22 @@ def test_gpu_global_residual_undoes_the_correction(pkg, monkeypatch):
     schwarz.gpu_global_residual(m)
     assert made == [1]  # one context per model
     schwarz.release_residual_solver(m)
+
+
+def test_schwarz_spec_is_a_parallel_spec(pkg, monkeypatch):
+    """A model whose parallel spec is a SchwarzSpec (the reference's SharedMemorySpec) takes the Schwarz
+    path in update_velocities; its subdomain models get the spec's subdomain_spec, a GPU spec by default."""
+    from wavi_gb300 import schwarz, synthetic
+    from wavi_gb300.model import GPUParallelSpec, Model, update_velocities
+    g, bed, p, sp, ic = synthetic.small_case(nx=32, ny=16, dx=4000.0)
+    spec = schwarz.SchwarzSpec(ngridsx=2, ngridsy=2, overlap=2, niterations=1)
+    assert isinstance(spec.subdomain_spec, GPUParallelSpec)
+    m = Model(g, bed, p, sp, ic, parallel_spec=spec)
+    calls = []
+    monkeypatch.setattr(schwarz, "update_velocities_schwarz", lambda model, s: calls.append((model, s)))
+    update_velocities(m)
+    assert calls == [(m, spec)]
+    subs = schwarz.build_subdomains(m, spec)
+    assert all(s.parallel_spec is spec.subdomain_spec for s in subs.values())
+    with pytest.raises(TypeError):
+        update_velocities(Model(g, bed, p, sp, ic, parallel_spec=object()))

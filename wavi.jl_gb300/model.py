@@ -343,9 +343,14 @@ def update_dsdh(model):
 
 
 def update_velocities(model):
-    """update_velocities!(model) dispatched on the parallel spec (update_velocities.jl:11-29)."""
+    """update_velocities!(model) dispatched on the parallel spec (update_velocities.jl:11-29): the GPU solve
+    for a GPUParallelSpec, restricted additive Schwarz for a schwarz.SchwarzSpec (SharedMemorySpec)."""
+    from .schwarz import SchwarzSpec, update_velocities_schwarz
+    if isinstance(model.parallel_spec, SchwarzSpec):
+        update_velocities_schwarz(model, model.parallel_spec)
+        return model
     if not isinstance(model.parallel_spec, GPUParallelSpec):
-        raise TypeError("only GPUParallelSpec is implemented by this package")
+        raise TypeError("the parallel spec must be a GPUParallelSpec or a SchwarzSpec")
     solver = _solver_for(model)
     model.last_stats = solver.solve(model.params, model.fields)
     return model

@@ -23,16 +23,21 @@ from .config import Grid, InitialConditions
 
 @dataclass
 class SchwarzSpec:
-    """SharedMemorySpec's parameters (src/SharedMemorySpec.jl:5-12): ngridsx x ngridsy subdomains,
-    `overlap` h cells of overlap on each side, niterations Schwarz iterations per Picard iteration, and
-    the damping of the prolongation."""
+    """SharedMemorySpec (src/SharedMemorySpec.jl:5-12) as a model's parallel spec: ngridsx x ngridsy
+    subdomains, `overlap` h cells of overlap on each side, niterations Schwarz iterations per Picard
+    iteration, and the damping of the prolongation.  ``subdomain_spec`` is the parallel spec of the
+    subdomain models (the reference gives them BasicParallelSpec(), :275); by default a GPUParallelSpec."""
     ngridsx: int = 1
     ngridsy: int = 1
     overlap: int = 1
     niterations: int = 0
     damping: float = 0.0
+    subdomain_spec: object = None
 
     def __post_init__(self):
+        if self.subdomain_spec is None:
+            from .model import GPUParallelSpec
+            self.subdomain_spec = GPUParallelSpec()
         # the reference does not check these; overlap 0 gives its partition of unity ramps of length 0 and
         # -1, and NaN weights
         if self.ngridsx < 1 or self.ngridsy < 1:
@@ -154,12 +159,12 @@ def prolong_velocities(model, model_g, igrid, jgrid, spec):
 def build_subdomains(model, spec, make=None):
     """update_preconditioner!(model, ::SharedMemorySpec) (:53-69): one subdomain model per (igrid, jgrid)
     from the global model's current state.  ``make(grid, bed, params, solver_params, initial_conditions)``
-    builds each one; by default a host Model with the global model's solver and parallel specs (so each
-    subdomain solves through its own velocity-solver context)."""
+    builds each one; by default a host Model with the global model's solver parameters and the spec's
+    subdomain_spec (so each subdomain solves through its own velocity-solver context)."""
     if make is None:
         from .model import Model
         make = lambda grid, bed, params, solver_params, ic: Model(grid, bed, params, solver_params, ic,
-                                                                   parallel_spec=model.parallel_spec)
+                                                                   parallel_spec=spec.subdomain_spec)
     subs = {}
     for igrid in range(1, spec.ngridsx + 1):
         for jgrid in range(1, spec.ngridsy + 1):
@@ -271,6 +276,8 @@ def gpu_global_residual(model):
     s = _RESIDUAL_SOLVERS.get(key)
     if s is None:
         ps = model.parallel_spec
+        if isinstance(ps, SchwarzSpec):
+            ps = ps.subdomain_spec
         s = gpu.VelocitySolver(model.grid, _replace(model.solver_params, maxiter_picard=1),
                                precision=getattr(ps, "precision", "fp64"), device=getattr(ps, "device", 0))
         _RESIDUAL_SOLVERS[key] = s
@@ -312,4 +319,5 @@ def update_velocities_schwarz(model, spec, global_residual=None, solve=None, sol
         if not converged:
             ras_sweeps(model, spec, subdomains, solve=solve, solve_all=solve_all)
     print(f"Solved momentum equation with residual {rel:.3g} at iteration {i}")
+    model.last_stats = {"picard_iterations": i, "rel_residual": rel, "converged": converged}
     return converged, rel, i
