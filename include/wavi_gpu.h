@@ -123,8 +123,9 @@ typedef enum wavi_coarse_solver {
   WAVI_COARSE_PIPELINED_CHEBYSHEV = 5 /* opt-in, never chosen by AUTO: pipelined CG (Ghysels & Vanroose
                                         2014) with the preconditioner of SRCG_CHEBYSHEV, whose grid
                                         reduction overlaps the iteration's preconditioner and operator;
-                                        residual replacement every 25 iterations; mixed precision, 16 x 16
-                                        tiles (levels <= 3) and the register-resident kernel only */
+                                        restarted from the true residual after every hundredfold fall of
+                                        |r|; mixed precision, 16 x 16 tiles (levels <= 3), register-
+                                        resident kernel */
 } wavi_coarse_solver;
 
 /* The model fields the velocity solve reads and writes (src/Models/update_velocities.jl:202-383,

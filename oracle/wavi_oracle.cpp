@@ -834,8 +834,8 @@ int coarse_cg(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, doubl
 //      the two inner products of an iteration computed together after its operator application
 //   3  the same, preconditioned by the Jacobi diagonal of R A P
 //   4  the same, preconditioned by Chebyshev-accelerated Jacobi steps (coarse_srcg_chebyshev)
-//   5  pipelined CG with variant 4's preconditioner and residual replacement (coarse_pipelined_chebyshev),
-//      the GPU library's opt-in WAVI_COARSE_PIPELINED_CHEBYSHEV
+//   5  pipelined CG with variant 4's preconditioner, restarted after every hundredfold fall of |r|
+//      (coarse_pipelined_chebyshev), the GPU library's opt-in WAVI_COARSE_PIPELINED_CHEBYSHEV
 // ---------------------------------------------------------------------------------------------
 int g_coarse_variant = 0;
 
@@ -1025,10 +1025,11 @@ int coarse_srcg_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const V
 //   x += α p;  r −= α s;  u −= α q;  w −= α z
 // started from r = b − A x, u = M⁻¹ r, w = A u.  The last iteration's m and n are computed and unused,
 // as they are on the GPU, where they run before the reduction that stops the loop is known.  In FP32 the
-// recursively updated residual drifts from b − A x (by ~1e-4 of ‖b‖ on the coarse systems here), so every
-// PCG_REPLACE iterations r, u, w are recomputed from x, and s = A p, q = M⁻¹ s, z = A q from p (residual
-// replacement), as the GPU library's k_pcg_persistent does; in FP64 that changes the iterates by rounding.
-constexpr int PCG_REPLACE = 25;
+// recursively updated residual drifts from b − A x (by ~1e-4 of ‖b‖ on the coarse systems here), so the
+// iteration restarts from x (r, u, w recomputed, β = 0 for that iteration) once |r| has fallen below
+// PCG_RESTART_FACTOR times its value at the start or the last restart, decided from the previous
+// iteration's reduction, as the GPU library's k_pcg_persistent does.
+constexpr double PCG_RESTART_FACTOR = 1e-2;
 int coarse_pipelined_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, double abstol,
                                int maxiter) {
   const size_t n = b.size();
@@ -1040,17 +1041,16 @@ int coarse_pipelined_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, co
   op_coarse(m, w, p, u, wv);
   Vec z(n, 0.0), q(n, 0.0), s(n, 0.0), pp(n, 0.0);
   const double reltol = std::sqrt(2.220446049250313e-16);
-  double tol = 0.0, gamma_prev = 0.0, alpha = 0.0;
+  double tol = 0.0, gamma_prev = 0.0, alpha = 0.0, rr_ref = 0.0;
+  bool restart_next = false;
   int it = 0;
   for (;;) {
-    if (it > 0 && it % PCG_REPLACE == 0) {
+    const bool restart = it > 0 && restart_next;
+    if (restart) {
       op_coarse(m, w, p, x, c);
       for (size_t i = 0; i < n; ++i) r[i] = b[i] - c[i];
       cheb_apply(m, w, p, cp, r, u);
       op_coarse(m, w, p, u, wv);
-      op_coarse(m, w, p, pp, s);
-      cheb_apply(m, w, p, cp, s, q);
-      op_coarse(m, w, p, q, z);
     }
     const double gamma = dotp(r, u), delta = dotp(wv, u), res = norm2(r);
     if (it == 0) tol = std::max(reltol * res, abstol);
@@ -1058,13 +1058,15 @@ int coarse_pipelined_chebyshev(Model& m, OpWork& w, const Precond& p, Vec& x, co
     op_coarse(m, w, p, mm, nn);
     if (it >= maxiter || res <= tol || !(res == res)) break;
     double beta = 0.0;
-    if (it == 0) {
+    if (it == 0 || restart) {
       alpha = gamma / delta;
+      rr_ref = res * res;
     } else {
       beta = gamma / gamma_prev;
       alpha = gamma / (delta - beta * gamma / alpha);
     }
     if (!(alpha == alpha) || std::isinf(alpha)) break;
+    restart_next = res * res < PCG_RESTART_FACTOR * PCG_RESTART_FACTOR * rr_ref;
     gamma_prev = gamma;
     for (size_t i = 0; i < n; ++i) {
       z[i] = nn[i] + beta * z[i];

@@ -93,8 +93,9 @@ def test_single_reduction_coarse_solves_reach_the_reference_fixed_point(oracle, 
 @pytest.mark.parametrize("mask", ["full", "disc"])
 def test_pipelined_cg_follows_the_single_reduction_iterates(oracle, reference_cg, mask):
     """Pipelined CG (variant 5) and single-reduction CG (variant 4) with the same Chebyshev preconditioner
-    produce the same Krylov iterates in exact arithmetic: in FP64 their Picard and coarse iteration counts
-    agree (to 1 %) and their converged velocities to the Picard tolerance."""
+    produce the same Krylov iterates in exact arithmetic between variant 5's restarts: in FP64 their
+    Picard counts agree, the restarts (after each hundredfold fall of |r|) cost at most 20 % more coarse
+    iterations (measured 14 % and 12 %), and their converged velocities agree to the Picard tolerance."""
     from wavi_gb300 import synthetic
     sols = {}
     for v in ("srcg_chebyshev", "pipelined_chebyshev"):
@@ -106,6 +107,6 @@ def test_pipelined_cg_follows_the_single_reduction_iterates(oracle, reference_cg
         sols[v] = (np.array(om.field("u")), np.array(om.field("v")), om.stats())
     (u0, v0, s0), (u1, v1, s1) = sols["srcg_chebyshev"], sols["pipelined_chebyshev"]
     assert s1["picard_iterations"] == s0["picard_iterations"]
-    assert abs(s1["coarse_cg_iterations"] - s0["coarse_cg_iterations"]) <= 0.01 * s0["coarse_cg_iterations"]
+    assert s0["coarse_cg_iterations"] <= s1["coarse_cg_iterations"] <= 1.2 * s0["coarse_cg_iterations"]
     err = np.sqrt(np.sum((u1 - u0) ** 2) + np.sum((v1 - v0) ** 2)) / np.sqrt(np.sum(u0 ** 2) + np.sum(v0 ** 2))
     assert err < 1e-9

@@ -13,8 +13,9 @@
 //   k_srcg_persistent single-reduction CG (Chronopoulos & Gear 1989), preconditioned by nothing, by
 //                     the Jacobi diagonal, or by Chebyshev-accelerated Jacobi steps: both inner products
 //                     of an iteration follow its operator application, one grid reduction per iteration
-//   k_pcg_persistent  pipelined CG with the Chebyshev preconditioner (FP32 fast path only; opt-in): the
-//                     grid reduction of an iteration completes while its preconditioner and operator run
+//   k_pcg_persistent  pipelined CG with the Chebyshev preconditioner, restarted from the true residual
+//                     after every hundredfold fall of |r| (FP32 fast path only; opt-in): the grid
+//                     reduction of an iteration completes while its preconditioner and operator run
 //
 // The FP64 and global-memory instantiations separate the prolongation from the operator by a grid
 // barrier.  The FP32 instantiations on 16 x 16 tiles (the fast path) keep the tiles' coefficients in
@@ -1061,6 +1062,55 @@ __device__ __forceinline__ void srcg_scalars(CGScalars<T>& sc, const typename CG
   sc.beta_t = (T)to_vec(sc.beta);
   sc.stop = stop;
 }
+// The CG scalars of k_pcg_persistent: srcg_scalars' (the pipelined iteration has the same α and β), except
+// that a restart (the recursively updated vectors replaced by recomputed ones) takes the first
+// iteration's β = 0, α = γ/δ while keeping the tolerance and the iteration limit; and the decision to
+// restart the next iteration: once |r| has fallen below kPcgRestartFactor times its value at the start or
+// the last restart.  (In an FP32 simulation on assembled coarse systems this kept the iteration counts
+// within 0.97-1.10x of single-reduction CG's, with two restarts per solve, where a fixed period of 25
+// cost up to 29 % more iterations in FP64 and replacing r, u, w without restarting broke convergence.)
+constexpr double kPcgRestartFactor = 1e-2;
+template <typename T>
+struct PcgScalars : CGScalars<T> {
+  typename CGReal<T>::type rr_ref;  // |r|² at the start or the last restart
+  int restart_next;
+};
+template <typename T>
+__device__ __forceinline__ void pcg_scalars(PcgScalars<T>& sc, const typename CGReal<T>::type* tot, bool first,
+                                            bool restart, int it, int maxit, double tol_coarse) {
+  using R = typename CGReal<T>::type;
+  constexpr bool f32 = std::is_same<T, float>::value;
+  if (first) {
+    srcg_scalars<T>(sc, tot, true, it, maxit, tol_coarse);
+    sc.rr_ref = sc.rr;
+    sc.restart_next = 0;
+    return;
+  }
+  const R gamma = tot[0], delta = tot[1];
+  sc.rr = tot[2];
+  if (!f32) sc.res = sqrt(dbl_of(tot[2]));
+  int stop;
+  if constexpr (f32)
+    stop = it >= maxit || sc.rr <= sc.tol2 || is_nan(sc.rr);
+  else
+    stop = it >= maxit || sc.res <= sc.tol || is_nan(sc.rr);
+  if (!stop) {
+    if (restart) {
+      sc.beta = R{};
+      sc.alpha = gamma / delta;
+    } else {
+      sc.beta = gamma / sc.gamma_prev;
+      sc.alpha = gamma / (delta - sc.beta * gamma / sc.alpha);
+    }
+  }
+  if (!stop && not_finite(sc.alpha)) stop = 1;
+  if (restart) sc.rr_ref = sc.rr;
+  sc.restart_next = !stop && dbl_of(sc.rr) < kPcgRestartFactor * kPcgRestartFactor * dbl_of(sc.rr_ref);
+  sc.gamma_prev = gamma;
+  sc.alpha_t = (T)to_vec(sc.alpha);
+  sc.beta_t = (T)to_vec(sc.beta);
+  sc.stop = stop;
+}
 // |r| of the final iterate for the statistics
 template <typename T>
 __device__ __forceinline__ double cg_final_res(const CGScalars<T>& sc) {
@@ -1497,12 +1547,12 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
 // grid_arrive) completes while the CTA applies M and A, which need only neighbour exchanges:
 //   γ = (r,u), δ = (w,u), |r|²  → arrive;  m = M⁻¹ w;  n = A m;  wait;  stop?
 //   z = n + β z;  q = m + β q;  s = w + β s;  p = u + β p;  x += α p;  r −= α s;  u −= α q;  w −= α z
-// from r = b − A x, u = M⁻¹ r, w = A u.  In FP32 the recursively updated r, u, w drift from b − A x, so
-// every kPcgReplace iterations they are recomputed (residual replacement), with s = A p, q = M⁻¹ s and
-// z = A q.  The oracle's coarse_pipelined_chebyshev states the same iteration, replacement included, in
-// FP64.  x, r, u, w and the preconditioner's vectors stay in registers; p, s, q, z live in shared memory
-// (each thread touches only its own points of them).
-constexpr int kPcgReplace = 25;
+// from r = b − A x, u = M⁻¹ r, w = A u.  In FP32 the recursively updated r, u, w drift from b − A x, so the
+// iteration restarts from x (r, u, w recomputed, β = 0) once |r| has fallen by kPcgRestartFactor since the
+// start or the last restart (pcg_scalars decides it from the previous iteration's reduction).  The
+// oracle's coarse_pipelined_chebyshev states the same iteration, restarts included, in FP64.  x, r, u, w
+// and the preconditioner's vectors stay in registers; p, s, q, z live in shared memory (each thread
+// touches only its own points of them).
 
 template <typename T, int TILE, int MAXT>
 struct PcgShared {
@@ -1518,7 +1568,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
   static_assert(!std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value, "the pipelined CG needs the FP32 fast path");
   __shared__ CGShared<T, TILE> sm;
   __shared__ SyncShared ss;
-  __shared__ CGScalars<T> sc;
+  __shared__ PcgScalars<T> sc;
   __shared__ FastSharedFor<T, TILE, MAXT> fs;
   __shared__ PcgShared<T, TILE, MAXT> pv;
   __shared__ T cheb_s[3];  // θ, δ, σ of the Chebyshev interval
@@ -1689,31 +1739,9 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
   if (!residual()) return;
   bool first = true;
   for (;;) {
-    if (!first && it % kPcgReplace == 0) {
-      // residual replacement: r, u, w from x; s = A p, q = M⁻¹ s, z = A q from p
-      if (!residual()) return;
-      T tu[MAXT], tv[MAXT], su_[MAXT], sv_[MAXT];
-#pragma unroll
-      for (int k = 0; k < MAXT; ++k) {
-        tu[k] = pv.v[VP][k][0][lin];
-        tv[k] = pv.v[VP][k][1][lin];
-      }
-      if (!op(tu, tv, su_, sv_)) return;
-      if (!precond(su_, sv_, tu, tv)) return;
-#pragma unroll
-      for (int k = 0; k < MAXT; ++k) {
-        pv.v[VS][k][0][lin] = su_[k];
-        pv.v[VS][k][1][lin] = sv_[k];
-        pv.v[VQ][k][0][lin] = tu[k];
-        pv.v[VQ][k][1][lin] = tv[k];
-      }
-      if (!op(tu, tv, su_, sv_)) return;
-#pragma unroll
-      for (int k = 0; k < MAXT; ++k) {
-        pv.v[VZ][k][0][lin] = su_[k];
-        pv.v[VZ][k][1][lin] = sv_[k];
-      }
-    }
+    // restart (decided by the previous iteration's scalars): r, u, w recomputed from x; β = 0 below
+    const bool restart = !first && sc.restart_next;
+    if (restart && !residual()) return;
     T a[4] = {T(0), T(0), T(0), first ? bb : T(0)};
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
@@ -1727,7 +1755,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
     if (!precond(wu, wv, mu, mv)) return;
     if (!op(mu, mv, nu, nv)) return;
     if (!grid_wait<4, T>(bar, partials, epoch, ss, [&](const typename CGReal<T>::type* tot) {
-          srcg_scalars<T>(sc, tot, first, it, maxit, tol_coarse);
+          pcg_scalars<T>(sc, tot, first, restart, it, maxit, tol_coarse);
         }))
       return;
     if (sc.stop) break;
