@@ -145,7 +145,8 @@ def test_iceberg_reaches_the_analytic_steady_state(oracle, pkg):
     assert synthetic.relative_error(om.field("v"), v0, vm) < 3.0e-4
 
 
-@pytest.mark.skipif(not os.environ.get("WAVI_SLOW_TESTS"), reason="20 000 oracle time steps (~4.5 min); WAVI_SLOW_TESTS=1")
+@pytest.mark.skipif(not os.environ.get("WAVI_SLOW_TESTS"),
+                    reason="20 000 oracle time steps (~4.5 min); WAVI_SLOW_TESTS=1")
 def test_mismip_plus_ice0_grounding_line(oracle, pkg):
     """The reference's MISMIP+ Ice0 verification (test/verification_tests.jl:14-36,
     verification_tests/MISMIP_PLUS_Ice0.jl): 10 000 yr of dt = 0.5 from a 100 m slab on the 8 km channel.

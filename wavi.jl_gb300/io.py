@@ -225,8 +225,9 @@ def _object_header(messages):
 
 def write_jld2(path, arrays, julia_version="1.8.3"):
     """Write the float64 arrays (and float64 scalars) of ``arrays`` (a name -> value mapping, in the order
-    the links are to be listed) as JLD2's ``@save`` does: each array's dimensions reversed into HDF5 order, its column-major
-    bytes stored compact (up to COMPACT_LIMIT bytes) or contiguous right after its object header.
+    the links are to be listed) as JLD2's ``@save`` does: each array's dimensions reversed into HDF5
+    order, its column-major bytes stored compact (up to COMPACT_LIMIT bytes) or contiguous right after its
+    object header.
     ``julia_version`` only fills the header's informational "(Julia x.y.z 64-bit LE)" field."""
     header = b"HDF5-based Julia Data Format, version 0.1.1\x00 (Julia " + julia_version.encode() + b" 64-bit LE)\x00"
     if len(header) > _JLD2_BASE:
