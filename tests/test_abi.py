@@ -58,3 +58,27 @@ def test_coarse_solver_names_match_the_header_enum(pkg):
     body = text[text.index("typedef enum wavi_coarse_solver"):text.index("} wavi_coarse_solver;")]
     enum = {m.group(1).lower(): int(m.group(2)) for m in re.finditer(r"WAVI_COARSE_(\w+)\s*=\s*(\d+)", body)}
     assert enum == {k: v for k, v in abi.COARSE_SOLVERS.items()}, (enum, abi.COARSE_SOLVERS)
+
+
+def test_ctx_create_rejects_bad_arguments_before_touching_a_device(lib, pkg):
+    """wavi_ctx_create checks its arguments before any CUDA call: each bad argument is WAVI_ERR_ARGUMENT (-1)
+    with a message from wavi_last_error(NULL), with or without a GPU."""
+    import dataclasses
+    from wavi_gb300 import abi, synthetic
+    g, bed, p, sp, ic = synthetic.small_case()
+    desc = g.descriptor()
+    ctx = C.c_void_p()
+
+    def create(d=desc.desc, s=sp, opt=abi.Options(0, 0, 0, 0), out=True):
+        return lib.wavi_ctx_create(C.byref(d), C.byref(s.to_c()), C.byref(opt), C.byref(ctx) if out else None)
+
+    assert create(out=False) == -1
+    small = abi.GridDesc.from_buffer_copy(desc.desc)
+    small.nx = 1
+    assert create(d=small) == -1 and b"nx" in lib.wavi_last_error(None)
+    assert create(s=dataclasses.replace(sp, levels=5)) == -1 and b"levels" in lib.wavi_last_error(None)
+    assert create(opt=abi.Options(0, 7, 0, 0)) == -1 and b"precision" in lib.wavi_last_error(None)
+    nomask = abi.GridDesc.from_buffer_copy(desc.desc)
+    nomask.h_mask = None
+    assert create(d=nomask) == -1
+    assert not ctx.value  # no context was made
