@@ -82,3 +82,23 @@ def test_ctx_create_rejects_bad_arguments_before_touching_a_device(lib, pkg):
     nomask.h_mask = None
     assert create(d=nomask) == -1
     assert not ctx.value  # no context was made
+
+
+def test_residual_noalloc_rejects_bad_arguments_before_touching_a_device(lib, pkg):
+    """wavi_residual_noalloc checks its arguments before any CUDA call (the pointers are not dereferenced
+    before then): null arguments, a grid below 2 x 2, and a grid beyond the static scratch's 16384 tiles
+    of 32 x 8 points are WAVI_ERR_ARGUMENT (-1) with a message."""
+    from wavi_gb300 import abi
+    buf = (C.c_double * 4)()
+    p = C.cast(buf, C.c_void_p)
+    ok = abi.OperatorDesc(16, 8, 1000.0, 1000.0, p, p, p, p, p, p)
+    assert lib.wavi_residual_noalloc(None, p, p, p, p, None) == -1
+    assert lib.wavi_residual_noalloc(C.byref(ok), None, p, p, p, None) == -1
+    assert b"null" in lib.wavi_last_error(None)
+    nocoef = abi.OperatorDesc(16, 8, 1000.0, 1000.0, p, None, p, p, p, p)
+    assert lib.wavi_residual_noalloc(C.byref(nocoef), p, p, p, p, None) == -1
+    tiny = abi.OperatorDesc(1, 8, 1000.0, 1000.0, p, p, p, p, p, p)
+    assert lib.wavi_residual_noalloc(C.byref(tiny), p, p, p, p, None) == -1
+    big = abi.OperatorDesc(32 * 129 - 1, 8 * 128, 1000.0, 1000.0, p, p, p, p, p, p)  # 129 x 129 tiles
+    assert lib.wavi_residual_noalloc(C.byref(big), p, p, p, p, None) == -1
+    assert b"too large" in lib.wavi_last_error(None)
