@@ -102,3 +102,24 @@ def test_residual_noalloc_rejects_bad_arguments_before_touching_a_device(lib, pk
     big = abi.OperatorDesc(32 * 129 - 1, 8 * 128, 1000.0, 1000.0, p, p, p, p, p, p)  # 129 x 129 tiles
     assert lib.wavi_residual_noalloc(C.byref(big), p, p, p, p, None) == -1
     assert b"too large" in lib.wavi_last_error(None)
+
+
+def test_ensemble_create_rejects_bad_arguments_before_touching_a_device(lib, pkg):
+    """wavi_ensemble_create: no members, null arrays, host-driven launches (members run as graphs) and a
+    member grid that its context rejects are WAVI_ERR_ARGUMENT (-1) before any CUDA call; the message
+    names the member."""
+    from wavi_gb300 import abi, synthetic
+    g, bed, p, sp, ic = synthetic.small_case()
+    d = g.descriptor()
+    grids = (abi.GridDesc * 2)(d.desc, d.desc)
+    sps = (abi.SolverParams * 2)(sp.to_c(), sp.to_c())
+    ens = C.c_void_p()
+    graphs = abi.Options(0, 0, 1, 0)
+    assert lib.wavi_ensemble_create(0, grids, sps, C.byref(graphs), 4, C.byref(ens)) == -1
+    assert lib.wavi_ensemble_create(2, None, sps, C.byref(graphs), 4, C.byref(ens)) == -1
+    assert lib.wavi_ensemble_create(2, grids, sps, C.byref(abi.Options(0, 0, 0, 0)), 4, C.byref(ens)) == -1
+    assert b"graphs" in lib.wavi_last_error(None)
+    grids[0].nx = 1
+    assert lib.wavi_ensemble_create(2, grids, sps, C.byref(graphs), 4, C.byref(ens)) == -1
+    assert b"member 0" in lib.wavi_last_error(None)
+    assert not ens.value
