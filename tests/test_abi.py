@@ -123,3 +123,26 @@ def test_ensemble_create_rejects_bad_arguments_before_touching_a_device(lib, pkg
     assert lib.wavi_ensemble_create(2, grids, sps, C.byref(graphs), 4, C.byref(ens)) == -1
     assert b"member 0" in lib.wavi_last_error(None)
     assert not ens.value
+
+
+def test_every_entry_point_rejects_a_null_context(lib, pkg):
+    """Each entry point that takes a context (or an ensemble) returns WAVI_ERR_ARGUMENT (-1) for a null one,
+    before touching anything; destroying a null context or ensemble is a no-op."""
+    calls = {
+        "wavi_solve_velocities": (None, None, None, None),
+        "wavi_solve_velocities_device": (None, None, None, None),
+        "wavi_relinearise_device": (None, None, None),
+        "wavi_apply_operator_device": (None, 0, None, None),
+        "wavi_time_operator_device": (None, 0, None, None, 1, None),
+        "wavi_op_diagonal_device": (None, 0, None),
+        "wavi_selftest_watchdog": (None, None),
+        "wavi_coarse_diagonal_device": (None, 0, None),
+        "wavi_adjoint_device": (None, None, None, None, None, None, 1e-10, 10, None),
+        "wavi_tangent_device": (None, None, None, None, None, None, 1e-10, 10, None),
+        "wavi_run_device": (None, None, 1.0, 1, None, None, None, None),
+        "wavi_haar_device": (None, 0, None, None, None),
+        "wavi_ensemble_solve_device": (None, None, None, None),
+    }
+    for name, args in calls.items():
+        assert getattr(lib, name)(*args) == -1, name
+    assert lib.wavi_ctx_destroy(None) == 0 and lib.wavi_ensemble_destroy(None) == 0
