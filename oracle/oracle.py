@@ -96,6 +96,8 @@ class OracleModel:
 
     def _shape(self, name, n):
         nx, ny, ns = self.nx, self.ny, self.ns
+        if name in ("coarse_b", "coarse_x0"):  # the last V-cycle's coarse problem, in the coarse order
+            return (n,)
         if name.startswith(("gu_", "wu_")) or name in self.U_NAMES:
             shp = (nx + 1, ny)
         elif name.startswith(("gv_", "wv_")) or name in self.V_NAMES:

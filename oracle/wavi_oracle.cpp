@@ -302,6 +302,8 @@ struct Model {
   long op_applies = 0;
   std::vector<int> cg_iter_history;
   Vec cheb_eig;           // coarse variants 4, 5: the power vector (full wavelet layout, u then v), per solve
+  Vec last_coarse_b;      // the last V-cycle's coarse right-hand side and starting point (the cached
+  Vec last_coarse_x0;     // correction), in the coarse order [u | v], for studies of the coarse solvers
   int cheb_vcycles = 0;   // coarse variants 4, 5: V-cycles so far in this solve
   std::string err;
 };
@@ -1108,6 +1110,8 @@ void vcycle(Model& m, OpWork& w, Precond& p, Vec& x, const Vec& b) {
   Vec bc;
   restrict_vec(m, p, r, bc);
   double abstol = m.S.tol_coarse * norm2(bc);
+  m.last_coarse_b = bc;
+  m.last_coarse_x0 = p.corr;
   p.last_cg = g_coarse_variant == 0   ? coarse_cg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
               : g_coarse_variant == 4 ? coarse_srcg_chebyshev(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
               : g_coarse_variant == 5 ? coarse_pipelined_chebyshev(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
@@ -1362,6 +1366,7 @@ Vec* field_by_name(Model& m, const std::string& n) {
   F("gv_dnegbeff", gv_dnegbeff) F("v", v) F("gv_residual", gv_resid)
   F("eta", eta) F("temperature", temperature) F("damage", damage) F("glen_b", glen_b)
   F("wu_correction_full", wu_corr) F("wv_correction_full", wv_corr) F("wu_wavelets", wu_wav) F("wv_wavelets", wv_wav)
+  F("coarse_b", last_coarse_b) F("coarse_x0", last_coarse_x0)
 #undef F
   return nullptr;
 }
