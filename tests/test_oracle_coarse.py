@@ -110,3 +110,20 @@ def test_pipelined_cg_follows_the_single_reduction_iterates(oracle, reference_cg
     assert s0["coarse_cg_iterations"] <= s1["coarse_cg_iterations"] <= 1.2 * s0["coarse_cg_iterations"]
     err = np.sqrt(np.sum((u1 - u0) ** 2) + np.sum((v1 - v0) ** 2)) / np.sqrt(np.sum(u0 ** 2) + np.sum(v0 ** 2))
     assert err < 1e-9
+
+
+def test_oracle_keeps_the_last_coarse_problem(oracle, reference_cg):
+    """coarse_b and coarse_x0 hold the last V-cycle's coarse right-hand side and starting point: sized as
+    the coarse space, the first V-cycle starting cold, the second from the first one's correction."""
+    from wavi_gb300 import synthetic
+    g, bed, p, sp, ic = synthetic.small_case(nx=24, ny=12, maxiter_picard=1)
+    om = oracle.build_model(g, bed, p, sp, ic)
+    om.pre_solve()
+    om.update_velocities()
+    n = int(om.mask("wu_mask").sum() + om.mask("wv_mask").sum())
+    b, x0 = np.array(om.field("coarse_b")), np.array(om.field("coarse_x0"))
+    assert b.shape == x0.shape == (n,) and np.linalg.norm(b) > 0 and not x0.any()
+    wu = np.asarray(om.field("wu_correction_full")).ravel(order="F")[om.mask("wu_mask").ravel(order="F") != 0]
+    wv = np.asarray(om.field("wv_correction_full")).ravel(order="F")[om.mask("wv_mask").ravel(order="F") != 0]
+    om.update_velocities()
+    assert np.array_equal(np.array(om.field("coarse_x0")), np.concatenate([wu, wv]))
