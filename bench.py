@@ -359,7 +359,8 @@ def gpu_arm(args):
     release_solver(m)
     g, p, sp = m.grid, m.params, m.solver_params
 
-    mixed = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=args.coarse_solver)
+    mixed = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=args.coarse_solver,
+                           cheb_steps=args.cheb_steps)
     fp64 = VelocitySolver(g, sp, precision="fp64", device=local)
 
     # float64 reference algorithm on the GPU
@@ -380,12 +381,13 @@ def gpu_arm(args):
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     # dominant kernel: the persistent coarse CG, per CG iteration
-    prof = VelocitySolver(g, sp, precision="mixed", device=local, use_graphs=False, coarse_solver=args.coarse_solver)
+    prof = VelocitySolver(g, sp, precision="mixed", device=local, use_graphs=False, coarse_solver=args.coarse_solver,
+                          cheb_steps=args.cheb_steps)
     sec_it, cg_its, cg_launches = coarse_roofline(torch, prof, p, snapshot)
     prof.close()
     # operator applications per CG iteration: 1, or CHEB_STEPS with the Chebyshev preconditioner (the
     # library's default mixed coarse solver on full ice masks: CHEB_STEPS - 1 in the preconditioner)
-    apps = CHEB_STEPS if stmix[-1]["coarse_solver"] in ("srcg_chebyshev", "pipelined_chebyshev") else 1
+    apps = (args.cheb_steps or CHEB_STEPS) if stmix[-1]["coarse_solver"] in ("srcg_chebyshev", "pipelined_chebyshev") else 1
     cg_bytes = apps * cg_iteration_bytes(g.nx, g.ny, 4)
     cg_achieved = cg_bytes / sec_it / 1e9
     # the fused operator on a grid larger than L2
@@ -663,7 +665,8 @@ def profile_case(args):
     release_solver(m)
     sp = SolverParams(**{**m.solver_params.__dict__, "maxiter_picard": args.picard})
     s = VelocitySolver(m.grid, sp, precision=args.precision, use_graphs=False,
-                       coarse_solver=args.coarse_solver if args.precision == "mixed" else "auto")
+                       coarse_solver=args.coarse_solver if args.precision == "mixed" else "auto",
+                       cheb_steps=args.cheb_steps)
     dev = {k: torch.from_numpy(np.ascontiguousarray(np.asarray(snapshot[k]).ravel(order="F"))).cuda()
            for k in solve_field_names()}
     st = s.solve_device(m.params, dev)
@@ -687,6 +690,8 @@ def main():
     ap.add_argument("--coarse-solver", default="auto",
                     choices=("auto", "cg", "srcg", "srcg_jacobi", "srcg_chebyshev", "pipelined_chebyshev"),
                     help="coarse solver of the mixed-precision solves (the FP64 solve keeps the reference's)")
+    ap.add_argument("--cheb-steps", type=int, default=0,
+                    help="Chebyshev steps of the Chebyshev coarse solvers (0: the library's default, 3; else odd)")
     ap.add_argument("--config", default="c2", choices=("c2", "c4", "c5"),
                     help="c2: the 640x80 solve (default); c4: the adjoint on 640x80; c5: the ragged 256-member ensemble")
     ap.add_argument("--directions", type=int, default=20, help="--config c4: finite-difference directions")

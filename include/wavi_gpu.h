@@ -102,7 +102,8 @@ typedef struct wavi_options {
   int32_t stencil_kernel;            /* operator and smoother sweeps: 0 = by grid size (row-streaming from
                                         2^19 points of the (nx+1) x (ny+1) index space), 1 = shared-memory
                                         tiles, 2 = row-streaming */
-  int32_t reserved0;
+  int32_t cheb_steps;                /* Chebyshev steps per preconditioner application of the Chebyshev
+                                        coarse solvers: 0 = the default, 3; else odd, 1..15 */
 } wavi_options;
 
 /* Coarse solve of each V-cycle (R A P x = b_c, update_preconditioners.jl:54-83).  The reference calls

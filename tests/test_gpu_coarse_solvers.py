@@ -148,3 +148,21 @@ def test_single_reduction_solvers_need_the_persistent_kernel(oracle):
     f = fields_from_oracle(om, g)
     assert s.solve(p, f)["status"] in (0, -4)
     s.close()
+
+
+def test_chebyshev_step_count_option(oracle):
+    """wavi_options.cheb_steps: an even count (the preconditioner would not stay positive definite) is
+    rejected; 3 and 5 steps both converge to the reference's FP64 solution."""
+    from wavi_gb300.abi import WaviError
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, "full", maxiter_picard=80, tol_picard=1e-7)
+    with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):
+        VelocitySolver(g, sp, precision="mixed", coarse_solver="srcg_chebyshev", cheb_steps=4)
+    f0 = fields_from_oracle(om, g)
+    om.update_velocities()
+    for steps in (3, 5):
+        f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
+        s = VelocitySolver(g, sp, precision="mixed", coarse_solver="srcg_chebyshev", cheb_steps=steps)
+        st = s.solve(p, f)
+        s.close()
+        assert st["status"] == 0 and uv_err(f, om) < 1e-6, (steps, st)

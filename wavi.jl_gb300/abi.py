@@ -56,7 +56,7 @@ class SolverParams(C.Structure):
 class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graphs", C.c_int32),
                 ("picard_test", C.c_int32), ("coarse_kernel", C.c_int32), ("coarse_solver", C.c_int32),
-                ("stencil_kernel", C.c_int32), ("reserved0", C.c_int32)]
+                ("stencil_kernel", C.c_int32), ("cheb_steps", C.c_int32)]
 
 
 FIELD_INPUTS = ("h", "s", "dsdh", "grounded_fraction", "weertman_c", "accumulation", "basal_melt",

@@ -426,6 +426,7 @@ int enqueue_cg_iteration(wavi_ctx* c, const CondHandles& h, int* live, Tally& t)
 // application (odd: the preconditioner stays positive definite if λmax is underestimated) and the ratio
 // of the interval's ends.
 constexpr int kChebSteps = 3;
+int cheb_steps(const wavi_ctx* c) { return c->opt.cheb_steps > 0 ? c->opt.cheb_steps : kChebSteps; }
 constexpr float kChebRatio = 120.0f;
 
 template <typename T, int TILE, int MAXT>
@@ -449,7 +450,7 @@ int launch_cg_persistent(wavi_ctx* c) {
     if constexpr (std::is_same<T, float>::value && TILE == 16 && MAXT <= 2) {
       CK(cudaLaunchKernelEx(&cfg, k_pcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c),
                             (const uint8_t*)c->wmask_uv, (const T*)c->dcoarse, (const T*)c->bc, (T*)c->xc, c->partials,
-                            c->S, (const DevParams*)c->P, c->bar, c->halo_box, kChebSteps, kChebRatio,
+                            c->S, (const DevParams*)c->P, c->bar, c->halo_box, cheb_steps(c), kChebRatio,
                             (T*)c->cheb_eig, c->ntx, c->nty));
     } else {
       return fail(c, WAVI_ERR_ARGUMENT, "the pipelined coarse CG has no kernel for this precision and tiling");
@@ -459,7 +460,7 @@ int launch_cg_persistent(wavi_ctx* c) {
     const T* dc = (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI || cheb) ? (const T*)c->dcoarse : nullptr;
     CK(cudaLaunchKernelEx(&cfg, k_srcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
                           dc, (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
-                          c->halo_box, cheb ? kChebSteps : 1, kChebRatio, (T*)c->cheb_eig, c->ntx, c->nty));
+                          c->halo_box, cheb ? cheb_steps(c) : 1, kChebRatio, (T*)c->cheb_eig, c->ntx, c->nty));
   }
   c->launches++;
   return 0;
@@ -1449,6 +1450,8 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_solver %d", want));
   if (opt->coarse_kernel < 0 || opt->coarse_kernel > 3)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_kernel %d", opt->coarse_kernel));
+  if (opt->cheb_steps != 0 && (opt->cheb_steps < 1 || opt->cheb_steps > 15 || opt->cheb_steps % 2 == 0))
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "cheb_steps must be 0 (default) or odd in 1..15 (got %d)", opt->cheb_steps));
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));
   // auto: FP64 runs the reference's cg!; mixed runs the Chebyshev-Jacobi single-reduction CG on domains

@@ -39,7 +39,7 @@ class VelocitySolver:
     STENCIL_KERNELS = {"auto": 0, "tiled": 1, "streaming": 2}
 
     def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0,
-                 coarse_kernel="auto", coarse_solver="auto", stencil_kernel="auto"):
+                 coarse_kernel="auto", coarse_solver="auto", stencil_kernel="auto", cheb_steps=0):
         self.lib = abi.load_library()
         self.grid = grid
         self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ
@@ -49,7 +49,7 @@ class VelocitySolver:
         self._sp = solver_params.to_c()
         self._opt = abi.Options(int(device), PRECISIONS[precision], 1 if use_graphs else 0, int(picard_test),
                                 self.COARSE_KERNELS[coarse_kernel], abi.COARSE_SOLVERS[coarse_solver],
-                                self.STENCIL_KERNELS[stencil_kernel], 0)
+                                self.STENCIL_KERNELS[stencil_kernel], int(cheb_steps))
         ctx = C.c_void_p()
         st = self.lib.wavi_ctx_create(C.byref(self._desc.desc), C.byref(self._sp), C.byref(self._opt), C.byref(ctx))
         if st != 0:
