@@ -118,9 +118,10 @@ typedef enum wavi_coarse_solver {
   WAVI_COARSE_SRCG = 2,              /* single-reduction CG, no preconditioner (same iterates as cg!) */
   WAVI_COARSE_SRCG_JACOBI = 3,       /* single-reduction CG preconditioned by diag(R A P) */
   WAVI_COARSE_SRCG_CHEBYSHEV = 4,    /* single-reduction CG preconditioned by cheb_steps (default 3)
-                                        Chebyshev-accelerated Jacobi steps on [b/120, b], b = 1.15 lambda_max(diag(R A P)^-1 R A P) from
-                                        power steps each V-cycle (12 in a solve's first, then 4, warm-
-                                        started); register-resident persistent kernel only */
+                                        Chebyshev-accelerated Jacobi steps on [b/120, b],
+                                        b = 1.15 lambda_max(diag(R A P)^-1 R A P) from power steps each
+                                        V-cycle (12 in a solve's first, then 4, warm-started);
+                                        register-resident persistent kernel only */
   WAVI_COARSE_PIPELINED_CHEBYSHEV = 5 /* opt-in, never chosen by AUTO: pipelined CG (Ghysels & Vanroose
                                         2014) with the preconditioner of SRCG_CHEBYSHEV, whose grid
                                         reduction overlaps the iteration's preconditioner and operator;
