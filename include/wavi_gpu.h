@@ -215,7 +215,11 @@ const char* wavi_last_error(const wavi_ctx* ctx);
 
 /* One velocity solve with host buffers: copies the inputs and Picard state to the device, runs
  * update_velocities! (update_velocities.jl:11-29) and copies the state and outputs back.
- * Replaces update_velocities.jl:11-29 as called from update_state.jl:154-157. */
+ * Replaces update_velocities.jl:11-29 as called from update_state.jl:154-157.
+ * Returns 0 whenever the solve ran to its end, with stats->status = WAVI_OK, or the soft
+ * WAVI_ERR_NOT_CONVERGED when maxiter_picard stopped it (every output written, as the reference stops
+ * silently); a negative return is a hard error.  Bindings should nevertheless treat a return of
+ * WAVI_ERR_NOT_CONVERGED or WAVI_ERR_COARSE_CAP as soft. */
 int wavi_solve_velocities(wavi_ctx* ctx, const wavi_params* params, wavi_fields* fields,
                           wavi_stats* stats);
 
@@ -292,7 +296,9 @@ typedef struct wavi_operator_desc {
  * (about 256 KiB) that every device loading the library keeps until the process exits; grids beyond
  * WAVI_NOALLOC_MAX_TILES tiles are rejected with WAVI_ERR_ARGUMENT and a message in
  * wavi_last_error(NULL).  The first call on each device looks up that array's device address (with the
- * device current) and caches it: make that first call before any stream capture.  Every call shares the
+ * device current) and caches it for the life of the process: make that first call before any stream
+ * capture, and do not call this entry point after cudaDeviceReset() on that device (the reset unloads the
+ * module that holds the array, so the cached address is stale).  Every call shares the
  * one array (its counter is cleared at the start of each call), so calls that overlap on the GPU — on
  * different streams, or from different host threads — race and must be ordered by the caller. */
 int wavi_residual_noalloc(const wavi_operator_desc* op, const double* x_uv, const double* b_uv, double* r_uv,

@@ -9,7 +9,7 @@ itself, and ``jld2_files.json``: each file's header Julia version, link order an
 files byte for byte with ``wavi_gb300.io.write_jld2``.  It reads the reference checkout and is run by hand
 on a machine that has it; the tests elsewhere only need the ``.npz`` files.
 
-Usage:  python tests/golden/make_golden.py [path-to-reference-checkout]
+Usage:  python tests/golden/make_golden.py <path-to-reference-checkout>
 """
 import hashlib
 import json
@@ -50,7 +50,9 @@ def file_record(path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the WAVI.jl source tree>")
+    ref = sys.argv[1]
     src = os.path.join(ref, "test", "version_update_test_verification")
     here = os.path.dirname(os.path.abspath(__file__))
     records = {}

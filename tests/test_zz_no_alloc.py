@@ -3,9 +3,11 @@ cudaMalloc (a framework owning the device heap through its own pool, code under 
 callback, a service with a fixed device-memory budget).  It takes every input and output from the
 caller and keeps its reduction scratch in a static device array.
 
-Checked against the existing entry point (wavi_apply_operator_device on a relinearised float64
-context): r = b - A x and ||r||^2 to the operator tests' 1e-12, on two calls in a row.  This file sorts
-last so that a run stopping at the first failure has already run every other test.
+Checked on two calls in a row against the existing entry point (wavi_apply_operator_device on a
+relinearised float64 context) and against the FP64 oracle's operator (op_fun!, utilities.jl:61-145) on
+the same x and b, which shares none of the library's stencil code: r = b - A x and ||r||^2 to the
+operator tests' 1e-12.  This file sorts last so that a run stopping at the first failure has already run
+every other test.
 """
 import ctypes as C
 
@@ -37,7 +39,7 @@ def _operator_arrays(om, g):
 
 
 @pytest.mark.parametrize("name", ["full", "disc"])
-def test_residual_noalloc_matches_operator_entry_point(oracle, name):
+def test_residual_noalloc_matches_operator_entry_point_and_oracle(oracle, name):
     from wavi_gb300 import abi, synthetic
     from wavi_gb300.gpu import VelocitySolver
     case = dict(nx=40, ny=16, dx=4000.0, mask="full") if name == "full" else dict(nx=24, ny=24, dx=4000.0, mask="disc")
@@ -56,13 +58,21 @@ def test_residual_noalloc_matches_operator_entry_point(oracle, name):
     desc = abi.OperatorDesc(g.nx, g.ny, g.dx, g.dy, *(C.c_void_p(dev[k].data_ptr()) for k in
                                                       ("heta_h", "heta_c", "dimp", "beta_m", "h_m", "inner")))
     n = inner.size
+    nu = (g.nx + 1) * g.ny
     for call in range(2):  # the static scratch is shared: the second call must not see the first's state
-        x = torch.from_numpy(rng.standard_normal(n) * inner).cuda()
-        b = torch.from_numpy(rng.standard_normal(n) * 1e3 * inner).cuda()
+        xh = rng.standard_normal(n) * inner
+        bh = rng.standard_normal(n) * 1e3 * inner
+        x = torch.from_numpy(xh).cuda()
+        b = torch.from_numpy(bh).cuda()
         y = torch.zeros_like(x)
         solver.apply_operator_device(x, y, "fp64")
         r_ref = (b - y).cpu().numpy() * inner
         rr_ref = float(np.sum(r_ref ** 2))
+        # the oracle's own operator on the same x: independent of the library's stencil helpers
+        ou, ov = om.apply_operator(xh[:nu].reshape((g.nx + 1, g.ny), order="F"),
+                                   xh[nu:].reshape((g.nx, g.ny + 1), order="F"))
+        r_orc = (bh - np.concatenate([np.asarray(ou).ravel(order="F"), np.asarray(ov).ravel(order="F")])) * inner
+        rr_orc = float(np.sum(r_orc ** 2))
         r = torch.full_like(x, float("nan"))
         rr = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
         st = lib.wavi_residual_noalloc(C.byref(desc), C.c_void_p(x.data_ptr()), C.c_void_p(b.data_ptr()),
@@ -71,6 +81,8 @@ def test_residual_noalloc_matches_operator_entry_point(oracle, name):
         torch.cuda.synchronize()
         assert rel(r.cpu().numpy(), r_ref) < 1e-12, call
         assert abs(float(rr.item()) - rr_ref) <= 1e-12 * rr_ref, call
+        assert rel(r.cpu().numpy(), r_orc) < 1e-12, call
+        assert abs(float(rr.item()) - rr_orc) <= 1e-12 * rr_orc, call
     solver.close()
 
 

@@ -10,7 +10,9 @@
 // The reduction scratch (block partial sums and the last-block counter) is a file-scope static
 // __device__ array of a fixed size, resident on every device that loads the library until the process
 // exits.  Host code cannot use the array's name as a device address, so the first call on each device
-// looks the address up with cudaGetSymbolAddress (with that device current) and caches it.
+// looks the address up with cudaGetSymbolAddress (with that device current) and caches it for the life
+// of the process.  cudaDeviceReset() unloads the module that holds the array, which leaves the cached
+// address stale: the header tells callers not to use this entry point on a device after a reset.
 #include <cuda_runtime.h>
 
 #include <mutex>

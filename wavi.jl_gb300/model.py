@@ -297,8 +297,8 @@ def pos_fraction(z1, mask=None):
                 # every candidate is evaluated; the ones a cell does not select may be inf or NaN
                 area = np.select([ix == 1, ix == 2, ix == 3, ix == 4, ix == 5, ix == 6, ix == 7, ix == 8],
                                  [0.0 * a, -A1, A2 - A1, A1 + A3, A3, A2 + A3, 1.0 - A2 + A1, 1.0 - A2], 1.0)
-            area = np.where(b < 0.0, 1.0 - area, area)
-            area = np.where(a1_ < 0.0, 1.0 - area, area)
+                area = np.where(b < 0.0, 1.0 - area, area)  # b may be NaN where no candidate is selected
+                area = np.where(a1_ < 0.0, 1.0 - area, area)
             afq[sc] = area
         afq[(z1 > 0.0) & (z2 > 0.0) & (z3 > 0.0)] = 1.0
         afq[(z1 <= 0.0) & (z2 <= 0.0) & (z3 <= 0.0)] = 0.0
