@@ -11,17 +11,24 @@ reference's other solver parameters).
            in HBM, device time per step from CUDA events on the solver's stream, L2 flushed between steps
   e2e      the same solve through the host C ABI (wavi_solve_velocities) from pinned host buffers, the
            host<->device copies inside the timed region
-  fp64_gpu the reference algorithm in float64 on the GPU (the comparison the metric names)
+  fp64_gpu the reference algorithm in float64 on the GPU (cg! coarse solve; the comparison the metric names)
+  fp64_gpu_same_solver  float64 with the mixed solve's own coarse solver: mixed_over_fp64_same_solver is
+           the gain of precision alone, mixed_over_fp64 that of precision and coarse solver together
+  rel_err_*_vs_oracle  relative velocity error of each GPU solve against the FP64 oracle's converged solve
+           of the same state (tests/golden/c2_oracle_solution.npz)
   roofline the dominant kernel of the step, the persistent coarse CG (k_srcg_persistent<float>), timed
            with CUDA events around each launch in a host-driven solve of the same state; per CG
-           iteration: algorithmic bytes / duration against the measured HBM peak (the kernel's working
-           set, ~3 MB, is on chip or in L2: it is bound by the latency of its grid reduction and of the
-           neighbour halo exchanges of its operator applications, not by HBM)
-  roofline_stencil the fused operator kernel (float32) on a 4096 x 1024 grid (~190 MB per application,
-           larger than L2), back-to-back launches timed with CUDA events: the HBM-bound stencil figure
-  cpu_baseline the CPU oracle (the FP64 restatement of the reference) on a bounded sample
+           iteration: algorithmic bytes / duration against the measured HBM peak for scale.  Its working
+           set (~3 MB) is on chip or in L2: it is bound by the latency of its grid reduction and of the
+           neighbour halo exchanges of its operator applications, which latency_model splits from the
+           Jacobi and Chebyshev coarse solves' per-iteration times
+  roofline_stencil the fused operator kernel (float32, k_op_stream) on a 4096 x 1024 grid (~190 MB per
+           application, larger than L2), back-to-back launches timed with CUDA events
+  cpu_baseline the CPU oracle (the FP64 restatement of the reference) on a bounded sample: the first
+           iterations of the solve on every host thread, scaled by the oracle's own profile
 
-``--impl reference`` times only the CPU oracle on all host cores and prints its own line.
+``--impl reference`` times only the CPU oracle on all host cores (a whole converged solve per thread, all
+threads at once, one step) and prints its own line.
 Under torchrun (N > 1) every rank solves its own replica (no collective); value is the sum.
 ``--profile solve|op`` runs one small untimed case for ncu (a host-driven solve of the workload capped
 at ``--picard`` Picard iterations, or operator launches on the 4096 x 1024 grid) and prints nothing.
@@ -273,32 +280,52 @@ def ncu_traffic(fn, key):
 
 
 # ---------------------------------------------------------------------------------------------------
-# CPU oracle (the reference restated in C++), bounded sample on host threads
+# CPU oracle (the reference restated in C++) on the host threads
 # ---------------------------------------------------------------------------------------------------
-def cpu_sample(threads, picard_iters_sample=1, state=None):
-    """Each thread builds the same perturbed-thickness state in its own oracle model and runs
-    ``picard_iters_sample`` Picard iterations of the solve.  Returns (seconds per Picard iteration per
-    thread, threads, picard count of the full solve measured by the oracle's warm-state run length)."""
-    oracle = __graft_entry__.load_oracle()
-    pkg = __graft_entry__.load_package()
-    from wavi_gb300 import synthetic
-    import ctypes as C
+C2_FIXTURE = os.path.join(ROOT, "tests", "golden", "c2_oracle_solution.npz")
 
-    def make():
-        g, bed, p, sp, ic = synthetic.channel_c2(tol_picard=TOL_PICARD, maxiter_picard=MAXITER_PICARD)
-        om = oracle.build_model(g, bed, p, sp, ic)
-        return om, g, p, sp
+
+def c2_fixture():
+    """The FP64 oracle's converged solve of this workload (tests/golden/make_c2_solution.py), or None."""
+    try:
+        return np.load(C2_FIXTURE)
+    except OSError:
+        return None
+
+
+def rel_err_uv(u, v, ref_u, ref_v):
+    """||(u, v) - (u, v)_ref||_2 / ||(u, v)_ref||_2 over the whole u and v grids."""
+    num = np.sqrt(np.sum((np.asarray(u).ravel() - np.asarray(ref_u).ravel(order="F")) ** 2) +
+                  np.sum((np.asarray(v).ravel() - np.asarray(ref_v).ravel(order="F")) ** 2))
+    return float(num / np.sqrt(np.sum(np.asarray(ref_u) ** 2) + np.sum(np.asarray(ref_v) ** 2)))
+
+
+def c2_config(m):
+    """The workload's config keys, the same on the GPU line and the reference line."""
+    return {"workload": WORKLOAD, "nx": m.grid.nx, "ny": m.grid.ny, "nsigma": m.grid.nσ, "dx_m": m.grid.dx,
+            "unknowns": int(m.u_inner.sum() + m.v_inner.sum()), "tol_picard": TOL_PICARD,
+            "maxiter_picard": MAXITER_PICARD,
+            "l2": "GPU: flushed between steps (256 MiB write); CPU: not applicable"}
+
+
+def cpu_solves(threads, maxiter_picard):
+    """Every host thread builds the workload's state in its own oracle model and solves it with
+    ``maxiter_picard`` (all threads at once, each solve single-threaded).  Returns ([(seconds, picard
+    iterations, final relative residual) per thread], wall seconds of the whole batch)."""
+    oracle = __graft_entry__.load_oracle()
+    __graft_entry__.load_package()
+    from wavi_gb300 import synthetic
 
     results = [None] * threads
 
     def work(i):
-        om, g, p, sp = make()
+        g, bed, p, sp, ic = synthetic.channel_c2(tol_picard=TOL_PICARD, maxiter_picard=maxiter_picard)
+        om = oracle.build_model(g, bed, p, sp, ic)
         om.pre_solve()
-        sp1 = type(sp)(**{**sp.__dict__, "maxiter_picard": picard_iters_sample})
-        oracle.lib().oracle_set_params(om.h, C.byref(p.to_c()), C.byref(sp1.to_c()), 0.0)
         t0 = time.perf_counter()
         om.update_velocities()
-        results[i] = (time.perf_counter() - t0) / picard_iters_sample
+        st = om.stats()
+        results[i] = (time.perf_counter() - t0, st["picard_iterations"], st["rel_residual"])
 
     ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
     t0 = time.perf_counter()
@@ -306,36 +333,55 @@ def cpu_sample(threads, picard_iters_sample=1, state=None):
         t.start()
     for t in ths:
         t.join()
-    wall = time.perf_counter() - t0
-    return results, wall
+    return results, time.perf_counter() - t0
 
 
-# Picard iterations of the timed solve (same algorithm and state on every arm; the FP64 GPU arm reports
-# its own count, which the CPU extrapolation uses when available).
-PICARD_FALLBACK = 40
+def cpu_baseline_sample(threads):
+    """The GPU line's cpu_baseline: a bounded sample — the first SAMPLE_PICARD Picard iterations of the solve
+    on every host thread at once — scaled to a whole solve by the oracle's own single-thread profile of
+    this workload (whole solve / those iterations, both timed when the committed fixture was made)."""
+    ref = c2_fixture()
+    if ref is None:
+        return None
+    k = int(ref["sample_picard"])
+    scale = float(ref["oracle_seconds"]) / float(ref["sample_seconds"])
+    res, wall = cpu_solves(threads, k)
+    sec = statistics.median(r[0] for r in res) * scale
+    return {"value": threads / sec, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"the first {k} Picard iterations of this solve on each of {threads} host threads at once "
+                      f"(median {sec / scale:.2f} s), scaled by {scale:.1f} = whole solve / those iterations in the "
+                      f"oracle's single-thread profile of this workload ({float(ref['oracle_seconds']):.0f} s / "
+                      f"{float(ref['sample_seconds']):.1f} s)"}
 
 
 def reference_arm(args):
+    """The reference's CPU path on the host cores: the FP64 oracle (the C++ restatement of the reference's
+    solve) solving the whole workload to convergence on every host thread at once, one single-threaded
+    solve per thread.  One step: a whole solve takes minutes, so the requested steps and warm-up (the
+    oracle has nothing to warm up) are not repeated; value = solves completed / wall time."""
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
+    pkg = __graft_entry__.load_package()
+    from wavi_gb300.model import release_solver
+    m = build_state(pkg)
+    release_solver(m)
     threads = os.cpu_count() or 1
-    per_iter = []
-    for it in range(args.warmup + args.steps):
-        res, wall = cpu_sample(threads)
-        if it >= args.warmup:
-            per_iter.append(statistics.median(res))
-    sec_per_iter = statistics.median(per_iter)
-    solves_per_s = threads / (sec_per_iter * PICARD_FALLBACK)
+    res, wall = cpu_solves(threads, MAXITER_PICARD)
+    per = statistics.median(r[0] for r in res)
+    value = threads / wall
     line = {
-        "impl": "reference", "metric": METRIC, "value": solves_per_s, "unit": "solves/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sec_per_iter * PICARD_FALLBACK,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "parallelism": f"{threads} host threads, independent replicas"},
-        "cpu_baseline": {"value": solves_per_s, "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": f"first Picard iteration of the solve per thread ({threads} threads), "
-                                   f"extrapolated x{PICARD_FALLBACK} Picard iterations"},
-        "e2e": {"value": solves_per_s, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": 1, "warmup": 0, "requested_steps": args.steps, "requested_warmup": args.warmup,
+        "ms_per_step": 1e3 * wall, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "config": c2_config(m),
+        "parallelism": f"{threads} host threads, one whole single-threaded solve each",
+        "single_thread": {"value": 1.0 / per, "unit": "solves/s", "seconds_per_solve": per},
+        "solves": {"picard_iterations": sorted({r[1] for r in res}), "rel_residual_max": max(r[2] for r in res)},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"one whole Picard-converged solve on each of {threads} host threads at once "
+                                   f"(wall {wall:.1f} s; median single-thread solve {per:.1f} s)"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -360,7 +406,8 @@ def gpu_arm(args):
     g, p, sp = m.grid, m.params, m.solver_params
 
     mixed = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=args.coarse_solver,
-                           cheb_steps=args.cheb_steps)
+                           cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums,
+                           viscosity=args.viscosity)
     fp64 = VelocitySolver(g, sp, precision="fp64", device=local)
 
     # float64 reference algorithm on the GPU
@@ -377,17 +424,63 @@ def gpu_arm(args):
 
     te2e, hb, db = time_host_solves(torch, mixed, p, snapshot, args.steps, max(1, args.warmup // 2))
     e2e_value = world * len(te2e) / sum(te2e)
+    mixed_solver = stmix[-1]["coarse_solver"]
+
+    # float64 with the mixed solve's own coarse solver: precision alone, the algorithm held fixed
+    same = None
+    if mixed_solver != "pipelined_chebyshev":
+        fp64s = VelocitySolver(g, sp, precision="fp64", device=local, coarse_solver=mixed_solver,
+                               cheb_steps=args.cheb_steps)
+        t64s, st64s, out64s = time_device_solves(torch, fp64s, p, snapshot, max(1, args.steps // 2), 1)
+        fp64s.close()
+        same = {"value": world * len(t64s) / sum(t64s), "unit": "solves/s", "ms_per_step": 1e3 * sum(t64s) / len(t64s),
+                "coarse_solver": st64s[-1]["coarse_solver"], "picard_iterations": st64s[-1]["picard_iterations"],
+                "coarse_cg_iterations": st64s[-1]["coarse_cg_iterations"], "status_name": st64s[-1]["status_name"]}
+
+    # the mixed solve with its coarse CG's dot products, sums and scalars in FP64 (WAVI_SUMS_FP64) instead of
+    # float-float grid sums over FP32 CTA sums
+    sums64, outm64 = None, None
+    if mixed_solver in ("srcg", "srcg_jacobi", "srcg_chebyshev") and args.coarse_sums != "fp64":
+        try:
+            m64 = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=mixed_solver,
+                                 cheb_steps=args.cheb_steps, coarse_sums="fp64", viscosity=args.viscosity)
+        except Exception as e:  # the register-resident kernel may not fit (reported, not fatal)
+            sums64 = {"unavailable": str(e)}
+        else:
+            tm64, stm64, outm64 = time_device_solves(torch, m64, p, snapshot, args.steps, 1)
+            m64.close()
+            sums64 = {"value": world * len(tm64) / sum(tm64), "unit": "solves/s",
+                      "ms_per_step": 1e3 * sum(tm64) / len(tm64), "picard_iterations": stm64[-1]["picard_iterations"],
+                      "coarse_cg_iterations": stm64[-1]["coarse_cg_iterations"],
+                      "status_name": stm64[-1]["status_name"]}
 
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
-    # dominant kernel: the persistent coarse CG, per CG iteration
+    # dominant kernel: the persistent coarse CG, per CG iteration, timed launch by launch in host-driven solves;
+    # with the Jacobi preconditioner (one operator application and one grid reduction per iteration) beside
+    # it, the two per-iteration times split into a grid reduction and an operator application with its
+    # neighbour exchange
     prof = VelocitySolver(g, sp, precision="mixed", device=local, use_graphs=False, coarse_solver=args.coarse_solver,
-                          cheb_steps=args.cheb_steps)
+                          cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums,
+                           viscosity=args.viscosity)
     sec_it, cg_its, cg_launches = coarse_roofline(torch, prof, p, snapshot)
     prof.close()
-    # operator applications per CG iteration: 1, or CHEB_STEPS with the Chebyshev preconditioner (the
-    # library's default mixed coarse solver on full ice masks: CHEB_STEPS - 1 in the preconditioner)
-    apps = (args.cheb_steps or CHEB_STEPS) if stmix[-1]["coarse_solver"] in ("srcg_chebyshev", "pipelined_chebyshev") else 1
+    apps = (args.cheb_steps or CHEB_STEPS) if mixed_solver in ("srcg_chebyshev", "pipelined_chebyshev") else 1
+    latency = None
+    if mixed_solver == "srcg_chebyshev" and apps > 1:
+        profj = VelocitySolver(g, sp, precision="mixed", device=local, use_graphs=False, coarse_solver="srcg_jacobi",
+                               coarse_sums=args.coarse_sums, viscosity=args.viscosity)
+        sec_j, cg_j, _ = coarse_roofline(torch, profj, p, snapshot)
+        profj.close()
+        e_op = (sec_it - sec_j) / (apps - 1)
+        latency = {"us_per_iteration": sec_it * 1e6, "us_per_grid_reduction": (sec_j - e_op) * 1e6,
+                   "us_per_operator_application": e_op * 1e6, "grid_reductions_per_iteration": 1,
+                   "operator_applications_per_iteration": apps, "jacobi_us_per_iteration": sec_j * 1e6,
+                   "jacobi_cg_iterations": cg_j,
+                   "method": "Jacobi iteration = 1 operator application (prolongation, neighbour halo exchange, "
+                             "stresses, restriction) + 1 grid reduction; Chebyshev iteration = %d applications + 1 "
+                             "reduction: the difference of the measured per-iteration times gives the "
+                             "application, the rest of the Jacobi iteration the reduction" % apps}
     cg_bytes = apps * cg_iteration_bytes(g.nx, g.ny, 4)
     cg_achieved = cg_bytes / sec_it / 1e9
     # the fused operator on a grid larger than L2
@@ -396,50 +489,64 @@ def gpu_arm(args):
     big.close()
     achieved = alg_bytes / dur / 1e9
 
-    err = np.sqrt(np.sum((outmix["u"] - out64["u"]) ** 2) + np.sum((outmix["v"] - out64["v"]) ** 2)) / \
-        np.sqrt(np.sum(out64["u"] ** 2) + np.sum(out64["v"] ** 2))
+    err = rel_err_uv(outmix["u"], outmix["v"], out64["u"].reshape((g.nx + 1, g.ny), order="F"),
+                     out64["v"].reshape((g.nx, g.ny + 1), order="F"))
+    ref = c2_fixture()
+    errs_oracle = {}
+    if ref is not None:
+        errs_oracle["rel_err_mixed_vs_oracle"] = rel_err_uv(outmix["u"], outmix["v"], ref["u"], ref["v"])
+        errs_oracle["rel_err_fp64_vs_oracle"] = rel_err_uv(out64["u"], out64["v"], ref["u"], ref["v"])
+        if same is not None:
+            errs_oracle["rel_err_fp64_same_solver_vs_oracle"] = rel_err_uv(out64s["u"], out64s["v"], ref["u"], ref["v"])
+        if outm64 is not None:
+            sums64["rel_err_vs_oracle"] = rel_err_uv(outm64["u"], outm64["v"], ref["u"], ref["v"])
+        errs_oracle["oracle"] = {"picard_iterations": int(ref["picard_iterations"]),
+                                 "coarse_cg_iterations": int(ref["coarse_cg_iterations"]),
+                                 "rel_residual": float(ref["rel_residual"]),
+                                 "source": "tests/golden/c2_oracle_solution.npz (FP64 oracle, same state)"}
     fp64_value = world * len(t64) / sum(t64)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        res, wall = cpu_sample(threads)
-        sec = statistics.median(res)
-        picard = int(statistics.median([s["picard_iterations"] for s in st64]))
-        cpu = {"value": threads / (sec * picard), "unit": "solves/s", "cores": threads, "kind": "port",
-               "sample": f"first Picard iteration of this solve on each of {threads} threads "
-                         f"({sec:.2f} s each), extrapolated x{picard} Picard iterations (the FP64 GPU count)"}
+        cpu = cpu_baseline_sample(os.cpu_count() or 1)
 
     launches = sum(s["kernel_launches"] for s in stmix)
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "nx": g.nx, "ny": g.ny, "nsigma": g.nσ, "dx_m": g.dx,
-                   "unknowns": int(m.u_inner.sum() + m.v_inner.sum()), "tol_picard": TOL_PICARD,
-                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}"},
+        "config": c2_config(m), "parallelism": f"replicas x{world}",
         "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(hb), "d2h_bytes_per_step": int(db)},
         "gpu_launches": int(launches),
         "fp64_gpu": {"value": fp64_value, "unit": "solves/s", "ms_per_step": 1e3 * sum(t64) / len(t64),
+                     "coarse_solver": st64[-1]["coarse_solver"],
                      "picard_iterations": st64[-1]["picard_iterations"],
                      "coarse_cg_iterations": st64[-1]["coarse_cg_iterations"]},
+        "fp64_gpu_same_solver": same,
         "mixed_over_fp64": value / fp64_value if fp64_value else None,
+        "mixed_over_fp64_same_solver": value / same["value"] if same else None,
+        "mixed_fp64_coarse_sums": sums64,
         "rel_err_mixed_vs_fp64": float(err),
+        **errs_oracle,
         "solve": {k: stmix[-1][k] for k in ("picard_iterations", "coarse_cg_iterations", "op_applications",
-                                             "rel_residual", "kernel_launches", "host_syncs", "status_name")},
-        "roofline": {"bound": "hbm", "achieved": cg_achieved, "peak": peak, "unit": "GB/s",
+                                             "rel_residual", "kernel_launches", "host_syncs", "status_name",
+                                             "coarse_solver")},
+        "roofline": {"bound": "latency", "achieved": cg_achieved, "peak": peak, "unit": "GB/s",
                      "frac": cg_achieved / peak,
                      "traffic": ncu_traffic("coarse_cg_c2.md", "traffic_bytes_per_cg_iteration"),
                      "kernel": "k_srcg_persistent<float> (coarse CG, one launch per V-cycle, 640x80)",
                      "per": "CG iteration", "alg_bytes_per_iteration": cg_bytes, "us_per_iteration": sec_it * 1e6,
-                     "operator_applications_per_iteration": apps, "coarse_solver": stmix[-1]["coarse_solver"],
+                     "operator_applications_per_iteration": apps, "coarse_solver": mixed_solver,
                      "cg_iterations": cg_its, "launches": cg_launches, "peak_source": "measured" if peaks else "fallback",
-                     "note": "on-chip/L2-resident working set; bound by the latency of one grid reduction and "
-                             "operator_applications_per_iteration neighbour halo exchanges per iteration"},
+                     "latency_model": latency,
+                     "note": "achieved = algorithmic bytes (L2-level: the working set, ~3 MB, stays on chip or in "
+                             "L2) / time, against the HBM peak for scale only; traffic = ncu DRAM bytes per "
+                             "iteration. The kernel is bound by the latency of its grid reduction and of the "
+                             "neighbour halo exchanges of its operator applications (latency_model)"},
         "roofline_stencil": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak,
                              "traffic": ncu_traffic("op_kernel_4096x1024.md", "traffic_bytes_per_launch"),
-                             "kernel": "k_op<float> (fused operator, %dx%d)" % STENCIL_GRID,
+                             "kernel": "k_op_stream<float> (fused operator, row streaming, %dx%d)" % STENCIL_GRID,
                              "alg_bytes_per_launch": alg_bytes, "avg_launch_us": dur * 1e6,
                              "peak_source": "measured" if peaks else "fallback"},
         "cpu_baseline": cpu,
@@ -451,6 +558,136 @@ def gpu_arm(args):
     fp64.close()
     if world > 1:
         dist.destroy_process_group()
+    return 0
+
+
+C3_WORKLOAD = ("2560x320 channel @250m, nsigma=8, log-normal C (median 1e4, sigma_log 0.5, 20 km correlation, seed 3), "
+               "A from a 243-268 K vertical temperature profile; Picard solve from the initial state, at most 30 "
+               "iterations, to ||du||/||u|| <= 1e-6 and ||b - A u||/||b|| < 1e-6")
+
+
+def relin_h_bytes(nx, ny, ns, mixed):
+    """Algorithmic bytes of one launch of the relinearisation's h-grid kernel, per h cell: reads u and v
+    (about one value of each per cell), the previous F2 and β, C·gf, h, ds/dh, and B and η on every σ level;
+    writes η on every level and twelve 2-D fields (strain rate, speeds, β, τ_b, ηav, F1, F2, βeff, hηav, the
+    two operator coefficients), plus their FP32 copies in mixed precision; one byte each of the h, c and
+    u/v masks (the u/v mask about twice)."""
+    Nh = nx * ny
+    return Nh * (8.0 * (7 + 2 * ns) + 8.0 * (12 + ns) + (8.0 if mixed else 0.0) + 4.0)
+
+
+def relin_uv_bytes(nx, ny):
+    """Algorithmic bytes of one launch of the u/v-grid relinearisation kernel: per u or v point the h-grid
+    βeff, grounded fraction and h ηav of its two neighbours (about one value of each per point), its own
+    grounded fraction and thickness, βeff written, and the operator coefficients β_m, h_m (FP64 and FP32) and
+    hη_c (per c cell), plus the masks."""
+    N = (nx + 1) * ny + nx * (ny + 1)
+    Nc = (nx - 1) * (ny - 1)
+    return N * (8.0 * 5 + 8.0 * 3 + 4.0 * 2 + 1.0) + Nc * (8.0 + 4.0 + 8.0) + 2.0 * nx * ny
+
+
+def c3_arm(args):
+    """The large single domain (2560 x 320 at 250 m, nσ = 8): the mixed solve (value) and the FP64 reference
+    algorithm once (fp64_gpu), both with the update-norm test of the configuration (picard_test = 1), and
+    the HBM rooflines of the relinearisation kernel (~285 MB per launch, larger than L2) and of the fused
+    operator on this grid, plus the persistent coarse CG's share."""
+    import torch
+    pkg = __graft_entry__.load_package()
+    from wavi_gb300 import build, synthetic
+    build.build_library()
+    from wavi_gb300.gpu import VelocitySolver
+    from wavi_gb300.model import GPUParallelSpec, Model, pre_solve, release_solver
+    g, bed, p, sp, ic = synthetic.channel_c3(tol_picard=1e-6, maxiter_picard=30)
+    m = Model(g, bed, p, sp, ic, parallel_spec=GPUParallelSpec(precision="fp64"))
+    pre_solve(m)
+    snapshot = {k: np.array(v, copy=True) for k, v in m.fields.items()}
+    release_solver(m)
+    p = m.params
+    mixed = VelocitySolver(g, sp, precision="mixed", picard_test=1, coarse_solver=args.coarse_solver,
+                           cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums,
+                           viscosity=args.viscosity)
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        tmix, stmix, outmix = time_device_solves(torch, mixed, p, snapshot, args.steps, args.warmup)
+    clocks = clk.summary()
+    value = len(tmix) / sum(tmix)
+    fp64 = VelocitySolver(g, sp, precision="fp64", picard_test=1)
+    t64, st64, out64 = time_device_solves(torch, fp64, p, snapshot, 1, 1)
+    err = rel_err_uv(outmix["u"], outmix["v"], out64["u"].reshape((g.nx + 1, g.ny), order="F"),
+                     out64["v"].reshape((g.nx, g.ny + 1), order="F"))
+    peaks = measured_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    src = "measured" if peaks else "fallback"
+    # relinearisation kernels on the solved state (each launch > L2 at nσ = 8)
+    rel = {}
+    for name, s_ in (("mixed", mixed), ("fp64", fp64)):
+        th, tuv = s_.time_relinearise_device(20)
+        bh = relin_h_bytes(g.nx, g.ny, g.nσ, name == "mixed")
+        rel[name] = {"kernel": "k_relin_h<%s>" % ("float" if name == "mixed" else "double"), "bound": "hbm",
+                     "alg_bytes_per_launch": bh, "avg_launch_us": th * 1e6, "achieved": bh / th / 1e9, "peak": peak,
+                     "unit": "GB/s", "frac": bh / th / 1e9 / peak, "peak_source": src,
+                     "uv_kernel": {"kernel": "k_relin_uv", "alg_bytes_per_launch": relin_uv_bytes(g.nx, g.ny),
+                                   "avg_launch_us": tuv * 1e6,
+                                   "achieved": relin_uv_bytes(g.nx, g.ny) / tuv / 1e9}}
+    # the fused FP32 operator on this grid: back to back (its ~38 MB stay in L2), and with L2 flushed
+    # (a 256 MiB write) before each launch
+    N = (g.nx + 1) * g.ny + g.nx * (g.ny + 1)
+    x = torch.randn(N, dtype=torch.float32, device="cuda")
+    y = torch.zeros_like(x)
+    ob = op_bytes(g.nx, g.ny, 4)
+    warm = mixed.time_operator_device(x, y, "mixed", 50)
+    stream = torch.cuda.ExternalStream(mixed.stream())
+    flush = torch.empty((256 << 20) // 4, dtype=torch.float32, device="cuda")
+    cold = []
+    for k in range(20):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        cold.append(mixed.time_operator_device(x, y, "mixed", 1))
+    cold_s = statistics.median(cold)
+    # the persistent coarse CG's share of a host-driven mixed solve
+    prof = VelocitySolver(g, sp, precision="mixed", use_graphs=False, picard_test=1, coarse_solver=args.coarse_solver,
+                          cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums,
+                           viscosity=args.viscosity)
+    names = solve_field_names()
+    dev = {k: torch.from_numpy(np.ascontiguousarray(np.asarray(snapshot[k]).ravel(order="F"))).cuda() for k in names}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    stp = prof.solve_device(p, dev)
+    wall = time.perf_counter() - t0
+    prof.close()
+    mixed.close()
+    fp64.close()
+    last = stmix[-1]
+    line = {
+        "metric": "converged velocity solves/s (2560x320 channel, nsigma=8, mixed precision)", "value": value,
+        "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(tmix) / len(tmix), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": C3_WORKLOAD, "nx": g.nx, "ny": g.ny, "nsigma": g.nσ, "dx_m": g.dx,
+                   "unknowns": int(m.u_inner.sum() + m.v_inner.sum()), "tol_picard": 1e-6, "maxiter_picard": 30,
+                   "picard_test": "||du||/||u|| <= tol and ||b - A u||/||b|| < tol",
+                   "l2": "flushed between steps (256 MiB write)"},
+        "solve": {k: last[k] for k in ("status_name", "picard_iterations", "coarse_cg_iterations", "rel_residual",
+                                       "rel_update", "coarse_solver", "kernel_launches")},
+        "fp64_gpu": {"value": len(t64) / sum(t64), "unit": "solves/s", "ms_per_step": 1e3 * sum(t64) / len(t64),
+                     **{k: st64[-1][k] for k in ("status_name", "picard_iterations", "coarse_cg_iterations",
+                                                  "rel_residual", "rel_update", "coarse_solver")}},
+        "mixed_over_fp64": value / (len(t64) / sum(t64)),
+        "rel_err_mixed_vs_fp64": err,
+        "roofline": rel["mixed"],
+        "roofline_relin_fp64": rel["fp64"],
+        "roofline_stencil": {"kernel": "k_op_stream<float> (fused operator, row streaming, 2560x320)", "bound": "hbm",
+                             "alg_bytes_per_launch": ob, "avg_launch_us_l2_flushed": cold_s * 1e6,
+                             "achieved": ob / cold_s / 1e9, "peak": peak, "unit": "GB/s",
+                             "frac": ob / cold_s / 1e9 / peak, "peak_source": src,
+                             "avg_launch_us_back_to_back": warm * 1e6, "achieved_back_to_back": ob / warm / 1e9,
+                             "note": "back to back the operator's ~38 MB stay in L2 (129 MB)"},
+        "coarse_cg_share": {"coarse_ms": stp["coarse_ms"], "solve_wall_ms": 1e3 * wall,
+                            "coarse_cg_iterations": stp["coarse_cg_iterations"], "coarse_solver": stp["coarse_solver"],
+                            "us_per_cg_iteration": 1e3 * stp["coarse_ms"] / max(1, stp["coarse_cg_iterations"])},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -690,16 +927,23 @@ def main():
     ap.add_argument("--coarse-solver", default="auto",
                     choices=("auto", "cg", "srcg", "srcg_jacobi", "srcg_chebyshev", "pipelined_chebyshev"),
                     help="coarse solver of the mixed-precision solves (the FP64 solve keeps the reference's)")
+    ap.add_argument("--coarse-sums", default="default", choices=("default", "float_float", "fp64"),
+                    help="accumulation of the mixed coarse CG's dot products (wavi_coarse_sums)")
+    ap.add_argument("--viscosity", default="default", choices=("default", "fp32", "fp64"),
+                    help="precision of the mixed solves' viscosity sweeps (wavi_viscosity)")
     ap.add_argument("--cheb-steps", type=int, default=0,
                     help="Chebyshev steps of the Chebyshev coarse solvers (0: the library's default, 3; else odd)")
-    ap.add_argument("--config", default="c2", choices=("c2", "c4", "c5"),
-                    help="c2: the 640x80 solve (default); c4: the adjoint on 640x80; c5: the ragged 256-member ensemble")
+    ap.add_argument("--config", default="c2", choices=("c2", "c3", "c4", "c5"),
+                    help="c2: the 640x80 solve (default); c3: the 2560x320 nsigma=8 solve; c4: the adjoint on 640x80; "
+                         "c5: the ragged 256-member ensemble")
     ap.add_argument("--directions", type=int, default=20, help="--config c4: finite-difference directions")
     ap.add_argument("--members", type=int, default=256, help="--config c5: ensemble members")
     ap.add_argument("--no-tune", action="store_true", help="--config c5: skip the autotuner")
     args = ap.parse_args()
     if args.profile:
         return profile_case(args)
+    if args.config == "c3":
+        return c3_arm(args)
     if args.config == "c4":
         return adjoint_arm(args)
     if args.config == "c5":

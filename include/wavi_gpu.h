@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define WAVI_ABI_VERSION 1
+#define WAVI_ABI_VERSION 2
 
 typedef enum wavi_status {
   WAVI_OK = 0,
@@ -47,8 +47,10 @@ typedef enum wavi_status {
 /* Precision modes of a context. */
 typedef enum wavi_precision {
   WAVI_PRECISION_FP64 = 0,         /* the reference algorithm in float64 throughout (parity mode) */
-  WAVI_PRECISION_MIXED = 1         /* float32 operator, viscosity and V-cycle; float64 Picard residual,
-                                      convergence test, CG scalars / coarse iterate and dot products */
+  WAVI_PRECISION_MIXED = 1         /* float32 operator coefficients and V-cycle (smoother, Haar transforms,
+                                      coarse CG; its sums per wavi_coarse_sums); float64 viscosity sweeps
+                                      (per wavi_viscosity), right-hand side, Picard residual, convergence
+                                      test and coarse-correction cache */
 } wavi_precision;
 
 /* Grid geometry and the masks that fix the problem's sparsity (src/Grid.jl:1-27, :66-201;
@@ -104,7 +106,31 @@ typedef struct wavi_options {
                                         tiles, 2 = row-streaming */
   int32_t cheb_steps;                /* Chebyshev steps per preconditioner application of the Chebyshev
                                         coarse solvers: 0 = the default, 3; else odd, 1..15 */
+  int32_t coarse_sums;               /* wavi_coarse_sums: how a mixed-precision coarse CG accumulates its
+                                        dot products (FP64 contexts always sum in FP64) */
+  int32_t viscosity;                 /* wavi_viscosity: precision of a mixed context's σ-level viscosity
+                                        sweeps (FP64 contexts always sweep in FP64) */
 } wavi_options;
+
+/* Precision of the relinearisation's viscosity sweeps (update_velocities.jl:264-283) in a mixed context.
+ * The operator coefficients of the FP64 Picard residual derive from η: with FP32 sweeps their rounding
+ * changes with every relinearisation, which puts a floor under ||b - A(u) u|| / ||b|| (measured 5e-6 on a
+ * 96 x 32 channel at 2 km, whose velocity nevertheless agrees with the FP64 solve to 1e-7). */
+typedef enum wavi_viscosity {
+  WAVI_VISCOSITY_DEFAULT = 0,        /* WAVI_VISCOSITY_FP64 */
+  WAVI_VISCOSITY_FP32 = 1,           /* FP32 sweeps (η, B, the stress term in float) */
+  WAVI_VISCOSITY_FP64 = 2            /* FP64 sweeps; the V-cycle's coefficients are then rounded to FP32 */
+} wavi_viscosity;
+
+/* Accumulation of the mixed-precision coarse CG's dot products and CG scalars. */
+typedef enum wavi_coarse_sums {
+  WAVI_SUMS_DEFAULT = 0,             /* WAVI_SUMS_FLOAT_FLOAT */
+  WAVI_SUMS_FLOAT_FLOAT = 1,         /* FP32 products, warp and CTA sums; float-float (~48-bit) grid sums
+                                        and CG scalars */
+  WAVI_SUMS_FP64 = 2                 /* every product and sum of the reductions, and the CG scalars, in FP64
+                                        from the FP32 vectors; the single-reduction solvers on the
+                                        register-resident 16 x 16 kernel only */
+} wavi_coarse_sums;
 
 /* Coarse solve of each V-cycle (R A P x = b_c, update_preconditioners.jl:54-83).  The reference calls
  * IterativeSolvers cg!; the single-reduction variants (not in the reference; Chronopoulos & Gear 1989)
@@ -112,8 +138,7 @@ typedef struct wavi_options {
  * unpreconditioned residual, and need the persistent coarse kernel. */
 typedef enum wavi_coarse_solver {
   WAVI_COARSE_AUTO = 0,              /* FP64: cg!; mixed: SRCG_CHEBYSHEV when the ice mask covers the whole
-                                        domain (SRCG_JACOBI where only the global-memory persistent kernel
-                                        fits), else cg! */
+                                        domain, else cg! */
   WAVI_COARSE_CG = 1,                /* the reference's cg! recurrence */
   WAVI_COARSE_SRCG = 2,              /* single-reduction CG, no preconditioner (same iterates as cg!) */
   WAVI_COARSE_SRCG_JACOBI = 3,       /* single-reduction CG preconditioned by diag(R A P) */
@@ -121,7 +146,8 @@ typedef enum wavi_coarse_solver {
                                         Chebyshev-accelerated Jacobi steps on [b/120, b],
                                         b = 1.15 lambda_max(diag(R A P)^-1 R A P) from power steps each
                                         V-cycle (12 in a solve's first, then 4, warm-started);
-                                        register-resident persistent kernel only */
+                                        persistent kernel (register-resident, or global-memory vectors
+                                        on grids too large for that) */
   WAVI_COARSE_PIPELINED_CHEBYSHEV = 5 /* opt-in, never chosen by AUTO: pipelined CG (Ghysels & Vanroose
                                         2014) with the preconditioner of SRCG_CHEBYSHEV, whose grid
                                         reduction overlaps the iteration's preconditioner and operator;
@@ -245,6 +271,14 @@ int wavi_apply_operator_device(wavi_ctx* ctx, int precision, const void* in_uv, 
 int wavi_time_operator_device(wavi_ctx* ctx, int precision, const void* in_uv, void* out_uv, int repeats,
                               double* avg_ms);
 
+/* Benchmark hook: `repeats` back-to-back launches of the relinearisation's h-grid kernel (the strain rate,
+ * speeds, Weertman β and τ_b, the σ-level viscosity sweeps and quadratures of update_velocities.jl:202-339,
+ * :374-383), then as many of its u/v-grid kernel (:348-366, :378), on the fields of the context's last
+ * solve or relinearisation (the launches keep iterating the viscosity in place), timed with CUDA events on
+ * the context's stream; *avg_ms_h and *avg_ms_uv receive the mean duration of one launch of each.  No
+ * counterpart in the reference. */
+int wavi_time_relinearise_device(wavi_ctx* ctx, int repeats, double* avg_ms_h, double* avg_ms_uv);
+
 /* Diagonal of the operator at the interior points (what get_op_diag probes, update_preconditioners.jl
  * :92-109), same vector layout and precision rules as wavi_apply_operator_device.  Test hook. */
 int wavi_op_diagonal_device(wavi_ctx* ctx, int precision, void* diag_uv);
@@ -261,6 +295,12 @@ int wavi_coarse_diagonal_device(wavi_ctx* ctx, int precision, void* diag_uv);
  * (restriction, default mask = the last uploaded wavelet mask), kind 2 = dwt(mask ⊙ in) (the forward
  * transform of update_wavelets!, default mask = the u/v model masks).  mask_uv may be null.  Test hook. */
 int wavi_haar_device(wavi_ctx* ctx, int kind, const double* in_uv, double* out_uv, const uint8_t* mask_uv);
+
+/* update_wavelets! (Wavelets/update_wavelets.jl:6-32) with the kernels of wavi_run_device's time step:
+ * the context's wavelet mask becomes |dwt(mask ⊙ in_uv)| >= wavelet_threshold (mask = the u/v model
+ * masks), its coarse-correction cache is cleared, and the new mask ([u | v] layout, one byte per point)
+ * is copied to the device buffer wmask_out.  in_uv: float64 device vector [u | v].  Test hook. */
+int wavi_update_wavelets_device(wavi_ctx* ctx, const double* in_uv, uint8_t* wmask_out);
 
 /* ---------------------------------------------------------------------------------------------------
  * Allocation-free entry point.  No counterpart in the reference: it exists for callers of this library

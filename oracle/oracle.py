@@ -59,6 +59,8 @@ def lib():
         L.oracle_stats.argtypes = [vp, C.POINTER(C.c_int), dp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.oracle_cg_history.restype = C.c_int
         L.oracle_cg_history.argtypes = [vp, C.POINTER(C.c_int), C.c_int]
+        L.oracle_picard_history.restype = C.c_int
+        L.oracle_picard_history.argtypes = [vp, dp, dp, C.c_int]
         L.oracle_pos_fraction.argtypes = [C.c_int, C.c_int, dp, u8p, dp, dp, dp]
         L.oracle_kron_apply.argtypes = [C.c_int, C.c_int, dp, C.c_int, C.c_int, dp, dp, dp]
         L.oracle_set_coarse_variant.argtypes = [C.c_int]
@@ -163,10 +165,14 @@ class OracleModel:
     def stats(self):
         p, r, cg, ops = C.c_int(), C.c_double(), C.c_int64(), C.c_int64()
         lib().oracle_stats(self.h, C.byref(p), C.byref(r), C.byref(cg), C.byref(ops))
-        hist = (C.c_int * 64)()
-        n = lib().oracle_cg_history(self.h, hist, 64)
+        cap = 4096
+        hist = (C.c_int * cap)()
+        n = lib().oracle_cg_history(self.h, hist, cap)
+        rel, upd = (C.c_double * cap)(), (C.c_double * cap)()
+        npic = lib().oracle_picard_history(self.h, rel, upd, cap)
         return {"picard_iterations": p.value, "rel_residual": r.value, "coarse_cg_iterations": cg.value,
-                "op_applications": ops.value, "cg_history": list(hist[:min(n, 64)])}
+                "op_applications": ops.value, "cg_history": list(hist[:min(n, cap)]),
+                "rel_history": list(rel[:min(npic, cap)]), "update_history": list(upd[:min(npic, cap)])}
 
     def apply_operator(self, u, v):
         u = np.asfortranarray(u, dtype=np.float64)

@@ -301,6 +301,7 @@ struct Model {
   long last_cg_iters = 0;
   long op_applies = 0;
   std::vector<int> cg_iter_history;
+  std::vector<double> rel_history, upd_history;  // per Picard iteration: ||b - A u|| / ||b||, ||du|| / ||u||
   Vec cheb_eig;           // coarse variants 4, 5: the power vector (full wavelet layout, u then v), per solve
   Vec last_coarse_b;      // the last V-cycle's coarse right-hand side and starting point (the cached
   Vec last_coarse_x0;     // correction), in the coarse order [u | v], for studies of the coarse solvers
@@ -1163,6 +1164,8 @@ bool precondition_model(Model& m, OpWork& w, double& rel) {
     for (size_t k = 0; k < p.wv_idx.size(); ++k) m.wv_corr[p.wv_idx[k]] = p.corr[p.wu_idx.size() + k];
   }
   for (int i = 0; i < ni; ++i) x[i] = x[i] + corr[i];
+  m.rel_history.push_back(rel);
+  m.upd_history.push_back(converged ? 0.0 : norm2(corr) / norm2(x));
   for (int k = 0; k < m.ni_u; ++k) m.u[m.u_inner_idx[k]] = x[k];  // set_velocities! :190-195
   for (int k = 0; k < m.ni_v; ++k) m.v[m.v_inner_idx[k]] = x[m.ni_u + k];
   return converged;
@@ -1176,6 +1179,8 @@ void update_velocities(Model& m) {
   double rel = INFINITY;
   m.last_cg_iters = 0;
   m.cg_iter_history.clear();
+  m.rel_history.clear();
+  m.upd_history.clear();
   m.cheb_eig.assign((size_t)(m.Nu + m.Nv), 0.0);
   m.cheb_vcycles = 0;
   while (!converged && it < m.S.maxiter_picard) {
@@ -1533,6 +1538,16 @@ int oracle_cg_history(void* h, int* out, int cap) {
   Model& m = *static_cast<Model*>(h);
   int n = (int)m.cg_iter_history.size();
   for (int i = 0; i < n && i < cap; ++i) out[i] = m.cg_iter_history[i];
+  return n;
+}
+// the last solve's per-Picard-iteration relative residual (before the correction) and relative update
+int oracle_picard_history(void* h, double* rel, double* upd, int cap) {
+  Model& m = *static_cast<Model*>(h);
+  int n = (int)m.rel_history.size();
+  for (int i = 0; i < n && i < cap; ++i) {
+    if (rel) rel[i] = m.rel_history[i];
+    if (upd) upd[i] = m.upd_history[i];
+  }
   return n;
 }
 // pos_fraction on an arbitrary m x n array (KAT hook, utilities.jl:255-396)

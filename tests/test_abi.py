@@ -134,6 +134,7 @@ def test_every_entry_point_rejects_a_null_context(lib, pkg):
         "wavi_relinearise_device": (None, None, None),
         "wavi_apply_operator_device": (None, 0, None, None),
         "wavi_time_operator_device": (None, 0, None, None, 1, None),
+        "wavi_time_relinearise_device": (None, 1, None, None),
         "wavi_op_diagonal_device": (None, 0, None),
         "wavi_selftest_watchdog": (None, None),
         "wavi_coarse_diagonal_device": (None, 0, None),
@@ -141,6 +142,7 @@ def test_every_entry_point_rejects_a_null_context(lib, pkg):
         "wavi_tangent_device": (None, None, None, None, None, None, 1e-10, 10, None),
         "wavi_run_device": (None, None, 1.0, 1, None, None, None, None),
         "wavi_haar_device": (None, 0, None, None, None),
+        "wavi_update_wavelets_device": (None, None, None),
         "wavi_ensemble_solve_device": (None, None, None, None),
     }
     for name, args in calls.items():

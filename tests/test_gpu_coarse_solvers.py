@@ -65,7 +65,8 @@ def test_coarse_diagonal_matches_oracle(oracle, name):
 
 
 KERNEL_SOLVERS = [("persistent", "srcg"), ("persistent", "srcg_jacobi"), ("persistent", "srcg_chebyshev"),
-                  ("persistent_global", "srcg"), ("persistent_global", "srcg_jacobi")]
+                  ("persistent_global", "srcg"), ("persistent_global", "srcg_jacobi"),
+                  ("persistent_global", "srcg_chebyshev")]
 
 
 @pytest.mark.parametrize("kernel,solver", KERNEL_SOLVERS)
@@ -117,12 +118,23 @@ def test_single_reduction_converged_solve_matches_reference(oracle, name, solver
         s.close()
 
 
-def test_chebyshev_needs_the_register_resident_kernel(oracle):
-    from wavi_gb300.abi import WaviError
+def test_chebyshev_on_the_global_memory_kernel_matches_the_register_kernel(oracle):
+    """The Chebyshev coarse solve with its vectors in global memory (k_srcg_cheb_global, the kernel of grids
+    too large for the register-resident one) and in registers (k_srcg_persistent): one Picard iteration
+    with a fixed count of 10 coarse iterations in FP64, the same iterates to rounding."""
     from wavi_gb300.gpu import VelocitySolver
-    g, p, sp, om = _setup(oracle, "full")
-    with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):
-        VelocitySolver(g, sp, precision="mixed", coarse_kernel="persistent_global", coarse_solver="srcg_chebyshev")
+    g, p, sp, om = _setup(oracle, "full", maxiter_picard=1, maxiter_coarse=10, tol_coarse=0.0)
+    f0 = fields_from_oracle(om, g)
+    out = {}
+    for kernel in ("persistent", "persistent_global"):
+        f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
+        s = VelocitySolver(g, sp, precision="fp64", coarse_kernel=kernel, coarse_solver="srcg_chebyshev")
+        st = s.solve(p, f)
+        s.close()
+        assert st["coarse_cg_iterations"] == 10 and st["coarse_solver"] == "srcg_chebyshev", st
+        out[kernel] = np.concatenate([f["u"].ravel(), f["v"].ravel()])
+    a, b = out["persistent"], out["persistent_global"]
+    assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(a)
 
 
 def test_mixed_default_is_chebyshev_on_full_masks(oracle):
@@ -166,3 +178,38 @@ def test_chebyshev_step_count_option(oracle):
         st = s.solve(p, f)
         s.close()
         assert st["status"] == 0 and uv_err(f, om) < 1e-6, (steps, st)
+
+
+@pytest.mark.parametrize("solver", ["srcg_jacobi", "srcg_chebyshev"])
+@pytest.mark.parametrize("name", ["full", "ragged"])
+def test_fp64_coarse_sums_converge_to_the_reference(oracle, name, solver):
+    """WAVI_SUMS_FP64: the mixed coarse CG with every dot-product term, sum and CG scalar in FP64 (the FP32
+    vectors unchanged) reaches the reference's fixed point to 1e-6, as the float-float default does."""
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, name, maxiter_picard=80, tol_picard=1e-7)
+    f0 = fields_from_oracle(om, g)
+    om.update_velocities()
+    for sums in ("float_float", "fp64"):
+        f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
+        s = VelocitySolver(g, sp, precision="mixed", coarse_solver=solver, coarse_sums=sums)
+        st = s.solve(p, f)
+        s.close()
+        print(name, solver, sums, st["picard_iterations"], st["coarse_cg_iterations"], uv_err(f, om))
+        assert st["status"] == 0, (sums, st)
+        assert uv_err(f, om) < 1e-6, (sums, st)
+
+
+def test_fp64_coarse_sums_need_the_single_reduction_register_kernel(oracle):
+    from wavi_gb300.abi import WaviError
+    from wavi_gb300.config import SolverParams
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, "full")
+    for kw in (dict(coarse_solver="cg"), dict(coarse_solver="pipelined_chebyshev"),
+               dict(coarse_solver="srcg_jacobi", coarse_kernel="persistent_global"),
+               dict(coarse_solver="srcg_jacobi", coarse_kernel="iterations")):
+        with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):
+            VelocitySolver(g, sp, precision="mixed", coarse_sums="fp64", **kw)
+    with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):  # 32 x 32 tiles
+        VelocitySolver(g, SolverParams(levels=4), precision="mixed", coarse_sums="fp64", coarse_solver="srcg_jacobi")
+    s = VelocitySolver(g, sp, precision="fp64", coarse_sums="fp64")  # FP64 contexts sum in FP64 anyway
+    s.close()

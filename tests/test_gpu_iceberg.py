@@ -1,18 +1,12 @@
 """The reference's iceberg verification (test/verification_tests/iceberg_test.jl) through the device-resident
 time stepping (wavi_run_device): a masked, floating domain with Dirichlet centre lines, 10 000 steps of
 dt = 0.1 with one Picard iteration each, against the closed-form steady state at the reference's
-tolerances.  The device-run tests so far cover full rectangles only, so this
-one has not yet run on a GPU: skipped unless WAVI_RUN_ICEBERG=1 (the oracle meets the same tolerances in
-tests/test_oracle.py)."""
-import os
-
+tolerances (the oracle meets the same tolerances in tests/test_oracle.py).  Unlike the channel and MISMIP+
+runs, this domain is masked and floating, with calving fronts and Dirichlet lines."""
 import numpy as np
 import pytest
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(not os.environ.get("WAVI_RUN_ICEBERG"),
-                                 reason="device time stepping on a masked domain not yet run on a GPU "
-                                        "(WAVI_RUN_ICEBERG=1)")]
+pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
 

@@ -159,8 +159,10 @@ def test_one_picard_iteration_matches_oracle(oracle, name):
                                   (True, "persistent_global")])
 @pytest.mark.parametrize("name", list(CASES))
 def test_converged_solve_matches_oracle(oracle, name, mode):
+    """Picard-converged FP64 solves (tol_picard = 1e-7: every case converges, in 40-51 iterations) through
+    each coarse-kernel mode: the same Picard count as the oracle and the same velocities to 1e-9."""
     from wavi_gb300.gpu import VelocitySolver
-    g, p, sp, om = _setup(oracle, name, maxiter_picard=30, tol_picard=1e-6)
+    g, p, sp, om = _setup(oracle, name, maxiter_picard=80, tol_picard=1e-7)
     f = fields_from_oracle(om, g)
     graphs, coarse = mode
     s = VelocitySolver(g, sp, precision="fp64", use_graphs=graphs, coarse_kernel=coarse)
@@ -219,3 +221,29 @@ def test_persistent_smoother_matches_per_step_smoother(oracle):
     assert s1["picard_iterations"] == s2["picard_iterations"]
     assert abs(s1["coarse_cg_iterations"] - s2["coarse_cg_iterations"]) <= 0.02 * s2["coarse_cg_iterations"]
     assert np.linalg.norm(x1 - x2) <= 1e-4 * np.linalg.norm(x2), np.linalg.norm(x1 - x2) / np.linalg.norm(x2)
+
+
+def test_mixed_viscosity_precision_and_the_residual_floor(oracle):
+    """A mixed solve's FP64 Picard residual uses operator coefficients derived from η.  With FP32 viscosity
+    sweeps (WAVI_VISCOSITY_FP32) their rounding changes at every relinearisation and the residual levels off
+    (on this 96 x 32 channel at 2 km, measured at 5e-6, with the velocity within 1e-7 of the oracle's);
+    with the default FP64 sweeps the mixed solve converges to the reference's tolerance like the FP64 one."""
+    from wavi_gb300 import synthetic
+    from wavi_gb300.gpu import VelocitySolver
+    g, bed, p, sp, ic = synthetic.small_case(nx=96, ny=32, dx=2000.0, mask="full", maxiter_picard=100, tol_picard=1e-6)
+    om = oracle.build_model(g, bed, p, sp, ic)
+    om.pre_solve()
+    f0 = fields_from_oracle(om, g)
+    om.update_velocities()
+    res = {}
+    for visc in ("default", "fp32"):
+        f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
+        s = VelocitySolver(g, sp, precision="mixed", viscosity=visc)
+        st = s.solve(p, f)
+        s.close()
+        res[visc] = (st, uv_err(f, om))
+        print(visc, st["status_name"], st["picard_iterations"], st["rel_residual"], res[visc][1])
+    st, err = res["default"]
+    assert st["status"] == 0, st
+    assert err < 1e-6
+    assert res["fp32"][1] < 1e-6  # the velocity is accurate either way

@@ -163,3 +163,36 @@ def test_mismip_plus_ice0_grounding_line(oracle, pkg):
     assert (t[3] - t[0]) / (t[3] + t[0]) < 1e-4 and (t[1] - t[2]) / (t[1] + t[2]) < 1e-4
     assert 480000 < t[0] < 550000 and 480000 < t[3] < 550000
     assert 430000 < t[1] < 490000 and 430000 < t[2] < 490000
+
+
+def test_c2_fixture_is_a_converged_solve_of_the_benchmark_state(oracle, pkg):
+    """tests/golden/c2_oracle_solution.npz (the oracle's converged 640 x 80 solve, which the GPU parity tests
+    at the benchmark's configuration compare against): made from the benchmark's own state (input
+    fingerprints), and its velocities meet the reference's stopping rule ||b - A(u) u|| / ||b|| < tol_picard
+    (update_velocities.jl:59-65) when the oracle relinearises at them (inner_update!, :32-45, repeated
+    until the viscosity has settled)."""
+    import sys
+    sys.path.insert(0, os.path.dirname(HERE))
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import bench
+    from make_c2_solution import fingerprints
+    from wavi_gb300 import synthetic
+    ref = np.load(os.path.join(HERE, "golden", "c2_oracle_solution.npz"))
+    m = bench.build_state(pkg)
+    assert np.allclose(fingerprints(m.fields), ref["fingerprints"], rtol=1e-12, atol=0.0)
+    g, bed, p, sp, ic = synthetic.channel_c2(tol_picard=bench.TOL_PICARD, maxiter_picard=bench.MAXITER_PICARD)
+    om = oracle.build_model(g, bed, p, sp, ic)
+    om.pre_solve()
+    for k in ("u", "v"):
+        om.field(k)[...] = ref[k]
+    # viscosity, drag and F2 iterate from their previous values (update_velocities.jl:227-283): repeated
+    # relinearisations at the fixed velocities bring them to their fixed point for those velocities
+    for _ in range(40):
+        om.inner_update()
+    bu, bv = om.rhs()
+    iu, iv = om.mask("u_inner").astype(bool), om.mask("v_inner").astype(bool)
+    au, av = om.apply_operator(ref["u"] * iu, ref["v"] * iv)
+    r = np.concatenate([(bu - au)[iu], (bv - av)[iv]])
+    rel = np.linalg.norm(r) / np.linalg.norm(np.concatenate([bu[iu], bv[iv]]))
+    assert rel < float(ref["tol_picard"]), rel
+    assert int(ref["picard_iterations"]) == 40

@@ -354,3 +354,23 @@ def test_schwarz_spec_is_a_parallel_spec(pkg, monkeypatch):
     assert all(s.parallel_spec is spec.subdomain_spec for s in subs.values())
     with pytest.raises(TypeError):
         update_velocities(Model(g, bed, p, sp, ic, parallel_spec=object()))
+
+
+def test_member_staging_keeps_an_empty_coarse_space_addressable(pkg):
+    """A subdomain whose wavelet mask is empty has zero-length compact corrections; they are staged with one
+    unused entry (a zero-length tensor has no device address, which the library rejects) and come back with
+    count(mask) entries."""
+    torch = pytest.importorskip("torch")
+    from wavi_gb300 import schwarz
+    from wavi_gb300.gpu import ALL_FIELDS
+    fields = {k: np.zeros((3, 2)) for k in ALL_FIELDS}
+    fields["wu_mask"] = np.zeros((3, 2), np.uint8)
+    fields["wv_mask"] = np.array([[1, 0], [0, 1], [0, 0]], np.uint8)
+    fields["wu_correction_coarse"] = np.zeros(0)
+    fields["wv_correction_coarse"] = np.array([2.0, 3.0])
+    t = schwarz._member_tensors(fields, "cpu")
+    assert t["wu_correction_coarse"].numel() == 1 and t["wv_correction_coarse"].numel() == 2
+    t["wv_correction_coarse"] += 1.0
+    schwarz._member_fields_back(fields, t)
+    assert fields["wu_correction_coarse"].shape == (0,)
+    assert np.array_equal(fields["wv_correction_coarse"], [3.0, 4.0])

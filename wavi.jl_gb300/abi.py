@@ -10,7 +10,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libwavi_gpu.so")
 
-WAVI_ABI_VERSION = 1
+WAVI_ABI_VERSION = 2
 
 STATUS = {
     0: "WAVI_OK", -1: "WAVI_ERR_ARGUMENT", -2: "WAVI_ERR_CUDA", -3: "WAVI_ERR_NONFINITE",
@@ -24,6 +24,8 @@ PRECISION_MIXED = 1
 
 COARSE_SOLVERS = {"auto": 0, "cg": 1, "srcg": 2, "srcg_jacobi": 3, "srcg_chebyshev": 4, "pipelined_chebyshev": 5}  # wavi_coarse_solver
 COARSE_SOLVER_NAMES = {v: k for k, v in COARSE_SOLVERS.items()}
+COARSE_SUMS = {"default": 0, "float_float": 1, "fp64": 2}  # wavi_coarse_sums
+VISCOSITY = {"default": 0, "fp32": 1, "fp64": 2}  # wavi_viscosity
 
 _dp = C.POINTER(C.c_double)
 _u8p = C.POINTER(C.c_uint8)
@@ -56,7 +58,8 @@ class SolverParams(C.Structure):
 class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graphs", C.c_int32),
                 ("picard_test", C.c_int32), ("coarse_kernel", C.c_int32), ("coarse_solver", C.c_int32),
-                ("stencil_kernel", C.c_int32), ("cheb_steps", C.c_int32)]
+                ("stencil_kernel", C.c_int32), ("cheb_steps", C.c_int32), ("coarse_sums", C.c_int32),
+                ("viscosity", C.c_int32)]
 
 
 FIELD_INPUTS = ("h", "s", "dsdh", "grounded_fraction", "weertman_c", "accumulation", "basal_melt",
@@ -143,7 +146,9 @@ def load_library(path=None):
         "wavi_op_diagonal_device": (C.c_int, [vp, C.c_int, vp]),
         "wavi_coarse_diagonal_device": (C.c_int, [vp, C.c_int, vp]),
         "wavi_time_operator_device": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, C.POINTER(C.c_double)]),
+        "wavi_time_relinearise_device": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "wavi_haar_device": (C.c_int, [vp, C.c_int, vp, vp, vp]),
+        "wavi_update_wavelets_device": (C.c_int, [vp, vp, vp]),
         "wavi_residual_noalloc": (C.c_int, [C.POINTER(OperatorDesc), vp, vp, vp, vp, vp]),
         "wavi_selftest_watchdog": (C.c_int, [vp, C.POINTER(C.c_int)]),
         "wavi_adjoint_device": (C.c_int, [vp, C.POINTER(Params), vp, vp, vp, vp, C.c_double, C.c_int,

@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(TX* TY)
       st->picard_it = it;
       bool conv = rel < P->tol_picard;
       if (conv && P->picard_test == 1 && it > 1 && !(st->rel_update <= P->tol_picard)) conv = false;
-      if (!(rel == rel)) {
+      if (!isfinite(rel)) {
         st->status = WAVI_ERR_NONFINITE;
         conv = true;  // stop: nothing sensible can follow a non-finite residual
       }

@@ -958,9 +958,9 @@ __device__ __forceinline__ float cheb_start(int q) {
 // CG scalars broadcast to the CTA (written by thread 0 inside grid_sync).  R = CGReal<T>: the FP64
 // kernels keep the reference's FP64 scalars; the FP32 kernels keep squared norms and the recurrence
 // scalars in float-float (no FP64 arithmetic per iteration; res and tol are FP64, set once per solve).
-template <typename T>
+template <typename T, typename RR = typename CGReal<T>::type>
 struct CGScalars {
-  using R = typename CGReal<T>::type;
+  using R = RR;      // the type of the sums and scalars: double, or float-float (FP32 kernels' default)
   double res, tol;   // |r| and the stopping tolerance
   double alpha_prev; // cg!'s "prev" (FP64 kernels)
   R rr, tol2;        // |r|^2 and tol^2
@@ -976,6 +976,13 @@ __device__ __forceinline__ T fmul_add(T a, T b, T c) {
 template <>
 __device__ __forceinline__ float fmul_add<float>(float a, float b, float c) {
   return fmaf(a, b, c);
+}
+
+// a b + c d in the accumulation type A of a reduction (the FP32 kernels' default A = float: the same
+// expression as written in float; A = double: every product and the sum in FP64)
+template <typename A, typename T>
+__device__ __forceinline__ A dot2(T a, T b, T c, T d) {
+  return (A)a * (A)b + (A)c * (A)d;
 }
 
 __device__ __forceinline__ float to_vec(ff v) { return v.hi; }
@@ -1027,12 +1034,12 @@ __device__ __forceinline__ void cg_next(CGScalars<T>& sc, const typename CGReal<
   sc.beta_t = (T)to_vec(sc.beta);
 }
 // Single-reduction CG scalars from γ = (r, z), δ = (w, z), |r|^2 (and |b_c|^2 in the first pass):
-// β = γ/γ',  α = γ / (δ - β γ / α')  (the oracle's coarse_srcg in FP64, the same order).
-template <typename T>
-__device__ __forceinline__ void srcg_scalars(CGScalars<T>& sc, const typename CGReal<T>::type* tot, bool first, int it,
-                                             int maxit, double tol_coarse) {
-  using R = typename CGReal<T>::type;
-  constexpr bool f32 = std::is_same<T, float>::value;
+// β = γ/γ',  α = γ / (δ - β γ / α')  (the oracle's coarse_srcg in FP64, the same order).  With float-float
+// sums (R = ff) the stopping test compares squared norms; with FP64 sums it is the FP64 kernels' test.
+template <typename T, typename R = typename CGReal<T>::type>
+__device__ __forceinline__ void srcg_scalars(CGScalars<T, R>& sc, const R* tot, bool first, int it, int maxit,
+                                             double tol_coarse) {
+  constexpr bool f32 = std::is_same<R, ff>::value;
   const R gamma = tot[0], delta = tot[1];
   sc.rr = tot[2];
   if (!f32 || first) sc.res = sqrt(dbl_of(tot[2]));
@@ -1112,9 +1119,9 @@ __device__ __forceinline__ void pcg_scalars(PcgScalars<T>& sc, const typename CG
   sc.stop = stop;
 }
 // |r| of the final iterate for the statistics
-template <typename T>
-__device__ __forceinline__ double cg_final_res(const CGScalars<T>& sc) {
-  if constexpr (std::is_same<T, float>::value)
+template <typename T, typename R>
+__device__ __forceinline__ double cg_final_res(const CGScalars<T, R>& sc) {
+  if constexpr (std::is_same<R, ff>::value)
     return sqrt(dbl_of(sc.rr));
   else
     return sc.res;
@@ -1279,15 +1286,19 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
 // iteration in FP64.  cheb > 1 replaces M⁻¹ by the Chebyshev-accelerated Jacobi iteration (precond
 // below): cheb - 1 more operator applications per iteration and ~0.4 of the iterations (and grid
 // reductions) for cheb = 3 on the channel workloads.
-template <typename T, int TILE, int MAXT>
+template <typename T, int TILE, int MAXT, bool ACC64 = false>
 __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
     k_srcg_persistent(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, const T* __restrict__ dcoarse,
                       T* __restrict__ w, const T* __restrict__ bc, T* __restrict__ xc, double* __restrict__ partials,
                       DevState* st, const DevParams* __restrict__ P, GridBar* bar, unsigned long long* __restrict__ halo,
                       int cheb, float cheb_ratio, T* __restrict__ eig, int ntx, int nty) {
+  // Acc: the type of the per-thread dot-product terms (T, or FP64 with ACC64: every product and sum of the
+  // reductions in FP64, from the FP32 vectors); S: that of the grid sums and CG scalars
+  using Acc = typename std::conditional<ACC64, double, T>::type;
+  using S = typename CGReal<Acc>::type;
   __shared__ CGShared<T, TILE> sm;
   __shared__ SyncShared ss;
-  __shared__ CGScalars<T> sc;
+  __shared__ CGScalars<T, S> sc;
   __shared__ FastSharedFor<T, TILE, MAXT> fs;
   PointCoef<T> pc[MAXT] = {};
   const int ntiles = ntx * nty;
@@ -1419,7 +1430,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
       for (int k = 0; k < MAXT; ++k)
         if (own[k]) prolong(k, eu[k], ev[k]);
       if (!halo_ready()) return;
-      T a2[4] = {T(0), T(0), T(0), T(0)};
+      Acc a2[4] = {Acc(0), Acc(0), Acc(0), Acc(0)};
 #pragma unroll
       for (int k = 0; k < MAXT; ++k)
         if (own[k]) {
@@ -1427,12 +1438,12 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
           if (!apply(k, tu, tv)) return;
           tu = iu[k] * tu;
           tv = iv[k] * tv;
-          a2[0] += tu * tu + tv * tv;
-          a2[1] += eu[k] * eu[k] + ev[k] * ev[k];
+          a2[0] += dot2<Acc>(tu, tu, tv, tv);
+          a2[1] += dot2<Acc>(eu[k], eu[k], ev[k], ev[k]);
           eu[k] = tu;
           ev[k] = tv;
         }
-      if (!grid_sync<2>(bar, partials, epoch, ss, a2, [&](const typename CGReal<T>::type* tot) {
+      if (!grid_sync<2>(bar, partials, epoch, ss, a2, [&](const S* tot) {
             const double tt = dbl_of(tot[0]), vv = dbl_of(tot[1]);
             const double lam = (vv > 0.0 && tt > 0.0) ? sqrt(tt / vv) : 1.0;
             const double bmax = 1.15 * lam, amin = bmax / (double)cheb_ratio;
@@ -1463,7 +1474,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
   for (int k = 0; k < MAXT; ++k)
     if (own[k]) prolong(k, xu[k], xv[k]);
   if (!halo_ready()) return;
-  T bb = 0;
+  Acc bb = 0;
 #pragma unroll
   for (int k = 0; k < MAXT; ++k)
     if (own[k]) {
@@ -1474,7 +1485,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
       const T bv = (i < d.nx && j <= d.ny) ? bc[vidx(d, i, j)] : (T)0;
       ru[k] = bu - cu;
       rv[k] = bv - cv;
-      bb += bu * bu + bv * bv;
+      bb += dot2<Acc>(bu, bu, bv, bv);
     }
   if (!precond()) return;
   // (every CTA has read the prolonged vector, from w or from the halo boxes: the barrier below orders the
@@ -1501,16 +1512,16 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) prolong(k, zu[k], zv[k]);
     if (!halo_ready()) return;
-    T a[4] = {T(0), T(0), T(0), first ? bb : T(0)};
+    Acc a[4] = {Acc(0), Acc(0), Acc(0), first ? bb : Acc(0)};
 #pragma unroll
     for (int k = 0; k < MAXT; ++k)
       if (own[k]) {
         if (!apply(k, wu[k], wv[k])) return;
-        a[0] += ru[k] * zu[k] + rv[k] * zv[k];
-        a[1] += wu[k] * zu[k] + wv[k] * zv[k];
-        a[2] += ru[k] * ru[k] + rv[k] * rv[k];
+        a[0] += dot2<Acc>(ru[k], zu[k], rv[k], zv[k]);
+        a[1] += dot2<Acc>(wu[k], zu[k], wv[k], zv[k]);
+        a[2] += dot2<Acc>(ru[k], ru[k], rv[k], rv[k]);
       }
-    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const typename CGReal<T>::type* tot) { srcg_scalars<T>(sc, tot, first, it, maxit, tol_coarse); }))
+    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const S* tot) { srcg_scalars(sc, tot, first, it, maxit, tol_coarse); }))
       return;
     if (sc.stop) break;
     const T beta = sc.beta_t;
@@ -1927,9 +1938,236 @@ __global__ void __launch_bounds__(TILE* TILE)
         g.gw[q] = wv;
       }
     }
-    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const typename CGReal<T>::type* tot) { srcg_scalars<T>(sc, tot, first, it, maxit, tol_coarse); }))
+    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const typename CGReal<T>::type* tot) { srcg_scalars(sc, tot, first, it, maxit, tol_coarse); }))
       return;
     if (sc.stop) break;
+    first = false;
+  }
+  if (blockIdx.x == 0 && tx == 0 && ty == 0) {
+    st->cg_it = it;
+    st->cg_total += it;
+    st->cg_res = cg_final_res(sc);
+    st->cg_tol = sc.tol;
+  }
+}
+
+// The single-reduction CG with the Chebyshev-accelerated Jacobi preconditioner (k_srcg_persistent with
+// cheb > 1) for grids whose tiles outnumber the resident CTAs: the vectors in global memory, each CTA
+// looping over tiles.  The same arithmetic per point as the register-resident kernel: λmax by npow power
+// steps from the previous V-cycle's vector (eig), then per iteration cheb - 1 Chebyshev steps and one
+// operator application with its two inner products and |r|² in one grid reduction.  Each Chebyshev step
+// applies the operator to the prolonged vector of the previous one and prolongs its own result in the
+// same tile pass, into the other of two prolongation buffers (w, w2), so that a step needs one grid barrier:
+// a buffer is rewritten only after the barrier that follows the pass in which every CTA read it.
+// gcd holds the Chebyshev direction.
+template <typename T, int TILE>
+__global__ void __launch_bounds__(TILE* TILE)
+    k_srcg_cheb_global(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask,
+                       const T* __restrict__ dcoarse, T* __restrict__ w, T* __restrict__ w2, const T* __restrict__ bc,
+                       T* __restrict__ xc, GlobalCG<T> g, T* __restrict__ gcd, T* __restrict__ eig, int cheb,
+                       float cheb_ratio, double* __restrict__ partials, DevState* st, const DevParams* __restrict__ P,
+                       GridBar* bar, int ntx, int nty) {
+  __shared__ CGShared<T, TILE> sm;
+  __shared__ SyncShared ss;
+  __shared__ CGScalars<T> sc;
+  __shared__ T cheb_s[3];  // θ, δ, σ of the Chebyshev interval
+  using S = typename CGReal<T>::type;
+  const int ntiles = ntx * nty;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  unsigned epoch = 0;
+  int it = 0;
+  const int maxit = P->maxiter_coarse;
+  const double tol_coarse = P->tol_coarse;
+  T* const wbuf[2] = {w, w2};
+  int wsel = 0;
+  auto minv = [&](int q) -> T {
+    const T dq = dcoarse[q];
+    return dq != (T)0 ? (T)1 / dq : (T)0;
+  };
+  // λmax of D⁻¹ R A P: power steps from eig (plus a small fixed perturbation), normalised by the grid sum
+  {
+    T scale = (T)1;
+    const int npow = st->picard_it <= 1 ? 12 : 4;
+    for (int pstep = 0; pstep < npow; ++pstep) {
+      auto e_of = [&](int q) -> T {
+        if (pstep > 0) return eig[q] * scale;
+        return minv(q) != (T)0 ? eig[q] + (T)1e-3 * cheb_start(q) : (T)0;
+      };
+      T* wo = wbuf[wsel];
+      wsel ^= 1;
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+        const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+        prolong_store<T, TILE>(d, levels, cf.inner, inu ? e_of(uidx(d, i, j)) : (T)0, inv ? e_of(vidx(d, i, j)) : (T)0,
+                               i0, j0, sm, wo);
+      }
+      if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+      T a2[4] = {T(0), T(0), T(0), T(0)};
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+        T tu, tv;
+        coarse_apply<T, TILE>(d, levels, cf, wmask, wo, i0, j0, sm, tu, tv);
+        if (i <= d.nx && j < d.ny) {
+          const int q = uidx(d, i, j);
+          const T e = e_of(q), tq = minv(q) * tu;
+          a2[0] += tq * tq;
+          a2[1] += e * e;
+          eig[q] = tq;
+        }
+        if (i < d.nx && j <= d.ny) {
+          const int q = vidx(d, i, j);
+          const T e = e_of(q), tq = minv(q) * tv;
+          a2[0] += tq * tq;
+          a2[1] += e * e;
+          eig[q] = tq;
+        }
+      }
+      if (!grid_sync<2>(bar, partials, epoch, ss, a2, [&](const S* tot) {
+            const double tt = dbl_of(tot[0]), vv = dbl_of(tot[1]);
+            const double lam = (vv > 0.0 && tt > 0.0) ? sqrt(tt / vv) : 1.0;
+            const double bmax = 1.15 * lam, amin = bmax / (double)cheb_ratio;
+            cheb_s[0] = (T)(0.5 * (bmax + amin));
+            cheb_s[1] = (T)(0.5 * (bmax - amin));
+            cheb_s[2] = (T)((bmax + amin) / (bmax - amin));
+            sc.alpha_t = (T)(tt > 0.0 ? 1.0 / sqrt(tt) : 0.0);  // the normalisation of the power vector
+          }))
+        return;
+      scale = sc.alpha_t;
+    }
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+      if (i <= d.nx && j < d.ny) eig[uidx(d, i, j)] *= scale;
+      if (i < d.nx && j <= d.ny) eig[vidx(d, i, j)] *= scale;
+    }
+  }
+  // z = M⁻¹ r (gr into gz): cheb steps of the Jacobi-preconditioned Chebyshev iteration on D⁻¹ R A P z = D⁻¹ r
+  // from z = 0; ends with z prolonged into wbuf[wsel ^ 1] (returned), which a grid barrier must precede
+  // any read of
+  auto precond = [&](T*& wout) -> bool {
+    const T th = cheb_s[0], de = cheb_s[1], sg = cheb_s[2];
+    T* wo = wbuf[wsel];
+    wsel ^= 1;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+      T zz[2] = {(T)0, (T)0};
+#pragma unroll
+      for (int comp = 0; comp < 2; ++comp) {
+        if (comp == 0 ? !(i <= d.nx && j < d.ny) : !(i < d.nx && j <= d.ny)) continue;
+        const int q = comp == 0 ? uidx(d, i, j) : vidx(d, i, j);
+        const T z = minv(q) * g.gr[q] / th;
+        g.gz[q] = z;
+        gcd[q] = z;
+        zz[comp] = z;
+      }
+      prolong_store<T, TILE>(d, levels, cf.inner, zz[0], zz[1], i0, j0, sm, wo);
+    }
+    T rho = (T)1 / sg;
+    for (int stp = 1; stp < cheb; ++stp) {
+      if (!grid_barrier<T>(bar, partials, epoch, ss)) return false;
+      const T rn = (T)1 / ((T)2 * sg - rho), c1 = rn * rho, c2 = (T)2 * rn / de;
+      T* wn = wbuf[wsel];
+      wsel ^= 1;
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+        T tt[2];
+        coarse_apply<T, TILE>(d, levels, cf, wmask, wo, i0, j0, sm, tt[0], tt[1]);
+        T zz[2] = {(T)0, (T)0};
+#pragma unroll
+        for (int comp = 0; comp < 2; ++comp) {
+          if (comp == 0 ? !(i <= d.nx && j < d.ny) : !(i < d.nx && j <= d.ny)) continue;
+          const int q = comp == 0 ? uidx(d, i, j) : vidx(d, i, j);
+          const T cd = c1 * gcd[q] + c2 * (minv(q) * (g.gr[q] - tt[comp]));
+          const T z = g.gz[q] + cd;
+          gcd[q] = cd;
+          g.gz[q] = z;
+          zz[comp] = z;
+        }
+        prolong_store<T, TILE>(d, levels, cf.inner, zz[0], zz[1], i0, j0, sm, wn);
+      }
+      wo = wn;
+      rho = rn;
+    }
+    wout = wo;
+    return true;
+  };
+  // r = b_c - R A P xc;  p = s = 0
+  T* wcur = wbuf[wsel];
+  wsel ^= 1;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+    const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;
+    prolong_store<T, TILE>(d, levels, cf.inner, inu ? xc[uidx(d, i, j)] : (T)0, inv ? xc[vidx(d, i, j)] : (T)0, i0,
+                           j0, sm, wcur);
+  }
+  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+  T bb = 0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+    T cu, cv;
+    coarse_apply<T, TILE>(d, levels, cf, wmask, wcur, i0, j0, sm, cu, cv);
+    if (i <= d.nx && j < d.ny) {
+      const int q = uidx(d, i, j);
+      const T bu = bc[q];
+      g.gr[q] = bu - cu;
+      g.gp[q] = g.gs[q] = (T)0;
+      bb += bu * bu;
+    }
+    if (i < d.nx && j <= d.ny) {
+      const int q = vidx(d, i, j);
+      const T bv = bc[q];
+      g.gr[q] = bv - cv;
+      g.gp[q] = g.gs[q] = (T)0;
+      bb += bv * bv;
+    }
+  }
+  if (!precond(wcur)) return;
+  if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
+  bool first = true;
+  for (;;) {
+    // w = R A P z with γ = (r, z), δ = (w, z), |r|²
+    T a[4] = {T(0), T(0), T(0), first ? bb : T(0)};
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+      T wu, wv;
+      coarse_apply<T, TILE>(d, levels, cf, wmask, wcur, i0, j0, sm, wu, wv);
+      if (i <= d.nx && j < d.ny) {
+        const int q = uidx(d, i, j);
+        const T r = g.gr[q], z = g.gz[q];
+        a[0] += r * z;
+        a[1] += wu * z;
+        a[2] += r * r;
+        g.gw[q] = wu;
+      }
+      if (i < d.nx && j <= d.ny) {
+        const int q = vidx(d, i, j);
+        const T r = g.gr[q], z = g.gz[q];
+        a[0] += r * z;
+        a[1] += wv * z;
+        a[2] += r * r;
+        g.gw[q] = wv;
+      }
+    }
+    if (!grid_sync<4>(bar, partials, epoch, ss, a, [&](const S* tot) { srcg_scalars(sc, tot, first, it, maxit, tol_coarse); }))
+      return;
+    if (sc.stop) break;
+    // p = z + β p;  s = w + β s;  x += α p;  r -= α s;  then z = M⁻¹ r
+    const T alpha = sc.alpha_t, beta = sc.beta_t;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
+#pragma unroll
+      for (int comp = 0; comp < 2; ++comp) {
+        if (comp == 0 ? !(i <= d.nx && j < d.ny) : !(i < d.nx && j <= d.ny)) continue;
+        const int q = comp == 0 ? uidx(d, i, j) : vidx(d, i, j);
+        const T pq = fmul_add(beta, g.gp[q], g.gz[q]), sq = fmul_add(beta, g.gs[q], g.gw[q]);
+        g.gp[q] = pq;
+        g.gs[q] = sq;
+        xc[q] = fmul_add(alpha, pq, xc[q]);
+        g.gr[q] = fmul_add(-alpha, sq, g.gr[q]);
+      }
+    }
+    ++it;
+    if (!precond(wcur)) return;
+    if (!grid_barrier<T>(bar, partials, epoch, ss)) return;
     first = false;
   }
   if (blockIdx.x == 0 && tx == 0 && ty == 0) {

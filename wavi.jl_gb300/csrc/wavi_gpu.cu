@@ -57,6 +57,7 @@ struct wavi_ctx {
   bool skipped = false;  // the last enqueued solve had maxiter_picard <= 0
   int pers_share = 1;    // persistent coarse kernels of this many contexts may run at once (ensembles)
   bool solved = false;   // a solve has left its converged state in the buffers (the adjoint linearises it)
+  bool fields_loaded = false;  // a solve, relinearisation or time-stepping run has uploaded model fields
   struct Adj {           // adjoint / tangent-linear buffers, allocated on first use
     bool ready = false;
     AdjCell cell{};
@@ -75,6 +76,8 @@ struct wavi_ctx {
   Dims d{};
   wavi_solver_params sp{};
   wavi_options opt{};
+  bool acc64 = false;  // mixed coarse CG with FP64 dot products and scalars (WAVI_SUMS_FP64)
+  bool visc32 = false;  // mixed: the σ-level viscosity sweeps in FP32 (WAVI_VISCOSITY_FP32)
   bool has_fixed = false;
   int tile = 16;  // Haar / coarse-operator tile: 16 (levels <= 3) or 32 (levels = 4)
   std::string err;
@@ -125,6 +128,7 @@ struct wavi_ctx {
   unsigned long long* selftest = nullptr;  // [0]: a tagged word nothing writes, [1]: the self-test's result
   int pers_maxt = 0, pers_grid = 0, ntx = 0, nty = 0;  // pers_maxt -1: CG vectors in global memory
   void *gz = nullptr, *gw = nullptr;                    // extra vectors of the global-memory variant
+  void *w2 = nullptr, *gcd = nullptr;                   // its Chebyshev solve: second prolongation buffer, direction
   int coarse_solver = WAVI_COARSE_CG;  // resolved coarse solver (never WAVI_COARSE_AUTO)
   void* dcoarse = nullptr;             // diag(R A P) for the Jacobi-preconditioned single-reduction CG
   void* cheb_eig = nullptr;            // the Chebyshev coarse solve's power vector (kept across V-cycles)
@@ -196,6 +200,8 @@ int dalloc(wavi_ctx* c, T** p, size_t n) {
 }
 
 bool mixed(const wavi_ctx* c) { return c->opt.precision == WAVI_PRECISION_MIXED; }
+// the relinearisation's viscosity sweeps in FP32 (mixed contexts with WAVI_VISCOSITY_FP32), else FP64
+bool visc32(const wavi_ctx* c) { return mixed(c) && c->visc32; }
 
 template <typename T>
 OpCoef<T> coef(const wavi_ctx* c);
@@ -203,6 +209,7 @@ template <>
 OpCoef<double> coef<double>(const wavi_ctx* c) {
   return {c->heta_h64, c->heta_c64, c->dimp64, c->beta_m64, c->h_m64, c->inner_uv};
 }
+
 template <>
 OpCoef<float> coef<float>(const wavi_ctx* c) {
   return {c->heta_h32, c->heta_c32, c->dimp32, c->beta_m32, c->h_m32, c->inner_uv};
@@ -230,7 +237,7 @@ int enqueue_picard_head(wavi_ctx* c, const CondHandles& h, Tally& t) {
                c->beta_eff, c->heta_h64, c->dimp64, mixed(c) ? c->heta_h32 : nullptr, mixed(c) ? c->dimp32 : nullptr,
                c->hn};
   const int nb = (d.Nh + 127) / 128;
-  if (mixed(c))
+  if (visc32(c))
     k_relin_h<float><<<nb, 128, 0, c->st>>>(d, in, out);
   else
     k_relin_h<double><<<nb, 128, 0, c->st>>>(d, in, out);
@@ -458,9 +465,20 @@ int launch_cg_persistent(wavi_ctx* c) {
   } else {
     const bool cheb = c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV;
     const T* dc = (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI || cheb) ? (const T*)c->dcoarse : nullptr;
-    CK(cudaLaunchKernelEx(&cfg, k_srcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
-                          dc, (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
-                          c->halo_box, cheb ? cheb_steps(c) : 1, kChebRatio, (T*)c->cheb_eig, c->ntx, c->nty));
+    if (c->acc64) {
+      if constexpr (std::is_same<T, float>::value && TILE == 16 && MAXT <= 2) {
+        CK(cudaLaunchKernelEx(&cfg, k_srcg_persistent<T, TILE, MAXT, true>, d, c->sp.levels, coef<T>(c),
+                              (const uint8_t*)c->wmask_uv, dc, (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S,
+                              (const DevParams*)c->P, c->bar, c->halo_box, cheb ? cheb_steps(c) : 1, kChebRatio,
+                              (T*)c->cheb_eig, c->ntx, c->nty));
+      } else {
+        return fail(c, WAVI_ERR_ARGUMENT, "FP64 coarse sums have no kernel for this precision and tiling");
+      }
+    } else {
+      CK(cudaLaunchKernelEx(&cfg, k_srcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
+                            dc, (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
+                            c->halo_box, cheb ? cheb_steps(c) : 1, kChebRatio, (T*)c->cheb_eig, c->ntx, c->nty));
+    }
   }
   c->launches++;
   return 0;
@@ -481,7 +499,12 @@ int launch_cg_global(wavi_ctx* c) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   const GlobalCG<T> g{(T*)c->rc, (T*)c->gz, (T*)c->uc, (T*)c->cc, (T*)c->gw};
-  if (c->coarse_solver == WAVI_COARSE_CG) {
+  if (c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV) {
+    CK(cudaLaunchKernelEx(&cfg, k_srcg_cheb_global<T, TILE>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
+                          (const T*)c->dcoarse, (T*)c->w, (T*)c->w2, (const T*)c->bc, (T*)c->xc, g, (T*)c->gcd,
+                          (T*)c->cheb_eig, cheb_steps(c), kChebRatio, c->partials, c->S, (const DevParams*)c->P, c->bar,
+                          c->ntx, c->nty));
+  } else if (c->coarse_solver == WAVI_COARSE_CG) {
     CK(cudaLaunchKernelEx(&cfg, k_cg_global<T, TILE>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv, (T*)c->w,
                           (const T*)c->bc, (T*)c->xc, g, c->partials, c->S, (const DevParams*)c->P, c->bar, c->ntx,
                           c->nty));
@@ -734,8 +757,17 @@ int build_graph(wavi_ctx* c) {
 // Persistent coarse CG: the smallest tiles-per-CTA (1, 2, 4) for which every CTA of the launch is
 // resident at once (the cooperative launch needs that); 0 if none fits.
 template <int MAXT, typename T, int TILE>
-int resident_ctas(int nsm, int solver) {
+int resident_ctas(int nsm, int solver, bool acc64) {
   int per_sm = 0;
+  if (acc64 && solver != WAVI_COARSE_CG && solver != WAVI_COARSE_PIPELINED_CHEBYSHEV) {
+    if constexpr (std::is_same<T, float>::value && TILE == 16 && MAXT <= 2) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_srcg_persistent<T, TILE, MAXT, true>, TILE * TILE, 0) !=
+          cudaSuccess)
+        return 0;
+      return per_sm * nsm;
+    }
+    return 0;
+  }
   if (solver == WAVI_COARSE_PIPELINED_CHEBYSHEV) {
     if constexpr (std::is_same<T, float>::value && TILE == 16 && MAXT <= 2) {
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent<T, TILE, MAXT>, TILE * TILE, 0) !=
@@ -761,8 +793,9 @@ void choose_persistent(wavi_ctx* c) {
   const long ntiles = (long)c->ntx * c->nty;
   const int s = c->coarse_solver;
   const int share = std::max(1, c->pers_share);
-  const int caps[3] = {resident_ctas<1, T, TILE>(nsm, s) / share, resident_ctas<2, T, TILE>(nsm, s) / share,
-                       resident_ctas<4, T, TILE>(nsm, s) / share};
+  const int caps[3] = {resident_ctas<1, T, TILE>(nsm, s, c->acc64) / share,
+                       resident_ctas<2, T, TILE>(nsm, s, c->acc64) / share,
+                       resident_ctas<4, T, TILE>(nsm, s, c->acc64) / share};
   const int maxts[3] = {1, 2, 4};
   for (int k = 0; k < 3 && c->opt.coarse_kernel != 3; ++k) {
     const long g = (ntiles + maxts[k] - 1) / maxts[k];
@@ -774,9 +807,11 @@ void choose_persistent(wavi_ctx* c) {
   }
   // global-memory vectors: one CTA per resident slot, looping over the tiles
   int per_sm = 0;
-  cudaError_t e = s == WAVI_COARSE_CG
-                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_global<T, TILE>, TILE * TILE, 0)
-                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_srcg_global<T, TILE>, TILE * TILE, 0);
+  cudaError_t e =
+      s == WAVI_COARSE_CG ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_global<T, TILE>, TILE * TILE, 0)
+      : s == WAVI_COARSE_SRCG_CHEBYSHEV
+          ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_srcg_cheb_global<T, TILE>, TILE * TILE, 0)
+          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_srcg_global<T, TILE>, TILE * TILE, 0);
   if (e != cudaSuccess || per_sm <= 0) return;
   c->pers_maxt = -1;
   c->pers_grid = (int)std::max<long>(1, std::min<long>(ntiles, (long)per_sm * nsm / share));
@@ -914,6 +949,7 @@ int map_coarse_cache(wavi_ctx* c, const uint8_t* mask, int n, int base, double* 
 }
 
 int upload(wavi_ctx* c, const wavi_fields* f, bool host) {
+  c->fields_loaded = true;
   const Dims& d = c->d;
   const cudaMemcpyKind k = host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
 #define IN(dst, src, n) TRY(copy_in(c, dst, src, n, k, #src));
@@ -1266,6 +1302,19 @@ int step_pre(wavi_ctx* c, double melt) {
   return 0;
 }
 
+// update_wavelets! (update_wavelets.jl:6-32) on the context's velocities: forward Haar transform of
+// mask ⊙ (u, v), the threshold |w| >= wavelet_threshold into the wavelet mask, the coarse cache cleared.
+int step_wavelets(wavi_ctx* c) {
+  const Dims& d = c->d;
+  k_haar<double, double, 2, false, false><<<c->haar_grid, c->haar_block, 0, c->st>>>(
+      d, c->sp.levels, c->uv, c->step.wav, nullptr, c->mask_uv, nullptr, c->partials, nullptr);
+  CKL();
+  k_step_wavelet_mask<<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->step.wav, c->sp.wavelet_threshold, c->wmask_uv,
+                                                               c->xc_full64);
+  CKL();
+  return 0;
+}
+
 // After the solve: velocities on the h grid, dh/dt, the wavelet coarse space (update_state.jl:17-19),
 // then update_thickness!.
 int step_post(wavi_ctx* c, double melt, double dt, double h_min) {
@@ -1273,12 +1322,7 @@ int step_post(wavi_ctx* c, double melt, double dt, double h_min) {
   const int hb = (d.Nh + 127) / 128;
   k_step_post_h<<<hb, 128, 0, c->st>>>(d, step_state(c), step_buf(c, melt), c->uv, c->beta, c->quad_f1, c->quad_f2);
   CKL();
-  k_haar<double, double, 2, false, false><<<c->haar_grid, c->haar_block, 0, c->st>>>(
-      d, c->sp.levels, c->uv, c->step.wav, nullptr, c->mask_uv, nullptr, c->partials, nullptr);
-  CKL();
-  k_step_wavelet_mask<<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->step.wav, c->sp.wavelet_threshold, c->wmask_uv,
-                                                               c->xc_full64);
-  CKL();
+  TRY(step_wavelets(c));
   k_step_thickness<<<hb, 128, 0, c->st>>>(d, step_state(c), step_buf(c, melt), dt, h_min);
   CKL();
   return 0;
@@ -1452,15 +1496,26 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_kernel %d", opt->coarse_kernel));
   if (opt->cheb_steps != 0 && (opt->cheb_steps < 1 || opt->cheb_steps > 15 || opt->cheb_steps % 2 == 0))
     return bail(fail(c, WAVI_ERR_ARGUMENT, "cheb_steps must be 0 (default) or odd in 1..15 (got %d)", opt->cheb_steps));
+  if (opt->coarse_sums < WAVI_SUMS_DEFAULT || opt->coarse_sums > WAVI_SUMS_FP64)
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_sums %d", opt->coarse_sums));
+  if (opt->viscosity < WAVI_VISCOSITY_DEFAULT || opt->viscosity > WAVI_VISCOSITY_FP64)
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown viscosity precision %d", opt->viscosity));
+  c->visc32 = mixed(c) && opt->viscosity == WAVI_VISCOSITY_FP32;
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));
   // auto: FP64 runs the reference's cg!; mixed runs the Chebyshev-Jacobi single-reduction CG on domains
-  // whose ice mask is full (the Jacobi one where only the global-memory kernel fits), and cg! where the
+  // whose ice mask is full (register-resident or, on grids too large for that, global-memory), and cg! where the
   // mask cuts the domain (calving fronts inside it): there the masked Haar functions can coincide on the
   // interior and R A P turns singular
   bool full_mask = true;
   for (int i = 0; i < d.Nh && full_mask; ++i) full_mask = hm[i] != 0;
   c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) && full_mask ? WAVI_COARSE_SRCG_CHEBYSHEV : WAVI_COARSE_CG) : want;
+  c->acc64 = mixed(c) && opt->coarse_sums == WAVI_SUMS_FP64;
+  if (c->acc64 && (c->tile != 16 || opt->coarse_kernel == 2 || opt->coarse_kernel == 3 || c->coarse_solver == WAVI_COARSE_CG ||
+                   c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV))
+    return bail(fail(c, WAVI_ERR_ARGUMENT,
+                     "FP64 coarse sums need a single-reduction coarse solver on the register-resident kernel with "
+                     "16 x 16 tiles"));
   if (opt->coarse_kernel != 2) {
     if (mixed(c))
       c->tile == 16 ? choose_persistent<float, 16>(c) : choose_persistent<float, 32>(c);
@@ -1475,14 +1530,11 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     }
     if ((opt->coarse_kernel == 1 || opt->coarse_kernel == 3) && c->pers_maxt == 0)
       return bail(fail(c, WAVI_ERR_ARGUMENT, "the persistent coarse CG does not fit this grid on this device"));
-    if (c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV && c->pers_maxt < 0) {
-      if (want != WAVI_COARSE_AUTO)
-        return bail(fail(c, WAVI_ERR_ARGUMENT, "the Chebyshev coarse solve needs the register-resident persistent kernel"));
-      c->coarse_solver = WAVI_COARSE_SRCG_JACOBI;
-    }
     if (c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV && (!mixed(c) || c->tile != 16 || c->pers_maxt <= 0))
       return bail(fail(c, WAVI_ERR_ARGUMENT,
                        "the pipelined coarse CG needs mixed precision, 16 x 16 tiles and the register-resident kernel"));
+    if (c->acc64 && (c->pers_maxt <= 0 || c->pers_maxt > 2))
+      return bail(fail(c, WAVI_ERR_ARGUMENT, "FP64 coarse sums: the register-resident kernel does not fit this grid"));
   } else {
     c->coarse_solver = WAVI_COARSE_CG;
   }
@@ -1513,6 +1565,12 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
       c->gz = q;
       if ((r = dalloc(c, &q, N))) return bail(r);
       c->gw = q;
+      if (c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV) {
+        if ((r = dalloc(c, &q, N))) return bail(r);
+        c->w2 = q;
+        if ((r = dalloc(c, &q, N))) return bail(r);
+        c->gcd = q;
+      }
     }
   }
   if ((r = dalloc(c, &c->P, 1))) return bail(r);
@@ -1588,7 +1646,7 @@ int wavi_relinearise_device(wavi_ctx* c, const wavi_params* p, wavi_fields* f) {
                c->beta_eff, c->heta_h64, c->dimp64, mixed(c) ? c->heta_h32 : nullptr, mixed(c) ? c->dimp32 : nullptr,
                c->hn};
   const int nb = (d.Nh + 127) / 128;
-  if (mixed(c))
+  if (visc32(c))
     k_relin_h<float><<<nb, 128, 0, c->st>>>(d, in, out);
   else
     k_relin_h<double><<<nb, 128, 0, c->st>>>(d, in, out);
@@ -1634,6 +1692,44 @@ int wavi_time_operator_device(wavi_ctx* c, int precision, const void* in_uv, voi
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   *avg_ms = (double)ms / repeats;
+  return 0;
+}
+
+int wavi_time_relinearise_device(wavi_ctx* c, int repeats, double* avg_ms_h, double* avg_ms_uv) {
+  TRY(check_ctx(c));
+  if (!avg_ms_h || !avg_ms_uv || repeats < 1) return fail(c, WAVI_ERR_ARGUMENT, "bad arguments");
+  if (!c->fields_loaded) return fail(c, WAVI_ERR_ARGUMENT, "no fields on the context yet (relinearise or solve first)");
+  const Dims& d = c->d;
+  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw, c->P};
+  RelinOut out{c->shelf, c->av_speed, c->bed_speed, c->beta, c->tau, c->eta, c->eta_av, c->quad_f1, c->quad_f2,
+               c->beta_eff, c->heta_h64, c->dimp64, mixed(c) ? c->heta_h32 : nullptr, mixed(c) ? c->dimp32 : nullptr,
+               c->hn};
+  RelinUVIn uin{c->mask_uv, c->h_mask, c->c_mask, c->beta_eff, c->gf, c->gf_uv, c->h_uv, c->hn};
+  RelinUVOut uout{c->beta_eff_uv, c->beta_m64, c->h_m64, c->heta_c64, mixed(c) ? c->beta_m32 : nullptr,
+                  mixed(c) ? c->h_m32 : nullptr, mixed(c) ? c->heta_c32 : nullptr};
+  const int nb = (d.Nh + 127) / 128;
+  float ms = 0.f;
+  CK(cudaEventRecord(c->ev0, c->st));
+  for (int k = 0; k < repeats; ++k) {
+    if (visc32(c))
+      k_relin_h<float><<<nb, 128, 0, c->st>>>(d, in, out);
+    else
+      k_relin_h<double><<<nb, 128, 0, c->st>>>(d, in, out);
+    CKL();
+  }
+  CK(cudaEventRecord(c->ev1, c->st));
+  CK(cudaEventSynchronize(c->ev1));
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  *avg_ms_h = (double)ms / repeats;
+  CK(cudaEventRecord(c->ev0, c->st));
+  for (int k = 0; k < repeats; ++k) {
+    k_relin_uv<<<c->pt_grid, c->pt_block, 0, c->st>>>(d, uin, uout);
+    CKL();
+  }
+  CK(cudaEventRecord(c->ev1, c->st));
+  CK(cudaEventSynchronize(c->ev1));
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  *avg_ms_uv = (double)ms / repeats;
   return 0;
 }
 
@@ -1854,6 +1950,21 @@ int wavi_haar_device(wavi_ctx* c, int kind, const double* in_uv, double* out_uv,
   else
     return fail(c, WAVI_ERR_ARGUMENT, "unknown transform %d", kind);
   CKL();
+  CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+// update_wavelets! (Wavelets/update_wavelets.jl:6-32) with the device time stepping's own kernels: the
+// forward Haar transform of the u/v model masks times the given velocities, the threshold, and the
+// cleared coarse-correction cache, on this context; the new wavelet mask is copied to wmask_out.
+int wavi_update_wavelets_device(wavi_ctx* c, const double* uv_in, uint8_t* wmask_out) {
+  TRY(check_ctx(c));
+  if (!uv_in || !wmask_out) return fail(c, WAVI_ERR_ARGUMENT, "null vector");
+  TRY(step_alloc(c));
+  const Dims& d = c->d;
+  CK(cudaMemcpyAsync(c->uv, uv_in, sizeof(double) * d.N, cudaMemcpyDeviceToDevice, c->st));
+  TRY(step_wavelets(c));
+  CK(cudaMemcpyAsync(wmask_out, c->wmask_uv, d.N, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return 0;
 }

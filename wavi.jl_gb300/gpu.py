@@ -39,7 +39,8 @@ class VelocitySolver:
     STENCIL_KERNELS = {"auto": 0, "tiled": 1, "streaming": 2}
 
     def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0,
-                 coarse_kernel="auto", coarse_solver="auto", stencil_kernel="auto", cheb_steps=0):
+                 coarse_kernel="auto", coarse_solver="auto", stencil_kernel="auto", cheb_steps=0,
+                 coarse_sums="default", viscosity="default"):
         self.lib = abi.load_library()
         self.grid = grid
         self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ
@@ -49,7 +50,8 @@ class VelocitySolver:
         self._sp = solver_params.to_c()
         self._opt = abi.Options(int(device), PRECISIONS[precision], 1 if use_graphs else 0, int(picard_test),
                                 self.COARSE_KERNELS[coarse_kernel], abi.COARSE_SOLVERS[coarse_solver],
-                                self.STENCIL_KERNELS[stencil_kernel], int(cheb_steps))
+                                self.STENCIL_KERNELS[stencil_kernel], int(cheb_steps),
+                                abi.COARSE_SUMS[coarse_sums], abi.VISCOSITY[viscosity])
         ctx = C.c_void_p()
         st = self.lib.wavi_ctx_create(C.byref(self._desc.desc), C.byref(self._sp), C.byref(self._opt), C.byref(ctx))
         if st != 0:
@@ -141,6 +143,15 @@ class VelocitySolver:
             raise self._err(st)
         return ms.value / 1e3
 
+    def time_relinearise_device(self, repeats=20):
+        """Mean durations (s) of one launch of the relinearisation's h-grid and u/v-grid kernels over
+        `repeats` back-to-back launches each, on the fields of the last solve or relinearisation."""
+        mh, muv = C.c_double(), C.c_double()
+        st = self.lib.wavi_time_relinearise_device(self.ctx, int(repeats), C.byref(mh), C.byref(muv))
+        if st != 0:
+            raise self._err(st)
+        return mh.value / 1e3, muv.value / 1e3
+
     def op_diagonal_device(self, out_uv, precision="fp64"):
         st = self.lib.wavi_op_diagonal_device(self.ctx, PRECISIONS[precision], C.c_void_p(out_uv.data_ptr()))
         if st != 0:
@@ -203,6 +214,13 @@ class VelocitySolver:
         if st != 0:
             raise self._err(st)
         return bool(fired.value)
+
+    def update_wavelets_device(self, in_uv, wmask_out):
+        """update_wavelets! with the device time step's kernels: the context's wavelet mask from the float64
+        velocities in_uv ([u | v]), copied to the uint8 device tensor wmask_out."""
+        st = self.lib.wavi_update_wavelets_device(self.ctx, C.c_void_p(in_uv.data_ptr()), C.c_void_p(wmask_out.data_ptr()))
+        if st != 0:
+            raise self._err(st)
 
     def haar_device(self, kind, in_uv, out_uv, mask_uv=None):
         m = C.c_void_p(mask_uv.data_ptr()) if mask_uv is not None else None

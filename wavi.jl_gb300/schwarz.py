@@ -237,26 +237,37 @@ class EnsembleSubdomainSolver:
         return stats
 
 
+_COARSE = ("wu_correction_coarse", "wv_correction_coarse")
+
+
 def _member_tensors(fields, device):
-    """The velocity solve's fields (column-major, masks as bytes) as flat tensors on ``device``."""
+    """The velocity solve's fields (column-major, masks as bytes) as flat tensors on ``device``.  A
+    subdomain's adaptive coarse space can be empty (update_wavelets! found no coefficient above the
+    threshold); its compact correction then has no entries, and a tensor of none has no device address,
+    so it is staged with one unused entry (the solve reads and writes count(mask) entries only)."""
     import torch
     from .gpu import ALL_FIELDS
     out = {}
     for name in ALL_FIELDS:
         a = np.asarray(fields[name])
         dt = np.uint8 if name in ("wu_mask", "wv_mask") else np.float64
-        out[name] = torch.from_numpy(np.ascontiguousarray(a.astype(dt).ravel(order="F"))).to(device)
+        flat = np.ascontiguousarray(a.astype(dt).ravel(order="F"))
+        if name in _COARSE and flat.size == 0:
+            flat = np.zeros(1)
+        out[name] = torch.from_numpy(flat).to(device)
     return out
 
 
 def _member_fields_back(fields, tensors):
-    """The solved member's fields back into the host model, in place where the shape is unchanged."""
+    """The solved member's fields back into the host model, in place where the shape is unchanged (the
+    compact coarse corrections keep count(wavelet mask) entries)."""
     from .gpu import ALL_FIELDS
     for name in ALL_FIELDS:
         host = tensors[name].cpu().numpy()
         cur = fields[name]
-        if name in ("wu_correction_coarse", "wv_correction_coarse"):
-            fields[name] = host.copy()
+        if name in _COARSE:
+            mask = fields["wu_mask" if name == "wu_correction_coarse" else "wv_mask"]
+            fields[name] = host[:int(np.count_nonzero(mask))].copy()
         else:
             cur[...] = host.reshape(cur.shape, order="F")
 
