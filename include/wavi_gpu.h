@@ -47,10 +47,10 @@ typedef enum wavi_status {
 /* Precision modes of a context. */
 typedef enum wavi_precision {
   WAVI_PRECISION_FP64 = 0,         /* the reference algorithm in float64 throughout (parity mode) */
-  WAVI_PRECISION_MIXED = 1         /* float32 operator coefficients and V-cycle (smoother, Haar transforms,
-                                      coarse CG; its sums per wavi_coarse_sums); float64 viscosity sweeps
-                                      (per wavi_viscosity), right-hand side, Picard residual, convergence
-                                      test and coarse-correction cache */
+  WAVI_PRECISION_MIXED = 1         /* float32 viscosity sweeps (per wavi_viscosity), operator coefficients
+                                      and V-cycle (smoother, Haar transforms, coarse CG; its sums per
+                                      wavi_coarse_sums); float64 right-hand side, Picard residual,
+                                      convergence test and coarse-correction cache */
 } wavi_precision;
 
 /* Grid geometry and the masks that fix the problem's sparsity (src/Grid.jl:1-27, :66-201;
@@ -113,11 +113,11 @@ typedef struct wavi_options {
 } wavi_options;
 
 /* Precision of the relinearisation's viscosity sweeps (update_velocities.jl:264-283) in a mixed context.
- * The operator coefficients of the FP64 Picard residual derive from η: with FP32 sweeps their rounding
- * changes with every relinearisation, which puts a floor under ||b - A(u) u|| / ||b|| (measured 5e-6 on a
- * 96 x 32 channel at 2 km, whose velocity nevertheless agrees with the FP64 solve to 1e-7). */
+ * FP32 sweeps (the default) keep the mixed solve within ~1e-7 of the FP64 reference solve; FP64 sweeps cost
+ * more (FP64 pow per σ level and cell) and bring it to ~1e-9 (on the 640 x 80 benchmark: 1.44e-7 against
+ * 2.85e-9, at 51.6 against 55.5 ms per solve). */
 typedef enum wavi_viscosity {
-  WAVI_VISCOSITY_DEFAULT = 0,        /* WAVI_VISCOSITY_FP64 */
+  WAVI_VISCOSITY_DEFAULT = 0,        /* WAVI_VISCOSITY_FP32 */
   WAVI_VISCOSITY_FP32 = 1,           /* FP32 sweeps (η, B, the stress term in float) */
   WAVI_VISCOSITY_FP64 = 2            /* FP64 sweeps; the V-cycle's coefficients are then rounded to FP32 */
 } wavi_viscosity;

@@ -223,11 +223,12 @@ def test_persistent_smoother_matches_per_step_smoother(oracle):
     assert np.linalg.norm(x1 - x2) <= 1e-4 * np.linalg.norm(x2), np.linalg.norm(x1 - x2) / np.linalg.norm(x2)
 
 
-def test_mixed_viscosity_precision_and_the_residual_floor(oracle):
-    """A mixed solve's FP64 Picard residual uses operator coefficients derived from η.  With FP32 viscosity
-    sweeps (WAVI_VISCOSITY_FP32) their rounding changes at every relinearisation and the residual levels off
-    (on this 96 x 32 channel at 2 km, measured at 5e-6, with the velocity within 1e-7 of the oracle's);
-    with the default FP64 sweeps the mixed solve converges to the reference's tolerance like the FP64 one."""
+def test_mixed_viscosity_precision_tracks_the_reference(oracle):
+    """The mixed solve against the FP64 oracle on a 96 x 32 channel at 2 km where the reference algorithm
+    itself does not reach tol_picard = 1e-6 within 100 Picard iterations (its residual oscillates between
+    3.6e-6 and 9e-6; every V-cycle's coarse solve converges): the GPU follows it there too.  With FP64
+    viscosity sweeps (WAVI_VISCOSITY_FP64) the velocities agree to 1e-9 and the final residual to 1 %
+    (GB300: 1.1e-11); with the default FP32 sweeps to 1e-6 (GB300: 9.9e-8)."""
     from wavi_gb300 import synthetic
     from wavi_gb300.gpu import VelocitySolver
     g, bed, p, sp, ic = synthetic.small_case(nx=96, ny=32, dx=2000.0, mask="full", maxiter_picard=100, tol_picard=1e-6)
@@ -235,15 +236,17 @@ def test_mixed_viscosity_precision_and_the_residual_floor(oracle):
     om.pre_solve()
     f0 = fields_from_oracle(om, g)
     om.update_velocities()
+    ost = om.stats()
+    assert ost["picard_iterations"] == 100  # the reference does not converge here
     res = {}
-    for visc in ("default", "fp32"):
+    for visc in ("fp64", "default"):
         f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
         s = VelocitySolver(g, sp, precision="mixed", viscosity=visc)
         st = s.solve(p, f)
         s.close()
         res[visc] = (st, uv_err(f, om))
-        print(visc, st["status_name"], st["picard_iterations"], st["rel_residual"], res[visc][1])
-    st, err = res["default"]
-    assert st["status"] == 0, st
-    assert err < 1e-6
-    assert res["fp32"][1] < 1e-6  # the velocity is accurate either way
+        print(visc, st["status_name"], st["picard_iterations"], st["rel_residual"], res[visc][1], ost["rel_residual"])
+    st, err = res["fp64"]
+    assert err < 1e-9, err
+    assert abs(st["rel_residual"] - ost["rel_residual"]) <= 1e-2 * ost["rel_residual"], (st, ost)
+    assert res["default"][1] < 1e-6

@@ -19,8 +19,9 @@ CASES = {
     "ragged": dict(nx=37, ny=13, dx=3000.0, mask="full"),
     "channel": dict(nx=96, ny=32, dx=2000.0, mask="full"),
 }
-# Picard tolerance per case: the 96 x 32 channel's FP32 V-cycle does not reach 1e-7 within 80 Picard
-# iterations with either Chebyshev solver (the FP32 limit of the correction); 1e-6 is the benchmark's
+# Picard tolerance per case: on the 96 x 32 channel the reference algorithm itself does not reach 1e-6
+# within 100 Picard iterations (the oracle's residual oscillates between 3.6e-6 and 9e-6); there the GPU
+# solves run the same 100 iterations and are compared with the oracle's at that point
 TOL = {"full": 1e-7, "ragged": 1e-7, "channel": 1e-6}
 
 
@@ -54,6 +55,7 @@ def test_pipelined_converged_solve_matches_reference(oracle, name):
     g, p, sp, om = _setup(oracle, name, maxiter_picard=100, tol_picard=TOL[name])
     f0 = fields_from_oracle(om, g)
     om.update_velocities()
+    converged = om.stats()["picard_iterations"] < 100
     stats = {}
     for solver in ("srcg_chebyshev", "pipelined_chebyshev"):
         f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
@@ -61,7 +63,7 @@ def test_pipelined_converged_solve_matches_reference(oracle, name):
         st = s.solve(p, f)
         s.close()
         print(name, solver, st["picard_iterations"], st["coarse_cg_iterations"], st["rel_residual"], uv_err(f, om))
-        assert st["status"] == 0, (solver, st)
+        assert (st["status"] == 0) == converged, (solver, st)
         assert st["coarse_solver"] == solver
         assert uv_err(f, om) < 1e-6, (solver, st)
         stats[solver] = st

@@ -11,6 +11,7 @@
 // accumulate in double.  The Picard residual uses the double instantiation.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 namespace wavi {
@@ -307,6 +308,65 @@ __global__ void k_relin_h(Dims d, RelinIn in, RelinOut out) {
       sx[tb] = acc;
     }
     shear = 0.5 * sx[0] + 0.5 * sx[1];
+  }
+  if constexpr (std::is_same<TR, float>::value) {
+    // FP32 viscosity sweeps (mixed precision): η carries float precision, so everything after the velocity
+    // differences runs in float too — speeds, β (powf), the sweeps, one reciprocal of η per level for the
+    // quadratures, βeff — and only the loads and stores of the FP64 fields convert.  (In FP64 these are a
+    // pow per cell and two divisions per level and cell, which bound the kernel on GB300's FP64 rate.)
+    const float fx = (float)ux, fy = (float)vy, fs = (float)shear;
+    const float ssr = sqrtf(fx * fx + fy * fy + fx * fy + 0.25f * (fs * fs));
+    const float uc = hm ? (float)(0.5 * u0 + 0.5 * u1) : 0.0f;
+    const float vc = hm ? (float)(0.5 * v0 + 0.5 * v1) : 0.0f;
+    const float avs = sqrtf(uc * uc + vc * vc);
+    const float f2_prev = (float)out.quad_f2[c], beta_prev = (float)out.beta[c];
+    const float bs = avs / (1.0f + f2_prev * beta_prev);
+    const float ur = (float)in.P->weertman_reg_speed;
+    const float beta = (float)in.wc[c] * powf(sqrtf(bs * bs + ur * ur), (float)(1.0 / in.P->weertman_m - 1.0));
+    const float tau = beta * bs;
+    out.shelf_strain_rate[c] = ssr;
+    out.av_speed[c] = avs;
+    out.bed_speed[c] = bs;
+    out.beta[c] = beta;
+    out.tau_bed[c] = tau;
+    float eav = 0.0f, f1 = 0.0f, f2 = 0.0f;
+    if (hm) {
+      const float ex = (float)(1.0 / in.P->glen_n - 1.0);
+      const float er2 = (float)(in.P->glen_reg_strain_rate * in.P->glen_reg_strain_rate);
+      const int n_iter_viscosity = in.P->n_iter_viscosity;
+      const float e2 = ssr * ssr;
+      const float hh = (float)in.h[c];
+      for (int k = 0; k < d.ns; ++k) {
+        const size_t q = (size_t)c + (size_t)d.Nh * k;
+        float eta = (float)out.eta[q];
+        const float B = (float)in.glen_b[q], zk = (float)in.zeta[k], wk = (float)in.qw[k];
+        const float tz = tau * zk;
+        for (int it = 0; it < n_iter_viscosity; ++it) {
+          const float t = tz / eta;
+          eta = 0.5f * B * powf(sqrtf(e2 + 0.25f * (t * t) + er2), ex);
+        }
+        out.eta[q] = eta;
+        const float ie = 1.0f / eta, hz = wk * hh * zk * ie;
+        eav += wk * eta;
+        f1 += hz;
+        f2 += hz * zk;
+      }
+    }
+    out.eta_av[c] = eav;
+    out.quad_f1[c] = f1;
+    out.quad_f2[c] = f2;
+    out.beta_eff[c] = beta / (1.0f + f2 * beta);
+    const float hn = (float)in.h[c] * eav;
+    out.hn[c] = hn;
+    const float hh_m = hm ? hn : 0.0f;
+    const double dm = hm ? in.P->c0 * in.dsdh[c] : 0.0;
+    out.heta_h64[c] = hh_m;
+    out.dimp64[c] = dm;
+    if (out.heta_h32) {
+      out.heta_h32[c] = hh_m;
+      out.dimp32[c] = (float)dm;
+    }
+    return;
   }
   const double ssr = sqrt(ux * ux + vy * vy + ux * vy + 0.25 * (shear * shear));
   // depth-averaged speed from centred velocities

@@ -77,7 +77,7 @@ struct wavi_ctx {
   wavi_solver_params sp{};
   wavi_options opt{};
   bool acc64 = false;  // mixed coarse CG with FP64 dot products and scalars (WAVI_SUMS_FP64)
-  bool visc32 = false;  // mixed: the σ-level viscosity sweeps in FP32 (WAVI_VISCOSITY_FP32)
+  bool visc32 = false;  // mixed: the σ-level viscosity sweeps in FP32 (the default; FP64 with WAVI_VISCOSITY_FP64)
   bool has_fixed = false;
   int tile = 16;  // Haar / coarse-operator tile: 16 (levels <= 3) or 32 (levels = 4)
   std::string err;
@@ -200,7 +200,7 @@ int dalloc(wavi_ctx* c, T** p, size_t n) {
 }
 
 bool mixed(const wavi_ctx* c) { return c->opt.precision == WAVI_PRECISION_MIXED; }
-// the relinearisation's viscosity sweeps in FP32 (mixed contexts with WAVI_VISCOSITY_FP32), else FP64
+// the relinearisation's viscosity sweeps in FP32 (mixed contexts unless WAVI_VISCOSITY_FP64), else FP64
 bool visc32(const wavi_ctx* c) { return mixed(c) && c->visc32; }
 
 template <typename T>
@@ -1500,7 +1500,7 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_sums %d", opt->coarse_sums));
   if (opt->viscosity < WAVI_VISCOSITY_DEFAULT || opt->viscosity > WAVI_VISCOSITY_FP64)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown viscosity precision %d", opt->viscosity));
-  c->visc32 = mixed(c) && opt->viscosity == WAVI_VISCOSITY_FP32;
+  c->visc32 = mixed(c) && opt->viscosity != WAVI_VISCOSITY_FP64;
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));
   // auto: FP64 runs the reference's cg!; mixed runs the Chebyshev-Jacobi single-reduction CG on domains

@@ -56,8 +56,12 @@ class EnsembleSolver:
         return [stats_dict(starr[k]) for k in range(n)]
 
 
-DEFAULT_CANDIDATES = tuple(dict(concurrency=s, coarse_kernel=ck) for s in (8, 16, 32, 64)
-                           for ck in ("auto", "iterations"))
+# Members in flight, coarse-CG kernel (persistent, register-resident where a member's share of the device
+# holds its tiles, else global-memory; or one launch per CG iteration) and stencil kernel of the operator and
+# smoother sweeps (shared-memory 32 x 8 tiles, or row streaming)
+DEFAULT_CANDIDATES = tuple(dict(concurrency=s, coarse_kernel=ck, stencil_kernel=sk) for s in (16, 32)
+                           for ck in ("auto", "iterations") for sk in ("tiled", "streaming")) + \
+    tuple(dict(concurrency=s, coarse_kernel="auto", stencil_kernel="auto") for s in (8, 64))
 
 
 def autotune(grids, solver_params, params, make_tensors, precision="mixed", device=0, candidates=DEFAULT_CANDIDATES,
