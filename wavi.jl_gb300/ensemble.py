@@ -56,19 +56,21 @@ class EnsembleSolver:
         return [stats_dict(starr[k]) for k in range(n)]
 
 
-# Members in flight, coarse-CG kernel (persistent, register-resident where a member's share of the device
-# holds its tiles, else global-memory; or one launch per CG iteration) and stencil kernel of the operator and
-# smoother sweeps (shared-memory 32 x 8 tiles, or row streaming)
-DEFAULT_CANDIDATES = tuple(dict(concurrency=s, coarse_kernel=ck, stencil_kernel=sk) for s in (16, 32)
-                           for ck in ("auto", "iterations") for sk in ("tiled", "streaming")) + \
-    tuple(dict(concurrency=s, coarse_kernel="auto", stencil_kernel="auto") for s in (8, 64))
+# Members in flight and stencil kernel of the operator and smoother sweeps (shared-memory 32 x 8 tiles, or
+# row streaming), with the persistent coarse-CG kernel (register-resident where a member's share of the device
+# holds its tiles, else global-memory).  On the 256-member workload per-iteration coarse kernels and 32 or 64
+# members in flight were slower in every trial (GB300), so they are left out of the default set.
+DEFAULT_CANDIDATES = tuple(dict(concurrency=s, coarse_kernel="auto", stencil_kernel=sk) for s in (8, 12, 16, 24)
+                           for sk in ("tiled", "streaming"))
 
 
 def autotune(grids, solver_params, params, make_tensors, precision="mixed", device=0, candidates=DEFAULT_CANDIDATES,
-             picard=2, sync=None):
+             picard=8, sync=None):
     """Pick the ensemble launch configuration: for each candidate (keyword arguments of EnsembleSolver:
     members in flight, coarse-CG kernel, stencil kernel) time one ensemble solve capped at `picard`
-    Picard iterations, after one untimed solve that instantiates the graphs.  `make_tensors()` returns
+    Picard iterations, after one untimed solve that instantiates the graphs.  The first V-cycles of a solve
+    run on the cold, all-true coarse space and cost far more than the later ones, so a cap of 2 ranked the
+    candidates differently from whole solves; 8 reaches the V-cycles a solve spends most of its time in.  `make_tensors()` returns
     fresh device copies of every member's fields.  Returns (best candidate, [(seconds, candidate), ...])."""
     capped = [dataclasses.replace(sp, maxiter_picard=picard) for sp in solver_params]
     timings = []
