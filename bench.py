@@ -31,8 +31,8 @@ reference's other solver parameters).
 threads at once, one step) and prints its own line.
 Under torchrun (N > 1) every rank solves its own replica (no collective); value is the sum.
 ``--profile solve|op|relin`` runs one small untimed case for ncu (a host-driven solve of the workload
-capped at ``--picard`` Picard iterations, operator launches on the 4096 x 1024 grid, or the relinearisation
-kernels on the 2560 x 320, nσ = 8 grid) and prints nothing.
+capped at ``--picard`` Picard iterations — of the 2560 x 320 state with ``--config c3`` —, operator launches
+on the 4096 x 1024 grid, or the relinearisation kernels on the 2560 x 320, nσ = 8 grid) and prints nothing.
 """
 import argparse
 import json
@@ -929,7 +929,14 @@ def profile_case(args):
         torch.cuda.synchronize()
         s.close()
         return 0
-    m = build_state(None)
+    if args.config == "c3":  # the 2560 x 320, nσ = 8 state instead of the 640 x 80 workload
+        from wavi_gb300 import synthetic
+        from wavi_gb300.model import GPUParallelSpec, Model, pre_solve
+        g3, bed3, p3, sp3, ic3 = synthetic.channel_c3(tol_picard=1e-6, maxiter_picard=30)
+        m = Model(g3, bed3, p3, sp3, ic3, parallel_spec=GPUParallelSpec(precision="fp64"))
+        pre_solve(m)
+    else:
+        m = build_state(None)
     snapshot = {k: np.array(v, copy=True) for k, v in m.fields.items()}
     release_solver(m)
     sp = SolverParams(**{**m.solver_params.__dict__, "maxiter_picard": args.picard})
