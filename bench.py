@@ -788,7 +788,7 @@ def ensemble_arm(args):
                 "others stall the same way in FP64 (the reference algorithm's one V-cycle per Picard iteration). "
                 "ensemble_over_fp64_loop compares member solves per second, converged or not, on both sides",
         "picard_iterations_mean": float(np.mean([st["picard_iterations"] for st in stats])),
-        "autotune": [{"seconds": t, **c} for t, c in timings],
+        "autotune": [{"seconds": t, "stage": stage, **c} for t, c, stage in timings],
     }
     print(json.dumps(line), flush=True)
     return 0

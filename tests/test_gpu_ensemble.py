@@ -87,6 +87,9 @@ def test_autotune_picks_a_candidate(oracle):
     mem = _members(oracle, maxiter_picard=5)
     cands = (dict(concurrency=2, coarse_kernel="auto"), dict(concurrency=6, coarse_kernel="iterations"))
     best, timings = autotune([m[0] for m in mem], [m[2] for m in mem], [m[1] for m in mem],
-                             lambda: [to_dev(m[4], torch) for m in mem], candidates=cands,
+                             lambda: [to_dev(m[4], torch) for m in mem], candidates=cands, picard=2, finalists=1,
                              sync=torch.cuda.synchronize)
-    assert best in cands and len(timings) == 2 and all(t > 0 for t, _ in timings)
+    # two capped solves, then the whole solve of the faster one, which is the choice
+    assert best in cands and len(timings) == 3 and all(t > 0 for t, _, _ in timings)
+    assert [st for _, _, st in timings] == ["capped", "capped", "whole"]
+    assert timings[2][1] == best == min(timings[:2], key=lambda t: t[0])[1]

@@ -451,8 +451,11 @@ static __global__ void k_relin_uv(Dims d, RelinUVIn in, RelinUVOut out) {
     if (in.mask[q]) {
       const double num = 0.5 * hv(in.beta_eff, a0, b0) + 0.5 * hv(in.beta_eff, a1, b1);
       const double den = 0.5 * hmk(a0, b0) + 0.5 * hmk(a1, b1);
-      double be = num / den;
-      const double ip = (0.5 * hv(in.gf, a0, b0) + 0.5 * hv(in.gf, a1, b1)) / den;
+      // den is 0, 0.5 or 1, so x / den is exactly x * (1 / den) — also 0 * inf = NaN = 0 / 0 and
+      // x * inf = ±inf = x / 0 — without an FP64 division (a long sequence on GB300's FP64 pipe)
+      const double rden = den == 1.0 ? 1.0 : den == 0.5 ? 2.0 : 1.0 / den;
+      double be = num * rden;
+      const double ip = (0.5 * hv(in.gf, a0, b0) + 0.5 * hv(in.gf, a1, b1)) * rden;
       if (ip > 0.0) be = be * in.gf_uv[q] / ip;
       out.beta_eff_uv[q] = be;
       bm = be;

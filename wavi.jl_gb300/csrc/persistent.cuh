@@ -1824,7 +1824,9 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
 // ------------------------------------------------------------------------------------------------
 // Grids whose tiles outnumber the device's resident CTAs: the same two solvers with the CG vectors in
 // global memory (L2-resident up to ~10^7 unknowns), each CTA looping over tiles t = blockIdx.x + k·gridDim.x
-// in every phase.  The arithmetic and its order are those of the register-resident kernels above.
+// in every phase.  The arithmetic and its order are those of the register-resident kernels above.  Their
+// tile passes wait on L2 loads (ncu at 2560x320: long-scoreboard stalls first, 25 % of warps active at two
+// CTAs per SM), so the 16 x 16 instantiations are held to 64 registers for four resident CTAs per SM.
 // Vectors (full layout, N entries): xc (iterate, in place), gr (residual), gz (z = M⁻¹ r, or cg!'s
 // direction u), gp, gs (C-G recurrences, or cg!'s c = R A u in gp), gw (R A z), w (prolonged vector).
 // ------------------------------------------------------------------------------------------------
@@ -1834,7 +1836,7 @@ struct GlobalCG {
 };
 
 template <typename T, int TILE>
-__global__ void __launch_bounds__(TILE* TILE)
+__global__ void __launch_bounds__(TILE* TILE, TILE == 16 ? 4 : 1)
     k_srcg_global(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, const T* __restrict__ dcoarse,
                   T* __restrict__ w, const T* __restrict__ bc, T* __restrict__ xc, GlobalCG<T> g,
                   double* __restrict__ partials, DevState* st, const DevParams* __restrict__ P, GridBar* bar, int ntx,
@@ -1961,7 +1963,7 @@ __global__ void __launch_bounds__(TILE* TILE)
 // a buffer is rewritten only after the barrier that follows the pass in which every CTA read it.
 // gcd holds the Chebyshev direction.
 template <typename T, int TILE>
-__global__ void __launch_bounds__(TILE* TILE)
+__global__ void __launch_bounds__(TILE* TILE, TILE == 16 ? 4 : 1)
     k_srcg_cheb_global(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask,
                        const T* __restrict__ dcoarse, T* __restrict__ w, T* __restrict__ w2, const T* __restrict__ bc,
                        T* __restrict__ xc, GlobalCG<T> g, T* __restrict__ gcd, T* __restrict__ eig, int cheb,
@@ -2180,7 +2182,7 @@ __global__ void __launch_bounds__(TILE* TILE)
 
 // cg! with global vectors: gz holds the direction u, gp holds c = R A u.
 template <typename T, int TILE>
-__global__ void __launch_bounds__(TILE* TILE)
+__global__ void __launch_bounds__(TILE* TILE, TILE == 16 ? 4 : 1)
     k_cg_global(Dims d, int levels, OpCoef<T> cf, const uint8_t* __restrict__ wmask, T* __restrict__ w,
                 const T* __restrict__ bc, T* __restrict__ xc, GlobalCG<T> g, double* __restrict__ partials, DevState* st,
                 const DevParams* __restrict__ P, GridBar* bar, int ntx, int nty) {

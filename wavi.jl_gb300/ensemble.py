@@ -65,17 +65,20 @@ DEFAULT_CANDIDATES = tuple(dict(concurrency=s, coarse_kernel="auto", stencil_ker
 
 
 def autotune(grids, solver_params, params, make_tensors, precision="mixed", device=0, candidates=DEFAULT_CANDIDATES,
-             picard=8, sync=None):
-    """Pick the ensemble launch configuration: for each candidate (keyword arguments of EnsembleSolver:
-    members in flight, coarse-CG kernel, stencil kernel) time one ensemble solve capped at `picard`
-    Picard iterations, after one untimed solve that instantiates the graphs.  The first V-cycles of a solve
-    run on the cold, all-true coarse space and cost far more than the later ones, so a cap of 2 ranked the
-    candidates differently from whole solves; 8 reaches the V-cycles a solve spends most of its time in.  `make_tensors()` returns
-    fresh device copies of every member's fields.  Returns (best candidate, [(seconds, candidate), ...])."""
+             picard=8, finalists=3, sync=None):
+    """Pick the ensemble launch configuration in two stages.  First, for each candidate (keyword arguments
+    of EnsembleSolver: members in flight, coarse-CG kernel, stencil kernel), time one ensemble solve capped
+    at `picard` Picard iterations, after one untimed solve that instantiates the graphs.  Then time one
+    whole solve (the members' own Picard limits) of each of the `finalists` fastest and keep the fastest of
+    those.  The capped solves are dominated by the first V-cycles, on the cold all-true coarse space, and
+    miss the tail of members that take many Picard iterations, so they rank the candidates only roughly.
+    `make_tensors()` returns fresh device copies of every member's fields.  Returns (best candidate,
+    [(seconds, candidate, stage), ...])."""
     capped = [dataclasses.replace(sp, maxiter_picard=picard) for sp in solver_params]
     timings = []
-    for cand in candidates:
-        ens = EnsembleSolver(grids, capped, precision=precision, device=device, **cand)
+
+    def timed(cand, sps):
+        ens = EnsembleSolver(grids, sps, precision=precision, device=device, **cand)
         try:
             ens.solve_device(params, make_tensors())
             tensors = make_tensors()
@@ -83,8 +86,16 @@ def autotune(grids, solver_params, params, make_tensors, precision="mixed", devi
                 sync()
             t0 = time.perf_counter()
             ens.solve_device(params, tensors)
-            timings.append((time.perf_counter() - t0, cand))
+            return time.perf_counter() - t0
         finally:
             ens.close()
-    best = min(timings, key=lambda tc: tc[0])[1]
+
+    for cand in candidates:
+        timings.append((timed(cand, capped), cand, "capped"))
+    ranked = sorted(timings, key=lambda t: t[0])[:max(1, finalists)]
+    full = []
+    for _, cand, _ in ranked:
+        full.append((timed(cand, solver_params), cand, "whole"))
+    timings += full
+    best = min(full, key=lambda t: t[0])[1]
     return best, timings
