@@ -137,8 +137,7 @@ typedef enum wavi_coarse_sums {
  * compute both inner products of an iteration in one grid reduction, keep cg!'s stopping rule on the
  * unpreconditioned residual, and need the persistent coarse kernel. */
 typedef enum wavi_coarse_solver {
-  WAVI_COARSE_AUTO = 0,              /* FP64: cg!; mixed: SRCG_CHEBYSHEV when the ice mask covers the whole
-                                        domain, else cg! */
+  WAVI_COARSE_AUTO = 0,              /* FP64: cg!; mixed: SRCG_CHEBYSHEV (cg! with per-iteration kernels) */
   WAVI_COARSE_CG = 1,                /* the reference's cg! recurrence */
   WAVI_COARSE_SRCG = 2,              /* single-reduction CG, no preconditioner (same iterates as cg!) */
   WAVI_COARSE_SRCG_JACOBI = 3,       /* single-reduction CG preconditioned by diag(R A P) */

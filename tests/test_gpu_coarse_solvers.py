@@ -139,9 +139,15 @@ def test_chebyshev_on_the_global_memory_kernel_matches_the_register_kernel(oracl
     assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(a)
 
 
-def test_mixed_default_is_chebyshev_on_full_masks(oracle):
+def test_mixed_default_is_chebyshev(oracle):
+    """The mixed default coarse solver is the Chebyshev single-reduction CG, on full and on masked domains;
+    FP64 keeps the reference's cg!."""
     from wavi_gb300.gpu import VelocitySolver
-    for name, want in (("full", "srcg_chebyshev"), ("disc", "cg")):
+    g, p, sp, om = _setup(oracle, "disc", maxiter_picard=2)
+    s = VelocitySolver(g, sp, precision="fp64")
+    assert s.solve(p, fields_from_oracle(om, g))["coarse_solver"] == "cg"
+    s.close()
+    for name, want in (("full", "srcg_chebyshev"), ("disc", "srcg_chebyshev"), ("fixed", "srcg_chebyshev")):
         g, p, sp, om = _setup(oracle, name, maxiter_picard=2)
         f = fields_from_oracle(om, g)
         s = VelocitySolver(g, sp, precision="mixed")

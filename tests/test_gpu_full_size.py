@@ -91,13 +91,16 @@ def test_operator_symmetry_sign_and_fp32_at_full_size(c3):
     x = torch.randn(inner.numel(), dtype=torch.float64, device="cuda") * inner
     z = torch.randn(inner.numel(), dtype=torch.float64, device="cuda") * inner
     ax, az = torch.zeros_like(x), torch.zeros_like(x)
+    torch.cuda.synchronize()  # the library runs on its context's own stream: x and z must be written first
     s.apply_operator_device(x, ax, "fp64")
     s.apply_operator_device(z, az, "fp64")
     lhs, rhs = float(torch.dot(ax, z)), float(torch.dot(x, az))
     assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs))
     assert float(torch.dot(ax, x)) < 0
     ax32 = torch.zeros_like(x, dtype=torch.float32)
-    sm.apply_operator_device(x.float(), ax32, "mixed")
+    x32 = x.float()
+    torch.cuda.synchronize()
+    sm.apply_operator_device(x32, ax32, "mixed")
     assert float(torch.linalg.norm(ax32.double() - ax) / torch.linalg.norm(ax)) < 1e-5
     s.close()
     sm.close()
@@ -112,6 +115,7 @@ def test_haar_transforms_at_full_size(c3):
     x = torch.randn(n, dtype=torch.float64, device="cuda")
     z = torch.randn(n, dtype=torch.float64, device="cuda")
     px, back, rz = torch.zeros_like(x), torch.zeros_like(x), torch.zeros_like(x)
+    torch.cuda.synchronize()  # the library runs on its context's own stream
     s.haar_device(0, x, px, ones)      # idwt x
     s.haar_device(2, px, back, ones)   # dwt(idwt x)
     assert float(torch.linalg.norm(back - x) / torch.linalg.norm(x)) < 1e-13

@@ -44,6 +44,7 @@ def test_device_wavelet_mask_is_bit_exact(oracle, name):
         ref = _cat(om.mask("wu_mask"), om.mask("wv_mask")).astype(np.uint8)
         uv = torch.from_numpy(_cat(u, v)).cuda()
         out = torch.full((ref.size,), 7, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()  # the library runs on its context's own stream: the fill must be done first
         s.update_wavelets_device(uv, out)
         got = out.cpu().numpy()
         assert got.max() <= 1

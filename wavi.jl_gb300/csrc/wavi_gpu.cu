@@ -1503,13 +1503,11 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   c->visc32 = mixed(c) && opt->viscosity != WAVI_VISCOSITY_FP64;
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));
-  // auto: FP64 runs the reference's cg!; mixed runs the Chebyshev-Jacobi single-reduction CG on domains
-  // whose ice mask is full (register-resident or, on grids too large for that, global-memory), and cg! where the
-  // mask cuts the domain (calving fronts inside it): there the masked Haar functions can coincide on the
-  // interior and R A P turns singular
-  bool full_mask = true;
-  for (int i = 0; i < d.Nh && full_mask; ++i) full_mask = hm[i] != 0;
-  c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) && full_mask ? WAVI_COARSE_SRCG_CHEBYSHEV : WAVI_COARSE_CG) : want;
+  // auto: FP64 runs the reference's cg!; mixed runs the Chebyshev-Jacobi single-reduction CG (register-
+  // resident or, on grids too large for that, global-memory), also where the ice mask cuts the domain: there
+  // masked Haar functions can coincide on the interior and R A P turns singular, which the FP32 solve
+  // survives because a coarse solve that misses its tolerance does not become the next warm start
+  c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) ? WAVI_COARSE_SRCG_CHEBYSHEV : WAVI_COARSE_CG) : want;
   c->acc64 = mixed(c) && opt->coarse_sums == WAVI_SUMS_FP64;
   if (c->acc64 && (c->tile != 16 || opt->coarse_kernel == 2 || opt->coarse_kernel == 3 || c->coarse_solver == WAVI_COARSE_CG ||
                    c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV))

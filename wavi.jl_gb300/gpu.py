@@ -8,6 +8,7 @@ Field names are those of ``wavi_fields``; arrays are float64, Fortran order, ref
 There is no CPU fallback: construction raises if the library or a GPU is missing.
 """
 import ctypes as C
+import sys
 
 import numpy as np
 
@@ -72,6 +73,18 @@ class VelocitySolver:
     def _err(self, st):
         return abi.WaviError(st, self.lib.wavi_last_error(self.ctx).decode())
 
+    def _after_caller(self):
+        """Order the context's stream (a non-blocking stream of its own) after the work already queued on
+        torch's current CUDA stream, so that device tensors a caller has just written with torch are
+        complete before the library reads them and not overwritten after it writes them.  Nothing to do
+        when torch is not in use (other callers order their streams themselves, wavi_ctx_stream)."""
+        torch = sys.modules.get("torch")
+        if torch is None or not torch.cuda.is_available():
+            return
+        cur = torch.cuda.current_stream()
+        if cur.cuda_stream != self.stream():
+            torch.cuda.ExternalStream(self.stream()).wait_stream(cur)
+
     # -- host arrays -------------------------------------------------------------------------------
     def _host_fields(self, fields):
         f = abi.Fields()
@@ -117,6 +130,7 @@ class VelocitySolver:
         """update_velocities! on device tensors (dict of name -> tensor with data_ptr()), in place."""
         f = self._device_fields(tensors)
         stats = abi.Stats()
+        self._after_caller()
         st = self.lib.wavi_solve_velocities_device(self.ctx, C.byref(params.to_c()), C.byref(f), C.byref(stats))
         if st != 0:
             raise self._err(st)
@@ -124,11 +138,13 @@ class VelocitySolver:
 
     def relinearise_device(self, params, tensors):
         f = self._device_fields(tensors)
+        self._after_caller()
         st = self.lib.wavi_relinearise_device(self.ctx, C.byref(params.to_c()), C.byref(f))
         if st != 0:
             raise self._err(st)
 
     def apply_operator_device(self, in_uv, out_uv, precision="fp64"):
+        self._after_caller()
         st = self.lib.wavi_apply_operator_device(self.ctx, PRECISIONS[precision], C.c_void_p(in_uv.data_ptr()),
                                                  C.c_void_p(out_uv.data_ptr()))
         if st != 0:
@@ -137,6 +153,7 @@ class VelocitySolver:
     def time_operator_device(self, in_uv, out_uv, precision="fp64", repeats=200):
         """Mean duration (s) of one operator launch over `repeats` back-to-back launches (CUDA events)."""
         ms = C.c_double()
+        self._after_caller()
         st = self.lib.wavi_time_operator_device(self.ctx, PRECISIONS[precision], C.c_void_p(in_uv.data_ptr()),
                                                 C.c_void_p(out_uv.data_ptr()), int(repeats), C.byref(ms))
         if st != 0:
@@ -147,12 +164,14 @@ class VelocitySolver:
         """Mean durations (s) of one launch of the relinearisation's h-grid and u/v-grid kernels over
         `repeats` back-to-back launches each, on the fields of the last solve or relinearisation."""
         mh, muv = C.c_double(), C.c_double()
+        self._after_caller()
         st = self.lib.wavi_time_relinearise_device(self.ctx, int(repeats), C.byref(mh), C.byref(muv))
         if st != 0:
             raise self._err(st)
         return mh.value / 1e3, muv.value / 1e3
 
     def op_diagonal_device(self, out_uv, precision="fp64"):
+        self._after_caller()
         st = self.lib.wavi_op_diagonal_device(self.ctx, PRECISIONS[precision], C.c_void_p(out_uv.data_ptr()))
         if st != 0:
             raise self._err(st)
@@ -171,6 +190,7 @@ class VelocitySolver:
             setattr(outs, k, t.data_ptr())
         f = device_fields(tensors)
         stats = abi.Stats()
+        self._after_caller()
         st = self.lib.wavi_run_device(self.ctx, C.byref(params.to_c()), float(dt), int(nsteps), C.byref(ins),
                                       C.byref(f), C.byref(outs), C.byref(stats))
         if st != 0:
@@ -182,6 +202,7 @@ class VelocitySolver:
         """Gradient of J w.r.t. per-cell log C and log A at the last solve's fixed point, from dJ/du, dJ/dv
         (device tensors in reference shapes, flattened column-major); writes grad_logC, grad_logA (nx*ny)."""
         st = abi.AdjointStats()
+        self._after_caller()
         r = self.lib.wavi_adjoint_device(self.ctx, C.byref(params.to_c()), C.c_void_p(dJ_du.data_ptr()),
                                          C.c_void_p(dJ_dv.data_ptr()), C.c_void_p(grad_logC.data_ptr()),
                                          C.c_void_p(grad_logA.data_ptr()), float(tol), int(maxiter), C.byref(st))
@@ -194,6 +215,7 @@ class VelocitySolver:
         """(du, dv) = d(u, v)/d(log C, log A) · (dlogC, dlogA) at the last solve's fixed point."""
         st = abi.AdjointStats()
         ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+        self._after_caller()
         r = self.lib.wavi_tangent_device(self.ctx, C.byref(params.to_c()), ptr(dlogC), ptr(dlogA), ptr(du), ptr(dv),
                                          float(tol), int(maxiter), C.byref(st))
         if r != 0:
@@ -203,6 +225,7 @@ class VelocitySolver:
 
     def coarse_diagonal_device(self, out_uv, precision="fp64"):
         """diag(R A P) for the current coefficients and wavelet mask, on the full wavelet grids."""
+        self._after_caller()
         st = self.lib.wavi_coarse_diagonal_device(self.ctx, PRECISIONS[precision], C.c_void_p(out_uv.data_ptr()))
         if st != 0:
             raise self._err(st)
@@ -218,12 +241,14 @@ class VelocitySolver:
     def update_wavelets_device(self, in_uv, wmask_out):
         """update_wavelets! with the device time step's kernels: the context's wavelet mask from the float64
         velocities in_uv ([u | v]), copied to the uint8 device tensor wmask_out."""
+        self._after_caller()
         st = self.lib.wavi_update_wavelets_device(self.ctx, C.c_void_p(in_uv.data_ptr()), C.c_void_p(wmask_out.data_ptr()))
         if st != 0:
             raise self._err(st)
 
     def haar_device(self, kind, in_uv, out_uv, mask_uv=None):
         m = C.c_void_p(mask_uv.data_ptr()) if mask_uv is not None else None
+        self._after_caller()
         st = self.lib.wavi_haar_device(self.ctx, int(kind), C.c_void_p(in_uv.data_ptr()), C.c_void_p(out_uv.data_ptr()), m)
         if st != 0:
             raise self._err(st)
