@@ -26,6 +26,9 @@ reference's other solver parameters).
            application, larger than L2), back-to-back launches timed with CUDA events
   cpu_baseline the CPU oracle (the FP64 restatement of the reference) on a bounded sample: the first
            iterations of the solve on every host thread, scaled by the oracle's own profile
+  other_configs compact lines of the 2560 x 320 domain (c3), the adjoint (c4) and the 256-member ensemble
+           (c5), measured after the timed work (one GPU; --no-extras leaves them out; --config c3/c4/c5
+           gives each in full)
 
 ``--impl reference`` times only the CPU oracle on all host cores (a whole converged solve per thread, all
 threads at once, one step) and prints its own line.
@@ -553,13 +556,49 @@ def gpu_arm(args):
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     mixed.close()
     fp64.close()
+    if rank == 0 and world == 1 and not args.no_extras:
+        line["other_configs"] = other_configs(args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def other_configs(args):
+    """Compact lines of the other configurations, measured in the same run after the timed C2 work (one GPU,
+    rank 0): the large single domain (2560x320, nσ = 8), the 256-member ensemble (the autotuner's choice
+    on GB300, one timed ensemble) and the adjoint (two finite-difference directions).  Each runs on its
+    own; a failure is reported in its entry and leaves the C2 line intact."""
+    import copy
+    out = {}
+    legs = (("c3", c3_arm, dict(steps=1, warmup=1),
+             ("metric", "value", "unit", "ms_per_step", "solve", "mixed_uncapped", "fp64_gpu", "mixed_over_fp64",
+              "rel_err_mixed_vs_fp64", "roofline", "roofline_relin_fp64", "roofline_stencil", "coarse_cg_share")),
+            ("c5", ensemble_arm, dict(steps=1, warmup=1, no_tune=True, members=256),
+             ("metric", "value", "unit", "ms_per_step", "members_converged", "all_members", "fp64_loop",
+              "ensemble_over_fp64_loop", "rel_err_vs_fp64_max", "rel_err_vs_fp64_median", "picard_iterations_mean")),
+            ("c4", adjoint_arm, dict(steps=2, warmup=1, directions=2),
+             ("metric", "value", "unit", "ms_per_step", "forward", "adjoint", "dot_test_rel_err", "fd_step",
+              "fd_directions", "fd_max_rel_err")))
+    for name, arm, kw, keys in legs:
+        sub = copy.copy(args)
+        for k, v in kw.items():
+            setattr(sub, k, v)
+        sub.quiet = True
+        t0 = time.perf_counter()
+        try:
+            ln = arm(sub)
+            entry = {k: ln[k] for k in keys if k in ln}
+            if name == "c5":
+                entry["launch"] = ln["config"]["launch"]
+        except Exception as e:  # reported, not fatal: the C2 line stands on its own
+            entry = {"error": f"{type(e).__name__}: {e}"}
+        entry["wall_s"] = time.perf_counter() - t0
+        out[name] = entry
+    return out
 
 
 C3_WORKLOAD = ("2560x320 channel @250m, nsigma=8, log-normal C (median 1e4, sigma_log 0.5, 20 km correlation, seed 3), "
@@ -698,6 +737,8 @@ def c3_arm(args):
                             "us_per_cg_iteration": 1e3 * stp["coarse_ms"] / max(1, stp["coarse_cg_iterations"])},
         "clocks": clocks,
     }
+    if getattr(args, "quiet", False):
+        return line
     print(json.dumps(line), flush=True)
     return 0
 
@@ -737,8 +778,8 @@ def ensemble_arm(args):
         return [{k: t.clone() for k, t in d.items()} for d in dev]
 
     n = len(grids)
-    if args.no_tune:
-        best, timings = dict(concurrency=16, coarse_kernel="auto"), []
+    if args.no_tune:  # the autotuner's choice on GB300 for this workload
+        best, timings = dict(concurrency=8, coarse_kernel="auto", stencil_kernel="tiled"), []
     else:
         best, timings = autotune(grids, sps, params, make_tensors, sync=torch.cuda.synchronize)
     ens = EnsembleSolver(grids, sps, precision="mixed", **best)
@@ -790,6 +831,8 @@ def ensemble_arm(args):
         "picard_iterations_mean": float(np.mean([st["picard_iterations"] for st in stats])),
         "autotune": [{"seconds": t, "stage": stage, **c} for t, c, stage in timings],
     }
+    if getattr(args, "quiet", False):
+        return line
     print(json.dumps(line), flush=True)
     return 0
 
@@ -891,8 +934,10 @@ def adjoint_arm(args):
         "fd_step_sweep": {str(h): e for h, e in sweep.items()}, "fd_step": h_best,
         "fd_directions": len(errs), "fd_max_rel_err": max(errs), "fd_median_rel_err": float(np.median(errs)),
     }
-    print(json.dumps(line), flush=True)
     solver.close()
+    if getattr(args, "quiet", False):
+        return line
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -980,7 +1025,12 @@ def main():
     ap.add_argument("--directions", type=int, default=20, help="--config c4: finite-difference directions")
     ap.add_argument("--members", type=int, default=256, help="--config c5: ensemble members")
     ap.add_argument("--no-tune", action="store_true", help="--config c5: skip the autotuner")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="c2: leave out the compact c3/c4/c5 lines measured after the timed work")
     args = ap.parse_args()
+    # more hardware work queues than the default 8, so that the ensemble's concurrent members do not
+    # serialise (set before the first CUDA call: the default line measures the ensemble too)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     if args.profile:
         return profile_case(args)
     if args.config == "c3":
@@ -988,8 +1038,6 @@ def main():
     if args.config == "c4":
         return adjoint_arm(args)
     if args.config == "c5":
-        # more hardware work queues than the default 8, so that concurrent members do not serialise
-        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
         return ensemble_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
