@@ -16,6 +16,9 @@ reference's other solver parameters).
            the gain of precision alone, mixed_over_fp64 that of precision and coarse solver together
   rel_err_*_vs_oracle  relative velocity error of each GPU solve against the FP64 oracle's converged solve
            of the same state (tests/golden/c2_oracle_solution.npz)
+  mixed_fp64_coarse_sums / mixed_fp64_coarse_solve  the mixed solve with the coarse CG's sums, or the
+           whole coarse CG, in FP64 (wavi_coarse_sums): what the default's float-float sums and FP32 coarse
+           solve save
   roofline the dominant kernel of the step, the persistent coarse CG (k_srcg_persistent<float>), timed
            with CUDA events around each launch in a host-driven solve of the same state; per CG
            iteration: algorithmic bytes / duration against the measured HBM peak for scale.  Its working
@@ -458,6 +461,22 @@ def gpu_arm(args):
                       "coarse_cg_iterations": stm64[-1]["coarse_cg_iterations"],
                       "status_name": stm64[-1]["status_name"]}
 
+    # the mixed solve with its whole coarse CG in FP64 (WAVI_SUMS_FP64_SOLVE)
+    solve64, outc64 = None, None
+    if mixed_solver != "pipelined_chebyshev":
+        try:
+            mc64 = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=mixed_solver,
+                                  cheb_steps=args.cheb_steps, coarse_sums="fp64_solve", viscosity=args.viscosity)
+        except Exception as e:  # reported, not fatal
+            solve64 = {"unavailable": str(e)}
+        else:
+            tc64, stc64, outc64 = time_device_solves(torch, mc64, p, snapshot, max(1, args.steps // 2), 1)
+            mc64.close()
+            solve64 = {"value": world * len(tc64) / sum(tc64), "unit": "solves/s",
+                       "ms_per_step": 1e3 * sum(tc64) / len(tc64), "picard_iterations": stc64[-1]["picard_iterations"],
+                       "coarse_cg_iterations": stc64[-1]["coarse_cg_iterations"],
+                       "status_name": stc64[-1]["status_name"]}
+
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     # dominant kernel: the persistent coarse CG, per CG iteration, timed launch by launch in host-driven solves;
@@ -504,6 +523,8 @@ def gpu_arm(args):
             errs_oracle["rel_err_fp64_same_solver_vs_oracle"] = rel_err_uv(out64s["u"], out64s["v"], ref["u"], ref["v"])
         if outm64 is not None:
             sums64["rel_err_vs_oracle"] = rel_err_uv(outm64["u"], outm64["v"], ref["u"], ref["v"])
+        if outc64 is not None:
+            solve64["rel_err_vs_oracle"] = rel_err_uv(outc64["u"], outc64["v"], ref["u"], ref["v"])
         errs_oracle["oracle"] = {"picard_iterations": int(ref["picard_iterations"]),
                                  "coarse_cg_iterations": int(ref["coarse_cg_iterations"]),
                                  "rel_residual": float(ref["rel_residual"]),
@@ -530,6 +551,7 @@ def gpu_arm(args):
         "mixed_over_fp64": value / fp64_value if fp64_value else None,
         "mixed_over_fp64_same_solver": value / same["value"] if same else None,
         "mixed_fp64_coarse_sums": sums64,
+        "mixed_fp64_coarse_solve": solve64,
         "rel_err_mixed_vs_fp64": float(err),
         **errs_oracle,
         "solve": {k: stmix[-1][k] for k in ("picard_iterations", "coarse_cg_iterations", "op_applications",

@@ -127,9 +127,14 @@ typedef enum wavi_coarse_sums {
   WAVI_SUMS_DEFAULT = 0,             /* WAVI_SUMS_FLOAT_FLOAT */
   WAVI_SUMS_FLOAT_FLOAT = 1,         /* FP32 products, warp and CTA sums; float-float (~48-bit) grid sums
                                         and CG scalars */
-  WAVI_SUMS_FP64 = 2                 /* every product and sum of the reductions, and the CG scalars, in FP64
+  WAVI_SUMS_FP64 = 2,                /* every product and sum of the reductions, and the CG scalars, in FP64
                                         from the FP32 vectors; the single-reduction solvers on the
                                         register-resident 16 x 16 kernel only */
+  WAVI_SUMS_FP64_SOLVE = 3           /* the whole coarse CG in FP64 — vectors, the coarse operator on the FP64
+                                        coefficients, sums and scalars (the kernels of FP64 contexts) —
+                                        inside the FP32 V-cycle, which hands it the restricted residual and
+                                        takes back its solution; persistent coarse kernels, not the
+                                        pipelined solver */
 } wavi_coarse_sums;
 
 /* Coarse solve of each V-cycle (R A P x = b_c, update_preconditioners.jl:54-83).  The reference calls

@@ -221,3 +221,32 @@ def test_fp64_coarse_sums_need_the_single_reduction_register_kernel(oracle):
         VelocitySolver(g, SolverParams(levels=4), precision="mixed", coarse_sums="fp64", coarse_solver="srcg_jacobi")
     s = VelocitySolver(g, sp, precision="fp64", coarse_sums="fp64")  # FP64 contexts sum in FP64 anyway
     s.close()
+
+
+@pytest.mark.parametrize("kernel", ["persistent", "persistent_global"])
+@pytest.mark.parametrize("name", ["full", "disc"])
+def test_fp64_coarse_solve_in_the_mixed_vcycle(oracle, name, kernel):
+    """WAVI_SUMS_FP64_SOLVE: the mixed V-cycle with its coarse CG in FP64 (the FP64 contexts' kernels on the
+    FP64 coefficients, the restricted residual widened and the solution narrowed): the converged solve
+    reaches the reference's fixed point to 1e-6 and uses the FP64 coarse kernel's stopping rule."""
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, name, maxiter_picard=80, tol_picard=1e-7)
+    f0 = fields_from_oracle(om, g)
+    om.update_velocities()
+    f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
+    s = VelocitySolver(g, sp, precision="mixed", coarse_kernel=kernel, coarse_sums="fp64_solve")
+    st = s.solve(p, f)
+    s.close()
+    print(name, kernel, st["picard_iterations"], st["coarse_cg_iterations"], st["coarse_solver"], uv_err(f, om))
+    assert st["status"] == 0, st
+    assert st["coarse_solver"] == "srcg_chebyshev"
+    assert uv_err(f, om) < 1e-6, st
+
+
+def test_fp64_coarse_solve_needs_a_persistent_kernel(oracle):
+    from wavi_gb300.abi import WaviError
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, "full")
+    for kw in (dict(coarse_kernel="iterations"), dict(coarse_solver="pipelined_chebyshev")):
+        with pytest.raises(WaviError, match="WAVI_ERR_ARGUMENT"):
+            VelocitySolver(g, sp, precision="mixed", coarse_sums="fp64_solve", **kw)

@@ -24,7 +24,7 @@ PRECISION_MIXED = 1
 
 COARSE_SOLVERS = {"auto": 0, "cg": 1, "srcg": 2, "srcg_jacobi": 3, "srcg_chebyshev": 4, "pipelined_chebyshev": 5}  # wavi_coarse_solver
 COARSE_SOLVER_NAMES = {v: k for k, v in COARSE_SOLVERS.items()}
-COARSE_SUMS = {"default": 0, "float_float": 1, "fp64": 2}  # wavi_coarse_sums
+COARSE_SUMS = {"default": 0, "float_float": 1, "fp64": 2, "fp64_solve": 3}  # wavi_coarse_sums
 VISCOSITY = {"default": 0, "fp32": 1, "fp64": 2}  # wavi_viscosity
 
 _dp = C.POINTER(C.c_double)

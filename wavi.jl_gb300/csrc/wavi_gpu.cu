@@ -129,6 +129,8 @@ struct wavi_ctx {
   int pers_maxt = 0, pers_grid = 0, ntx = 0, nty = 0;  // pers_maxt -1: CG vectors in global memory
   void *gz = nullptr, *gw = nullptr;                    // extra vectors of the global-memory variant
   void *w2 = nullptr, *gcd = nullptr;                   // its Chebyshev solve: second prolongation buffer, direction
+  bool coarse64 = false;                                // mixed: the coarse CG in FP64 (WAVI_SUMS_FP64_SOLVE)
+  double *bc64 = nullptr, *xc64 = nullptr;              // its right-hand side and iterate
   int coarse_solver = WAVI_COARSE_CG;  // resolved coarse solver (never WAVI_COARSE_AUTO)
   void* dcoarse = nullptr;             // diag(R A P) for the Jacobi-preconditioned single-reduction CG
   void* cheb_eig = nullptr;            // the Chebyshev coarse solve's power vector (kept across V-cycles)
@@ -437,7 +439,9 @@ int cheb_steps(const wavi_ctx* c) { return c->opt.cheb_steps > 0 ? c->opt.cheb_s
 constexpr float kChebRatio = 120.0f;
 
 template <typename T, int TILE, int MAXT>
-int launch_cg_persistent(wavi_ctx* c) {
+int launch_cg_persistent(wavi_ctx* c, const void* bcv, void* xcv) {
+  const T* bc = (const T*)bcv;
+  T* xc = (T*)xcv;
   const Dims& d = c->d;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)c->pers_grid);
@@ -451,12 +455,12 @@ int launch_cg_persistent(wavi_ctx* c) {
   cfg.numAttrs = 1;
   if (c->coarse_solver == WAVI_COARSE_CG) {
     CK(cudaLaunchKernelEx(&cfg, k_cg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
-                          (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
+                          (T*)c->w, bc, xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
                           c->halo_box, c->ntx, c->nty));
   } else if (c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV) {
     if constexpr (std::is_same<T, float>::value && TILE == 16 && MAXT <= 2) {
       CK(cudaLaunchKernelEx(&cfg, k_pcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c),
-                            (const uint8_t*)c->wmask_uv, (const T*)c->dcoarse, (const T*)c->bc, (T*)c->xc, c->partials,
+                            (const uint8_t*)c->wmask_uv, (const T*)c->dcoarse, bc, xc, c->partials,
                             c->S, (const DevParams*)c->P, c->bar, c->halo_box, cheb_steps(c), kChebRatio,
                             (T*)c->cheb_eig, c->ntx, c->nty));
     } else {
@@ -468,7 +472,7 @@ int launch_cg_persistent(wavi_ctx* c) {
     if (c->acc64) {
       if constexpr (std::is_same<T, float>::value && TILE == 16 && MAXT <= 2) {
         CK(cudaLaunchKernelEx(&cfg, k_srcg_persistent<T, TILE, MAXT, true>, d, c->sp.levels, coef<T>(c),
-                              (const uint8_t*)c->wmask_uv, dc, (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S,
+                              (const uint8_t*)c->wmask_uv, dc, (T*)c->w, bc, xc, c->partials, c->S,
                               (const DevParams*)c->P, c->bar, c->halo_box, cheb ? cheb_steps(c) : 1, kChebRatio,
                               (T*)c->cheb_eig, c->ntx, c->nty));
       } else {
@@ -476,7 +480,7 @@ int launch_cg_persistent(wavi_ctx* c) {
       }
     } else {
       CK(cudaLaunchKernelEx(&cfg, k_srcg_persistent<T, TILE, MAXT>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
-                            dc, (T*)c->w, (const T*)c->bc, (T*)c->xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
+                            dc, (T*)c->w, bc, xc, c->partials, c->S, (const DevParams*)c->P, c->bar,
                             c->halo_box, cheb ? cheb_steps(c) : 1, kChebRatio, (T*)c->cheb_eig, c->ntx, c->nty));
     }
   }
@@ -486,7 +490,9 @@ int launch_cg_persistent(wavi_ctx* c) {
 
 // The same with the CG vectors in global memory (grids with more tiles than resident CTAs).
 template <typename T, int TILE>
-int launch_cg_global(wavi_ctx* c) {
+int launch_cg_global(wavi_ctx* c, const void* bcv, void* xcv) {
+  const T* bc = (const T*)bcv;
+  T* xc = (T*)xcv;
   const Dims& d = c->d;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)c->pers_grid);
@@ -501,17 +507,17 @@ int launch_cg_global(wavi_ctx* c) {
   const GlobalCG<T> g{(T*)c->rc, (T*)c->gz, (T*)c->uc, (T*)c->cc, (T*)c->gw};
   if (c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV) {
     CK(cudaLaunchKernelEx(&cfg, k_srcg_cheb_global<T, TILE>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv,
-                          (const T*)c->dcoarse, (T*)c->w, (T*)c->w2, (const T*)c->bc, (T*)c->xc, g, (T*)c->gcd,
+                          (const T*)c->dcoarse, (T*)c->w, (T*)c->w2, bc, xc, g, (T*)c->gcd,
                           (T*)c->cheb_eig, cheb_steps(c), kChebRatio, c->partials, c->S, (const DevParams*)c->P, c->bar,
                           c->ntx, c->nty));
   } else if (c->coarse_solver == WAVI_COARSE_CG) {
     CK(cudaLaunchKernelEx(&cfg, k_cg_global<T, TILE>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv, (T*)c->w,
-                          (const T*)c->bc, (T*)c->xc, g, c->partials, c->S, (const DevParams*)c->P, c->bar, c->ntx,
+                          bc, xc, g, c->partials, c->S, (const DevParams*)c->P, c->bar, c->ntx,
                           c->nty));
   } else {
     const T* dc = c->coarse_solver == WAVI_COARSE_SRCG_JACOBI ? (const T*)c->dcoarse : nullptr;
     CK(cudaLaunchKernelEx(&cfg, k_srcg_global<T, TILE>, d, c->sp.levels, coef<T>(c), (const uint8_t*)c->wmask_uv, dc,
-                          (T*)c->w, (const T*)c->bc, (T*)c->xc, g, c->partials, c->S, (const DevParams*)c->P, c->bar,
+                          (T*)c->w, bc, xc, g, c->partials, c->S, (const DevParams*)c->P, c->bar,
                           c->ntx, c->nty));
   }
   c->launches++;
@@ -539,13 +545,13 @@ int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& t
   k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar, (const DevParams*)c->P);
   CKL();
   if (c->pers_maxt < 0)
-    TRY((launch_cg_global<T, TILE>(c)));
+    TRY((launch_cg_global<T, TILE>(c, c->bc, c->xc)));
   else if (c->pers_maxt == 1)
-    TRY((launch_cg_persistent<T, TILE, 1>(c)));
+    TRY((launch_cg_persistent<T, TILE, 1>(c, c->bc, c->xc)));
   else if (c->pers_maxt == 2)
-    TRY((launch_cg_persistent<T, TILE, 2>(c)));
+    TRY((launch_cg_persistent<T, TILE, 2>(c, c->bc, c->xc)));
   else
-    TRY((launch_cg_persistent<T, TILE, 4>(c)));
+    TRY((launch_cg_persistent<T, TILE, 4>(c, c->bc, c->xc)));
   k_check_barrier<<<1, 32, 0, c->st>>>(c->bar, c->S, h);
   CKL();
   tv.launches += 3;
@@ -553,6 +559,53 @@ int enqueue_cg_persistent(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& t
   tc.ops++;
   tc.bytes += op_bytes(d, sizeof(T), false) + sizeof(T) * 2.0 * d.N + d.N;
   return 0;
+}
+
+// The mixed V-cycle's coarse solve in FP64 (WAVI_SUMS_FP64_SOLVE): the FP32 restricted residual and warm
+// start widened to FP64, the FP64 persistent kernels on the FP64 coefficients (the same kernels as an FP64
+// context's), the solution narrowed back for the FP32 prolongation.
+template <int TILE>
+int enqueue_cg_persistent64(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& tc) {
+  const Dims& d = c->d;
+  k_convert<float, double><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, (const float*)c->bc, c->bc64);
+  CKL();
+  k_convert<float, double><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, (const float*)c->xc, c->xc64);
+  CKL();
+  if (c->coarse_solver == WAVI_COARSE_SRCG_JACOBI || c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV) {
+    launch_coarse_diag<double, TILE>(c, (double*)c->dcoarse);
+    CKL();
+    tv.launches++;
+  }
+  k_reset_barrier<<<1, 32, 0, c->st>>>(c->bar, (const DevParams*)c->P);
+  CKL();
+  if (c->pers_maxt < 0)
+    TRY((launch_cg_global<double, TILE>(c, c->bc64, c->xc64)));
+  else if (c->pers_maxt == 1)
+    TRY((launch_cg_persistent<double, TILE, 1>(c, c->bc64, c->xc64)));
+  else if (c->pers_maxt == 2)
+    TRY((launch_cg_persistent<double, TILE, 2>(c, c->bc64, c->xc64)));
+  else
+    TRY((launch_cg_persistent<double, TILE, 4>(c, c->bc64, c->xc64)));
+  k_check_barrier<<<1, 32, 0, c->st>>>(c->bar, c->S, h);
+  CKL();
+  k_convert<double, float><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->xc64, (float*)c->xc);
+  CKL();
+  tv.launches += 6;
+  tv.bytes += 4.0 * (4 + 8) * d.N;
+  tv.ops++;
+  tc.ops++;
+  tc.bytes += op_bytes(d, 8, false) + 8.0 * 2.0 * d.N + d.N;
+  return 0;
+}
+
+// The coarse solve of a V-cycle: the persistent kernel in the context's precision, or FP64 in a mixed
+// context with WAVI_SUMS_FP64_SOLVE.
+template <typename T, int TILE>
+int enqueue_coarse(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& tc) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (c->coarse64) return enqueue_cg_persistent64<TILE>(c, h, tv, tc);
+  }
+  return enqueue_cg_persistent<T, TILE>(c, h, tv, tc);
 }
 
 template <typename T, int TILE>
@@ -624,7 +677,7 @@ int enqueue_all_host_driven(wavi_ctx* c) {
   Tally tp, tv, tc;
   k_state_init<<<1, 32, 0, c->st>>>(c->S);
   CKL();
-  if (c->cheb_eig) CK(cudaMemsetAsync(c->cheb_eig, 0, c->d.N * sizeof(T), c->st));  // every solve starts cold
+  if (c->cheb_eig) CK(cudaMemsetAsync(c->cheb_eig, 0, c->d.N * sizeof(double), c->st));  // every solve starts cold (N doubles in every context)
   for (;;) {
     TRY(enqueue_picard_head(c, h, tp));
     CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
@@ -634,7 +687,7 @@ int enqueue_all_host_driven(wavi_ctx* c) {
     if (c->hS->vcycle_needed && c->pers_maxt != 0) {
       TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
       CK(cudaEventRecord(c->evc0, c->st));
-      TRY((enqueue_cg_persistent<T, TILE>(c, h, tv, tc)));
+      TRY((enqueue_coarse<T, TILE>(c, h, tv, tc)));
       CK(cudaEventRecord(c->evc1, c->st));
       c->coarse_pending = true;
       TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
@@ -708,7 +761,7 @@ int build_graph(wavi_ctx* c) {
   TRY(begin_capture(c, top, {}));
   k_state_init<<<1, 32, 0, c->st>>>(c->S);
   CKL();
-  if (c->cheb_eig) CK(cudaMemsetAsync(c->cheb_eig, 0, c->d.N * sizeof(T), c->st));  // every solve starts cold
+  if (c->cheb_eig) CK(cudaMemsetAsync(c->cheb_eig, 0, c->d.N * sizeof(double), c->st));  // every solve starts cold (N doubles in every context)
   TRY(end_capture(c, top, sinks));
   cudaGraph_t pbody = nullptr, vbody = nullptr, cbody = nullptr;
   cudaGraphNode_t pnode, vnode, cnode;
@@ -723,7 +776,7 @@ int build_graph(wavi_ctx* c) {
     // V-cycle body: pre part, one persistent coarse-CG kernel, post part
     TRY(begin_capture(c, vbody, {}));
     TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
-    TRY((enqueue_cg_persistent<T, TILE>(c, h, tv, tc)));
+    TRY((enqueue_coarse<T, TILE>(c, h, tv, tc)));
     TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
     TRY(end_capture(c, vbody, sinks));
   } else {
@@ -1125,7 +1178,7 @@ int adj_vcycle_body(wavi_ctx* c, const double* v, double* out) {
   Tally tv, tc;
   if (c->pers_maxt != 0) {
     TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
-    TRY((enqueue_cg_persistent<T, TILE>(c, h, tv, tc)));
+    TRY((enqueue_coarse<T, TILE>(c, h, tv, tc)));
     TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
   } else {
     TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv)));
@@ -1496,7 +1549,7 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_kernel %d", opt->coarse_kernel));
   if (opt->cheb_steps != 0 && (opt->cheb_steps < 1 || opt->cheb_steps > 15 || opt->cheb_steps % 2 == 0))
     return bail(fail(c, WAVI_ERR_ARGUMENT, "cheb_steps must be 0 (default) or odd in 1..15 (got %d)", opt->cheb_steps));
-  if (opt->coarse_sums < WAVI_SUMS_DEFAULT || opt->coarse_sums > WAVI_SUMS_FP64)
+  if (opt->coarse_sums < WAVI_SUMS_DEFAULT || opt->coarse_sums > WAVI_SUMS_FP64_SOLVE)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_sums %d", opt->coarse_sums));
   if (opt->viscosity < WAVI_VISCOSITY_DEFAULT || opt->viscosity > WAVI_VISCOSITY_FP64)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown viscosity precision %d", opt->viscosity));
@@ -1509,13 +1562,18 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   // survives because a coarse solve that misses its tolerance does not become the next warm start
   c->coarse_solver = want == WAVI_COARSE_AUTO ? (mixed(c) ? WAVI_COARSE_SRCG_CHEBYSHEV : WAVI_COARSE_CG) : want;
   c->acc64 = mixed(c) && opt->coarse_sums == WAVI_SUMS_FP64;
+  c->coarse64 = mixed(c) && opt->coarse_sums == WAVI_SUMS_FP64_SOLVE;
+  if (c->coarse64 && (opt->coarse_kernel == 2 || c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV))
+    return bail(fail(c, WAVI_ERR_ARGUMENT,
+                     "the FP64 coarse solve runs in the persistent coarse kernels, with a solver other than the "
+                     "pipelined one"));
   if (c->acc64 && (c->tile != 16 || opt->coarse_kernel == 2 || opt->coarse_kernel == 3 || c->coarse_solver == WAVI_COARSE_CG ||
                    c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV))
     return bail(fail(c, WAVI_ERR_ARGUMENT,
                      "FP64 coarse sums need a single-reduction coarse solver on the register-resident kernel with "
                      "16 x 16 tiles"));
   if (opt->coarse_kernel != 2) {
-    if (mixed(c))
+    if (mixed(c) && !c->coarse64)
       c->tile == 16 ? choose_persistent<float, 16>(c) : choose_persistent<float, 32>(c);
     else
       c->tile == 16 ? choose_persistent<double, 16>(c) : choose_persistent<double, 32>(c);
@@ -1523,8 +1581,8 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
       if (want != WAVI_COARSE_AUTO)
         return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse CG does not fit this grid on this device"));
       c->coarse_solver = WAVI_COARSE_CG;
-      c->tile == 16 ? (mixed(c) ? choose_persistent<float, 16>(c) : choose_persistent<double, 16>(c))
-                    : (mixed(c) ? choose_persistent<float, 32>(c) : choose_persistent<double, 32>(c));
+      c->tile == 16 ? (mixed(c) && !c->coarse64 ? choose_persistent<float, 16>(c) : choose_persistent<double, 16>(c))
+                    : (mixed(c) && !c->coarse64 ? choose_persistent<float, 32>(c) : choose_persistent<double, 32>(c));
     }
     if ((opt->coarse_kernel == 1 || opt->coarse_kernel == 3) && c->pers_maxt == 0)
       return bail(fail(c, WAVI_ERR_ARGUMENT, "the persistent coarse CG does not fit this grid on this device"));
@@ -1557,6 +1615,10 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     if (c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV || c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV) {
       if ((r = dalloc(c, &q, N))) return bail(r);
       c->cheb_eig = q;
+    }
+    if (c->coarse64) {
+      if ((r = dalloc(c, &c->bc64, N))) return bail(r);
+      if ((r = dalloc(c, &c->xc64, N))) return bail(r);
     }
     if (c->pers_maxt < 0) {
       if ((r = dalloc(c, &q, N))) return bail(r);
