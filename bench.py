@@ -447,7 +447,7 @@ def gpu_arm(args):
     # the mixed solve with its coarse CG's dot products, sums and scalars in FP64 (WAVI_SUMS_FP64) instead of
     # float-float grid sums over FP32 CTA sums
     sums64, outm64 = None, None
-    if mixed_solver in ("srcg", "srcg_jacobi", "srcg_chebyshev") and args.coarse_sums != "fp64":
+    if mixed_solver in ("srcg", "srcg_jacobi", "srcg_chebyshev") and args.coarse_sums == "default":
         try:
             m64 = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=mixed_solver,
                                  cheb_steps=args.cheb_steps, coarse_sums="fp64", viscosity=args.viscosity)
@@ -463,7 +463,7 @@ def gpu_arm(args):
 
     # the mixed solve with its whole coarse CG in FP64 (WAVI_SUMS_FP64_SOLVE)
     solve64, outc64 = None, None
-    if mixed_solver != "pipelined_chebyshev":
+    if mixed_solver != "pipelined_chebyshev" and args.coarse_sums == "default":
         try:
             mc64 = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=mixed_solver,
                                   cheb_steps=args.cheb_steps, coarse_sums="fp64_solve", viscosity=args.viscosity)
@@ -590,10 +590,10 @@ def gpu_arm(args):
 
 
 def other_configs(args):
-    """Compact lines of the other configurations, measured in the same run after the timed C2 work (one GPU,
+    """Compact lines of the other configurations, measured in the same run after the timed 640 x 80 work (one GPU,
     rank 0): the large single domain (2560x320, nσ = 8), the 256-member ensemble (the autotuner's choice
     on GB300, one timed ensemble) and the adjoint (two finite-difference directions).  Each runs on its
-    own; a failure is reported in its entry and leaves the C2 line intact."""
+    own; a failure is reported in its entry and leaves the 640 x 80 line intact."""
     import copy
     out = {}
     legs = (("c3", c3_arm, dict(steps=1, warmup=1),
@@ -616,7 +616,7 @@ def other_configs(args):
             entry = {k: ln[k] for k in keys if k in ln}
             if name == "c5":
                 entry["launch"] = ln["config"]["launch"]
-        except Exception as e:  # reported, not fatal: the C2 line stands on its own
+        except Exception as e:  # reported, not fatal: the 640 x 80 line stands on its own
             entry = {"error": f"{type(e).__name__}: {e}"}
         entry["wall_s"] = time.perf_counter() - t0
         out[name] = entry
@@ -1035,7 +1035,7 @@ def main():
     ap.add_argument("--coarse-solver", default="auto",
                     choices=("auto", "cg", "srcg", "srcg_jacobi", "srcg_chebyshev", "pipelined_chebyshev"),
                     help="coarse solver of the mixed-precision solves (the FP64 solve keeps the reference's)")
-    ap.add_argument("--coarse-sums", default="default", choices=("default", "float_float", "fp64"),
+    ap.add_argument("--coarse-sums", default="default", choices=("default", "float_float", "fp64", "fp64_solve"),
                     help="accumulation of the mixed coarse CG's dot products (wavi_coarse_sums)")
     ap.add_argument("--viscosity", default="default", choices=("default", "fp32", "fp64"),
                     help="precision of the mixed solves' viscosity sweeps (wavi_viscosity)")
