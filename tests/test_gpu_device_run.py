@@ -98,3 +98,39 @@ def test_run_simulation_device_run_matches_host_loop(oracle, pkg):
     for key, tol in TOL.items():
         assert _rel(m.fields[key], om.field(key)) < tol, key
     assert m.fields["wu_correction_coarse"].size == int(np.count_nonzero(m.fields["wu_mask"]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mismip_plus_ice0_grounding_line_on_device(oracle, pkg, precision):
+    """The reference's MISMIP+ Ice0 verification (test/verification_tests.jl:14-36,
+    verification_tests/MISMIP_PLUS_Ice0.jl) through the device time stepping: 10 000 yr of dt = 0.5 from a
+    100 m slab on the 8 km channel, 20 000 steps in one wavi_run_device call.  The grounding line crosses
+    every row, is symmetric about the centre line to 1e-4 and lies in the reference's loose bands (the tight
+    bands are marked broken there at this resolution), within one grid cell (8 km) of the oracle's own run of
+    the same test (edge rows 543.1 km, centre rows 489.4 km; tests/test_oracle.py, opt-in there: 265 s)."""
+    from wavi_gb300 import config
+    from wavi_gb300.model import GPUParallelSpec, Model, grounding_line_x
+    from wavi_gb300.synthetic import mismip_plus_bed
+    g = config.Grid(nx=80, ny=10, nσ=4, x0=0.0, y0=-40000.0, dx=8000.0, dy=8000.0, u_iszero=["north"],
+                    v_iszero=["west", "east"])
+    p = config.Params(default_thickness=100.0, accumulation_rate=0.3, default_temperature=265.700709)
+    sp = config.SolverParams(maxiter_picard=1)
+    m = Model(g, lambda x, y: float(mismip_plus_bed(x, y)), p, sp, parallel_spec=GPUParallelSpec(precision="fp64"))
+    from wavi_gb300.gpu import ALL_FIELDS, VelocitySolver
+    s = VelocitySolver(m.grid, m.solver_params, precision=precision)
+    f = m.fields
+    t = {k: _dev(f[k], np.uint8 if k in ("wu_mask", "wv_mask") else np.float64) for k in ALL_FIELDS}
+    st, _ = s.run_device(m.params, 0.5, 20000, _dev(f["b"]), _dev(m.weertman_c_param), _dev(m.accumulation_param),
+                         _dev(m.h_isfixed, np.uint8), m.melt_rate, t)
+    s.close()
+    h = t["h"].cpu().numpy().reshape((g.nx, g.ny), order="F")
+    haf = h - (p.density_ocean / p.density_ice) * (p.sea_level_wrt_geoid - np.asarray(f["b"]))
+    glx = grounding_line_x(haf, g.xxh)
+    ny = g.ny
+    print(precision, glx, st["picard_iterations"])
+    assert glx.size == ny and np.all(np.isfinite(glx))
+    t4 = glx[[0, ny // 2 - 1, ny // 2, ny - 1]]
+    assert (t4[3] - t4[0]) / (t4[3] + t4[0]) < 1e-4 and (t4[1] - t4[2]) / (t4[1] + t4[2]) < 1e-4
+    assert 480000 < t4[0] < 550000 and 480000 < t4[3] < 550000
+    assert 430000 < t4[1] < 490000 and 430000 < t4[2] < 490000
+    assert abs(t4[0] - 543100.0) < 8000.0 and abs(t4[1] - 489400.0) < 8000.0
