@@ -56,7 +56,6 @@ sys.path.insert(0, ROOT)
 import __graft_entry__  # noqa: E402
 
 TOL_PICARD = 1e-6
-CHEB_STEPS = 3  # operator applications per iteration of the library's Chebyshev coarse solve
 MAXITER_PICARD = 100
 WORKLOAD = ("8 km channel refined to 640x80 @1km, nsigma=4, 5% thickness perturbation, Picard-converged solve "
             "from the initial state to rel. residual < 1e-6")
@@ -488,7 +487,7 @@ def gpu_arm(args):
                            viscosity=args.viscosity)
     sec_it, cg_its, cg_launches = coarse_roofline(torch, prof, p, snapshot)
     prof.close()
-    apps = (args.cheb_steps or CHEB_STEPS) if mixed_solver in ("srcg_chebyshev", "pipelined_chebyshev") else 1
+    apps = stmix[-1]["cheb_steps"] or 1  # operator applications per coarse-CG iteration (the library reports it)
     latency = None
     if mixed_solver == "srcg_chebyshev" and apps > 1:
         profj = VelocitySolver(g, sp, precision="mixed", device=local, use_graphs=False, coarse_solver="srcg_jacobi",
@@ -556,7 +555,7 @@ def gpu_arm(args):
         **errs_oracle,
         "solve": {k: stmix[-1][k] for k in ("picard_iterations", "coarse_cg_iterations", "op_applications",
                                              "rel_residual", "kernel_launches", "host_syncs", "status_name",
-                                             "coarse_solver")},
+                                             "coarse_solver", "coarse_kernel", "cheb_steps")},
         "roofline": {"bound": "latency", "achieved": cg_achieved, "peak": peak, "unit": "GB/s",
                      "frac": cg_achieved / peak,
                      "traffic": ncu_traffic("coarse_cg_c2.md", "traffic_bytes_per_cg_iteration"),

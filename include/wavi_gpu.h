@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define WAVI_ABI_VERSION 2
+#define WAVI_ABI_VERSION 3
 
 typedef enum wavi_status {
   WAVI_OK = 0,
@@ -105,7 +105,9 @@ typedef struct wavi_options {
                                         2^19 points of the (nx+1) x (ny+1) index space), 1 = shared-memory
                                         tiles, 2 = row-streaming */
   int32_t cheb_steps;                /* Chebyshev steps per preconditioner application of the Chebyshev
-                                        coarse solvers: 0 = the default, 3; else odd, 1..15 */
+                                        coarse solvers: 0 = the default (5 in the register-resident
+                                        single-reduction kernel, 3 in the global-memory and pipelined
+                                        kernels); else odd, 1..15 */
   int32_t coarse_sums;               /* wavi_coarse_sums: how a mixed-precision coarse CG accumulates its
                                         dot products (FP64 contexts always sum in FP64) */
   int32_t viscosity;                 /* wavi_viscosity: precision of a mixed context's σ-level viscosity
@@ -146,7 +148,7 @@ typedef enum wavi_coarse_solver {
   WAVI_COARSE_CG = 1,                /* the reference's cg! recurrence */
   WAVI_COARSE_SRCG = 2,              /* single-reduction CG, no preconditioner (same iterates as cg!) */
   WAVI_COARSE_SRCG_JACOBI = 3,       /* single-reduction CG preconditioned by diag(R A P) */
-  WAVI_COARSE_SRCG_CHEBYSHEV = 4,    /* single-reduction CG preconditioned by cheb_steps (default 3)
+  WAVI_COARSE_SRCG_CHEBYSHEV = 4,    /* single-reduction CG preconditioned by cheb_steps (default 5 or 3)
                                         Chebyshev-accelerated Jacobi steps on [b/120, b],
                                         b = 1.15 lambda_max(diag(R A P)^-1 R A P) from power steps each
                                         V-cycle (12 in a solve's first, then 4, warm-started);
@@ -212,6 +214,11 @@ typedef struct wavi_stats {
                                         host-driven solves, use_graphs = 0, only; else -1) */
   int32_t coarse_solver;             /* the wavi_coarse_solver the solve used (never AUTO) */
   int32_t coarse_launches;           /* persistent coarse-CG launches timed in coarse_ms */
+  int32_t coarse_kernel;             /* the coarse-CG kernel the solve ran: 1 = persistent, vectors in
+                                        registers; 2 = per-iteration kernels; 3 = persistent, vectors in
+                                        global memory (the wavi_options.coarse_kernel codes) */
+  int32_t cheb_steps;                /* Chebyshev steps per preconditioner application (0: the coarse
+                                        solver has no Chebyshev preconditioner) */
 } wavi_stats;
 
 typedef struct wavi_ctx wavi_ctx;

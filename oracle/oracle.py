@@ -64,6 +64,7 @@ def lib():
         L.oracle_pos_fraction.argtypes = [C.c_int, C.c_int, dp, u8p, dp, dp, dp]
         L.oracle_kron_apply.argtypes = [C.c_int, C.c_int, dp, C.c_int, C.c_int, dp, dp, dp]
         L.oracle_set_coarse_variant.argtypes = [C.c_int]
+        L.oracle_set_chebyshev.argtypes = [C.c_int, C.c_double]
         L.oracle_coarse_diag.argtypes = [vp, dp, dp]
         _lib = L
     return _lib
@@ -222,6 +223,15 @@ def set_coarse_variant(name):
     """Coarse solve of every later oracle V-cycle: the reference's cg! ("cg", the default) or a restatement
     of one of the GPU library's opt-in coarse solvers."""
     lib().oracle_set_coarse_variant(COARSE_VARIANTS[name])
+
+
+CHEB_DEFAULT = (3, 120.0)
+
+
+def set_chebyshev(steps=CHEB_DEFAULT[0], ratio=CHEB_DEFAULT[1]):
+    """The Chebyshev preconditioner of the "srcg_chebyshev" and "pipelined_chebyshev" variants: steps per
+    application (odd) and the ratio b/a of its interval [a, b].  The defaults are the GPU library's."""
+    lib().oracle_set_chebyshev(int(steps), float(ratio))
 
 
 def pos_fraction(z, mask=None):

@@ -917,13 +917,14 @@ int coarse_srcg(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, dou
   return it;
 }
 
-// Variant 4: coarse_srcg with M⁻¹ r replaced by CHEB_STEPS steps of the Chebyshev-accelerated Jacobi
-// iteration on D⁻¹ R A P z = D⁻¹ r from z = 0 (D = diag(R A P)), on the interval [b / CHEB_RATIO, b],
+// Variant 4: coarse_srcg with M⁻¹ r replaced by g_cheb_steps steps of the Chebyshev-accelerated Jacobi
+// iteration on D⁻¹ R A P z = D⁻¹ r from z = 0 (D = diag(R A P)), on the interval [b / g_cheb_ratio, b],
 // b = 1.15 λmax(D⁻¹ R A P).  λmax by power steps (12 in a solve's first V-cycle, then 4) from the
 // previous V-cycle's vector (zero at a solve's start) plus 1e-3 times a fixed hash of the full index.
 // The GPU library's WAVI_COARSE_SRCG_CHEBYSHEV with its constants, in the same order of operations.
-constexpr int CHEB_STEPS = 3;
-constexpr double CHEB_RATIO = 120.0;
+// The GPU library's defaults (wavi_gpu.cu: kChebSteps, kChebRatio); oracle_set_chebyshev changes them.
+static int g_cheb_steps = 3;
+static double g_cheb_ratio = 120.0;
 static float cheb_start(int q) {  // in [-1, 1)
   const unsigned h = (unsigned)q * 2654435761u;
   return (float)((h >> 8) & 0xffffu) * (1.0f / 32768.0f) - 1.0f;
@@ -950,7 +951,7 @@ ChebPrec cheb_setup(Model& m, OpWork& w, const Precond& p) {
     for (size_t k = 0; k < n; ++k) t[k] = c.minv[k] * t[k];
     const double tt = dotp(t, t), vv = dotp(v, v);
     const double lam = (vv > 0.0 && tt > 0.0) ? std::sqrt(tt / vv) : 1.0;
-    const double bmax = 1.15 * lam, amin = bmax / CHEB_RATIO;
+    const double bmax = 1.15 * lam, amin = bmax / g_cheb_ratio;
     c.th = 0.5 * (bmax + amin);
     c.de = 0.5 * (bmax - amin);
     c.sg = (bmax + amin) / (bmax - amin);
@@ -960,7 +961,7 @@ ChebPrec cheb_setup(Model& m, OpWork& w, const Precond& p) {
   for (size_t k = 0; k < n; ++k) m.cheb_eig[full(k)] = v[k];
   return c;
 }
-// z = CHEB_STEPS Chebyshev steps on D⁻¹ R A P z = D⁻¹ r from z = 0
+// z = g_cheb_steps Chebyshev steps on D⁻¹ R A P z = D⁻¹ r from z = 0
 void cheb_apply(Model& m, OpWork& w, const Precond& p, const ChebPrec& c, const Vec& r, Vec& z) {
   const size_t n = r.size();
   z.resize(n);
@@ -971,7 +972,7 @@ void cheb_apply(Model& m, OpWork& w, const Precond& p, const ChebPrec& c, const 
     dd[k] = z[k];
   }
   double rho = 1.0 / c.sg;
-  for (int st = 1; st < CHEB_STEPS; ++st) {
+  for (int st = 1; st < g_cheb_steps; ++st) {
     op_coarse(m, w, p, z, tt2);
     const double rn = 1.0 / (2.0 * c.sg - rho), c1 = rn * rho, c2 = 2.0 * rn / c.de;
     for (size_t k = 0; k < n; ++k) {
@@ -1510,6 +1511,12 @@ int oracle_vcycle(void* h, const double* ru, const double* rv, double* cu, doubl
   return p.last_cg;
 }
 void oracle_set_coarse_variant(int variant) { g_coarse_variant = variant; }
+// The Chebyshev preconditioner of variants 4 and 5: steps per application (odd, >= 1) and the interval's
+// ratio b / a.
+void oracle_set_chebyshev(int steps, double ratio) {
+  g_cheb_steps = steps;
+  g_cheb_ratio = ratio;
+}
 // diag(R A P) of the model's current linearisation and coarse space, scattered to the full wavelet
 // grids (zero off the coarse space).
 void oracle_coarse_diag(void* h, double* du, double* dv) {

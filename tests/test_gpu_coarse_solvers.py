@@ -84,7 +84,13 @@ def test_single_reduction_fixed_cg_count_matches_oracle(oracle, reference_cg, na
     s = VelocitySolver(g, sp, precision="fp64", coarse_kernel=kernel, coarse_solver=solver)
     st = s.solve(p, f)
     oracle.set_coarse_variant(solver)
-    om.update_velocities()
+    if solver == "srcg_chebyshev":  # the library's default step count for this kernel (5 or 3)
+        assert st["cheb_steps"] == (5 if kernel == "persistent" else 3), st
+        oracle.set_chebyshev(st["cheb_steps"])
+    try:
+        om.update_velocities()
+    finally:
+        oracle.set_chebyshev()
     ost = om.stats()
     assert st["picard_iterations"] == 1
     assert st["coarse_cg_iterations"] == ost["coarse_cg_iterations"] == 10
@@ -120,20 +126,24 @@ def test_single_reduction_converged_solve_matches_reference(oracle, name, solver
         s.close()
 
 
-def test_chebyshev_on_the_global_memory_kernel_matches_the_register_kernel(oracle):
+@pytest.mark.parametrize("steps", [3, 5])
+def test_chebyshev_on_the_global_memory_kernel_matches_the_register_kernel(oracle, steps):
     """The Chebyshev coarse solve with its vectors in global memory (k_srcg_cheb_global, the kernel of grids
     too large for the register-resident one) and in registers (k_srcg_persistent): one Picard iteration
-    with a fixed count of 10 coarse iterations in FP64, the same iterates to rounding."""
+    with a fixed count of 10 coarse iterations in FP64 at the same step count, the same iterates to
+    rounding."""
     from wavi_gb300.gpu import VelocitySolver
     g, p, sp, om = _setup(oracle, "full", maxiter_picard=1, maxiter_coarse=10, tol_coarse=0.0)
     f0 = fields_from_oracle(om, g)
     out = {}
     for kernel in ("persistent", "persistent_global"):
         f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
-        s = VelocitySolver(g, sp, precision="fp64", coarse_kernel=kernel, coarse_solver="srcg_chebyshev")
+        s = VelocitySolver(g, sp, precision="fp64", coarse_kernel=kernel, coarse_solver="srcg_chebyshev",
+                           cheb_steps=steps)
         st = s.solve(p, f)
         s.close()
         assert st["coarse_cg_iterations"] == 10 and st["coarse_solver"] == "srcg_chebyshev", st
+        assert st["cheb_steps"] == steps and st["coarse_kernel"] == kernel, st
         out[kernel] = np.concatenate([f["u"].ravel(), f["v"].ravel()])
     a, b = out["persistent"], out["persistent_global"]
     assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(a)
@@ -153,7 +163,13 @@ def test_mixed_default_is_chebyshev(oracle):
         s = VelocitySolver(g, sp, precision="mixed")
         st = s.solve(p, f)
         assert st["coarse_solver"] == want, (name, st)
+        # 5 Chebyshev steps in the register-resident kernel, 3 with the vectors in global memory
+        assert st["coarse_kernel"] == "persistent" and st["cheb_steps"] == 5, (name, st)
         s.close()
+    s = VelocitySolver(g, sp, precision="mixed", coarse_kernel="persistent_global")
+    st = s.solve(p, fields_from_oracle(om, g))
+    assert st["coarse_kernel"] == "persistent_global" and st["cheb_steps"] == 3, st
+    s.close()
 
 
 def test_single_reduction_solvers_need_the_persistent_kernel(oracle):

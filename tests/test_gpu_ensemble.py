@@ -93,3 +93,37 @@ def test_autotune_picks_a_candidate(oracle):
     assert best in cands and len(timings) == 3 and all(t > 0 for t, _, _ in timings)
     assert [st for _, _, st in timings] == ["capped", "capped", "whole"]
     assert timings[2][1] == best == min(timings[:2], key=lambda t: t[0])[1]
+
+
+@pytest.fixture(scope="module")
+def ragged_members(oracle):
+    """Three of the smallest members of the benchmark's 256-member ragged ensemble (77 x 24, 147 x 17 and
+    84 x 28 at 2 km), with the oracle's converged solves (tol 1e-6, about 17 s of oracle time)."""
+    from wavi_gb300 import synthetic
+    ens = synthetic.ensemble_members()
+    out = []
+    for k in (186, 45, 160):
+        g, bed, p, sp, ic = ens[k]
+        om = oracle.build_model(g, bed, p, sp, ic)
+        om.pre_solve()
+        f = fields_from_oracle(om, g)
+        om.update_velocities()
+        out.append((g, p, sp, om, f))
+    return out
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-7), ("mixed", 2e-6)])
+def test_benchmark_ensemble_members_match_oracle(ragged_members, precision, tol):
+    """Members of the measured ensemble itself, solved together at the benchmark's tolerance, against the
+    oracle's own converged solves of the same members."""
+    from wavi_gb300.ensemble import EnsembleSolver
+    mem = ragged_members
+    ens = EnsembleSolver([m[0] for m in mem], [m[2] for m in mem], precision=precision, concurrency=3)
+    tensors = [to_dev(m[4], torch) for m in mem]
+    stats = ens.solve_device([m[1] for m in mem], tensors)
+    for k, (g, p, sp, om, f) in enumerate(mem):
+        got = {name: np.array(a, copy=True, order="F") for name, a in f.items()}  # f stays the initial state
+        from_dev(tensors[k], got)
+        assert stats[k]["status"] == 0 and stats[k]["rel_residual"] < sp.tol_picard, (k, stats[k])
+        assert uv_err(got, om) < tol, (k, uv_err(got, om), stats[k], om.stats()["picard_iterations"])
+    ens.close()

@@ -10,7 +10,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libwavi_gpu.so")
 
-WAVI_ABI_VERSION = 2
+WAVI_ABI_VERSION = 3
 
 STATUS = {
     0: "WAVI_OK", -1: "WAVI_ERR_ARGUMENT", -2: "WAVI_ERR_CUDA", -3: "WAVI_ERR_NONFINITE",
@@ -82,7 +82,8 @@ class Stats(C.Structure):
                 ("rel_residual", C.c_double), ("rel_update", C.c_double),
                 ("algorithmic_bytes", C.c_double), ("elapsed_ms", C.c_double),
                 ("kernel_launches", C.c_int32), ("host_syncs", C.c_int32),
-                ("coarse_ms", C.c_double), ("coarse_solver", C.c_int32), ("coarse_launches", C.c_int32)]
+                ("coarse_ms", C.c_double), ("coarse_solver", C.c_int32), ("coarse_launches", C.c_int32),
+                ("coarse_kernel", C.c_int32), ("cheb_steps", C.c_int32)]
 
 
 class OperatorDesc(C.Structure):

@@ -433,9 +433,18 @@ int enqueue_cg_iteration(wavi_ctx* c, const CondHandles& h, int* live, Tally& t)
 // The whole coarse CG as one cooperative persistent kernel (persistent.cuh), then the watchdog check.
 // The Chebyshev coarse solve: steps of the Chebyshev-accelerated Jacobi iteration per preconditioner
 // application (odd: the preconditioner stays positive definite if λmax is underestimated) and the ratio
-// of the interval's ends.
-constexpr int kChebSteps = 3;
-int cheb_steps(const wavi_ctx* c) { return c->opt.cheb_steps > 0 ? c->opt.cheb_steps : kChebSteps; }
+// of the interval's ends.  Default steps: 5 in the register-resident single-reduction kernel, whose grid
+// reduction (~3.2 µs on GB300) outweighs an operator application with its neighbour exchange (~2.5 µs), so
+// that more steps per reduction pay (640 x 80: 2 611 iterations of 15.5 µs against 4 000 of 10.8 µs with
+// 3 steps, 47.0 against 49.5 ms per solve; 7 steps 47.9 ms); 3 in the global-memory kernel, where every
+// step is a pass over all tiles behind a grid barrier (2560 x 320: 1.96 s per solve with 5 steps against
+// 1.79 s with 3), and in the pipelined kernel.  The interval's ratio moves the iteration count by a few
+// per cent between 60 and 1000 (the oracle on 640 x 80).
+constexpr int kChebStepsResident = 5, kChebStepsOther = 3;
+int cheb_steps(const wavi_ctx* c) {
+  if (c->opt.cheb_steps > 0) return c->opt.cheb_steps;
+  return c->pers_maxt > 0 && c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV ? kChebStepsResident : kChebStepsOther;
+}
 constexpr float kChebRatio = 120.0f;
 
 template <typename T, int TILE, int MAXT>
@@ -925,11 +934,20 @@ int solve_enqueue(wavi_ctx* c, const wavi_params* p) {
   return 0;
 }
 
+// The coarse-CG kernel the context runs (the wavi_options.coarse_kernel codes 1-3) and the Chebyshev steps
+// of its preconditioner (0 if the coarse solver has none).
+void fill_coarse_kind(const wavi_ctx* c, wavi_stats* st) {
+  st->coarse_kernel = c->pers_maxt > 0 ? 1 : c->pers_maxt < 0 ? 3 : 2;
+  const bool cheb = c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV || c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV;
+  st->cheb_steps = cheb ? cheb_steps(c) : 0;
+}
+
 int solve_finish(wavi_ctx* c, wavi_stats* st) {
   if (c->skipped) {
     if (st) {
       *st = wavi_stats{};
       st->coarse_solver = c->coarse_solver;
+      fill_coarse_kind(c, st);
     }
     return 0;
   }
@@ -960,6 +978,7 @@ int solve_finish(wavi_ctx* c, wavi_stats* st) {
     st->coarse_ms = c->opt.use_graphs ? -1.0 : c->coarse_ms;
     st->coarse_solver = c->coarse_solver;
     st->coarse_launches = c->opt.use_graphs ? 0 : c->coarse_launches;
+    fill_coarse_kind(c, st);
   }
   return 0;  // not converging is reported through stats.status only, like the reference's silent stop
 }

@@ -15,6 +15,7 @@ import numpy as np
 from . import abi
 
 PRECISIONS = {"fp64": abi.PRECISION_FP64, "mixed": abi.PRECISION_MIXED}
+COARSE_KERNEL_NAMES = {1: "persistent", 2: "iterations", 3: "persistent_global"}  # wavi_stats.coarse_kernel
 
 
 def _shape_of(name, nx, ny, ns):
@@ -273,4 +274,5 @@ def stats_dict(s):
             "algorithmic_bytes": s.algorithmic_bytes, "elapsed_ms": s.elapsed_ms,
             "kernel_launches": s.kernel_launches, "host_syncs": s.host_syncs, "coarse_ms": s.coarse_ms,
             "coarse_solver": abi.COARSE_SOLVER_NAMES.get(s.coarse_solver, s.coarse_solver),
-            "coarse_launches": s.coarse_launches}
+            "coarse_launches": s.coarse_launches,
+            "coarse_kernel": COARSE_KERNEL_NAMES.get(s.coarse_kernel, s.coarse_kernel), "cheb_steps": s.cheb_steps}
