@@ -433,6 +433,15 @@ const char* wavi_ensemble_last_error(const wavi_ensemble* ens);
  * the wait gave up as designed.  Not part of the reference interface (a test hook). */
 int wavi_selftest_watchdog(wavi_ctx* ctx, int* fired);
 
+/* ---- Self-test of the integer conversions -------------------------------------------------------
+ * The float relinearisation of a mixed context converts between the caller's FP64 fields and float with
+ * integer operations (round to nearest even; exact widening), because GB300 runs the hardware conversions
+ * on its FP64 pipe.  This call compares them with the hardware conversions on the context's device over
+ * n hashed bit patterns of each width (every exponent, rounding ties, subnormal and overflowing results;
+ * 0 <= n <= 2^32): *mismatches = the results that differ (two NaNs agree).  Not part of the reference
+ * interface (a test hook). */
+int wavi_selftest_conversions(wavi_ctx* ctx, long long n, long long* mismatches);
+
 #ifdef __cplusplus
 }
 #endif

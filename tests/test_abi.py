@@ -137,6 +137,7 @@ def test_every_entry_point_rejects_a_null_context(lib, pkg):
         "wavi_time_relinearise_device": (None, 1, None, None),
         "wavi_op_diagonal_device": (None, 0, None),
         "wavi_selftest_watchdog": (None, None),
+        "wavi_selftest_conversions": (None, 1, None),
         "wavi_coarse_diagonal_device": (None, 0, None),
         "wavi_adjoint_device": (None, None, None, None, None, None, 1e-10, 10, None),
         "wavi_tangent_device": (None, None, None, None, None, None, 1e-10, 10, None),

@@ -80,6 +80,25 @@ def test_relinearise_and_operator_match_oracle_at_full_size(c3):
     s.close()
 
 
+def test_float_relinearise_matches_oracle_at_full_size(c3):
+    """The mixed context's float relinearisation (integer conversions of the FP64 fields, FP64 velocity
+    differences, the float chain) on the 2560 x 320, nσ = 8 state against the oracle's FP64 one, within
+    float rounding of each field."""
+    from wavi_gb300.gpu import ALL_FIELDS, VelocitySolver
+    m, g, p, sp, f, om, rng = c3
+    s = VelocitySolver(g, sp, precision="mixed")
+    t = _dev({k: f[k] for k in ALL_FIELDS})
+    s.relinearise_device(p, t)
+    for k in SOLVE_FIELDS:  # the oracle back at the fixture's state (an earlier test relinearised it)
+        om.field(k)[...] = f[k]
+    om.inner_update()
+    for k in ("shelf_strain_rate", "av_speed", "bed_speed", "beta", "tau_bed", "eta", "eta_av", "quad_f1",
+              "quad_f2", "beta_eff", "gu_beta_eff", "gv_beta_eff"):
+        got = t[k].cpu().numpy().reshape(np.asarray(om.field(k)).shape, order="F")
+        assert rel(got, om.field(k)) < 2e-6, (k, rel(got, om.field(k)))
+    s.close()
+
+
 def test_operator_symmetry_sign_and_fp32_at_full_size(c3):
     from wavi_gb300.gpu import ALL_FIELDS, VelocitySolver
     m, g, p, sp, f, om, rng = c3

@@ -55,6 +55,54 @@ def test_relinearise_matches_oracle(oracle, name):
     s.close()
 
 
+RELIN_FIELDS = ("shelf_strain_rate", "av_speed", "bed_speed", "beta", "tau_bed", "eta", "eta_av", "quad_f1",
+                "quad_f2", "beta_eff", "gu_beta_eff", "gv_beta_eff")
+
+
+@pytest.mark.parametrize("field", ["random", "smooth"])
+@pytest.mark.parametrize("name", list(CASES))
+def test_float_relinearise_matches_oracle(oracle, name, field):
+    """The mixed context's relinearisation (FP32 viscosity sweeps, the float chain with integer conversions
+    of the FP64 fields and FP64 velocity differences) against the oracle's FP64 one, within float rounding
+    of each field.  "smooth": 800 m/yr plus small variations, where neighbouring velocities nearly cancel
+    in the strain rates."""
+    from wavi_gb300.gpu import VelocitySolver
+    g, p, sp, om = _setup(oracle, name)
+    rng = np.random.default_rng(6)
+    u, v = om.field("u"), om.field("v")
+    if field == "random":
+        u[...] = 50 * rng.standard_normal(u.shape)
+        v[...] = 20 * rng.standard_normal(v.shape)
+    else:
+        xu = np.arange(u.shape[0])[:, None] + 0.3 * np.arange(u.shape[1])[None, :]
+        xv = np.arange(v.shape[0])[:, None] - 0.2 * np.arange(v.shape[1])[None, :]
+        u[...] = 800.0 + 3.0 * np.sin(0.3 * xu)
+        v[...] = -150.0 + 2.0 * np.cos(0.25 * xv)
+    f = fields_from_oracle(om, g)
+    s = VelocitySolver(g, sp, precision="mixed")
+    t = to_dev(f, torch)
+    s.relinearise_device(p, t)
+    from_dev(t, f)
+    om.inner_update()
+    errs = {k: rel(f[k], om.field(k)) for k in RELIN_FIELDS}
+    print(name, field, {k: f"{e:.1e}" for k, e in errs.items()})
+    for k, e in errs.items():
+        assert e < 2e-6, (k, e)
+    s.close()
+
+
+def test_integer_conversions_match_the_hardware():
+    """wavi_selftest_conversions: the integer binary64 -> binary32 (round to nearest even) and binary32 ->
+    binary64 conversions of the float relinearisation equal the hardware conversions on 2^28 hashed
+    patterns of each width (every exponent, ties, subnormal and overflowing results)."""
+    from wavi_gb300 import synthetic
+    from wavi_gb300.gpu import VelocitySolver
+    g, bed, p, sp, ic = synthetic.small_case(nx=24, ny=12)
+    s = VelocitySolver(g, sp, precision="mixed")
+    assert s.selftest_conversions(1 << 28) == 0
+    s.close()
+
+
 @pytest.mark.parametrize("stencil", ["tiled", "streaming"])
 @pytest.mark.parametrize("name", list(CASES))
 def test_operator_and_diagonal_match_oracle(oracle, name, stencil):

@@ -152,6 +152,7 @@ def load_library(path=None):
         "wavi_update_wavelets_device": (C.c_int, [vp, vp, vp]),
         "wavi_residual_noalloc": (C.c_int, [C.POINTER(OperatorDesc), vp, vp, vp, vp, vp]),
         "wavi_selftest_watchdog": (C.c_int, [vp, C.POINTER(C.c_int)]),
+        "wavi_selftest_conversions": (C.c_int, [vp, C.c_longlong, C.POINTER(C.c_longlong)]),
         "wavi_adjoint_device": (C.c_int, [vp, C.POINTER(Params), vp, vp, vp, vp, C.c_double, C.c_int,
                                           C.POINTER(AdjointStats)]),
         "wavi_tangent_device": (C.c_int, [vp, C.POINTER(Params), vp, vp, vp, vp, C.c_double, C.c_int,

@@ -246,7 +246,59 @@ struct DevParams {
   double tol_picard, tol_coarse, omega;
   int maxiter_picard, maxiter_coarse, nsmooth, n_iter_viscosity;
   int picard_test;
+  // the float relinearisation's uniform constants, rounded once on the host: 1/m - 1, 1/n - 1 (the
+  // exponents of β and of the viscosity), the squared strain-rate regularisation, the speed regularisation
+  float weertman_ex_f, glen_ex_f, glen_er2_f, weertman_reg_speed_f;
 };
+
+// IEEE 754 conversions between binary64 and binary32 by integer operations: binary64 -> binary32 rounds to
+// nearest, ties to even (subnormal results, overflow to infinity, NaN stays NaN); binary32 -> binary64 is
+// exact.  GB300 runs the hardware conversions (cvt.rn.f32.f64, cvt.f64.f32) on its FP64 pipe at about one
+// per SM and cycle, where these take a dozen integer operations on the integer pipes; the float
+// relinearisation converts ~50 values per cell between the caller's FP64 fields and float.  Their results
+// equal the hardware conversions bit for bit (NaN: any NaN), checked by wavi_selftest_conversions.
+static __device__ __noinline__ float f32_rn_bits_general(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ffu);
+  const unsigned long long m = b & 0xfffffffffffffull;
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u));  // ±inf, NaN
+  const int ef = e - 1023 + 127;  // the binary32 biased exponent of a normal result
+  if (ef >= 0xff) return __uint_as_float(sign | 0x7f800000u);
+  if (ef <= 0) {
+    // below 2^-126: a subnormal binary32 (or zero), k·2^-149 with k < 2^23, from the 53-bit significand
+    if (ef < -24) return __uint_as_float(sign);  // below 2^-150: rounds to zero
+    const unsigned long long sig = m | (1ull << 52);
+    const int drop = 30 - ef;  // 30..54 bits dropped
+    const unsigned long long rem = sig & ((1ull << drop) - 1ull), half = 1ull << (drop - 1);
+    unsigned k = (unsigned)(sig >> drop);
+    if (rem > half || (rem == half && (k & 1u))) ++k;  // a carry into bit 23 gives the smallest normal
+    return __uint_as_float(sign | k);
+  }
+  unsigned r = ((unsigned)ef << 23) | (unsigned)(m >> 29);
+  const unsigned rem = (unsigned)(m & 0x1fffffffull);
+  if (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ++r;  // a carry may reach the exponent (or inf)
+  return __uint_as_float(sign | r);
+}
+static __device__ __noinline__ double f64_exact_bits_general(float x) {
+  const unsigned b = __float_as_uint(x);
+  const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+  const unsigned e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  unsigned long long r;
+  if (e == 0xffu) {
+    r = sign | 0x7ff0000000000000ull | ((unsigned long long)m << 29);  // ±inf, NaN (payload kept)
+  } else if (e != 0u) {
+    r = sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+  } else if (m == 0u) {
+    r = sign;  // ±0
+  } else {
+    // subnormal binary32 m·2^-149 with its leading one at bit p: a normal binary64 1.f·2^(p-149)
+    const int p = 31 - __clz((int)m);
+    const unsigned f = (m << (23 - p)) & 0x7fffffu;
+    r = sign | ((unsigned long long)(1023 + p - 149) << 52) | ((unsigned long long)f << 29);
+  }
+  return __longlong_as_double((long long)r);
+}
 
 struct RelinIn {
   const double* uv;      // velocities (u | v), full rectangles
@@ -260,6 +312,8 @@ struct RelinIn {
   const double* zeta;    // ns (device)
   const double* qw;      // ns (device)
   const DevParams* P;
+  const float* zeta_f;   // ns: zeta and qw rounded to float (the float relinearisation)
+  const float* qw_f;
 };
 struct RelinOut {
   double *shelf_strain_rate, *av_speed, *bed_speed, *beta, *tau_bed, *eta, *eta_av, *quad_f1, *quad_f2, *beta_eff;
@@ -270,12 +324,122 @@ struct RelinOut {
   double* hn;        // h*ηav (all cells) for the c-grid centring
 };
 
+// The conversions a kernel calls: the common cases (results in binary32's normal range, zeros) on the two
+// 32-bit halves of the binary64 pattern in a few integer operations, the rest (subnormal, infinite and NaN
+// results, overflow) in the general forms above.
+__device__ __forceinline__ float f32_rn_bits(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned ahi = hi & 0x7fffffffu;
+  if (ahi - 0x38100000u < 0x47f00000u - 0x38100000u) {  // biased exponent 897..1150: a normal binary32
+    // (e - 896) << 23 | the top 23 mantissa bits, rounded to nearest even on the 29 dropped bits (a carry
+    // may reach the exponent, up to infinity)
+    unsigned r = ((ahi - 0x38000000u) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    r += (rem + (r & 1u)) > 0x10000000u;
+    return __uint_as_float(r | (hi & 0x80000000u));
+  }
+  if ((ahi | lo) == 0u) return __uint_as_float(hi & 0x80000000u);  // ±0
+  return f32_rn_bits_general(x);
+}
+__device__ __forceinline__ double f64_exact_bits(float x) {
+  const unsigned b = __float_as_uint(x), e = (b >> 23) & 0xffu;
+  if (e - 1u < 254u)  // normal: the exponent rebiased by 1023 - 127 = 896, the mantissa moved up by 29 bits
+    return __hiloint2double((int)((b & 0x80000000u) | (((b & 0x7fffffffu) >> 3) + 0x38000000u)), (int)(b << 29));
+  if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);  // ±0
+  return f64_exact_bits_general(x);
+}
+
+// Self-test of f32_rn_bits and f64_exact_bits against the hardware conversions over n hashed bit patterns
+// of each width: binary64 patterns over every exponent, every other one with its exponent within binary32's
+// range ± 30 binades (subnormal, normal and overflowing results) and every fourth an exact rounding tie;
+// binary32 patterns over every exponent.  Adds the mismatches (two NaNs agree) to *bad.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {  // SplitMix64's finaliser
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+static __global__ void k_selftest_conversions(long long n, unsigned long long* bad) {
+  unsigned long long local = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    const unsigned long long h = mix64(0x9e3779b97f4a7c15ull * (unsigned long long)(k + 1));
+    unsigned long long b = h;
+    if (k & 1) {
+      const unsigned long long e = 1023 - 160 + mix64(h) % 290;
+      b = (b & 0x800fffffffffffffull) | (e << 52);
+      if (k & 2) b = (b & ~0x1fffffffull) | 0x10000000ull;
+    }
+    const double x = __longlong_as_double((long long)b);
+    const float a = f32_rn_bits(x), hw = __double2float_rn(x);
+    local += !(__float_as_uint(a) == __float_as_uint(hw) || (isnan(a) && isnan(hw)));
+    const float f = __uint_as_float((unsigned)(h >> 17));
+    const double a2 = f64_exact_bits(f), hw2 = (double)f;
+    local += !(__double_as_longlong(a2) == __double_as_longlong(hw2) || (isnan(a2) && isnan(hw2)));
+  }
+  if (local) atomicAdd(bad, local);
+}
+
 template <typename TR>
 __device__ __forceinline__ TR powT(TR a, TR b);
 template <>
 __device__ __forceinline__ double powT<double>(double a, double b) { return pow(a, b); }
 template <>
 __device__ __forceinline__ float powT<float>(float a, float b) { return powf(a, b); }
+
+// The float relinearisation of one h cell after its strain rate ssr and centred speed avs (both zero off
+// the ice): drag (update_β!, update_basal_drag!), the σ-level viscosity sweeps (update_viscosity!), the
+// quadratures (update_av_viscosity!, update_quadrature_f1/f2!) and βeff, with the FP64 fields converted by
+// integer operations.
+__device__ __forceinline__ void relin_h_float_cell(const Dims& d, const RelinIn& in, const RelinOut& out, int c,
+                                                   float ssr, float avs, bool hm) {
+  const DevParams* P = in.P;
+  const float f2_prev = f32_rn_bits(out.quad_f2[c]), beta_prev = f32_rn_bits(out.beta[c]);
+  const float bs = avs / (1.0f + f2_prev * beta_prev);
+  const float ur = P->weertman_reg_speed_f;
+  const float beta = f32_rn_bits(in.wc[c]) * powf(sqrtf(bs * bs + ur * ur), P->weertman_ex_f);
+  const float tau = beta * bs;
+  out.shelf_strain_rate[c] = f64_exact_bits(ssr);
+  out.av_speed[c] = f64_exact_bits(avs);
+  out.bed_speed[c] = f64_exact_bits(bs);
+  out.beta[c] = f64_exact_bits(beta);
+  out.tau_bed[c] = f64_exact_bits(tau);
+  const float hh = f32_rn_bits(in.h[c]);
+  float eav = 0.0f, f1 = 0.0f, f2 = 0.0f;
+  if (hm) {
+    const float ex = P->glen_ex_f, er2 = P->glen_er2_f;
+    const int n_iter_viscosity = P->n_iter_viscosity;
+    const float e2 = ssr * ssr;
+    for (int k = 0; k < d.ns; ++k) {
+      const size_t q = (size_t)c + (size_t)d.Nh * k;
+      float eta = f32_rn_bits(out.eta[q]);
+      const float B = f32_rn_bits(in.glen_b[q]), zk = in.zeta_f[k], wk = in.qw_f[k];
+      const float tz = tau * zk;
+      for (int it = 0; it < n_iter_viscosity; ++it) {
+        const float t = tz / eta;
+        eta = 0.5f * B * powf(sqrtf(e2 + 0.25f * (t * t) + er2), ex);
+      }
+      out.eta[q] = f64_exact_bits(eta);
+      const float ie = 1.0f / eta, hz = wk * hh * zk * ie;
+      eav += wk * eta;
+      f1 += hz;
+      f2 += hz * zk;
+    }
+  }
+  out.eta_av[c] = f64_exact_bits(eav);
+  out.quad_f1[c] = f64_exact_bits(f1);
+  out.quad_f2[c] = f64_exact_bits(f2);
+  out.beta_eff[c] = f64_exact_bits(beta / (1.0f + f2 * beta));
+  const float hn = hh * eav;
+  out.hn[c] = f64_exact_bits(hn);
+  const float hh_m = hm ? hn : 0.0f;
+  const double dm = hm ? P->c0 * in.dsdh[c] : 0.0;
+  out.heta_h64[c] = f64_exact_bits(hh_m);
+  out.dimp64[c] = dm;
+  if (out.heta_h32) {
+    out.heta_h32[c] = hh_m;
+    out.dimp32[c] = f32_rn_bits(dm);
+  }
+}
 
 template <typename TR>
 __global__ void k_relin_h(Dims d, RelinIn in, RelinOut out) {
@@ -288,6 +452,39 @@ __global__ void k_relin_h(Dims d, RelinIn in, RelinOut out) {
   const bool hm = in.h_mask[c];
   // strain-rate components (masked velocities: gu.crop*gu.u)
   const double u0 = um(i, j), u1 = um(i + 1, j), v0 = vm(i, j), v1 = vm(i, j + 1);
+  if constexpr (std::is_same<TR, float>::value) {
+    // FP32 viscosity sweeps (mixed precision): η carries float precision, so everything after the velocity
+    // differences runs in float too — speeds, β (powf), the sweeps, one reciprocal of η per level for the
+    // quadratures, βeff.  FP64 arithmetic is left only where float would lose the result: the differences
+    // of neighbouring velocities (each rounded to float afterwards) and the FP64 coefficient c0·∂s/∂h.
+    // Every load and store of an FP64 field converts by integer operations (f32_rn_bits, f64_exact_bits):
+    // GB300's FP64 pipe, which the hardware conversions use, bounded this kernel.
+    if (hm) {
+      const float rdx = f32_rn_bits(d.rdx), rdy = f32_rn_bits(d.rdy);
+      const float fx = f32_rn_bits(u1 - u0) * rdx, fy = f32_rn_bits(v1 - v0) * rdy;
+      float sx[2] = {0.0f, 0.0f};
+      for (int tb = 0; tb < 2; ++tb) {
+        const int cb = j - 1 + tb;
+        float acc = 0.0f;
+        for (int ta = 0; ta < 2; ++ta) {
+          const int ca = i - 1 + ta;
+          if (ca < 0 || ca >= d.nx - 1 || cb < 0 || cb >= d.ny - 1) continue;
+          if (!in.c_mask[cidx(d, ca, cb)]) continue;
+          const float uy = f32_rn_bits(um(ca + 1, cb + 1) - um(ca + 1, cb)) * rdy;
+          const float vx = f32_rn_bits(vm(ca + 1, cb + 1) - vm(ca, cb + 1)) * rdx;
+          acc += 0.5f * (uy + vx);
+        }
+        sx[tb] = acc;
+      }
+      const float fs = 0.5f * sx[0] + 0.5f * sx[1];
+      const float ssr = sqrtf(fx * fx + fy * fy + fx * fy + 0.25f * (fs * fs));
+      const float uc = 0.5f * f32_rn_bits(u0 + u1), vc = 0.5f * f32_rn_bits(v0 + v1);
+      relin_h_float_cell(d, in, out, c, ssr, sqrtf(uc * uc + vc * vc), true);
+    } else {
+      relin_h_float_cell(d, in, out, c, 0.0f, 0.0f, false);
+    }
+    return;
+  }
   const double ux = hm ? (u1 * d.rdx - u0 * d.rdx) : 0.0;
   const double vy = hm ? (v1 * d.rdy - v0 * d.rdy) : 0.0;
   // c -> h average of the c-masked shear at the up-to-four surrounding corners (CGrid.jl:45)
@@ -308,65 +505,6 @@ __global__ void k_relin_h(Dims d, RelinIn in, RelinOut out) {
       sx[tb] = acc;
     }
     shear = 0.5 * sx[0] + 0.5 * sx[1];
-  }
-  if constexpr (std::is_same<TR, float>::value) {
-    // FP32 viscosity sweeps (mixed precision): η carries float precision, so everything after the velocity
-    // differences runs in float too — speeds, β (powf), the sweeps, one reciprocal of η per level for the
-    // quadratures, βeff — and only the loads and stores of the FP64 fields convert.  (In FP64 these are a
-    // pow per cell and two divisions per level and cell, which bound the kernel on GB300's FP64 rate.)
-    const float fx = (float)ux, fy = (float)vy, fs = (float)shear;
-    const float ssr = sqrtf(fx * fx + fy * fy + fx * fy + 0.25f * (fs * fs));
-    const float uc = hm ? (float)(0.5 * u0 + 0.5 * u1) : 0.0f;
-    const float vc = hm ? (float)(0.5 * v0 + 0.5 * v1) : 0.0f;
-    const float avs = sqrtf(uc * uc + vc * vc);
-    const float f2_prev = (float)out.quad_f2[c], beta_prev = (float)out.beta[c];
-    const float bs = avs / (1.0f + f2_prev * beta_prev);
-    const float ur = (float)in.P->weertman_reg_speed;
-    const float beta = (float)in.wc[c] * powf(sqrtf(bs * bs + ur * ur), (float)(1.0 / in.P->weertman_m - 1.0));
-    const float tau = beta * bs;
-    out.shelf_strain_rate[c] = ssr;
-    out.av_speed[c] = avs;
-    out.bed_speed[c] = bs;
-    out.beta[c] = beta;
-    out.tau_bed[c] = tau;
-    float eav = 0.0f, f1 = 0.0f, f2 = 0.0f;
-    if (hm) {
-      const float ex = (float)(1.0 / in.P->glen_n - 1.0);
-      const float er2 = (float)(in.P->glen_reg_strain_rate * in.P->glen_reg_strain_rate);
-      const int n_iter_viscosity = in.P->n_iter_viscosity;
-      const float e2 = ssr * ssr;
-      const float hh = (float)in.h[c];
-      for (int k = 0; k < d.ns; ++k) {
-        const size_t q = (size_t)c + (size_t)d.Nh * k;
-        float eta = (float)out.eta[q];
-        const float B = (float)in.glen_b[q], zk = (float)in.zeta[k], wk = (float)in.qw[k];
-        const float tz = tau * zk;
-        for (int it = 0; it < n_iter_viscosity; ++it) {
-          const float t = tz / eta;
-          eta = 0.5f * B * powf(sqrtf(e2 + 0.25f * (t * t) + er2), ex);
-        }
-        out.eta[q] = eta;
-        const float ie = 1.0f / eta, hz = wk * hh * zk * ie;
-        eav += wk * eta;
-        f1 += hz;
-        f2 += hz * zk;
-      }
-    }
-    out.eta_av[c] = eav;
-    out.quad_f1[c] = f1;
-    out.quad_f2[c] = f2;
-    out.beta_eff[c] = beta / (1.0f + f2 * beta);
-    const float hn = (float)in.h[c] * eav;
-    out.hn[c] = hn;
-    const float hh_m = hm ? hn : 0.0f;
-    const double dm = hm ? in.P->c0 * in.dsdh[c] : 0.0;
-    out.heta_h64[c] = hh_m;
-    out.dimp64[c] = dm;
-    if (out.heta_h32) {
-      out.heta_h32[c] = hh_m;
-      out.dimp32[c] = (float)dm;
-    }
-    return;
   }
   const double ssr = sqrt(ux * ux + vy * vy + ux * vy + 0.25 * (shear * shear));
   // depth-averaged speed from centred velocities

@@ -90,6 +90,7 @@ struct wavi_ctx {
   double *h = nullptr, *s = nullptr, *dsdh = nullptr, *gf = nullptr, *wc = nullptr, *acc = nullptr, *melt = nullptr;
   double *h_uv = nullptr, *s_uv = nullptr, *gf_uv = nullptr, *glen_b = nullptr;
   double *zeta = nullptr, *qw = nullptr;
+  float *zeta_f = nullptr, *qw_f = nullptr;  // the same rounded to float
   // state
   double *uv = nullptr, *eta = nullptr, *beta = nullptr, *quad_f2 = nullptr;
   double* xc_full64 = nullptr;  // coarse correction cache (full layout, float64)
@@ -234,7 +235,7 @@ struct Tally {
 
 int enqueue_picard_head(wavi_ctx* c, const CondHandles& h, Tally& t) {
   const Dims& d = c->d;
-  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw, c->P};
+  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw, c->P, c->zeta_f, c->qw_f};
   RelinOut out{c->shelf, c->av_speed, c->bed_speed, c->beta, c->tau, c->eta, c->eta_av, c->quad_f1, c->quad_f2,
                c->beta_eff, c->heta_h64, c->dimp64, mixed(c) ? c->heta_h32 : nullptr, mixed(c) ? c->dimp32 : nullptr,
                c->hn};
@@ -905,6 +906,10 @@ int set_params(wavi_ctx* c, const wavi_params* p) {
   P.nsmooth = c->sp.nsmooth;
   P.n_iter_viscosity = c->sp.n_iter_viscosity;
   P.picard_test = c->opt.picard_test;
+  P.weertman_ex_f = (float)(1.0 / p->weertman_m - 1.0);
+  P.glen_ex_f = (float)(1.0 / p->glen_n - 1.0);
+  P.glen_er2_f = (float)(p->glen_reg_strain_rate * p->glen_reg_strain_rate);
+  P.weertman_reg_speed_f = (float)p->weertman_reg_speed;
   CK(cudaMemcpyAsync(c->P, c->hP, sizeof(DevParams), cudaMemcpyHostToDevice, c->st));
   return 0;
 }
@@ -1519,6 +1524,7 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   A(h_mask, Nh) A(c_mask, Nc) A(mask_uv, N) A(inner_uv, N) A(fixed_uv, N) A(wmask_uv, N)
   A(h, Nh) A(s, Nh) A(dsdh, Nh) A(gf, Nh) A(wc, Nh) A(acc, Nh) A(melt, Nh)
   A(h_uv, N) A(s_uv, N) A(gf_uv, N) A(glen_b, N3) A(zeta, (size_t)d.ns) A(qw, (size_t)d.ns)
+  A(zeta_f, (size_t)d.ns) A(qw_f, (size_t)d.ns)
   A(uv, N) A(eta, N3) A(beta, Nh) A(quad_f2, Nh) A(xc_full64, N)
   A(shelf, Nh) A(av_speed, Nh) A(bed_speed, Nh) A(tau, Nh) A(eta_av, Nh) A(quad_f1, Nh) A(beta_eff, Nh)
   A(beta_eff_uv, N) A(resid_uv, N) A(hn, Nh)
@@ -1666,6 +1672,13 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   e = (e != cudaSuccess) ? e : cudaMemcpy(c->fixed_uv, fx.data(), N, cudaMemcpyHostToDevice);
   e = (e != cudaSuccess) ? e : cudaMemcpy(c->zeta, zeta.data(), sizeof(double) * d.ns, cudaMemcpyHostToDevice);
   e = (e != cudaSuccess) ? e : cudaMemcpy(c->qw, g->quadrature_weights, sizeof(double) * d.ns, cudaMemcpyHostToDevice);
+  std::vector<float> zeta_f((size_t)d.ns), qw_f((size_t)d.ns);
+  for (int k = 0; k < d.ns; ++k) {
+    zeta_f[k] = (float)zeta[k];
+    qw_f[k] = (float)g->quadrature_weights[k];
+  }
+  e = (e != cudaSuccess) ? e : cudaMemcpy(c->zeta_f, zeta_f.data(), sizeof(float) * d.ns, cudaMemcpyHostToDevice);
+  e = (e != cudaSuccess) ? e : cudaMemcpy(c->qw_f, qw_f.data(), sizeof(float) * d.ns, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return bail(fail(c, WAVI_ERR_CUDA, "mask upload: %s", cudaGetErrorString(e)));
   *out = c;
   return WAVI_OK;
@@ -1720,7 +1733,7 @@ int wavi_relinearise_device(wavi_ctx* c, const wavi_params* p, wavi_fields* f) {
   TRY(upload(c, f, false));
   TRY(set_params(c, p));
   const Dims& d = c->d;
-  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw, c->P};
+  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw, c->P, c->zeta_f, c->qw_f};
   RelinOut out{c->shelf, c->av_speed, c->bed_speed, c->beta, c->tau, c->eta, c->eta_av, c->quad_f1, c->quad_f2,
                c->beta_eff, c->heta_h64, c->dimp64, mixed(c) ? c->heta_h32 : nullptr, mixed(c) ? c->dimp32 : nullptr,
                c->hn};
@@ -1779,7 +1792,7 @@ int wavi_time_relinearise_device(wavi_ctx* c, int repeats, double* avg_ms_h, dou
   if (!avg_ms_h || !avg_ms_uv || repeats < 1) return fail(c, WAVI_ERR_ARGUMENT, "bad arguments");
   if (!c->fields_loaded) return fail(c, WAVI_ERR_ARGUMENT, "no fields on the context yet (relinearise or solve first)");
   const Dims& d = c->d;
-  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw, c->P};
+  RelinIn in{c->uv, c->mask_uv, c->h_mask, c->c_mask, c->h, c->wc, c->glen_b, c->dsdh, c->zeta, c->qw, c->P, c->zeta_f, c->qw_f};
   RelinOut out{c->shelf, c->av_speed, c->bed_speed, c->beta, c->tau, c->eta, c->eta_av, c->quad_f1, c->quad_f2,
                c->beta_eff, c->heta_h64, c->dimp64, mixed(c) ? c->heta_h32 : nullptr, mixed(c) ? c->dimp32 : nullptr,
                c->hn};
@@ -1823,6 +1836,22 @@ int wavi_op_diagonal_device(wavi_ctx* c, int precision, void* diag_uv) {
     return fail(c, WAVI_ERR_ARGUMENT, "float32 diagonal needs a mixed-precision context");
   CKL();
   CK(cudaStreamSynchronize(c->st));
+  return 0;
+}
+
+int wavi_selftest_conversions(wavi_ctx* c, long long n, long long* mismatches) {
+  TRY(check_ctx(c));
+  if (!mismatches) return fail(c, WAVI_ERR_ARGUMENT, "null pointer");
+  if (n < 0 || n > (1LL << 32)) return fail(c, WAVI_ERR_ARGUMENT, "n must be in 0..2^32 (got %lld)", n);
+  CK(cudaMemsetAsync(c->selftest, 0, 2 * sizeof(unsigned long long), c->st));
+  int nsm = 0;
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev));
+  k_selftest_conversions<<<std::max(1, nsm) * 8, 256, 0, c->st>>>(n, c->selftest);
+  CKL();
+  unsigned long long out = 0;
+  CK(cudaMemcpyAsync(&out, c->selftest, sizeof(out), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  *mismatches = (long long)out;
   return 0;
 }
 

@@ -231,6 +231,15 @@ class VelocitySolver:
         if st != 0:
             raise self._err(st)
 
+    def selftest_conversions(self, n=1 << 26):
+        """Compare the library's integer binary64 <-> binary32 conversions with the hardware ones over n
+        hashed patterns of each width (wavi_selftest_conversions).  Returns the number of mismatches."""
+        bad = C.c_longlong()
+        st = self.lib.wavi_selftest_conversions(self.ctx, int(n), C.byref(bad))
+        if st != 0:
+            raise self._err(st)
+        return bad.value
+
     def selftest_watchdog(self):
         """Run the bounded-wait self-test (wavi_selftest_watchdog): True if the wait gave up as designed."""
         fired = C.c_int(0)
