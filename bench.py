@@ -7,15 +7,21 @@ initial all-true wavelet coarse space) after the update_state! steps that preced
 step restores that state and solves it to ||b - A u|| / ||b|| < 1e-6 (maxiter_picard = 100; the
 reference's other solver parameters).
 
-  value    mixed precision (float32 operator / V-cycle, float64 residual and reductions), fields resident
-           in HBM, device time per step from CUDA events on the solver's stream, L2 flushed between steps
+  value    mixed precision (float32 operator / V-cycle, float64 residual and reductions) with its default
+           Picard iteration (Anderson-accelerated, wavi_picard_accel; --picard-accel), fields resident in
+           HBM, device time per step from CUDA events on the solver's stream, L2 flushed between steps
+  mixed_plain / mixed_anderson  the same mixed solve with the other Picard iteration (the reference's
+           plain one beside the accelerated default), with its error against the oracle
   e2e      the same solve through the host C ABI (wavi_solve_velocities) from pinned host buffers, the
            host<->device copies inside the timed region
   fp64_gpu the reference algorithm in float64 on the GPU (cg! coarse solve; the comparison the metric names)
-  fp64_gpu_same_solver  float64 with the mixed solve's own coarse solver: mixed_over_fp64_same_solver is
-           the gain of precision alone, mixed_over_fp64 that of precision and coarse solver together
+  fp64_gpu_same_solver  float64 with the mixed solve's own coarse solver and Picard iteration:
+           mixed_over_fp64_same_solver is the gain of precision alone, mixed_over_fp64 that of precision,
+           coarse solver and Picard acceleration together
   rel_err_*_vs_oracle  relative velocity error of each GPU solve against the FP64 oracle's converged solve
-           of the same state (tests/golden/c2_oracle_solution.npz)
+           of the same state with the reference's algorithm and stopping rule
+           (tests/golden/c2_oracle_solution.npz); *_vs_oracle_fixed_point against the oracle's solve of the
+           same state to 1e-11 (tests/golden/c2_oracle_fixed_point.npz)
   mixed_fp64_coarse_sums / mixed_fp64_coarse_solve  the mixed solve with the coarse CG's sums, or the
            whole coarse CG, in FP64 (wavi_coarse_sums): what the default's float-float sums and FP32 coarse
            solve save
@@ -299,6 +305,14 @@ def c2_fixture():
         return None
 
 
+def c2_fixed_point():
+    """The FP64 oracle's solve of this workload to 1e-11 (tests/golden/make_c2_fixed_point.py), or None."""
+    try:
+        return np.load(os.path.join(os.path.dirname(C2_FIXTURE), "c2_oracle_fixed_point.npz"))
+    except OSError:
+        return None
+
+
 def rel_err_uv(u, v, ref_u, ref_v):
     """||(u, v) - (u, v)_ref||_2 / ||(u, v)_ref||_2 over the whole u and v grids."""
     num = np.sqrt(np.sum((np.asarray(u).ravel() - np.asarray(ref_u).ravel(order="F")) ** 2) +
@@ -413,7 +427,7 @@ def gpu_arm(args):
 
     mixed = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=args.coarse_solver,
                            cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums,
-                           viscosity=args.viscosity)
+                           viscosity=args.viscosity, picard_accel=args.picard_accel)
     fp64 = VelocitySolver(g, sp, precision="fp64", device=local)
 
     # float64 reference algorithm on the GPU
@@ -436,11 +450,12 @@ def gpu_arm(args):
     same = None
     if mixed_solver != "pipelined_chebyshev":
         fp64s = VelocitySolver(g, sp, precision="fp64", device=local, coarse_solver=mixed_solver,
-                               cheb_steps=args.cheb_steps)
+                               cheb_steps=args.cheb_steps, picard_accel=stmix[-1]["picard_accel"])
         t64s, st64s, out64s = time_device_solves(torch, fp64s, p, snapshot, max(1, args.steps // 2), 1)
         fp64s.close()
         same = {"value": world * len(t64s) / sum(t64s), "unit": "solves/s", "ms_per_step": 1e3 * sum(t64s) / len(t64s),
-                "coarse_solver": st64s[-1]["coarse_solver"], "picard_iterations": st64s[-1]["picard_iterations"],
+                "coarse_solver": st64s[-1]["coarse_solver"], "picard_accel": st64s[-1]["picard_accel"],
+                "picard_iterations": st64s[-1]["picard_iterations"],
                 "coarse_cg_iterations": st64s[-1]["coarse_cg_iterations"], "status_name": st64s[-1]["status_name"]}
 
     # the mixed solve with its coarse CG's dot products, sums and scalars in FP64 (WAVI_SUMS_FP64) instead of
@@ -475,6 +490,19 @@ def gpu_arm(args):
                        "ms_per_step": 1e3 * sum(tc64) / len(tc64), "picard_iterations": stc64[-1]["picard_iterations"],
                        "coarse_cg_iterations": stc64[-1]["coarse_cg_iterations"],
                        "status_name": stc64[-1]["status_name"]}
+
+    # the mixed solve with the other Picard iteration (wavi_picard_accel): the reference's plain iteration
+    # beside an accelerated headline, or Anderson acceleration beside a plain one
+    other_accel = "anderson" if args.picard_accel == "plain" else "plain"
+    mo = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=args.coarse_solver,
+                        cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums, viscosity=args.viscosity,
+                        picard_accel=other_accel)
+    tao, stao, outao = time_device_solves(torch, mo, p, snapshot, args.steps, 1)
+    mo.close()
+    accel_other = {"picard_accel": other_accel, "value": world * len(tao) / sum(tao), "unit": "solves/s",
+                   "ms_per_step": 1e3 * sum(tao) / len(tao),
+                   **{k: stao[-1][k] for k in ("picard_iterations", "coarse_cg_iterations", "anderson_steps",
+                                                "rel_residual", "status_name")}}
 
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
@@ -524,10 +552,21 @@ def gpu_arm(args):
             sums64["rel_err_vs_oracle"] = rel_err_uv(outm64["u"], outm64["v"], ref["u"], ref["v"])
         if outc64 is not None:
             solve64["rel_err_vs_oracle"] = rel_err_uv(outc64["u"], outc64["v"], ref["u"], ref["v"])
+        accel_other["rel_err_vs_oracle"] = rel_err_uv(outao["u"], outao["v"], ref["u"], ref["v"])
         errs_oracle["oracle"] = {"picard_iterations": int(ref["picard_iterations"]),
                                  "coarse_cg_iterations": int(ref["coarse_cg_iterations"]),
                                  "rel_residual": float(ref["rel_residual"]),
                                  "source": "tests/golden/c2_oracle_solution.npz (FP64 oracle, same state)"}
+    fpt = c2_fixed_point()
+    if fpt is not None:
+        # against the oracle's solve to 1e-11: the fixed point both Picard iterations converge to
+        errs_oracle["rel_err_mixed_vs_oracle_fixed_point"] = rel_err_uv(outmix["u"], outmix["v"], fpt["u"], fpt["v"])
+        errs_oracle["rel_err_fp64_vs_oracle_fixed_point"] = rel_err_uv(out64["u"], out64["v"], fpt["u"], fpt["v"])
+        accel_other["rel_err_vs_oracle_fixed_point"] = rel_err_uv(outao["u"], outao["v"], fpt["u"], fpt["v"])
+        errs_oracle["oracle_fixed_point"] = {"picard_iterations": int(fpt["picard_iterations"]),
+                                             "rel_residual": float(fpt["rel_residual"]),
+                                             "source": "tests/golden/c2_oracle_fixed_point.npz (FP64 oracle, same "
+                                                       "state, solved to 1e-11)"}
     fp64_value = world * len(t64) / sum(t64)
 
     cpu = None
@@ -549,13 +588,15 @@ def gpu_arm(args):
         "fp64_gpu_same_solver": same,
         "mixed_over_fp64": value / fp64_value if fp64_value else None,
         "mixed_over_fp64_same_solver": value / same["value"] if same else None,
+        "picard_accel": stmix[-1]["picard_accel"],
+        "mixed_" + other_accel: accel_other,
         "mixed_fp64_coarse_sums": sums64,
         "mixed_fp64_coarse_solve": solve64,
         "rel_err_mixed_vs_fp64": float(err),
         **errs_oracle,
         "solve": {k: stmix[-1][k] for k in ("picard_iterations", "coarse_cg_iterations", "op_applications",
                                              "rel_residual", "kernel_launches", "host_syncs", "status_name",
-                                             "coarse_solver", "coarse_kernel", "cheb_steps")},
+                                             "coarse_solver", "coarse_kernel", "cheb_steps", "anderson_steps")},
         "roofline": {"bound": "latency", "achieved": cg_achieved, "peak": peak, "unit": "GB/s",
                      "frac": cg_achieved / peak,
                      "traffic": ncu_traffic("coarse_cg_c2.md", "traffic_bytes_per_cg_iteration"),
@@ -596,10 +637,12 @@ def other_configs(args):
     import copy
     out = {}
     legs = (("c3", c3_arm, dict(steps=1, warmup=1),
-             ("metric", "value", "unit", "ms_per_step", "solve", "mixed_uncapped", "fp64_gpu", "mixed_over_fp64",
+             ("metric", "value", "unit", "ms_per_step", "solve", "picard_accel", "mixed_anderson", "mixed_plain",
+              "mixed_uncapped", "fp64_gpu", "mixed_over_fp64",
               "rel_err_mixed_vs_fp64", "roofline", "roofline_relin_fp64", "roofline_stencil", "coarse_cg_share")),
             ("c5", ensemble_arm, dict(steps=1, warmup=1, no_tune=True, members=256),
-             ("metric", "value", "unit", "ms_per_step", "members_converged", "all_members", "fp64_loop",
+             ("metric", "value", "unit", "ms_per_step", "members_converged", "picard_accel", "mixed_anderson",
+              "mixed_plain", "all_members", "fp64_loop",
               "ensemble_over_fp64_loop", "rel_err_vs_fp64_max", "rel_err_vs_fp64_median", "picard_iterations_mean")),
             ("c4", adjoint_arm, dict(steps=2, warmup=1, directions=2),
              ("metric", "value", "unit", "ms_per_step", "forward", "adjoint", "dot_test_rel_err", "fd_step",
@@ -666,7 +709,7 @@ def c3_arm(args):
     p = m.params
     mixed = VelocitySolver(g, sp, precision="mixed", picard_test=1, coarse_solver=args.coarse_solver,
                            cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums,
-                           viscosity=args.viscosity)
+                           viscosity=args.viscosity, picard_accel=args.picard_accel)
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         tmix, stmix, outmix = time_device_solves(torch, mixed, p, snapshot, args.steps, args.warmup)
@@ -676,9 +719,17 @@ def c3_arm(args):
     from dataclasses import replace as _replace
     long_sp = _replace(sp, maxiter_picard=200)
     mlong = VelocitySolver(g, long_sp, precision="mixed", picard_test=1, coarse_solver=args.coarse_solver,
-                           cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums, viscosity=args.viscosity)
+                           cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums, viscosity=args.viscosity,
+                           picard_accel="plain")
     tl, stl, _ = time_device_solves(torch, mlong, p, snapshot, 1, 0)
     mlong.close()
+    # the mixed solve with the other Picard iteration (wavi_picard_accel), at the configuration's cap
+    other_accel = "anderson" if args.picard_accel == "plain" else "plain"
+    mo = VelocitySolver(g, sp, precision="mixed", picard_test=1, coarse_solver=args.coarse_solver,
+                        cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums, viscosity=args.viscosity,
+                        picard_accel=other_accel)
+    tao, stao, outao = time_device_solves(torch, mo, p, snapshot, 1, 1)
+    mo.close()
     fp64 = VelocitySolver(g, sp, precision="fp64", picard_test=1)
     t64, st64, out64 = time_device_solves(torch, fp64, p, snapshot, 1, 1)
     err = rel_err_uv(outmix["u"], outmix["v"], out64["u"].reshape((g.nx + 1, g.ny), order="F"),
@@ -736,13 +787,18 @@ def c3_arm(args):
                    "picard_test": "||du||/||u|| <= tol and ||b - A u||/||b|| < tol",
                    "l2": "flushed between steps (256 MiB write)"},
         "solve": {k: last[k] for k in ("status_name", "picard_iterations", "coarse_cg_iterations", "rel_residual",
-                                       "rel_update", "coarse_solver", "kernel_launches")},
+                                       "rel_update", "coarse_solver", "kernel_launches", "anderson_steps")},
         "fp64_gpu": {"value": len(t64) / sum(t64), "unit": "solves/s", "ms_per_step": 1e3 * sum(t64) / len(t64),
                      **{k: st64[-1][k] for k in ("status_name", "picard_iterations", "coarse_cg_iterations",
                                                   "rel_residual", "rel_update", "coarse_solver")}},
-        "mixed_uncapped": {"maxiter_picard": 200, "seconds": tl[0],
+        "mixed_uncapped": {"maxiter_picard": 200, "picard_accel": "plain", "seconds": tl[0],
                            **{k: stl[-1][k] for k in ("status_name", "picard_iterations", "coarse_cg_iterations",
                                                       "rel_residual", "rel_update")}},
+        "picard_accel": last["picard_accel"],
+        "mixed_" + other_accel: {"picard_accel": other_accel, "value": len(tao) / sum(tao), "unit": "solves/s",
+                                 "ms_per_step": 1e3 * sum(tao) / len(tao),
+                                 **{k: stao[-1][k] for k in ("status_name", "picard_iterations", "coarse_cg_iterations",
+                                                              "anderson_steps", "rel_residual", "rel_update")}},
         "mixed_over_fp64": value / (len(t64) / sum(t64)),
         "rel_err_mixed_vs_fp64": err,
         "roofline": rel["mixed"],
@@ -803,7 +859,7 @@ def ensemble_arm(args):
         best, timings = dict(concurrency=8, coarse_kernel="auto", stencil_kernel="tiled"), []
     else:
         best, timings = autotune(grids, sps, params, make_tensors, sync=torch.cuda.synchronize)
-    ens = EnsembleSolver(grids, sps, precision="mixed", **best)
+    ens = EnsembleSolver(grids, sps, precision="mixed", picard_accel=args.picard_accel, **best)
     times, stats = [], None
     for it in range(args.warmup + args.steps):
         work = make_tensors()
@@ -816,6 +872,20 @@ def ensemble_arm(args):
     ens.close()
     conv = sum(1 for st in stats if st["status"] == 0)
     value = conv * len(times) / sum(times)  # converged solves only
+    # one ensemble solve with the other Picard iteration (wavi_picard_accel)
+    other_accel = "anderson" if args.picard_accel == "plain" else "plain"
+    eo = EnsembleSolver(grids, sps, precision="mixed", picard_accel=other_accel, **best)
+    eo.solve_device(params, make_tensors())  # graph instantiation
+    work_o = make_tensors()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    stats_o = eo.solve_device(params, work_o)
+    t_o = time.perf_counter() - t0
+    eo.close()
+    conv_o = sum(1 for st in stats_o if st["status"] == 0)
+    accel_other = {"picard_accel": other_accel, "value": conv_o / t_o, "unit": "solves/s", "seconds": t_o,
+                   "members_converged": conv_o,
+                   "picard_iterations_mean": float(np.mean([st["picard_iterations"] for st in stats_o]))}
     # looping the single-domain FP64 GPU solve, on every 8th member
     subset = list(range(0, n, 8))
     t64, errs = 0.0, []
@@ -846,6 +916,8 @@ def ensemble_arm(args):
         "rel_err_vs_fp64_max": max(errs) if errs else None,
         "rel_err_vs_fp64_median": float(np.median(errs)) if errs else None, "rel_err_members": len(errs),
         "members_converged": conv,
+        "picard_accel": stats[0]["picard_accel"],
+        "mixed_" + other_accel: accel_other,
         "note": "value counts the members that reach 1e-6 within maxiter_picard = 100 (members_converged); the "
                 "others stall the same way in FP64 (the reference algorithm's one V-cycle per Picard iteration). "
                 "ensemble_over_fp64_loop compares member solves per second, converged or not, on both sides",
@@ -1038,6 +1110,9 @@ def main():
                     help="accumulation of the mixed coarse CG's dot products (wavi_coarse_sums)")
     ap.add_argument("--viscosity", default="default", choices=("default", "fp32", "fp64"),
                     help="precision of the mixed solves' viscosity sweeps (wavi_viscosity)")
+    ap.add_argument("--picard-accel", default="auto", choices=("auto", "plain", "anderson"),
+                    help="Picard iteration of the timed mixed solves (wavi_picard_accel; auto = Anderson in mixed "
+                         "precision); the other one is reported beside it")
     ap.add_argument("--cheb-steps", type=int, default=0,
                     help="Chebyshev steps of the Chebyshev coarse solvers (0: the library's default, 3; else odd)")
     ap.add_argument("--config", default="c2", choices=("c2", "c3", "c4", "c5"),

@@ -65,6 +65,7 @@ def lib():
         L.oracle_kron_apply.argtypes = [C.c_int, C.c_int, dp, C.c_int, C.c_int, dp, dp, dp]
         L.oracle_set_coarse_variant.argtypes = [C.c_int]
         L.oracle_set_chebyshev.argtypes = [C.c_int, C.c_double]
+        L.oracle_set_anderson.argtypes = [C.c_int, C.c_double]
         L.oracle_coarse_diag.argtypes = [vp, dp, dp]
         _lib = L
     return _lib
@@ -232,6 +233,16 @@ def set_chebyshev(steps=CHEB_DEFAULT[0], ratio=CHEB_DEFAULT[1]):
     """The Chebyshev preconditioner of the "srcg_chebyshev" and "pipelined_chebyshev" variants: steps per
     application (odd) and the ratio b/a of its interval [a, b].  The defaults are the GPU library's."""
     lib().oracle_set_chebyshev(int(steps), float(ratio))
+
+
+ANDERSON_DEFAULT = (3, 0.3)
+
+
+def set_anderson(depth=0, start_rel=ANDERSON_DEFAULT[1]):
+    """Anderson acceleration of every later oracle solve's Picard loop: depth 0 (the reference's plain
+    iteration, the default) or 1..5 columns, from the first Picard iteration whose relative residual is
+    below start_rel.  Restates the GPU library's opt-in WAVI_PICARD_ANDERSON."""
+    lib().oracle_set_anderson(int(depth), float(start_rel))
 
 
 def pos_fraction(z, mask=None):

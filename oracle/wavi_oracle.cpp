@@ -1124,8 +1124,94 @@ void vcycle(Model& m, OpWork& w, Precond& p, Vec& x, const Vec& b) {
   smoother(m, w, p, x, b, bwd);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Anderson acceleration of the Picard loop (not in the reference; the GPU library's opt-in
+// wavi_options.picard_accel = WAVI_PICARD_ANDERSON, restated step for step).  Walker & Ni, "Anderson
+// acceleration for fixed-point iterations", SIAM J. Numer. Anal. 49 (2011), with the Picard iteration
+// x -> g(x) = x + V(x)(b(x) - A(x) x) (relinearisation, one V-cycle) as the fixed-point map.  The
+// acceleration starts at the first Picard iteration whose relative residual is below start_rel (the
+// iterations before it, from u = 0 and the default viscosity, are far from the asymptotic regime);
+// from then on each iteration keeps f = g(x) - x and g = g(x), stores the differences of consecutive
+// f and g in a ring of `depth` columns, and moves to x = g - dG gamma with gamma the least-squares
+// solution of min |f - dF gamma|: the normal equations with the columns newest first, by Cholesky;
+// at the first pivot that falls below 1e-10 of its diagonal entry (a column numerically in the span
+// of the newer ones) that column and every older one are left out.
+// ---------------------------------------------------------------------------------------------
+int g_aa_depth = 0;           // 0: the reference's plain Picard iteration
+double g_aa_start_rel = 0.3;  // first relative residual at which the acceleration acts
+constexpr int kAAMax = 5;
+constexpr double kAAPivot = 1e-10;
+
+struct Anderson {
+  bool started = false, have_prev = false;
+  int cols = 0, head = 0;  // columns held, next ring slot
+  Vec dF[kAAMax], dG[kAAMax], fprev, gprev;
+};
+
+// The accelerated iterate from x (before the V-cycle) and the V-cycle's correction f (g = x + f);
+// returns the columns used.
+int anderson_step(Anderson& a, const Vec& x, const Vec& f, Vec& out) {
+  const size_t n = x.size();
+  const int depth = std::min(g_aa_depth, kAAMax);
+  Vec g(n);
+  for (size_t i = 0; i < n; ++i) g[i] = x[i] + f[i];
+  if (a.have_prev) {
+    Vec& cf = a.dF[a.head];
+    Vec& cg = a.dG[a.head];
+    cf.resize(n);
+    cg.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+      cf[i] = f[i] - a.fprev[i];
+      cg[i] = g[i] - a.gprev[i];
+    }
+    a.head = (a.head + 1) % depth;
+    a.cols = std::min(a.cols + 1, depth);
+  }
+  a.fprev = f;
+  a.gprev = g;
+  a.have_prev = true;
+  out = g;
+  if (a.cols == 0) return 0;
+  int slot[kAAMax];  // newest first
+  for (int k = 0; k < a.cols; ++k) slot[k] = ((a.head - 1 - k) % depth + depth) % depth;
+  double G[kAAMax][kAAMax], rhs[kAAMax], L[kAAMax][kAAMax] = {};
+  for (int p = 0; p < a.cols; ++p) {
+    for (int q = 0; q <= p; ++q) G[p][q] = G[q][p] = dotp(a.dF[slot[p]], a.dF[slot[q]]);
+    rhs[p] = dotp(a.dF[slot[p]], f);
+  }
+  int used = 0;
+  for (int p = 0; p < a.cols; ++p) {
+    for (int q = 0; q < p; ++q) {
+      double s = G[p][q];
+      for (int k = 0; k < q; ++k) s -= L[p][k] * L[q][k];
+      L[p][q] = s / L[q][q];
+    }
+    double s = G[p][p];
+    for (int k = 0; k < p; ++k) s -= L[p][k] * L[p][k];
+    if (!(s > kAAPivot * G[p][p])) break;
+    L[p][p] = std::sqrt(s);
+    used = p + 1;
+  }
+  double y[kAAMax], gam[kAAMax];
+  for (int p = 0; p < used; ++p) {
+    double s = rhs[p];
+    for (int k = 0; k < p; ++k) s -= L[p][k] * y[k];
+    y[p] = s / L[p][p];
+  }
+  for (int p = used - 1; p >= 0; --p) {
+    double s = y[p];
+    for (int k = p + 1; k < used; ++k) s -= L[k][p] * gam[k];
+    gam[p] = s / L[p][p];
+  }
+  for (int p = 0; p < used; ++p) {
+    const Vec& c = a.dG[slot[p]];
+    for (size_t i = 0; i < n; ++i) out[i] -= gam[p] * c[i];
+  }
+  return used;
+}
+
 // precondition!(model, ::BasicParallelSpec)                              update_velocities.jl:50-83
-bool precondition_model(Model& m, OpWork& w, double& rel) {
+bool precondition_model(Model& m, OpWork& w, double& rel, Anderson* aa = nullptr) {
   const int ni = m.ni_u + m.ni_v;
   Vec x((size_t)ni);  // get_start_guess :92-97
   for (int k = 0; k < m.ni_u; ++k) x[k] = m.u[m.u_inner_idx[k]];
@@ -1164,7 +1250,17 @@ bool precondition_model(Model& m, OpWork& w, double& rel) {
     for (size_t k = 0; k < p.wu_idx.size(); ++k) m.wu_corr[p.wu_idx[k]] = p.corr[k];  // set_correction_coarse!
     for (size_t k = 0; k < p.wv_idx.size(); ++k) m.wv_corr[p.wv_idx[k]] = p.corr[p.wu_idx.size() + k];
   }
-  for (int i = 0; i < ni; ++i) x[i] = x[i] + corr[i];
+  if (aa && !converged && !aa->started && rel < g_aa_start_rel) aa->started = true;
+  if (aa && !converged && aa->started) {
+    Vec xa;
+    anderson_step(*aa, x, corr, xa);
+    for (int i = 0; i < ni; ++i) {
+      corr[i] = xa[i] - x[i];  // the iteration's whole update
+      x[i] = xa[i];
+    }
+  } else {
+    for (int i = 0; i < ni; ++i) x[i] = x[i] + corr[i];
+  }
   m.rel_history.push_back(rel);
   m.upd_history.push_back(converged ? 0.0 : norm2(corr) / norm2(x));
   for (int k = 0; k < m.ni_u; ++k) m.u[m.u_inner_idx[k]] = x[k];  // set_velocities! :190-195
@@ -1184,10 +1280,11 @@ void update_velocities(Model& m) {
   m.upd_history.clear();
   m.cheb_eig.assign((size_t)(m.Nu + m.Nv), 0.0);
   m.cheb_vcycles = 0;
+  Anderson aa;
   while (!converged && it < m.S.maxiter_picard) {
     ++it;
     inner_update(m);
-    converged = precondition_model(m, w, rel);
+    converged = precondition_model(m, w, rel, g_aa_depth > 0 ? &aa : nullptr);
   }
   m.last_picard = it;
   m.last_rel_resid = rel;
@@ -1511,6 +1608,12 @@ int oracle_vcycle(void* h, const double* ru, const double* rv, double* cu, doubl
   return p.last_cg;
 }
 void oracle_set_coarse_variant(int variant) { g_coarse_variant = variant; }
+// Anderson acceleration of later solves: depth 0 (the reference's Picard loop) or 1..5 columns, from the
+// first Picard iteration whose relative residual is below start_rel.
+void oracle_set_anderson(int depth, double start_rel) {
+  g_aa_depth = std::max(0, std::min(depth, kAAMax));
+  g_aa_start_rel = start_rel;
+}
 // The Chebyshev preconditioner of variants 4 and 5: steps per application (odd, >= 1) and the interval's
 // ratio b / a.
 void oracle_set_chebyshev(int steps, double ratio) {

@@ -260,7 +260,8 @@ def test_persistent_smoother_matches_per_step_smoother(oracle):
     out = {}
     for stencil in ("tiled", "streaming"):
         f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
-        s = VelocitySolver(g, sp, precision="mixed", stencil_kernel=stencil, coarse_solver=solver)
+        s = VelocitySolver(g, sp, precision="mixed", stencil_kernel=stencil, coarse_solver=solver,
+                           picard_accel="plain")  # the smoother under test, not the Picard loop's acceleration
         st = s.solve(p, f)  # 12 Picard iterations (the tolerance is out of reach)
         s.close()
         assert st["picard_iterations"] == 12, (stencil, st)
@@ -276,7 +277,9 @@ def test_mixed_viscosity_precision_tracks_the_reference(oracle):
     itself does not reach tol_picard = 1e-6 within 100 Picard iterations (its residual oscillates between
     3.6e-6 and 9e-6; every V-cycle's coarse solve converges): the GPU follows it there too.  With FP64
     viscosity sweeps (WAVI_VISCOSITY_FP64) the velocities agree to 1e-9 and the final residual to 1 %
-    (GB300: 1.1e-11); with the default FP32 sweeps to 1e-6 (GB300: 9.9e-8)."""
+    (GB300: 1.1e-11); with the default FP32 sweeps to 1e-6 (GB300: 9.9e-8).  Both with the reference's
+    plain Picard iteration; the mixed default, Anderson-accelerated, converges here (the reference's loop
+    does not)."""
     from wavi_gb300 import synthetic
     from wavi_gb300.gpu import VelocitySolver
     g, bed, p, sp, ic = synthetic.small_case(nx=96, ny=32, dx=2000.0, mask="full", maxiter_picard=100, tol_picard=1e-6)
@@ -287,14 +290,17 @@ def test_mixed_viscosity_precision_tracks_the_reference(oracle):
     ost = om.stats()
     assert ost["picard_iterations"] == 100  # the reference does not converge here
     res = {}
-    for visc in ("fp64", "default"):
+    for visc, accel in (("fp64", "plain"), ("default", "plain"), ("default", "auto")):
         f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
-        s = VelocitySolver(g, sp, precision="mixed", viscosity=visc)
+        s = VelocitySolver(g, sp, precision="mixed", viscosity=visc, picard_accel=accel)
         st = s.solve(p, f)
         s.close()
-        res[visc] = (st, uv_err(f, om))
-        print(visc, st["status_name"], st["picard_iterations"], st["rel_residual"], res[visc][1], ost["rel_residual"])
-    st, err = res["fp64"]
+        res[visc, accel] = (st, uv_err(f, om))
+        print(visc, accel, st["status_name"], st["picard_iterations"], st["rel_residual"], res[visc, accel][1],
+              ost["rel_residual"])
+    st, err = res["fp64", "plain"]
     assert err < 1e-9, err
     assert abs(st["rel_residual"] - ost["rel_residual"]) <= 1e-2 * ost["rel_residual"], (st, ost)
-    assert res["default"][1] < 1e-6
+    assert res["default", "plain"][1] < 1e-6
+    st, err = res["default", "auto"]
+    assert st["picard_accel"] == "anderson" and st["status"] == 0, st

@@ -10,7 +10,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libwavi_gpu.so")
 
-WAVI_ABI_VERSION = 3
+WAVI_ABI_VERSION = 4
 
 STATUS = {
     0: "WAVI_OK", -1: "WAVI_ERR_ARGUMENT", -2: "WAVI_ERR_CUDA", -3: "WAVI_ERR_NONFINITE",
@@ -26,6 +26,8 @@ COARSE_SOLVERS = {"auto": 0, "cg": 1, "srcg": 2, "srcg_jacobi": 3, "srcg_chebysh
 COARSE_SOLVER_NAMES = {v: k for k, v in COARSE_SOLVERS.items()}
 COARSE_SUMS = {"default": 0, "float_float": 1, "fp64": 2, "fp64_solve": 3}  # wavi_coarse_sums
 VISCOSITY = {"default": 0, "fp32": 1, "fp64": 2}  # wavi_viscosity
+PICARD_ACCEL = {"auto": 0, "plain": 1, "anderson": 2}  # wavi_picard_accel
+PICARD_ACCEL_NAMES = {v: k for k, v in PICARD_ACCEL.items()}
 
 _dp = C.POINTER(C.c_double)
 _u8p = C.POINTER(C.c_uint8)
@@ -59,7 +61,7 @@ class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graphs", C.c_int32),
                 ("picard_test", C.c_int32), ("coarse_kernel", C.c_int32), ("coarse_solver", C.c_int32),
                 ("stencil_kernel", C.c_int32), ("cheb_steps", C.c_int32), ("coarse_sums", C.c_int32),
-                ("viscosity", C.c_int32)]
+                ("viscosity", C.c_int32), ("picard_accel", C.c_int32), ("anderson_depth", C.c_int32)]
 
 
 FIELD_INPUTS = ("h", "s", "dsdh", "grounded_fraction", "weertman_c", "accumulation", "basal_melt",
@@ -83,7 +85,8 @@ class Stats(C.Structure):
                 ("algorithmic_bytes", C.c_double), ("elapsed_ms", C.c_double),
                 ("kernel_launches", C.c_int32), ("host_syncs", C.c_int32),
                 ("coarse_ms", C.c_double), ("coarse_solver", C.c_int32), ("coarse_launches", C.c_int32),
-                ("coarse_kernel", C.c_int32), ("cheb_steps", C.c_int32)]
+                ("coarse_kernel", C.c_int32), ("cheb_steps", C.c_int32), ("anderson_steps", C.c_int32),
+                ("picard_accel", C.c_int32)]
 
 
 class OperatorDesc(C.Structure):

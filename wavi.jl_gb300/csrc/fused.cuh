@@ -17,6 +17,19 @@
 
 namespace wavi {
 
+// Anderson acceleration of the Picard loop (anderson.cuh): at most kAAMax columns; a pivot below kAAPivot
+// of its diagonal entry drops that column and every older one.
+constexpr int kAAMax = 5;
+constexpr double kAAPivot = 1e-10;
+struct AAState {
+  int started, have_prev;  // the acceleration acts from this iteration on; f and g of the last are kept
+  int cols, head;          // columns held; ring slot of the newest
+  int used, steps;         // columns in the last step's gamma; accelerated steps in this solve
+  int slot[kAAMax];        // ring slots of gamma[0..used), newest first
+  double gamma[kAAMax];
+  double gram[kAAMax][kAAMax];  // dF^T dF by ring slot
+};
+
 // Device-side solver state: scalars, counters and the flags that steer the conditional nodes.
 struct DevState {
   double rr, bb, rel, rel_prev_update;   // Picard residual norms
@@ -25,8 +38,9 @@ struct DevState {
   int picard_it, picard_continue, vcycle_needed, converged;
   int cg_it, cg_continue, cg_total, status;
   unsigned counter[8];                   // last-block counters, one per reduction site
+  AAState aa;
 };
-enum { CNT_A = 0, CNT_B = 1, CNT_C = 2, CNT_D = 3 };
+enum { CNT_A = 0, CNT_B = 1, CNT_C = 2, CNT_D = 3, CNT_AA_STAGE = 4, CNT_AA_APPLY = 5 };
 
 struct CondHandles {
   cudaGraphConditionalHandle picard, vcycle, cg;

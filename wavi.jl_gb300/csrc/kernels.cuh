@@ -246,6 +246,8 @@ struct DevParams {
   double tol_picard, tol_coarse, omega;
   int maxiter_picard, maxiter_coarse, nsmooth, n_iter_viscosity;
   int picard_test;
+  int aa_depth;         // Anderson acceleration of the Picard loop: columns (0: the reference's iteration)
+  double aa_start_rel;  // ... from the first Picard iteration whose relative residual is below this
   // the float relinearisation's uniform constants, rounded once on the host: 1/m - 1, 1/n - 1 (the
   // exponents of β and of the viscosity), the squared strain-rate regularisation, the speed regularisation
   float weertman_ex_f, glen_ex_f, glen_er2_f, weertman_reg_speed_f;

@@ -34,6 +34,7 @@
 #include "persistent.cuh"
 #include "adjoint.cuh"
 #include "timestep.cuh"
+#include "anderson.cuh"
 
 using namespace wavi;
 
@@ -43,6 +44,9 @@ constexpr int EW_THREADS = 256;
 constexpr int CG_BATCH = 8;
 // grids with at least this many (nx+1) x (ny+1) points use the row-streaming operator by default
 constexpr long kStreamMinPoints = 1L << 19;
+// Anderson acceleration: default columns, and the relative residual below which it starts
+constexpr int kAADefaultDepth = 3;
+constexpr double kAAStartRel = 0.3;
 
 }  // namespace
 
@@ -135,6 +139,8 @@ struct wavi_ctx {
   int coarse_solver = WAVI_COARSE_CG;  // resolved coarse solver (never WAVI_COARSE_AUTO)
   void* dcoarse = nullptr;             // diag(R A P) for the Jacobi-preconditioned single-reduction CG
   void* cheb_eig = nullptr;            // the Chebyshev coarse solve's power vector (kept across V-cycles)
+  int aa_depth = 0;                    // Anderson acceleration of the Picard loop: columns (0: off)
+  AAWork aa{};                         // its columns, previous f and g, and reduction partials
   // coarse-correction cache mapping: block offsets of the mask scan (u part, then v part from
   // mask_offsets_v), staging for host callers, and the host masks' counts
   int* mask_offsets = nullptr;
@@ -664,6 +670,15 @@ int enqueue_vcycle_post(wavi_ctx* c, const CondHandles& h, Tally& t) {
   CKL();
   t.launches++;
   t.bytes += (double)(2 * sizeof(T) + 8 * 3) * d.N + d.N;
+  if (c->aa_depth > 0) {  // Anderson acceleration: both launches return at once until it has started
+    k_aa_stage<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, c->x64, corr[cur], c->aa, c->S,
+                                                          (const DevParams*)c->P);
+    CKL();
+    k_aa_apply<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, c->x64, corr[cur], c->aa, c->uv, c->S);
+    CKL();
+    t.launches += 2;
+    t.bytes += (double)(2 * sizeof(T) + 2 + 8 * (8 + 2 * c->aa_depth)) * d.N;
+  }
   return 0;
 }
 
@@ -906,6 +921,8 @@ int set_params(wavi_ctx* c, const wavi_params* p) {
   P.nsmooth = c->sp.nsmooth;
   P.n_iter_viscosity = c->sp.n_iter_viscosity;
   P.picard_test = c->opt.picard_test;
+  P.aa_depth = c->aa_depth;
+  P.aa_start_rel = kAAStartRel;
   P.weertman_ex_f = (float)(1.0 / p->weertman_m - 1.0);
   P.glen_ex_f = (float)(1.0 / p->glen_n - 1.0);
   P.glen_er2_f = (float)(p->glen_reg_strain_rate * p->glen_reg_strain_rate);
@@ -943,6 +960,7 @@ int solve_enqueue(wavi_ctx* c, const wavi_params* p) {
 // of its preconditioner (0 if the coarse solver has none).
 void fill_coarse_kind(const wavi_ctx* c, wavi_stats* st) {
   st->coarse_kernel = c->pers_maxt > 0 ? 1 : c->pers_maxt < 0 ? 3 : 2;
+  st->picard_accel = c->aa_depth > 0 ? WAVI_PICARD_ANDERSON : WAVI_PICARD_PLAIN;
   const bool cheb = c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV || c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV;
   st->cheb_steps = cheb ? cheb_steps(c) : 0;
 }
@@ -984,6 +1002,7 @@ int solve_finish(wavi_ctx* c, wavi_stats* st) {
     st->coarse_solver = c->coarse_solver;
     st->coarse_launches = c->opt.use_graphs ? 0 : c->coarse_launches;
     fill_coarse_kind(c, st);
+    st->anderson_steps = S.aa.steps;
   }
   return 0;  // not converging is reported through stats.status only, like the reference's silent stop
 }
@@ -1578,6 +1597,13 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_sums %d", opt->coarse_sums));
   if (opt->viscosity < WAVI_VISCOSITY_DEFAULT || opt->viscosity > WAVI_VISCOSITY_FP64)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown viscosity precision %d", opt->viscosity));
+  if (opt->picard_accel < WAVI_PICARD_AUTO || opt->picard_accel > WAVI_PICARD_ANDERSON)
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown picard_accel %d", opt->picard_accel));
+  if (opt->anderson_depth < 0 || opt->anderson_depth > kAAMax)
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "anderson_depth must be 0 (default) or 1..%d (got %d)", kAAMax,
+                     opt->anderson_depth));
+  const bool anderson = opt->picard_accel == WAVI_PICARD_ANDERSON || (opt->picard_accel == WAVI_PICARD_AUTO && mixed(c));
+  c->aa_depth = anderson ? (opt->anderson_depth > 0 ? opt->anderson_depth : kAADefaultDepth) : 0;
   c->visc32 = mixed(c) && opt->viscosity != WAVI_VISCOSITY_FP64;
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));
@@ -1657,6 +1683,13 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
         c->gcd = q;
       }
     }
+  }
+  if (c->aa_depth > 0) {
+    if ((r = dalloc(c, &c->aa.dF, (size_t)c->aa_depth * N))) return bail(r);
+    if ((r = dalloc(c, &c->aa.dG, (size_t)c->aa_depth * N))) return bail(r);
+    if ((r = dalloc(c, &c->aa.fprev, N))) return bail(r);
+    if ((r = dalloc(c, &c->aa.gprev, N))) return bail(r);
+    if ((r = dalloc(c, &c->aa.partials, (size_t)2 * kAAMax * c->ew_blocks))) return bail(r);
   }
   if ((r = dalloc(c, &c->P, 1))) return bail(r);
   if ((r = dalloc(c, &c->S, 1))) return bail(r);

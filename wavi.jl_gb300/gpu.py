@@ -42,7 +42,7 @@ class VelocitySolver:
 
     def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0,
                  coarse_kernel="auto", coarse_solver="auto", stencil_kernel="auto", cheb_steps=0,
-                 coarse_sums="default", viscosity="default"):
+                 coarse_sums="default", viscosity="default", picard_accel="auto", anderson_depth=0):
         self.lib = abi.load_library()
         self.grid = grid
         self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ
@@ -53,7 +53,8 @@ class VelocitySolver:
         self._opt = abi.Options(int(device), PRECISIONS[precision], 1 if use_graphs else 0, int(picard_test),
                                 self.COARSE_KERNELS[coarse_kernel], abi.COARSE_SOLVERS[coarse_solver],
                                 self.STENCIL_KERNELS[stencil_kernel], int(cheb_steps),
-                                abi.COARSE_SUMS[coarse_sums], abi.VISCOSITY[viscosity])
+                                abi.COARSE_SUMS[coarse_sums], abi.VISCOSITY[viscosity],
+                                abi.PICARD_ACCEL[picard_accel], int(anderson_depth))
         ctx = C.c_void_p()
         st = self.lib.wavi_ctx_create(C.byref(self._desc.desc), C.byref(self._sp), C.byref(self._opt), C.byref(ctx))
         if st != 0:
@@ -284,4 +285,6 @@ def stats_dict(s):
             "kernel_launches": s.kernel_launches, "host_syncs": s.host_syncs, "coarse_ms": s.coarse_ms,
             "coarse_solver": abi.COARSE_SOLVER_NAMES.get(s.coarse_solver, s.coarse_solver),
             "coarse_launches": s.coarse_launches,
-            "coarse_kernel": COARSE_KERNEL_NAMES.get(s.coarse_kernel, s.coarse_kernel), "cheb_steps": s.cheb_steps}
+            "coarse_kernel": COARSE_KERNEL_NAMES.get(s.coarse_kernel, s.coarse_kernel), "cheb_steps": s.cheb_steps,
+            "anderson_steps": s.anderson_steps,
+            "picard_accel": abi.PICARD_ACCEL_NAMES.get(s.picard_accel, s.picard_accel)}

@@ -34,6 +34,8 @@ class GPUParallelSpec:
     coarse_solver: str = "auto"  # "auto", "cg" (reference), "srcg", "srcg_jacobi", "srcg_chebyshev" (single-reduction
     #                              CG), "pipelined_chebyshev" (opt-in)
     device_run: bool = False     # run_simulation without a callback keeps the model on the device (wavi_run_device)
+    picard_accel: str = "auto"   # "auto" (fp64: the reference's Picard iteration; mixed: Anderson acceleration),
+    #                              "plain" or "anderson"
 
 
 _SOLVERS = {}
@@ -46,7 +48,7 @@ def _solver_for(model):
         ps = model.parallel_spec
         s = gpu.VelocitySolver(model.grid, model.solver_params, precision=ps.precision, device=ps.device,
                                use_graphs=ps.use_graphs, picard_test=ps.picard_test,
-                               coarse_solver=ps.coarse_solver)
+                               coarse_solver=ps.coarse_solver, picard_accel=ps.picard_accel)
         _SOLVERS[key] = s
     return s
 
