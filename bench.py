@@ -8,10 +8,11 @@ step restores that state and solves it to ||b - A u|| / ||b|| < 1e-6 (maxiter_pi
 reference's other solver parameters).
 
   value    mixed precision (float32 operator / V-cycle, float64 residual and reductions) with its default
-           Picard iteration (Anderson-accelerated, wavi_picard_accel; --picard-accel), fields resident in
-           HBM, device time per step from CUDA events on the solver's stream, L2 flushed between steps
-  mixed_plain / mixed_anderson  the same mixed solve with the other Picard iteration (the reference's
-           plain one beside the accelerated default), with its error against the oracle
+           Picard iteration (Anderson-accelerated, wavi_picard_accel; --picard-accel) and coarse tolerance
+           (adaptive, wavi_coarse_forcing; --coarse-forcing), fields resident in HBM, device time per step
+           from CUDA events on the solver's stream, L2 flushed between steps
+  mixed_plain / mixed_anderson  the same mixed solve with the reference's Picard iteration and coarse
+           tolerance beside the accelerated defaults (or the reverse), with its error against the oracle
   e2e      the same solve through the host C ABI (wavi_solve_velocities) from pinned host buffers, the
            host<->device copies inside the timed region
   fp64_gpu the reference algorithm in float64 on the GPU (cg! coarse solve; the comparison the metric names)
@@ -297,6 +298,15 @@ def ncu_traffic(fn, key):
 C2_FIXTURE = os.path.join(ROOT, "tests", "golden", "c2_oracle_solution.npz")
 
 
+def other_iteration(args):
+    """The Picard iteration and coarse tolerance of the comparison arm: the reference's (plain Picard,
+    fixed tol_coarse) beside an accelerated headline, or the mixed defaults (Anderson, adaptive) beside a
+    plain one.  Returns (key suffix, picard_accel, coarse_forcing)."""
+    if args.picard_accel == "plain" and args.coarse_forcing == "fixed":
+        return "anderson", "anderson", "adaptive"
+    return "plain", "plain", "fixed"
+
+
 def c2_fixture():
     """The FP64 oracle's converged solve of this workload (tests/golden/make_c2_solution.py), or None."""
     try:
@@ -427,7 +437,8 @@ def gpu_arm(args):
 
     mixed = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=args.coarse_solver,
                            cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums,
-                           viscosity=args.viscosity, picard_accel=args.picard_accel)
+                           viscosity=args.viscosity, picard_accel=args.picard_accel,
+                           coarse_forcing=args.coarse_forcing)
     fp64 = VelocitySolver(g, sp, precision="fp64", device=local)
 
     # float64 reference algorithm on the GPU
@@ -450,11 +461,13 @@ def gpu_arm(args):
     same = None
     if mixed_solver != "pipelined_chebyshev":
         fp64s = VelocitySolver(g, sp, precision="fp64", device=local, coarse_solver=mixed_solver,
-                               cheb_steps=args.cheb_steps, picard_accel=stmix[-1]["picard_accel"])
+                               cheb_steps=args.cheb_steps, picard_accel=stmix[-1]["picard_accel"],
+                               coarse_forcing=stmix[-1]["coarse_forcing"])
         t64s, st64s, out64s = time_device_solves(torch, fp64s, p, snapshot, max(1, args.steps // 2), 1)
         fp64s.close()
         same = {"value": world * len(t64s) / sum(t64s), "unit": "solves/s", "ms_per_step": 1e3 * sum(t64s) / len(t64s),
                 "coarse_solver": st64s[-1]["coarse_solver"], "picard_accel": st64s[-1]["picard_accel"],
+                "coarse_forcing": st64s[-1]["coarse_forcing"],
                 "picard_iterations": st64s[-1]["picard_iterations"],
                 "coarse_cg_iterations": st64s[-1]["coarse_cg_iterations"], "status_name": st64s[-1]["status_name"]}
 
@@ -491,15 +504,16 @@ def gpu_arm(args):
                        "coarse_cg_iterations": stc64[-1]["coarse_cg_iterations"],
                        "status_name": stc64[-1]["status_name"]}
 
-    # the mixed solve with the other Picard iteration (wavi_picard_accel): the reference's plain iteration
-    # beside an accelerated headline, or Anderson acceleration beside a plain one
-    other_accel = "anderson" if args.picard_accel == "plain" else "plain"
+    # the mixed solve with the other Picard iteration and coarse tolerance (wavi_picard_accel,
+    # wavi_coarse_forcing): the reference's beside the accelerated defaults, or the reverse
+    other_accel, o_accel, o_forcing = other_iteration(args)
     mo = VelocitySolver(g, sp, precision="mixed", device=local, coarse_solver=args.coarse_solver,
                         cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums, viscosity=args.viscosity,
-                        picard_accel=other_accel)
+                        picard_accel=o_accel, coarse_forcing=o_forcing)
     tao, stao, outao = time_device_solves(torch, mo, p, snapshot, args.steps, 1)
     mo.close()
-    accel_other = {"picard_accel": other_accel, "value": world * len(tao) / sum(tao), "unit": "solves/s",
+    accel_other = {"picard_accel": o_accel, "coarse_forcing": o_forcing, "value": world * len(tao) / sum(tao),
+                   "unit": "solves/s",
                    "ms_per_step": 1e3 * sum(tao) / len(tao),
                    **{k: stao[-1][k] for k in ("picard_iterations", "coarse_cg_iterations", "anderson_steps",
                                                 "rel_residual", "status_name")}}
@@ -588,7 +602,7 @@ def gpu_arm(args):
         "fp64_gpu_same_solver": same,
         "mixed_over_fp64": value / fp64_value if fp64_value else None,
         "mixed_over_fp64_same_solver": value / same["value"] if same else None,
-        "picard_accel": stmix[-1]["picard_accel"],
+        "picard_accel": stmix[-1]["picard_accel"], "coarse_forcing": stmix[-1]["coarse_forcing"],
         "mixed_" + other_accel: accel_other,
         "mixed_fp64_coarse_sums": sums64,
         "mixed_fp64_coarse_solve": solve64,
@@ -596,7 +610,8 @@ def gpu_arm(args):
         **errs_oracle,
         "solve": {k: stmix[-1][k] for k in ("picard_iterations", "coarse_cg_iterations", "op_applications",
                                              "rel_residual", "kernel_launches", "host_syncs", "status_name",
-                                             "coarse_solver", "coarse_kernel", "cheb_steps", "anderson_steps")},
+                                             "coarse_solver", "coarse_kernel", "cheb_steps", "anderson_steps",
+                                             "picard_accel", "coarse_forcing")},
         "roofline": {"bound": "latency", "achieved": cg_achieved, "peak": peak, "unit": "GB/s",
                      "frac": cg_achieved / peak,
                      "traffic": ncu_traffic("coarse_cg_c2.md", "traffic_bytes_per_cg_iteration"),
@@ -637,11 +652,13 @@ def other_configs(args):
     import copy
     out = {}
     legs = (("c3", c3_arm, dict(steps=1, warmup=1),
-             ("metric", "value", "unit", "ms_per_step", "solve", "picard_accel", "mixed_anderson", "mixed_plain",
+             ("metric", "value", "unit", "ms_per_step", "solve", "picard_accel", "coarse_forcing", "mixed_anderson",
+              "mixed_plain",
               "mixed_uncapped", "fp64_gpu", "mixed_over_fp64",
               "rel_err_mixed_vs_fp64", "roofline", "roofline_relin_fp64", "roofline_stencil", "coarse_cg_share")),
             ("c5", ensemble_arm, dict(steps=1, warmup=1, no_tune=True, members=256),
-             ("metric", "value", "unit", "ms_per_step", "members_converged", "picard_accel", "mixed_anderson",
+             ("metric", "value", "unit", "ms_per_step", "members_converged", "picard_accel", "coarse_forcing",
+              "mixed_anderson",
               "mixed_plain", "all_members", "fp64_loop",
               "ensemble_over_fp64_loop", "rel_err_vs_fp64_max", "rel_err_vs_fp64_median", "picard_iterations_mean")),
             ("c4", adjoint_arm, dict(steps=2, warmup=1, directions=2),
@@ -709,7 +726,8 @@ def c3_arm(args):
     p = m.params
     mixed = VelocitySolver(g, sp, precision="mixed", picard_test=1, coarse_solver=args.coarse_solver,
                            cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums,
-                           viscosity=args.viscosity, picard_accel=args.picard_accel)
+                           viscosity=args.viscosity, picard_accel=args.picard_accel,
+                           coarse_forcing=args.coarse_forcing)
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         tmix, stmix, outmix = time_device_solves(torch, mixed, p, snapshot, args.steps, args.warmup)
@@ -720,14 +738,14 @@ def c3_arm(args):
     long_sp = _replace(sp, maxiter_picard=200)
     mlong = VelocitySolver(g, long_sp, precision="mixed", picard_test=1, coarse_solver=args.coarse_solver,
                            cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums, viscosity=args.viscosity,
-                           picard_accel="plain")
+                           picard_accel="plain", coarse_forcing="fixed")
     tl, stl, _ = time_device_solves(torch, mlong, p, snapshot, 1, 0)
     mlong.close()
-    # the mixed solve with the other Picard iteration (wavi_picard_accel), at the configuration's cap
-    other_accel = "anderson" if args.picard_accel == "plain" else "plain"
+    # the mixed solve with the other Picard iteration and coarse tolerance, at the configuration's cap
+    other_accel, o_accel, o_forcing = other_iteration(args)
     mo = VelocitySolver(g, sp, precision="mixed", picard_test=1, coarse_solver=args.coarse_solver,
                         cheb_steps=args.cheb_steps, coarse_sums=args.coarse_sums, viscosity=args.viscosity,
-                        picard_accel=other_accel)
+                        picard_accel=o_accel, coarse_forcing=o_forcing)
     tao, stao, outao = time_device_solves(torch, mo, p, snapshot, 1, 1)
     mo.close()
     fp64 = VelocitySolver(g, sp, precision="fp64", picard_test=1)
@@ -791,11 +809,13 @@ def c3_arm(args):
         "fp64_gpu": {"value": len(t64) / sum(t64), "unit": "solves/s", "ms_per_step": 1e3 * sum(t64) / len(t64),
                      **{k: st64[-1][k] for k in ("status_name", "picard_iterations", "coarse_cg_iterations",
                                                   "rel_residual", "rel_update", "coarse_solver")}},
-        "mixed_uncapped": {"maxiter_picard": 200, "picard_accel": "plain", "seconds": tl[0],
+        "mixed_uncapped": {"maxiter_picard": 200, "picard_accel": "plain", "coarse_forcing": "fixed",
+                           "seconds": tl[0],
                            **{k: stl[-1][k] for k in ("status_name", "picard_iterations", "coarse_cg_iterations",
                                                       "rel_residual", "rel_update")}},
-        "picard_accel": last["picard_accel"],
-        "mixed_" + other_accel: {"picard_accel": other_accel, "value": len(tao) / sum(tao), "unit": "solves/s",
+        "picard_accel": last["picard_accel"], "coarse_forcing": last["coarse_forcing"],
+        "mixed_" + other_accel: {"picard_accel": o_accel, "coarse_forcing": o_forcing, "value": len(tao) / sum(tao),
+                                 "unit": "solves/s",
                                  "ms_per_step": 1e3 * sum(tao) / len(tao),
                                  **{k: stao[-1][k] for k in ("status_name", "picard_iterations", "coarse_cg_iterations",
                                                               "anderson_steps", "rel_residual", "rel_update")}},
@@ -859,7 +879,8 @@ def ensemble_arm(args):
         best, timings = dict(concurrency=8, coarse_kernel="auto", stencil_kernel="tiled"), []
     else:
         best, timings = autotune(grids, sps, params, make_tensors, sync=torch.cuda.synchronize)
-    ens = EnsembleSolver(grids, sps, precision="mixed", picard_accel=args.picard_accel, **best)
+    ens = EnsembleSolver(grids, sps, precision="mixed", picard_accel=args.picard_accel,
+                         coarse_forcing=args.coarse_forcing, **best)
     times, stats = [], None
     for it in range(args.warmup + args.steps):
         work = make_tensors()
@@ -872,9 +893,9 @@ def ensemble_arm(args):
     ens.close()
     conv = sum(1 for st in stats if st["status"] == 0)
     value = conv * len(times) / sum(times)  # converged solves only
-    # one ensemble solve with the other Picard iteration (wavi_picard_accel)
-    other_accel = "anderson" if args.picard_accel == "plain" else "plain"
-    eo = EnsembleSolver(grids, sps, precision="mixed", picard_accel=other_accel, **best)
+    # one ensemble solve with the other Picard iteration and coarse tolerance
+    other_accel, o_accel, o_forcing = other_iteration(args)
+    eo = EnsembleSolver(grids, sps, precision="mixed", picard_accel=o_accel, coarse_forcing=o_forcing, **best)
     eo.solve_device(params, make_tensors())  # graph instantiation
     work_o = make_tensors()
     torch.cuda.synchronize()
@@ -883,7 +904,8 @@ def ensemble_arm(args):
     t_o = time.perf_counter() - t0
     eo.close()
     conv_o = sum(1 for st in stats_o if st["status"] == 0)
-    accel_other = {"picard_accel": other_accel, "value": conv_o / t_o, "unit": "solves/s", "seconds": t_o,
+    accel_other = {"picard_accel": o_accel, "coarse_forcing": o_forcing, "value": conv_o / t_o, "unit": "solves/s",
+                   "seconds": t_o,
                    "members_converged": conv_o,
                    "picard_iterations_mean": float(np.mean([st["picard_iterations"] for st in stats_o]))}
     # looping the single-domain FP64 GPU solve, on every 8th member
@@ -916,7 +938,7 @@ def ensemble_arm(args):
         "rel_err_vs_fp64_max": max(errs) if errs else None,
         "rel_err_vs_fp64_median": float(np.median(errs)) if errs else None, "rel_err_members": len(errs),
         "members_converged": conv,
-        "picard_accel": stats[0]["picard_accel"],
+        "picard_accel": stats[0]["picard_accel"], "coarse_forcing": stats[0]["coarse_forcing"],
         "mixed_" + other_accel: accel_other,
         "note": "value counts the members that reach 1e-6 within maxiter_picard = 100 (members_converged); the "
                 "others stall the same way in FP64 (the reference algorithm's one V-cycle per Picard iteration). "
@@ -1113,6 +1135,9 @@ def main():
     ap.add_argument("--picard-accel", default="auto", choices=("auto", "plain", "anderson"),
                     help="Picard iteration of the timed mixed solves (wavi_picard_accel; auto = Anderson in mixed "
                          "precision); the other one is reported beside it")
+    ap.add_argument("--coarse-forcing", default="auto", choices=("auto", "fixed", "adaptive"),
+                    help="coarse-CG tolerance of the timed mixed solves (wavi_coarse_forcing; auto = adaptive in "
+                         "mixed precision)")
     ap.add_argument("--cheb-steps", type=int, default=0,
                     help="Chebyshev steps of the Chebyshev coarse solvers (0: the library's default, 3; else odd)")
     ap.add_argument("--config", default="c2", choices=("c2", "c3", "c4", "c5"),

@@ -66,6 +66,7 @@ def lib():
         L.oracle_set_coarse_variant.argtypes = [C.c_int]
         L.oracle_set_chebyshev.argtypes = [C.c_int, C.c_double]
         L.oracle_set_anderson.argtypes = [C.c_int, C.c_double]
+        L.oracle_set_coarse_forcing.argtypes = [C.c_int]
         L.oracle_coarse_diag.argtypes = [vp, dp, dp]
         _lib = L
     return _lib
@@ -243,6 +244,13 @@ def set_anderson(depth=0, start_rel=ANDERSON_DEFAULT[1]):
     iteration, the default) or 1..5 columns, from the first Picard iteration whose relative residual is
     below start_rel.  Restates the GPU library's opt-in WAVI_PICARD_ANDERSON."""
     lib().oracle_set_anderson(int(depth), float(start_rel))
+
+
+def set_coarse_forcing(on=False):
+    """The coarse CG's relative tolerance in every later V-cycle: the reference's tol_coarse (False, the
+    default) or max(tol_coarse, min(0.1, 0.1 x the Picard relative residual)) (True).  Restates the GPU
+    library's opt-in WAVI_FORCING_ADAPTIVE."""
+    lib().oracle_set_coarse_forcing(1 if on else 0)
 
 
 def pos_fraction(z, mask=None):

@@ -306,6 +306,7 @@ struct Model {
   Vec last_coarse_b;      // the last V-cycle's coarse right-hand side and starting point (the cached
   Vec last_coarse_x0;     // correction), in the coarse order [u | v], for studies of the coarse solvers
   int cheb_vcycles = 0;   // coarse variants 4, 5: V-cycles so far in this solve
+  double picard_rel = 0;  // the current Picard iteration's relative residual (the adaptive coarse tolerance)
   std::string err;
 };
 
@@ -1103,6 +1104,17 @@ void smoother(Model& m, OpWork& w, const Precond& p, Vec& x, const Vec& b, const
     }
 }
 
+// Relative tolerance of the coarse CG.  The reference's: tol_coarse.  With g_coarse_forcing (not in the
+// reference; the GPU library's opt-in wavi_options.coarse_forcing = WAVI_FORCING_ADAPTIVE, restated):
+// max(tol_coarse, min(0.1, 0.1 x the Picard iteration's relative residual)) — inexact Newton's forcing
+// terms (Eisenstat & Walker, SIAM J. Sci. Comput. 17, 1996); only in solves of more than one Picard
+// iteration.
+int g_coarse_forcing = 0;
+double coarse_reltol(const Model& m) {
+  return g_coarse_forcing && m.S.maxiter_picard > 1 ? std::max(m.S.tol_coarse, std::min(0.1, 0.1 * m.picard_rel))
+                                                    : m.S.tol_coarse;
+}
+
 // precondition!(x, p, b) — one V-cycle                                   :54-83
 void vcycle(Model& m, OpWork& w, Precond& p, Vec& x, const Vec& b) {
   static const int fwd[4] = {1, 3, 2, 4}, bwd[4] = {4, 2, 3, 1};
@@ -1111,7 +1123,7 @@ void vcycle(Model& m, OpWork& w, Precond& p, Vec& x, const Vec& b) {
   resid_sampled(m, w, x, b, r);
   Vec bc;
   restrict_vec(m, p, r, bc);
-  double abstol = m.S.tol_coarse * norm2(bc);
+  double abstol = coarse_reltol(m) * norm2(bc);
   m.last_coarse_b = bc;
   m.last_coarse_x0 = p.corr;
   p.last_cg = g_coarse_variant == 0   ? coarse_cg(m, w, p, p.corr, bc, abstol, m.S.maxiter_coarse)
@@ -1224,6 +1236,7 @@ bool precondition_model(Model& m, OpWork& w, double& rel, Anderson* aa = nullptr
   for (int k = 0; k < m.ni_v; ++k) m.gv_resid[m.v_inner_idx[k]] = r[m.ni_u + k];
   rel = norm2(r) / norm2(b);
   bool converged = rel < m.S.tol_picard;
+  m.picard_rel = rel;
   Vec corr((size_t)ni, 0.0);
   if (!converged) {
     Precond p;  // get_preconditioner :7-43
@@ -1608,6 +1621,8 @@ int oracle_vcycle(void* h, const double* ru, const double* rv, double* cu, doubl
   return p.last_cg;
 }
 void oracle_set_coarse_variant(int variant) { g_coarse_variant = variant; }
+// The adaptive coarse tolerance in later V-cycles (1) or the reference's tol_coarse (0).
+void oracle_set_coarse_forcing(int on) { g_coarse_forcing = on ? 1 : 0; }
 // Anderson acceleration of later solves: depth 0 (the reference's Picard loop) or 1..5 columns, from the
 // first Picard iteration whose relative residual is below start_rel.
 void oracle_set_anderson(int depth, double start_rel) {

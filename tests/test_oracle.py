@@ -261,3 +261,39 @@ def test_c2_fixed_point_fixture(oracle, pkg):
     d = np.sqrt(np.sum((plain["u"] - fp["u"]) ** 2) + np.sum((plain["v"] - fp["v"]) ** 2)) / den
     assert np.isclose(d, float(fp["reference_stop_distance"]), rtol=1e-6)
     assert d < 1e-5
+
+
+def test_adaptive_coarse_tolerance_restatement(oracle, pkg):
+    """The oracle's restatement of the opt-in adaptive coarse tolerance (max(tol_coarse, min(0.1, 0.1 rel)))
+    on the 8 km channel, with and without the Anderson acceleration: the same Picard count (within 1), the
+    same distance from the fixed point (within a factor 2 and below 1e-6 with the acceleration), and at
+    least a quarter fewer coarse iterations (measured 2 791 -> 1 857 plain, 1 897 -> 1 224 accelerated)."""
+    from wavi_gb300 import synthetic
+
+    def solve(depth, forcing, tol=1e-6):
+        g, bed, p, sp, ic = synthetic.channel_c1(tol_picard=tol, maxiter_picard=200)
+        m = oracle.build_model(g, bed, p, sp, ic)
+        m.pre_solve()
+        oracle.set_coarse_variant("srcg_chebyshev")
+        oracle.set_chebyshev(5)
+        oracle.set_anderson(depth)
+        oracle.set_coarse_forcing(forcing)
+        try:
+            m.update_velocities()
+        finally:
+            oracle.set_anderson(0)
+            oracle.set_coarse_forcing(False)
+            oracle.set_coarse_variant("cg")
+            oracle.set_chebyshev()
+        return m.stats(), np.concatenate([np.ravel(m.field("u")), np.ravel(m.field("v"))])
+
+    _, x_fp = solve(3, False, 1e-11)
+    err = lambda x: np.linalg.norm(x - x_fp) / np.linalg.norm(x_fp)
+    for depth in (0, 3):
+        st0, x0 = solve(depth, False)
+        st1, x1 = solve(depth, True)
+        assert st1["rel_residual"] < 1e-6
+        assert abs(st1["picard_iterations"] - st0["picard_iterations"]) <= 1, (st0, st1)
+        assert st1["coarse_cg_iterations"] <= 0.75 * st0["coarse_cg_iterations"], (st0, st1)
+        assert err(x1) < 2 * err(x0) + 1e-8, (err(x0), err(x1))
+    assert err(x1) < 1e-6

@@ -10,7 +10,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libwavi_gpu.so")
 
-WAVI_ABI_VERSION = 4
+WAVI_ABI_VERSION = 5
 
 STATUS = {
     0: "WAVI_OK", -1: "WAVI_ERR_ARGUMENT", -2: "WAVI_ERR_CUDA", -3: "WAVI_ERR_NONFINITE",
@@ -28,6 +28,8 @@ COARSE_SUMS = {"default": 0, "float_float": 1, "fp64": 2, "fp64_solve": 3}  # wa
 VISCOSITY = {"default": 0, "fp32": 1, "fp64": 2}  # wavi_viscosity
 PICARD_ACCEL = {"auto": 0, "plain": 1, "anderson": 2}  # wavi_picard_accel
 PICARD_ACCEL_NAMES = {v: k for k, v in PICARD_ACCEL.items()}
+COARSE_FORCING = {"auto": 0, "fixed": 1, "adaptive": 2}  # wavi_coarse_forcing
+COARSE_FORCING_NAMES = {v: k for k, v in COARSE_FORCING.items()}
 
 _dp = C.POINTER(C.c_double)
 _u8p = C.POINTER(C.c_uint8)
@@ -61,7 +63,8 @@ class Options(C.Structure):
     _fields_ = [("device", C.c_int32), ("precision", C.c_int32), ("use_graphs", C.c_int32),
                 ("picard_test", C.c_int32), ("coarse_kernel", C.c_int32), ("coarse_solver", C.c_int32),
                 ("stencil_kernel", C.c_int32), ("cheb_steps", C.c_int32), ("coarse_sums", C.c_int32),
-                ("viscosity", C.c_int32), ("picard_accel", C.c_int32), ("anderson_depth", C.c_int32)]
+                ("viscosity", C.c_int32), ("picard_accel", C.c_int32), ("anderson_depth", C.c_int32),
+                ("coarse_forcing", C.c_int32), ("reserved0", C.c_int32)]
 
 
 FIELD_INPUTS = ("h", "s", "dsdh", "grounded_fraction", "weertman_c", "accumulation", "basal_melt",
@@ -86,7 +89,7 @@ class Stats(C.Structure):
                 ("kernel_launches", C.c_int32), ("host_syncs", C.c_int32),
                 ("coarse_ms", C.c_double), ("coarse_solver", C.c_int32), ("coarse_launches", C.c_int32),
                 ("coarse_kernel", C.c_int32), ("cheb_steps", C.c_int32), ("anderson_steps", C.c_int32),
-                ("picard_accel", C.c_int32)]
+                ("picard_accel", C.c_int32), ("coarse_forcing", C.c_int32), ("reserved1", C.c_int32)]
 
 
 class OperatorDesc(C.Structure):

@@ -156,8 +156,8 @@ __global__ void __launch_bounds__(256) k_aa_stage(int n, const uint8_t* __restri
 template <typename T>
 __global__ void __launch_bounds__(256) k_aa_apply(int n, const uint8_t* __restrict__ inner, double* __restrict__ x,
                                                   const T* __restrict__ corr, AAWork w, double* __restrict__ uv,
-                                                  DevState* st) {
-  if (!st->aa.started || st->aa.used == 0) return;  // the same decision in every block
+                                                  DevState* st, const DevParams* __restrict__ P) {
+  if (P->aa_depth <= 0 || !st->aa.started || st->aa.used == 0) return;  // the same decision in every block
   const int used = st->aa.used;
   double gam[kAAMax];
   const double* col[kAAMax];

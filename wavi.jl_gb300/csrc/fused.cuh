@@ -42,6 +42,19 @@ struct DevState {
 };
 enum { CNT_A = 0, CNT_B = 1, CNT_C = 2, CNT_D = 3, CNT_AA_STAGE = 4, CNT_AA_APPLY = 5 };
 
+// Relative tolerance of a V-cycle's coarse CG (abstol = tolerance x |b_c|, update_preconditioners.jl:73).
+// The reference's is tol_coarse.  With coarse_forcing (wavi_options.coarse_forcing; inexact Newton's forcing
+// terms, Eisenstat & Walker 1996) it is max(tol_coarse, min(kForcingMax, kForcingRatio x rel)), rel the
+// Picard iteration's relative residual: early, far from the fixed point, where the relinearisation
+// rather than the linear solve limits the next iterate, the coarse CG stops sooner; from
+// rel <= tol_coarse / kForcingRatio on it is the reference's.  Only in solves of more than one Picard
+// iteration: with maxiter_picard = 1 (a time step's single V-cycle) no later iteration follows.
+constexpr double kForcingRatio = 0.1, kForcingMax = 0.1;
+__device__ __forceinline__ double coarse_tolerance(const DevParams* P, const DevState* st) {
+  return P->coarse_forcing && P->maxiter_picard > 1 ? fmax(P->tol_coarse, fmin(kForcingMax, kForcingRatio * st->rel))
+                                                    : P->tol_coarse;
+}
+
 struct CondHandles {
   cudaGraphConditionalHandle picard, vcycle, cg;
   int active;  // 0: launched outside a graph, do not touch the handles
@@ -803,7 +816,7 @@ __global__ void __launch_bounds__(TILE* TILE)
     if (flat_tid() == 0) {
       if (START) {
         const double res = sqrt(tot[0]);
-        const double abstol = P->tol_coarse * st->cg_bnorm;
+        const double abstol = coarse_tolerance(P, st) * st->cg_bnorm;
         st->cg_res = res;
         st->cg_prev = 1.0;
         st->cg_tol = fmax(1.4901161193847656e-08 * res, abstol);  // reltol = sqrt(eps(Float64))

@@ -247,6 +247,7 @@ struct DevParams {
   int maxiter_picard, maxiter_coarse, nsmooth, n_iter_viscosity;
   int picard_test;
   int aa_depth;         // Anderson acceleration of the Picard loop: columns (0: the reference's iteration)
+  int coarse_forcing;   // 1: the coarse CG's relative tolerance follows the Picard residual (coarse_tolerance)
   double aa_start_rel;  // ... from the first Picard iteration whose relative residual is below this
   // the float relinearisation's uniform constants, rounded once on the host: 1/m - 1, 1/n - 1 (the
   // exponents of β and of the viscosity), the squared strain-rate regularisation, the speed regularisation

@@ -1160,7 +1160,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
-  const double tol_coarse = P->tol_coarse;
+  const double tol_coarse = coarse_tolerance(P, st);
   constexpr bool kFast = !std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value;
   T hu[MAXT], hv[MAXT];  // fast path: the tiles' prolonged vectors (inner ⊙ P u)
   TagState ts{halo, 0u, 0u};
@@ -1331,7 +1331,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
-  const double tol_coarse = P->tol_coarse;
+  const double tol_coarse = coarse_tolerance(P, st);
   constexpr bool kFast = !std::is_same<FastSharedFor<T, TILE, MAXT>, char>::value;
   T hu[MAXT], hv[MAXT];  // fast path: the tiles' prolonged vectors (inner ⊙ P u)
   // two box sets (by exchange parity): the Chebyshev steps exchange without a grid reduction in between
@@ -1613,7 +1613,7 @@ __global__ void __launch_bounds__(TILE* TILE, (TILE == 16 && MAXT <= 2) ? 2 : 1)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
-  const double tol_coarse = P->tol_coarse;
+  const double tol_coarse = coarse_tolerance(P, st);
   TagState ts{halo, 0u, 0u, (size_t)ntiles * 8 * TILE};
   ts.base = *(volatile unsigned*)&bar->gen << 21;
   volatile int* fail = &fs.fail;
@@ -1849,7 +1849,7 @@ __global__ void __launch_bounds__(TILE* TILE, TILE == 16 ? 4 : 1)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
-  const double tol_coarse = P->tol_coarse;
+  const double tol_coarse = coarse_tolerance(P, st);
   const bool use_m = dcoarse != nullptr;
   auto minv = [&](int q) -> T {
     if (!use_m) return (T)1;
@@ -1979,7 +1979,7 @@ __global__ void __launch_bounds__(TILE* TILE, TILE == 16 ? 4 : 1)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
-  const double tol_coarse = P->tol_coarse;
+  const double tol_coarse = coarse_tolerance(P, st);
   T* const wbuf[2] = {w, w2};
   int wsel = 0;
   auto minv = [&](int q) -> T {
@@ -2194,7 +2194,7 @@ __global__ void __launch_bounds__(TILE* TILE, TILE == 16 ? 4 : 1)
   unsigned epoch = 0;
   int it = 0;
   const int maxit = P->maxiter_coarse;
-  const double tol_coarse = P->tol_coarse;
+  const double tol_coarse = coarse_tolerance(P, st);
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int i0 = (t % ntx) * TILE, j0 = (t / ntx) * TILE, i = i0 + tx, j = j0 + ty;
     const bool inu = i <= d.nx && j < d.ny, inv = i < d.nx && j <= d.ny;

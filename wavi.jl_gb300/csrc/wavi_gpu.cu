@@ -140,6 +140,7 @@ struct wavi_ctx {
   void* dcoarse = nullptr;             // diag(R A P) for the Jacobi-preconditioned single-reduction CG
   void* cheb_eig = nullptr;            // the Chebyshev coarse solve's power vector (kept across V-cycles)
   int aa_depth = 0;                    // Anderson acceleration of the Picard loop: columns (0: off)
+  bool forcing = false;                // the coarse CG's tolerance follows the Picard residual
   AAWork aa{};                         // its columns, previous f and g, and reduction partials
   // coarse-correction cache mapping: block offsets of the mask scan (u part, then v part from
   // mask_offsets_v), staging for host callers, and the host masks' counts
@@ -624,8 +625,10 @@ int enqueue_coarse(wavi_ctx* c, const CondHandles& h, Tally& tv, Tally& tc) {
   return enqueue_cg_persistent<T, TILE>(c, h, tv, tc);
 }
 
+// picard: the V-cycle of a Picard iteration (then followed by the Anderson step where enabled); false for
+// the adjoint's preconditioner applications.
 template <typename T, int TILE>
-int enqueue_vcycle_post(wavi_ctx* c, const CondHandles& h, Tally& t) {
+int enqueue_vcycle_post(wavi_ctx* c, const CondHandles& h, Tally& t, bool picard = true) {
   (void)h;
   const Dims& d = c->d;
   const int L = c->sp.levels;
@@ -670,11 +673,12 @@ int enqueue_vcycle_post(wavi_ctx* c, const CondHandles& h, Tally& t) {
   CKL();
   t.launches++;
   t.bytes += (double)(2 * sizeof(T) + 8 * 3) * d.N + d.N;
-  if (c->aa_depth > 0) {  // Anderson acceleration: both launches return at once until it has started
+  if (picard && c->aa_depth > 0) {  // Anderson acceleration: both launches return at once until it has started
     k_aa_stage<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, c->x64, corr[cur], c->aa, c->S,
                                                           (const DevParams*)c->P);
     CKL();
-    k_aa_apply<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, c->x64, corr[cur], c->aa, c->uv, c->S);
+    k_aa_apply<T><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(d.N, c->inner_uv, c->x64, corr[cur], c->aa, c->uv, c->S,
+                                                          (const DevParams*)c->P);
     CKL();
     t.launches += 2;
     t.bytes += (double)(2 * sizeof(T) + 2 + 8 * (8 + 2 * c->aa_depth)) * d.N;
@@ -922,6 +926,7 @@ int set_params(wavi_ctx* c, const wavi_params* p) {
   P.n_iter_viscosity = c->sp.n_iter_viscosity;
   P.picard_test = c->opt.picard_test;
   P.aa_depth = c->aa_depth;
+  P.coarse_forcing = c->forcing ? 1 : 0;
   P.aa_start_rel = kAAStartRel;
   P.weertman_ex_f = (float)(1.0 / p->weertman_m - 1.0);
   P.glen_ex_f = (float)(1.0 / p->glen_n - 1.0);
@@ -961,6 +966,7 @@ int solve_enqueue(wavi_ctx* c, const wavi_params* p) {
 void fill_coarse_kind(const wavi_ctx* c, wavi_stats* st) {
   st->coarse_kernel = c->pers_maxt > 0 ? 1 : c->pers_maxt < 0 ? 3 : 2;
   st->picard_accel = c->aa_depth > 0 ? WAVI_PICARD_ANDERSON : WAVI_PICARD_PLAIN;
+  st->coarse_forcing = c->forcing ? WAVI_FORCING_ADAPTIVE : WAVI_FORCING_FIXED;
   const bool cheb = c->coarse_solver == WAVI_COARSE_SRCG_CHEBYSHEV || c->coarse_solver == WAVI_COARSE_PIPELINED_CHEBYSHEV;
   st->cheb_steps = cheb ? cheb_steps(c) : 0;
 }
@@ -1222,7 +1228,7 @@ int adj_vcycle_body(wavi_ctx* c, const double* v, double* out) {
   if (c->pers_maxt != 0) {
     TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv, false)));
     TRY((enqueue_coarse<T, TILE>(c, h, tv, tc)));
-    TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
+    TRY((enqueue_vcycle_post<T, TILE>(c, h, tv, false)));
   } else {
     TRY((enqueue_vcycle_pre<T, TILE>(c, h, tv)));
     CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
@@ -1233,7 +1239,7 @@ int adj_vcycle_body(wavi_ctx* c, const double* v, double* out) {
       CK(cudaMemcpyAsync(c->hS, c->S, sizeof(DevState), cudaMemcpyDeviceToHost, c->st));
       CK(cudaStreamSynchronize(c->st));
     }
-    TRY((enqueue_vcycle_post<T, TILE>(c, h, tv)));
+    TRY((enqueue_vcycle_post<T, TILE>(c, h, tv, false)));
   }
   CK(cudaMemcpyAsync(out, c->x64, bytes, cudaMemcpyDeviceToDevice, c->st));
   return 0;
@@ -1333,6 +1339,8 @@ int adj_prepare(wavi_ctx* c, const wavi_params* p) {
   {
     DevParams pa = *c->hP;
     pa.maxiter_coarse = std::min(pa.maxiter_coarse, kAdjCoarseIters);
+    pa.aa_depth = 0;  // a fixed preconditioner: no Picard acceleration and the fixed coarse tolerance
+    pa.coarse_forcing = 0;
     CK(cudaMemcpyAsync(c->P_adj, &pa, sizeof(DevParams), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));  // (pa lives on this stack frame)
   }
@@ -1604,6 +1612,9 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
                      opt->anderson_depth));
   const bool anderson = opt->picard_accel == WAVI_PICARD_ANDERSON || (opt->picard_accel == WAVI_PICARD_AUTO && mixed(c));
   c->aa_depth = anderson ? (opt->anderson_depth > 0 ? opt->anderson_depth : kAADefaultDepth) : 0;
+  if (opt->coarse_forcing < WAVI_FORCING_AUTO || opt->coarse_forcing > WAVI_FORCING_ADAPTIVE)
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_forcing %d", opt->coarse_forcing));
+  c->forcing = opt->coarse_forcing == WAVI_FORCING_ADAPTIVE || (opt->coarse_forcing == WAVI_FORCING_AUTO && mixed(c));
   c->visc32 = mixed(c) && opt->viscosity != WAVI_VISCOSITY_FP64;
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));

@@ -17,7 +17,8 @@ class EnsembleSolver:
     """``wavi_ensemble``: one context per member grid, solved concurrently."""
 
     def __init__(self, grids, solver_params, precision="mixed", device=0, concurrency=16, coarse_kernel="auto",
-                 coarse_solver="auto", stencil_kernel="auto", picard_accel="auto"):
+                 coarse_solver="auto", stencil_kernel="auto", picard_accel="auto",
+                 coarse_forcing="auto"):
         self.lib = abi.load_library()
         self.n = n = len(grids)
         if len(solver_params) != n:
@@ -29,13 +30,15 @@ class EnsembleSolver:
         opt = abi.Options(int(device), PRECISIONS[precision], 1, 0, VelocitySolver.COARSE_KERNELS[coarse_kernel],
                           abi.COARSE_SOLVERS[coarse_solver], VelocitySolver.STENCIL_KERNELS[stencil_kernel], 0)
         opt.picard_accel = abi.PICARD_ACCEL[picard_accel]
+        opt.coarse_forcing = abi.COARSE_FORCING[coarse_forcing]
         ens = C.c_void_p()
         st = self.lib.wavi_ensemble_create(n, garr, sparr, C.byref(opt), int(concurrency), C.byref(ens))
         if st != 0:
             raise abi.WaviError(st, self.lib.wavi_last_error(None).decode())
         self.ens = ens
         self.config = dict(concurrency=int(concurrency), coarse_kernel=coarse_kernel, coarse_solver=coarse_solver,
-                           stencil_kernel=stencil_kernel, picard_accel=picard_accel)
+                           stencil_kernel=stencil_kernel, picard_accel=picard_accel,
+                           coarse_forcing=coarse_forcing)
 
     def close(self):
         if getattr(self, "ens", None) and self.ens.value:

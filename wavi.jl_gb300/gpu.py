@@ -42,7 +42,8 @@ class VelocitySolver:
 
     def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0,
                  coarse_kernel="auto", coarse_solver="auto", stencil_kernel="auto", cheb_steps=0,
-                 coarse_sums="default", viscosity="default", picard_accel="auto", anderson_depth=0):
+                 coarse_sums="default", viscosity="default", picard_accel="auto", anderson_depth=0,
+                 coarse_forcing="auto"):
         self.lib = abi.load_library()
         self.grid = grid
         self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ
@@ -54,7 +55,8 @@ class VelocitySolver:
                                 self.COARSE_KERNELS[coarse_kernel], abi.COARSE_SOLVERS[coarse_solver],
                                 self.STENCIL_KERNELS[stencil_kernel], int(cheb_steps),
                                 abi.COARSE_SUMS[coarse_sums], abi.VISCOSITY[viscosity],
-                                abi.PICARD_ACCEL[picard_accel], int(anderson_depth))
+                                abi.PICARD_ACCEL[picard_accel], int(anderson_depth),
+                                abi.COARSE_FORCING[coarse_forcing])
         ctx = C.c_void_p()
         st = self.lib.wavi_ctx_create(C.byref(self._desc.desc), C.byref(self._sp), C.byref(self._opt), C.byref(ctx))
         if st != 0:
@@ -287,4 +289,5 @@ def stats_dict(s):
             "coarse_launches": s.coarse_launches,
             "coarse_kernel": COARSE_KERNEL_NAMES.get(s.coarse_kernel, s.coarse_kernel), "cheb_steps": s.cheb_steps,
             "anderson_steps": s.anderson_steps,
-            "picard_accel": abi.PICARD_ACCEL_NAMES.get(s.picard_accel, s.picard_accel)}
+            "picard_accel": abi.PICARD_ACCEL_NAMES.get(s.picard_accel, s.picard_accel),
+            "coarse_forcing": abi.COARSE_FORCING_NAMES.get(s.coarse_forcing, s.coarse_forcing)}

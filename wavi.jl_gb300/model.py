@@ -36,6 +36,8 @@ class GPUParallelSpec:
     device_run: bool = False     # run_simulation without a callback keeps the model on the device (wavi_run_device)
     picard_accel: str = "auto"   # "auto" (fp64: the reference's Picard iteration; mixed: Anderson acceleration),
     #                              "plain" or "anderson"
+    coarse_forcing: str = "auto"  # "auto" (fp64: the reference's fixed tol_coarse; mixed: adaptive), "fixed",
+    #                               "adaptive"
 
 
 _SOLVERS = {}
@@ -48,7 +50,8 @@ def _solver_for(model):
         ps = model.parallel_spec
         s = gpu.VelocitySolver(model.grid, model.solver_params, precision=ps.precision, device=ps.device,
                                use_graphs=ps.use_graphs, picard_test=ps.picard_test,
-                               coarse_solver=ps.coarse_solver, picard_accel=ps.picard_accel)
+                               coarse_solver=ps.coarse_solver, picard_accel=ps.picard_accel,
+                               coarse_forcing=ps.coarse_forcing)
         _SOLVERS[key] = s
     return s
 
