@@ -127,8 +127,8 @@ typedef struct wavi_options {
  * forcing terms of inexact Newton methods, Eisenstat & Walker 1996) uses max(tol_coarse, min(0.1, 0.1 rel)),
  * rel the Picard iteration's relative residual: far from the fixed point the relinearisation, not the
  * linear solve, limits the next iterate, so the coarse CG stops sooner there; once rel <= 10 tol_coarse the
- * tolerance is the reference's.  On the channel and disc test cases it saves 35-45 % of the coarse
- * iterations at the same Picard count and accuracy. */
+ * tolerance is the reference's.  Only in solves of maxiter_picard > 1.  On the channel and disc test cases
+ * it saves 35-45 % of the coarse iterations at the same Picard count and accuracy. */
 typedef enum wavi_coarse_forcing {
   WAVI_FORCING_AUTO = 0,             /* FP64: FIXED (the reference algorithm); mixed: ADAPTIVE */
   WAVI_FORCING_FIXED = 1,            /* tol_coarse */

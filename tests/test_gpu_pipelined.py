@@ -48,7 +48,8 @@ def test_pipelined_needs_mixed_precision_and_16x16_tiles(oracle):
 @pytest.mark.parametrize("name", list(CASES))
 def test_pipelined_converged_solve_matches_reference(oracle, name):
     """The pipelined coarse solve changes the V-cycle, not the fixed point: the converged mixed solve (the
-    reference's plain Picard iteration, like the oracle's) agrees with the reference's FP64 solve to 1e-6.  Its restarts from the true residual and the FP32 drift of its
+    reference's plain Picard iteration and coarse tolerance, like the oracle's) agrees with the reference's
+    FP64 solve to 1e-6.  Its restarts from the true residual and the FP32 drift of its
     recurrences cost coarse iterations: at most 2.5x those of the single-reduction Chebyshev solve with the
     same 3 Chebyshev steps (GB300: 1.35x and 1.96x on the first two cases)."""
     from wavi_gb300.gpu import VelocitySolver
@@ -59,7 +60,8 @@ def test_pipelined_converged_solve_matches_reference(oracle, name):
     stats = {}
     for solver in ("srcg_chebyshev", "pipelined_chebyshev"):
         f = {k: np.array(v, copy=True, order="F") for k, v in f0.items()}
-        s = VelocitySolver(g, sp, precision="mixed", coarse_solver=solver, cheb_steps=3, picard_accel="plain")
+        s = VelocitySolver(g, sp, precision="mixed", coarse_solver=solver, cheb_steps=3, picard_accel="plain",
+                           coarse_forcing="fixed")
         st = s.solve(p, f)
         s.close()
         print(name, solver, st["picard_iterations"], st["coarse_cg_iterations"], st["rel_residual"], uv_err(f, om))

@@ -36,34 +36,48 @@ struct AAWork {
 };
 
 // Every block contributes K values; the last block to finish gets the K totals, each summed over the
-// blocks' partials in block order (deterministic), in tot[0..K) for thread 0, and returns true.
+// blocks' partials in block order (deterministic), in tot[0..K) for thread 0, and returns true.  The K
+// values go through one shuffle tree per warp each and one shared-memory pass (a single __syncthreads),
+// and the last block sums each value's partials with one warp.
 template <int K>
 __device__ __forceinline__ bool last_block_sumk(const double (&v)[K], double* __restrict__ partials, unsigned* counter,
                                                 double (&tot)[K]) {
-  __shared__ double sh[32];
+  __shared__ double sw[32][K];
+  __shared__ double stot[K];
   __shared__ int slast;
-  const int t = flat_tid(), nb = flat_nblocks(), b = flat_bid();
+  const int t = flat_tid(), lane = t & 31, wid = t >> 5, nw = (flat_nthreads() + 31) >> 5;
+  const int nb = flat_nblocks(), b = flat_bid();
+#pragma unroll
   for (int k = 0; k < K; ++k) {
-    const double s = block_sum_any(v[k], sh);
-    __syncthreads();
-    if (t == 0) partials[(size_t)k * nb + b] = s;
+    const double s = warp_sum(v[k]);
+    if (lane == 0) sw[wid][k] = s;
   }
-  if (t == 0) {
+  __syncthreads();
+  if (t < K) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += sw[w][t];
+    partials[(size_t)t * nb + b] = s;
     __threadfence();
+  }
+  __syncthreads();
+  if (t == 0) {
     const unsigned prev = atomicAdd(counter, 1u);
     slast = (prev == (unsigned)nb - 1u);
   }
   __syncthreads();
   if (!slast) return false;
   __threadfence();
-  for (int k = 0; k < K; ++k) {
+  for (int k = wid; k < K; k += nw) {
     double a = 0.0;
-    for (int q = t; q < nb; q += flat_nthreads()) a += __ldcg(partials + (size_t)k * nb + q);
-    a = block_sum_any(a, sh);
-    __syncthreads();
-    tot[k] = a;  // valid in thread 0
+    for (int q = lane; q < nb; q += 32) a += __ldcg(partials + (size_t)k * nb + q);
+    a = warp_sum(a);
+    if (lane == 0) stot[k] = a;
   }
-  if (t == 0) *counter = 0u;
+  __syncthreads();
+  if (t == 0) {
+    for (int k = 0; k < K; ++k) tot[k] = stot[k];
+    *counter = 0u;
+  }
   return true;
 }
 
