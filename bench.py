@@ -876,7 +876,7 @@ def ensemble_arm(args):
 
     n = len(grids)
     if args.no_tune:  # the autotuner's choice on GB300 for this workload
-        best, timings = dict(concurrency=8, coarse_kernel="auto", stencil_kernel="tiled"), []
+        best, timings = dict(concurrency=16, coarse_kernel="auto", stencil_kernel="tiled"), []
     else:
         best, timings = autotune(grids, sps, params, make_tensors, sync=torch.cuda.synchronize)
     ens = EnsembleSolver(grids, sps, precision="mixed", picard_accel=args.picard_accel,
