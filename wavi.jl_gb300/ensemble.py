@@ -60,6 +60,24 @@ class EnsembleSolver:
         return [stats_dict(starr[k]) for k in range(n)]
 
 
+def shard_members(costs, world):
+    """The members each of `world` GPUs solves when an ensemble is split across GPUs (one process per GPU,
+    no exchange between them: the members are independent): longest first onto the least-loaded rank, by
+    the estimated cost of each member (its h cells), ties to the lower rank.  Returns one ascending index
+    list per rank; every member appears exactly once, and no rank carries more than the average load plus
+    the largest member."""
+    world = int(world)
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    load = [0.0] * world
+    out = [[] for _ in range(world)]
+    for k in sorted(range(len(costs)), key=lambda i: (-float(costs[i]), i)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        out[r].append(k)
+        load[r] += float(costs[k])
+    return [sorted(ix) for ix in out]
+
+
 # Members in flight and stencil kernel of the operator and smoother sweeps (shared-memory 32 x 8 tiles, or
 # row streaming), with the persistent coarse-CG kernel (register-resident where a member's share of the device
 # holds its tiles, else global-memory).  On the 256-member workload per-iteration coarse kernels and 32 or 64
