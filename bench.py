@@ -675,7 +675,8 @@ def other_configs(args):
               "mixed_plain", "all_members", "fp64_loop",
               "ensemble_over_fp64_loop", "rel_err_vs_fp64_max", "rel_err_vs_fp64_median", "picard_iterations_mean")),
             ("c4", adjoint_arm, dict(steps=2, warmup=1, directions=2),
-             ("metric", "value", "unit", "ms_per_step", "forward", "adjoint", "dot_test_rel_err", "fd_step",
+             ("metric", "value", "unit", "ms_per_step", "forward", "adjoint", "adjoint_fp64_precond",
+              "dot_test_rel_err", "fd_step",
               "fd_directions", "fd_max_rel_err")))
     for name, arm, kw, keys in legs:
         sub = copy.copy(args)
@@ -1048,6 +1049,18 @@ def adjoint_arm(args):
             times.append(time.perf_counter() - t0)
     grad_c = gc.cpu().numpy().reshape((g.nx, g.ny), order="F")
     grad_a = ga.cpu().numpy().reshape((g.nx, g.ny), order="F")
+    # the same gradient with the solve's own FP64 V-cycle as the FGMRES preconditioner (wavi_adjoint_precond)
+    s64 = VelocitySolver(g, sp, precision="fp64", adjoint_precond="fp64")
+    s64.solve(params, {k: np.array(v, copy=True, order="F") for k, v in state["m"].fields.items()})
+    gc64, ga64 = torch.zeros_like(gc), torch.zeros_like(ga)
+    t64 = []
+    for it in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ast64 = s64.adjoint_device(params, dev(gu), dev(gv), gc64, ga64, tol=1e-12, maxiter=400)
+        t64.append(time.perf_counter() - t0)
+    s64.close()
+    gdiff = float(torch.linalg.norm(torch.cat([gc - gc64, ga - ga64])) / torch.linalg.norm(torch.cat([gc64, ga64])))
     # dot-product test
     rng = np.random.default_rng(6)
     vc, va = rng.standard_normal((g.nx, g.ny)), rng.standard_normal((g.nx, g.ny))
@@ -1087,7 +1100,11 @@ def adjoint_arm(args):
                    "timing": "host wall clock around wavi_adjoint_device"},
         "forward": {"picard_iterations": st0["picard_iterations"], "rel_residual": st0["rel_residual"],
                     "status": st0["status_name"]},
-        "adjoint": {"fgmres_iterations": ast["iterations"], "rel_residual": ast["rel_residual"]},
+        "adjoint": {"fgmres_iterations": ast["iterations"], "rel_residual": ast["rel_residual"],
+                    "preconditioner": "V-cycle in FP32 where it fits (wavi_adjoint_precond auto)"},
+        "adjoint_fp64_precond": {"seconds": min(t64), "fgmres_iterations": ast64["iterations"],
+                                 "rel_residual": ast64["rel_residual"], "gradient_rel_diff": gdiff,
+                                 "note": "the same gradient with the solve's FP64 V-cycle as the preconditioner"},
         "tangent": {"fgmres_iterations": tst["iterations"], "rel_residual": tst["rel_residual"]},
         "dot_test_rel_err": abs(lhs - rhs) / max(abs(lhs), abs(rhs)),
         "fd_step_sweep": {str(h): e for h, e in sweep.items()}, "fd_step": h_best,

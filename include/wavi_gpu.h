@@ -119,8 +119,19 @@ typedef struct wavi_options {
   int32_t coarse_forcing;            /* wavi_coarse_forcing: the coarse CG's tolerance, the reference's fixed
                                         tol_coarse or one that follows the Picard residual (the mixed
                                         default) */
-  int32_t reserved0;
+  int32_t adjoint_precond;           /* wavi_adjoint_precond: precision of the V-cycle that preconditions the
+                                        adjoint's and tangent linear's FGMRES */
 } wavi_options;
+
+/* Precision of the preconditioner V-cycle inside wavi_adjoint_device / wavi_tangent_device.  FGMRES is
+ * flexible and keeps its residual and Krylov basis in FP64, so an FP32 V-cycle (on the FP32-rounded
+ * coefficients of the linearisation) changes its iteration count, not the accuracy it stops at. */
+typedef enum wavi_adjoint_precond {
+  WAVI_ADJ_PRECOND_AUTO = 0,         /* FP32 where its coarse kernel fits the context's cooperative grid
+                                        (16 x 16 coarse tiles), else FP64 */
+  WAVI_ADJ_PRECOND_FP64 = 1,         /* the solve's own FP64 V-cycle */
+  WAVI_ADJ_PRECOND_FP32 = 2          /* FP32 (an error where it cannot run) */
+} wavi_adjoint_precond;
 
 /* Relative tolerance of each V-cycle's coarse CG (abstol = tolerance x |b_c|, update_preconditioners.jl:73).
  * The reference's is tol_coarse in every Picard iteration.  The adaptive rule (not in the reference; the
@@ -403,8 +414,8 @@ int wavi_residual_noalloc(const wavi_operator_desc* op, const double* x_uv, cons
  * differentiation of the Picard fixed point of the last solve on this context (update_velocities.jl
  * :11-29 at convergence: A(coef) x = b together with the per-cell viscosity and drag fixed points
  * :227-339): one linear solve with the transposed linearised operator J_Fᵀ (viscosity and drag
- * derivatives included), by FGMRES preconditioned with one V-cycle of the solve's preconditioner.  The
- * reference has no adjoint.  Preconditions: a float64 context, no u/v_isfixed points, a preceding solve
+ * derivatives included), by FGMRES preconditioned with one V-cycle of the solve's preconditioner (in
+ * FP32 or FP64, wavi_options.adjoint_precond; FGMRES itself is FP64).  The reference has no adjoint.  Preconditions: a float64 context, no u/v_isfixed points, a preceding solve
  * converged tightly (the linearisation is exact at the fixed point).  Device pointers: dJ_du (nx+1)*ny,
  * dJ_dv nx*(ny+1) in, dJ_dlogC and dJ_dlogA nx*ny out.  The solve's state is left unchanged. */
 typedef struct wavi_adjoint_stats {

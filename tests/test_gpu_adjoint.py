@@ -134,3 +134,32 @@ def test_autograd_function_backward_is_the_adjoint():
     lhs = float(torch.dot(wu, du) + torch.dot(wv, dv))
     rhs = float(torch.dot(logC.grad, _dev(vc)) + torch.dot(logA.grad, _dev(va)))
     assert abs(lhs - rhs) <= 1e-8 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+@pytest.mark.parametrize("kw", [dict(nx=40, ny=16, dx=4000.0, mask="full"), dict(nx=37, ny=13, dx=3000.0, mask="full")])
+def test_fp32_preconditioner_gives_the_fp64_gradient(kw):
+    """The adjoint's FGMRES preconditioned by an FP32 V-cycle (wavi_options.adjoint_precond) and by the
+    solve's own FP64 V-cycle: both stop at the same FP64 residual (1e-12), so the gradients agree to that
+    level; the FP32 preconditioner may take a few more iterations."""
+    from wavi_gb300.gpu import VelocitySolver
+    case = Case(**kw)
+    g = case.g
+    params, _ = case.solve()
+    m = case.m
+    rng = np.random.default_rng(31)
+    wu = np.where(m.u_inner, rng.standard_normal((g.nx + 1, g.ny)), 0.0)
+    wv = np.where(m.v_inner, rng.standard_normal((g.nx, g.ny + 1)), 0.0)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        s = VelocitySolver(g, case.sp, precision="fp64", adjoint_precond=prec)
+        st = s.solve(params, {k: np.array(v, copy=True, order="F") for k, v in m.fields.items()})
+        assert st["status"] == 0, st
+        gc = torch.zeros(g.nx * g.ny, dtype=torch.float64, device="cuda")
+        ga = torch.zeros_like(gc)
+        ast = s.adjoint_device(params, _dev(wu), _dev(wv), gc, ga, tol=1e-12)
+        s.close()
+        assert ast["status"] == 0, (prec, ast)
+        out[prec] = (torch.cat([gc, ga]).cpu().numpy(), ast)
+        print(prec, ast)
+    a, b = out["fp64"][0], out["fp32"][0]
+    assert np.linalg.norm(a - b) <= 1e-9 * np.linalg.norm(a), np.linalg.norm(a - b) / np.linalg.norm(a)

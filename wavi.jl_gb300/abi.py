@@ -30,6 +30,7 @@ PICARD_ACCEL = {"auto": 0, "plain": 1, "anderson": 2}  # wavi_picard_accel
 PICARD_ACCEL_NAMES = {v: k for k, v in PICARD_ACCEL.items()}
 COARSE_FORCING = {"auto": 0, "fixed": 1, "adaptive": 2}  # wavi_coarse_forcing
 COARSE_FORCING_NAMES = {v: k for k, v in COARSE_FORCING.items()}
+ADJOINT_PRECOND = {"auto": 0, "fp64": 1, "fp32": 2}  # wavi_adjoint_precond
 
 _dp = C.POINTER(C.c_double)
 _u8p = C.POINTER(C.c_uint8)
@@ -64,7 +65,7 @@ class Options(C.Structure):
                 ("picard_test", C.c_int32), ("coarse_kernel", C.c_int32), ("coarse_solver", C.c_int32),
                 ("stencil_kernel", C.c_int32), ("cheb_steps", C.c_int32), ("coarse_sums", C.c_int32),
                 ("viscosity", C.c_int32), ("picard_accel", C.c_int32), ("anderson_depth", C.c_int32),
-                ("coarse_forcing", C.c_int32), ("reserved0", C.c_int32)]
+                ("coarse_forcing", C.c_int32), ("adjoint_precond", C.c_int32)]
 
 
 FIELD_INPUTS = ("h", "s", "dsdh", "grounded_fraction", "weertman_c", "accumulation", "basal_melt",

@@ -141,6 +141,7 @@ struct wavi_ctx {
   void* cheb_eig = nullptr;            // the Chebyshev coarse solve's power vector (kept across V-cycles)
   int aa_depth = 0;                    // Anderson acceleration of the Picard loop: columns (0: off)
   bool forcing = false;                // the coarse CG's tolerance follows the Picard residual
+  bool adj_fp32 = false;               // the adjoint's preconditioner V-cycle runs in FP32
   AAWork aa{};                         // its columns, previous f and g, and reduction partials
   // coarse-correction cache mapping: block offsets of the mask scan (u part, then v part from
   // mask_offsets_v), staging for host callers, and the host masks' counts
@@ -1246,7 +1247,33 @@ int adj_vcycle_body(wavi_ctx* c, const double* v, double* out) {
 }
 
 int adj_precond(wavi_ctx* c, const double* v, double* out) {
+  if (c->adj_fp32) return adj_vcycle<float, 16>(c, v, out);
   return c->tile == 16 ? adj_vcycle<double, 16>(c, v, out) : adj_vcycle<double, 32>(c, v, out);
+}
+
+// Whether the FP32 V-cycle's coarse kernel can run on this FP64 context's cooperative grid (pers_grid
+// CTAs of pers_maxt tiles, sized for the FP64 kernel): the FP32 kernel must keep as many CTAs resident.
+bool adj_float_fits(wavi_ctx* c) {
+  if (c->tile != 16) return false;
+  if (c->pers_maxt == 0) return true;  // per-iteration kernels: no cooperative launch
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->dev);
+  const int share = std::max(1, c->pers_share);
+  if (c->pers_maxt < 0) {
+    int per_sm = 0;
+    cudaError_t e = c->coarse_solver == WAVI_COARSE_CG
+                        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_global<float, 16>, 256, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_srcg_global<float, 16>, 256, 0);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return (long)per_sm * nsm / share >= c->pers_grid;
+  }
+  const int cap = c->pers_maxt == 1   ? resident_ctas<1, float, 16>(nsm, c->coarse_solver, false)
+                  : c->pers_maxt == 2 ? resident_ctas<2, float, 16>(nsm, c->coarse_solver, false)
+                                      : resident_ctas<4, float, 16>(nsm, c->coarse_solver, false);
+  return cap / share >= c->pers_grid;
 }
 
 // Solve K x = b (K = J_F or J_Fᵀ) by FGMRES(ADJ_RESTART) to ||b - K x|| <= tol ||b||.
@@ -1343,6 +1370,23 @@ int adj_prepare(wavi_ctx* c, const wavi_params* p) {
     pa.coarse_forcing = 0;
     CK(cudaMemcpyAsync(c->P_adj, &pa, sizeof(DevParams), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));  // (pa lives on this stack frame)
+  }
+  // the preconditioner's precision: an FP32 V-cycle on the FP32-rounded coefficients of the linearisation
+  // (FGMRES is flexible and keeps its own FP64 residual), where the FP32 coarse kernel fits this context
+  const bool fits = adj_float_fits(c);
+  if (c->opt.adjoint_precond == WAVI_ADJ_PRECOND_FP32 && !fits)
+    return fail(c, WAVI_ERR_ARGUMENT, "the FP32 adjoint preconditioner needs 16 x 16 coarse tiles and a resident FP32 coarse kernel");
+  c->adj_fp32 = c->opt.adjoint_precond != WAVI_ADJ_PRECOND_FP64 && fits;
+  if (c->adj_fp32) {
+    const Dims& dd = c->d;
+    const double* src[5] = {c->heta_h64, c->dimp64, c->heta_c64, c->beta_m64, c->h_m64};
+    float* dst[5] = {c->heta_h32, c->dimp32, c->heta_c32, c->beta_m32, c->h_m32};
+    const int n[5] = {dd.Nh, dd.Nh, dd.Nc, dd.N, dd.N};
+    for (int k = 0; k < 5; ++k) {
+      if (n[k] <= 0) continue;
+      k_convert<double, float><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(n[k], src[k], dst[k]);
+      CKL();
+    }
   }
   auto& a = c->adj;
   const Dims& d = c->d;
@@ -1615,6 +1659,8 @@ static int create_ctx(const wavi_grid_desc* g, const wavi_solver_params* sp, con
   if (opt->coarse_forcing < WAVI_FORCING_AUTO || opt->coarse_forcing > WAVI_FORCING_ADAPTIVE)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown coarse_forcing %d", opt->coarse_forcing));
   c->forcing = opt->coarse_forcing == WAVI_FORCING_ADAPTIVE || (opt->coarse_forcing == WAVI_FORCING_AUTO && mixed(c));
+  if (opt->adjoint_precond < WAVI_ADJ_PRECOND_AUTO || opt->adjoint_precond > WAVI_ADJ_PRECOND_FP32)
+    return bail(fail(c, WAVI_ERR_ARGUMENT, "unknown adjoint_precond %d", opt->adjoint_precond));
   c->visc32 = mixed(c) && opt->viscosity != WAVI_VISCOSITY_FP64;
   if (want != WAVI_COARSE_AUTO && want != WAVI_COARSE_CG && opt->coarse_kernel == 2)
     return bail(fail(c, WAVI_ERR_ARGUMENT, "the single-reduction coarse solvers run only in the persistent coarse kernel"));

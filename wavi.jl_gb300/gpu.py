@@ -43,7 +43,7 @@ class VelocitySolver:
     def __init__(self, grid, solver_params, precision="fp64", device=0, use_graphs=True, picard_test=0,
                  coarse_kernel="auto", coarse_solver="auto", stencil_kernel="auto", cheb_steps=0,
                  coarse_sums="default", viscosity="default", picard_accel="auto", anderson_depth=0,
-                 coarse_forcing="auto"):
+                 coarse_forcing="auto", adjoint_precond="auto"):
         self.lib = abi.load_library()
         self.grid = grid
         self.nx, self.ny, self.ns = grid.nx, grid.ny, grid.nσ
@@ -56,7 +56,7 @@ class VelocitySolver:
                                 self.STENCIL_KERNELS[stencil_kernel], int(cheb_steps),
                                 abi.COARSE_SUMS[coarse_sums], abi.VISCOSITY[viscosity],
                                 abi.PICARD_ACCEL[picard_accel], int(anderson_depth),
-                                abi.COARSE_FORCING[coarse_forcing])
+                                abi.COARSE_FORCING[coarse_forcing], abi.ADJOINT_PRECOND[adjoint_precond])
         ctx = C.c_void_p()
         st = self.lib.wavi_ctx_create(C.byref(self._desc.desc), C.byref(self._sp), C.byref(self._opt), C.byref(ctx))
         if st != 0:
