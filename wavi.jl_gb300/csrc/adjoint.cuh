@@ -409,4 +409,39 @@ static __global__ void k_scale(int n, double alpha, const double* __restrict__ x
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) y[k] = alpha * x[k];
 }
 
+// Batched Gram-Schmidt pieces of FGMRES (classical Gram-Schmidt twice: two passes h = Vᵀw, w -= V h, the
+// Hessenberg column the sum of both), so that an Arnoldi step needs one host round trip instead of one per
+// basis vector.  Dot products: grid (blocks, m), block (bx, j) sums V[j]·w over its chunk into
+// partials[j * gridDim.x + bx]; k_sum_rows then adds each row in block order (deterministic).
+static __global__ void __launch_bounds__(256) k_multi_dot(int n, const double* const* __restrict__ V,
+                                                          const double* __restrict__ w, double* __restrict__ partials) {
+  __shared__ double sh[32];
+  const int j = blockIdx.y;
+  const double* __restrict__ v = V[j];
+  double s = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) s += v[k] * w[k];
+  s = block_sum_any(s, sh);
+  if (threadIdx.x == 0) partials[(size_t)j * gridDim.x + blockIdx.x] = s;
+}
+// out[j] (+)= Σ_b partials[j * nb + b] for j < m, one warp per row; accumulate: add to out (the second pass)
+static __global__ void k_sum_rows(const double* __restrict__ partials, int nb, int m, double* __restrict__ out,
+                                  int accumulate) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = wid; j < m; j += nw) {
+    double s = 0.0;
+    for (int b = lane; b < nb; b += 32) s += partials[(size_t)j * nb + b];
+    s = warp_sum(s);
+    if (lane == 0) out[j] = accumulate ? out[j] + s : s;
+  }
+}
+// w -= Σ_{j<m} h[j] V[j], h read from device memory
+static __global__ void __launch_bounds__(256) k_multi_axpy(int n, const double* const* __restrict__ V, int m,
+                                                           const double* __restrict__ h, double* __restrict__ w) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    double s = w[k];
+    for (int j = 0; j < m; ++j) s -= h[j] * V[j][k];
+    w[k] = s;
+  }
+}
+
 }  // namespace wavi

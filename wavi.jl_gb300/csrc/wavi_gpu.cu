@@ -70,6 +70,9 @@ struct wavi_ctx {
            *x = nullptr, *uv_keep = nullptr, *xc_keep = nullptr, *dotv = nullptr;
     unsigned* counter = nullptr;
     std::vector<double*> V, Z;
+    double** Vdev = nullptr;  // the Krylov basis pointers, for the batched Gram-Schmidt kernels
+    double* hdev = nullptr;   // [first pass | second pass | ||w||^2] of one Arnoldi step
+    double* gs_partials = nullptr;
   } adj;
   struct Step {          // device time stepping buffers, allocated on first use
     bool ready = false;
@@ -1139,6 +1142,7 @@ int check_params(wavi_ctx* c, const wavi_params* p) {
 // ---------------------------------------------------------------------------------------------
 constexpr int ADJ_RESTART = 40;
 constexpr int kAdjCoarseIters = 100;  // coarse-CG iterations of the adjoint's preconditioner V-cycle
+constexpr int kGsBlocks = 152;        // blocks per basis vector of the batched Gram-Schmidt dot products
 
 int adj_alloc(wavi_ctx* c) {
   auto& a = c->adj;
@@ -1160,6 +1164,11 @@ int adj_alloc(wavi_ctx* c) {
     if ((r = dalloc(c, &v, N))) return r;
   for (auto& v : a.Z)
     if ((r = dalloc(c, &v, N))) return r;
+  if ((r = dalloc(c, &a.Vdev, (size_t)ADJ_RESTART + 1))) return r;
+  if ((r = dalloc(c, &a.hdev, (size_t)2 * (ADJ_RESTART + 1) + 1))) return r;
+  if ((r = dalloc(c, &a.gs_partials, (size_t)(ADJ_RESTART + 1) * kGsBlocks))) return r;
+  if (cudaMemcpy(a.Vdev, a.V.data(), sizeof(double*) * a.V.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(c, WAVI_ERR_CUDA, "adjoint basis pointers upload failed");
   a.ready = true;
   return 0;
 }
@@ -1305,14 +1314,26 @@ int adj_fgmres(wavi_ctx* c, bool transpose, const double* b, double* x, double t
     for (; k < m && *iters < maxit; ++k) {
       TRY(adj_precond(c, a.V[k], a.Z[k]));
       TRY(adj_apply(c, transpose, a.Z[k], a.V[k + 1]));
-      for (int i = 0; i <= k; ++i) {
-        Hij(i, k) = adj_dot(c, a.V[k + 1], a.V[i], &err);
-        if (err) return err;
-        k_axpy<<<nb, EW_THREADS, 0, c->st>>>(n, -Hij(i, k), a.V[i], a.V[k + 1]);
+      // w = V[k+1] against V[0..k]: classical Gram-Schmidt twice, then |w|², one host round trip
+      double* w = a.V[k + 1];
+      const int m1 = k + 1;
+      for (int pass = 0; pass < 2; ++pass) {
+        k_multi_dot<<<dim3(kGsBlocks, m1), 256, 0, c->st>>>(n, a.Vdev, w, a.gs_partials);
+        CKL();
+        k_sum_rows<<<1, 256, 0, c->st>>>(a.gs_partials, kGsBlocks, m1, a.hdev + pass * (ADJ_RESTART + 1), 0);
+        CKL();
+        k_multi_axpy<<<nb, EW_THREADS, 0, c->st>>>(n, a.Vdev, m1, a.hdev + pass * (ADJ_RESTART + 1), w);
         CKL();
       }
-      const double hn = std::sqrt(adj_dot(c, a.V[k + 1], a.V[k + 1], &err));
-      if (err) return err;
+      k_multi_dot<<<dim3(kGsBlocks, 1), 256, 0, c->st>>>(n, a.Vdev + k + 1, w, a.gs_partials);
+      CKL();
+      k_sum_rows<<<1, 256, 0, c->st>>>(a.gs_partials, kGsBlocks, 1, a.hdev + 2 * (ADJ_RESTART + 1), 0);
+      CKL();
+      double hh[2 * (ADJ_RESTART + 1) + 1];
+      CK(cudaMemcpyAsync(hh, a.hdev, sizeof(hh), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      for (int i = 0; i <= k; ++i) Hij(i, k) = hh[i] + hh[ADJ_RESTART + 1 + i];
+      const double hn = std::sqrt(std::max(0.0, hh[2 * (ADJ_RESTART + 1)]));
       Hij(k + 1, k) = hn;
       if (hn > 0.0) {
         k_scale<<<nb, EW_THREADS, 0, c->st>>>(n, 1.0 / hn, a.V[k + 1], a.V[k + 1]);
