@@ -126,9 +126,12 @@ __global__ void __launch_bounds__(256) k_aa_stage(int n, const uint8_t* __restri
   const bool have_prev = st->aa.have_prev != 0;
   const int newest = have_prev ? (st->aa.cols == 0 ? 0 : (st->aa.head + 1) % depth) : 0;
   const int ncols = have_prev ? min(st->aa.cols + 1, depth) : 0;
+  // fixed-bound loops with guards keep slot[] and v[] in registers (no dynamic indexing)
   int slot[kAAMax];
-  for (int p = 0; p < ncols; ++p) slot[p] = ((newest - p) % depth + depth) % depth;
+#pragma unroll
+  for (int p = 0; p < kAAMax; ++p) slot[p] = p < ncols ? ((newest - p) % depth + depth) % depth : 0;
   double v[2 * kAAMax];
+#pragma unroll
   for (int k = 0; k < 2 * kAAMax; ++k) v[k] = 0.0;
   const size_t N = (size_t)n;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -140,11 +143,13 @@ __global__ void __launch_bounds__(256) k_aa_stage(int n, const uint8_t* __restri
       w.dG[(size_t)newest * N + k] = cg;
       v[0] += cf * cf;
       v[kAAMax] += cf * f;
-      for (int p = 1; p < ncols; ++p) {
-        const double o = w.dF[(size_t)slot[p] * N + k];
-        v[p] += cf * o;
-        v[kAAMax + p] += o * f;
-      }
+#pragma unroll
+      for (int p = 1; p < kAAMax; ++p)
+        if (p < ncols) {
+          const double o = w.dF[(size_t)slot[p] * N + k];
+          v[p] += cf * o;
+          v[kAAMax + p] += o * f;
+        }
     }
     w.fprev[k] = f;
     w.gprev[k] = g;
@@ -175,19 +180,22 @@ __global__ void __launch_bounds__(256) k_aa_apply(int n, const uint8_t* __restri
   const int used = st->aa.used;
   double gam[kAAMax];
   const double* col[kAAMax];
-  for (int p = 0; p < used; ++p) {
-    gam[p] = st->aa.gamma[p];
-    col[p] = w.dG + (size_t)st->aa.slot[p] * (size_t)n;
+#pragma unroll
+  for (int p = 0; p < kAAMax; ++p) {
+    gam[p] = p < used ? st->aa.gamma[p] : 0.0;
+    col[p] = w.dG + (size_t)(p < used ? st->aa.slot[p] : 0) * (size_t)n;
   }
   double v[2] = {0.0, 0.0};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     if (!inner[k]) continue;
     double xn = x[k], dx = (double)corr[k];
-    for (int p = 0; p < used; ++p) {
-      const double c = gam[p] * col[p][k];
-      xn -= c;
-      dx -= c;
-    }
+#pragma unroll
+    for (int p = 0; p < kAAMax; ++p)
+      if (p < used) {
+        const double c = gam[p] * col[p][k];
+        xn -= c;
+        dx -= c;
+      }
     x[k] = xn;
     uv[k] = xn;
     v[0] += dx * dx;
