@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(256) k_aa_stage(int n, const uint8_t* __restri
         a.head = newest;
         a.cols = ncols;
         a.used = aa_solve(a, depth, tot + kAAMax);
-        a.steps++;
+        if (a.used > 0) a.steps++;
       }
       a.have_prev = 1;
     }
