@@ -149,3 +149,34 @@ def test_every_entry_point_rejects_a_null_context(lib, pkg):
     for name, args in calls.items():
         assert getattr(lib, name)(*args) == -1, name
     assert lib.wavi_ctx_destroy(None) == 0 and lib.wavi_ensemble_destroy(None) == 0
+
+
+def _header_struct_fields(text, name):
+    """Field names, in order, of `typedef struct name { ... } name;` in the header (comments dropped)."""
+    import re
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), text, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        # "int32_t a, b" / "double x, y" / "const double* p": the names after the type
+        _, _, names = decl.partition(" ")
+        for n in names.split(","):
+            fields.append(n.strip().lstrip("*").strip())
+    return fields
+
+
+@pytest.mark.parametrize("cname,mirror", [("wavi_options", "Options"), ("wavi_stats", "Stats"),
+                                          ("wavi_solver_params", "SolverParams"), ("wavi_params", "Params")])
+def test_ctypes_mirror_field_order_matches_header(pkg, cname, mirror):
+    """The ctypes structs list the header's fields in the header's order (equal sizes alone would not catch
+    two int32 fields swapped, e.g. a new option added in the wrong place)."""
+    from wavi_gb300 import abi
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with open(os.path.join(root, "include", "wavi_gpu.h")) as fh:
+        text = fh.read()
+    want = _header_struct_fields(text, cname)
+    have = [f[0] for f in getattr(abi, mirror)._fields_]
+    assert have == want, (cname, have, want)
