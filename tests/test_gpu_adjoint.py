@@ -136,11 +136,14 @@ def test_autograd_function_backward_is_the_adjoint():
     assert abs(lhs - rhs) <= 1e-8 * max(abs(lhs), abs(rhs)), (lhs, rhs)
 
 
-@pytest.mark.parametrize("kw", [dict(nx=40, ny=16, dx=4000.0, mask="full"), dict(nx=37, ny=13, dx=3000.0, mask="full")])
-def test_fp32_preconditioner_gives_the_fp64_gradient(kw):
+@pytest.mark.parametrize("kw,coarse", [(dict(nx=40, ny=16, dx=4000.0, mask="full"), "auto"),
+                                       (dict(nx=37, ny=13, dx=3000.0, mask="full"), "auto"),
+                                       (dict(nx=40, ny=16, dx=4000.0, mask="full"), "srcg_chebyshev")])
+def test_fp32_preconditioner_gives_the_fp64_gradient(kw, coarse):
     """The adjoint's FGMRES preconditioned by an FP32 V-cycle (wavi_options.adjoint_precond) and by the
     solve's own FP64 V-cycle: both stop at the same FP64 residual (1e-12), so the gradients agree to that
-    level; the FP32 preconditioner may take a few more iterations."""
+    level; the FP32 preconditioner may take a few more iterations.  Also with the Chebyshev coarse solve,
+    whose power vector the FP32 V-cycle restarts from zero."""
     from wavi_gb300.gpu import VelocitySolver
     case = Case(**kw)
     g = case.g
@@ -151,7 +154,7 @@ def test_fp32_preconditioner_gives_the_fp64_gradient(kw):
     wv = np.where(m.v_inner, rng.standard_normal((g.nx, g.ny + 1)), 0.0)
     out = {}
     for prec in ("fp64", "fp32"):
-        s = VelocitySolver(g, case.sp, precision="fp64", adjoint_precond=prec)
+        s = VelocitySolver(g, case.sp, precision="fp64", adjoint_precond=prec, coarse_solver=coarse)
         st = s.solve(params, {k: np.array(v, copy=True, order="F") for k, v in m.fields.items()})
         assert st["status"] == 0, st
         gc = torch.zeros(g.nx * g.ny, dtype=torch.float64, device="cuda")

@@ -1408,6 +1408,8 @@ int adj_prepare(wavi_ctx* c, const wavi_params* p) {
       k_convert<double, float><<<c->ew_blocks, EW_THREADS, 0, c->st>>>(n[k], src[k], dst[k]);
       CKL();
     }
+    // a Chebyshev coarse solve's power vector holds the FP64 solve's doubles: start the FP32 one from zero
+    if (c->cheb_eig) CK(cudaMemsetAsync(c->cheb_eig, 0, c->d.N * sizeof(double), c->st));
   }
   auto& a = c->adj;
   const Dims& d = c->d;
