@@ -161,10 +161,9 @@ def _header_struct_fields(text, name):
         decl = decl.strip()
         if not decl:
             continue
-        # "int32_t a, b" / "double x, y" / "const double* p": the names after the type
-        _, _, names = decl.partition(" ")
-        for n in names.split(","):
-            fields.append(n.strip().lstrip("*").strip())
+        # "int32_t a, b" / "double x, y" / "const uint8_t* p, *q": the last word of each comma-separated part
+        for part in decl.split(","):
+            fields.append(re.split(r"[\s*]+", part.strip())[-1])
     return fields
 
 
@@ -180,3 +179,25 @@ def test_ctypes_mirror_field_order_matches_header(pkg, cname, mirror):
     want = _header_struct_fields(text, cname)
     have = [f[0] for f in getattr(abi, mirror)._fields_]
     assert have == want, (cname, have, want)
+
+
+def _julia_struct_fields(text, name):
+    """Field names, in order, of `struct name` / `mutable struct name` ... `end` in the Julia binding."""
+    import re
+    m = re.search(r"(?:mutable )?struct %s\n(.*?)\nend" % name, text, re.S)
+    body = re.sub(r"#.*", "", m.group(1))
+    return [f.split("::")[0].strip() for f in re.findall(r"\b\w+::\w+(?:\{[^}]*\})?", body)]
+
+
+@pytest.mark.parametrize("jname,cname", [("WaviOptions", "wavi_options"), ("WaviStats", "wavi_stats"),
+                                         ("WaviSolverParams", "wavi_solver_params"), ("WaviParams", "wavi_params"),
+                                         ("WaviGridDesc", "wavi_grid_desc")])
+def test_julia_binding_structs_match_header(jname, cname):
+    """The Julia binding documented in INTEGRATION.md declares the header's struct fields in the header's
+    order (the layout its ccall passes)."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with open(os.path.join(root, "include", "wavi_gpu.h")) as fh:
+        header = fh.read()
+    with open(os.path.join(root, "INTEGRATION.md")) as fh:
+        julia = fh.read()
+    assert _julia_struct_fields(julia, jname) == _header_struct_fields(header, cname)
